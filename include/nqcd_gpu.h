@@ -1,0 +1,180 @@
+/*
+ * nqcd_gpu.h -- C ABI of the GB300 ensemble trajectory engine.
+ *
+ * The engine runs NQCDynamics.jl's ensemble trajectory loop (FSSH surface
+ * hopping on two-state models, ring-polymer surface hopping) on one GPU.
+ * It is the body of a GPU `ensemble_algorithm` that `run_dynamics` forwards to
+ * `SciMLBase.solve` (reference: src/Ensembles/run_dynamics.jl:42-136, the
+ * solve call at :91-97), so that a Julia host calls it through `ccall` in
+ * place of the per-trajectory CPU loop of `EnsembleSerial`/`EnsembleThreads`.
+ *
+ * Conventions
+ *  - Every entry point returns 0 (NQCD_OK) or a negative NQCD_ERR_* code;
+ *    no C++ exception crosses the boundary.  nqcd_last_error() gives text.
+ *  - Host arrays use the reference's (Julia, column-major) layout with the
+ *    trajectory index slowest: positions/velocities as (ndofs, natoms, ntraj)
+ *    or (ndofs, natoms, nbeads, ntraj), density matrices as
+ *    (nstates, nstates, ntraj).  States are 0-based.
+ *  - The caller owns host buffers; the handle owns device memory and its
+ *    CUDA stream until nqcd_destroy().  A handle is used by one host thread
+ *    at a time; separate handles may run concurrently.
+ *  - There is no CPU fallback: without a usable GPU, nqcd_create() fails
+ *    with NQCD_ERR_CUDA.
+ */
+#ifndef NQCD_GPU_H
+#define NQCD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NQCD_ABI_VERSION 100
+
+enum nqcd_status {
+    NQCD_OK = 0,
+    NQCD_ERR_ARG = -1,         /* invalid argument or configuration */
+    NQCD_ERR_CUDA = -2,        /* CUDA runtime error (message in nqcd_last_error) */
+    NQCD_ERR_OOM = -3,         /* device or host allocation failed */
+    NQCD_ERR_TIMEOUT = -4,     /* a bounded device wait gave up */
+    NQCD_ERR_NAN = -5,         /* non-finite values detected in the final state */
+    NQCD_ERR_UNSUPPORTED = -6, /* method/model/output combination not supported */
+    NQCD_ERR_STATE = -7        /* call out of order (e.g. run before set_initial) */
+};
+
+enum nqcd_method { NQCD_METHOD_FSSH = 1, NQCD_METHOD_RPSH = 2, NQCD_METHOD_IESH = 3, NQCD_METHOD_MDEF = 4 };
+
+enum nqcd_model {
+    NQCD_MODEL_TULLY1 = 1,    /* params: A, B, C, D */
+    NQCD_MODEL_TULLY2 = 2,    /* params: A, B, C, D, E0 */
+    NQCD_MODEL_TULLY3 = 3,    /* params: A, B, C */
+    NQCD_MODEL_SPINBOSON = 10 /* params: eps, Delta; bath_a = c_j, bath_b = omega_j */
+};
+
+enum nqcd_precision {
+    NQCD_PREC_FP64 = 0, /* plain path: bit-identical to the FP64 reference integration */
+    NQCD_PREC_FP32 = 1  /* fast path: FP32 electronic structure, FP64 accumulation */
+};
+
+enum nqcd_rescaling { NQCD_RESCALE_STANDARD = 0, NQCD_RESCALE_VINVERSION = 1, NQCD_RESCALE_OFF = 2 };
+
+enum nqcd_init {
+    NQCD_INIT_GIVEN = 0,          /* density matrix and state from nqcd_set_initial */
+    NQCD_INIT_ADIABATIC_PURE = 1, /* PureState(init_state, Adiabatic()) */
+    NQCD_INIT_DIABATIC_PURE = 2   /* PureState(init_state, Diabatic()): rotated, state sampled */
+};
+
+typedef struct nqcd_config {
+    int32_t method;       /* nqcd_method */
+    int32_t model;        /* nqcd_model */
+    int32_t precision;    /* nqcd_precision */
+    int32_t rescaling;    /* nqcd_rescaling (FSSH `rescaling` keyword) */
+    int32_t ndofs;        /* degrees of freedom per atom */
+    int32_t natoms;       /* atoms */
+    int32_t nstates;      /* electronic states (2 for the supported models) */
+    int32_t nbeads_max;   /* ring polymer: largest bead count (0 or 1 for classical nuclei) */
+    int32_t nparams;      /* entries of params */
+    const double* params; /* model parameters, see nqcd_model */
+    int32_t nbath;        /* spin-boson bath modes (== natoms * ndofs) */
+    const double* bath_a; /* spin-boson: couplings c_j */
+    const double* bath_b; /* spin-boson: frequencies omega_j */
+    const double* masses; /* [natoms] */
+    double beta;          /* ring polymer: inverse temperature 1/kT (atomic units) */
+    int64_t ntraj_max;    /* capacity: trajectories per run */
+    int32_t init_kind;    /* nqcd_init */
+    int32_t init_state;   /* 0-based state for NQCD_INIT_*_PURE */
+    int32_t save_stride;  /* population correlation every save_stride steps (0 = off) */
+    int32_t max_hops;     /* hop-log capacity per trajectory (0 = no log) */
+    double terminate_x;   /* ring polymer: stop a trajectory once |centroid x| > terminate_x (0 = off) */
+    double gap_fp64;      /* fast path: propagate electronics in FP64 when the adiabatic gap is below this */
+    int64_t traj_offset;  /* global index of trajectory 0 (Philox counter), for sharded ensembles */
+    int32_t reserved[6];
+} nqcd_config;
+
+typedef struct nqcd_outputs {
+    /* Ensemble means (MeanReduction, src/Ensembles/reductions.jl:36-52).  Host pointers; NULL to skip. */
+    double* scattering;             /* [2][nstates]: reflection, transmission (OutputStateResolvedScattering1D) */
+    double* population_correlation; /* [nsave][nstates][nstates] (PopulationCorrelationFunction, Diabatic) */
+    int32_t nsave;                  /* out: save points written */
+    int32_t reserved;
+} nqcd_outputs;
+
+typedef struct nqcd_stats {
+    int64_t traj_steps;     /* nuclear steps summed over trajectories */
+    int64_t hops;           /* accepted hops */
+    int64_t frustrated;     /* frustrated hops */
+    int64_t flagged;        /* trajectories with non-finite final state */
+    double device_ms;       /* CUDA-event time of the whole call's device work on the engine stream */
+    double kernel_ms;       /* CUDA-event time of the ensemble kernel alone */
+    double wall_ms;         /* host wall time of the call */
+    int64_t h2d_bytes;      /* bytes copied host->device inside the call */
+    int64_t d2h_bytes;      /* bytes copied device->host inside the call */
+    int32_t kernel_launches;/* engine kernels launched by the call */
+    int32_t reserved;
+} nqcd_stats;
+
+typedef struct nqcd_handle nqcd_handle;
+
+/* ABI version (NQCD_ABI_VERSION). */
+int nqcd_version(void);
+
+/* Create an engine for one Simulation (reference: Simulation/RingPolymerSimulation
+ * constructors, src/simulations.jl:12-73, with the method of
+ * src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:206-213).  Allocates device
+ * memory for cfg->ntraj_max trajectories. */
+int nqcd_create(const nqcd_config* cfg, nqcd_handle** out);
+
+/* Initial conditions for `ntraj` trajectories (reference: Selection /
+ * sample_distribution, src/Ensembles/selections.jl:70-99, and
+ * DynamicsVariables, fssh.jl:215-233).  r0, v0: (ndofs, natoms[, nbeads], ntraj).
+ * sig_re/sig_im/state0 are read only for NQCD_INIT_GIVEN (else may be NULL).
+ * nbeads: per-trajectory bead counts for ring polymers (NULL = nbeads_max). */
+int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, const double* sig_re,
+                     const double* sig_im, const int32_t* state0, const int32_t* nbeads);
+
+/* Same as nqcd_set_initial with r0/v0 already on the device in the engine's
+ * structure-of-arrays layout [dof][trajectory] (dof = ndofs*natoms[*nbeads]). */
+int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0_soa, const double* d_v0_soa,
+                            const int32_t* nbeads);
+
+/* Run the ensemble from t0 to t1 with step dt (reference: the ensemble solve,
+ * src/Ensembles/run_dynamics.jl:91-97, with the method's integrator,
+ * src/DynamicsMethods/IntegrationAlgorithms/bab_electronics.jl:61-91 or
+ * bcb_electronics.jl:53-97, and hopping callback surface_hopping.jl:2-16).
+ * Every run starts from the initial conditions last set.  Random numbers are
+ * Philox4x32-10 keyed by `seed` with counter (trajectory, step, stream). */
+int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out,
+             nqcd_stats* stats);
+
+/* Final per-trajectory state of the last run (any pointer may be NULL):
+ * r, v as in nqcd_set_initial; sig_re/sig_im (nstates, nstates, ntraj);
+ * state, nhops, nfrustrated, nsteps [ntraj]; energy [ntraj][2] (initial, final
+ * total energy, DynamicsOutputs.OutputTotalEnergy). */
+int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double* sig_im, int32_t* state,
+                   int32_t* nhops, int32_t* nfrustrated, int32_t* nsteps, double* energy);
+
+/* Accepted hops of the last run, [ntraj][max_hops][3] = (step, from, to), -1 padded
+ * (DynamicsOutputs.OutputSurfaceHops, src/DynamicsOutputs.jl:235-243). */
+int nqcd_get_hop_log(nqcd_handle* h, int32_t* log);
+
+/* Message of the last failed call on this handle (or of the last failed
+ * nqcd_create in this thread when h is NULL). */
+const char* nqcd_last_error(const nqcd_handle* h);
+
+/* Free the handle, its device memory and stream. */
+void nqcd_destroy(nqcd_handle* h);
+
+/* Page-lock caller memory for asynchronous copies (cudaHostRegister). */
+int nqcd_pin_host(void* ptr, int64_t bytes);
+int nqcd_unpin_host(void* ptr);
+
+/* Measure this GPU's FP64 and FP32 CUDA-core fused multiply-add throughput
+ * (TFLOP/s, 2 flops per FMA) with a register-resident FMA chain kernel. */
+int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NQCD_GPU_H */

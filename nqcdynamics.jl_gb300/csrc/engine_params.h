@@ -1,0 +1,54 @@
+// Launch parameters of the ensemble kernels (device pointers only).
+// Layout in HBM: structure-of-arrays with the trajectory index fastest, so
+// that consecutive threads (one trajectory each) touch consecutive words.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace nqcd {
+
+struct FsshParams {
+    // model
+    int32_t model;
+    double mp[8];
+    int32_t ndof;             // degrees of freedom per trajectory (spin-boson: bath modes)
+    const double* mass;       // [ndof]
+    const double* bath_c;     // [ndof] (spin-boson)
+    const double* bath_w2;    // [ndof] (spin-boson)
+    double sum_c2_over_m;     // sum_j c_j^2 / m_j (spin-boson fast path)
+    // method
+    int32_t rescaling;
+    int32_t init_kind;
+    int32_t init_state;
+    float gap_fp64;           // fast path: FP64 electronics below this adiabatic gap
+    // run
+    int64_t ntraj;
+    int64_t traj_offset;
+    double t0, t1, dt;
+    uint64_t seed;
+    int32_t save_stride;
+    int32_t nsave;
+    int32_t max_hops;
+    // state, SoA [component][ntraj]
+    double* r;                // [ndof][ntraj]
+    double* v;                // [ndof][ntraj]
+    double* scratch;          // plain spin-boson: per-DoF couplings [ndof][ntraj]
+    double* sigma;            // [8][ntraj]
+    int32_t* state;           // [ntraj]
+    // outputs
+    int32_t* nhops;           // [ntraj]
+    int32_t* nfrustrated;     // [ntraj]
+    int32_t* nsteps;          // [ntraj]
+    int32_t* hop_log;         // [max_hops][3][ntraj]
+    double* energy;           // [2][ntraj]
+    double* popcorr_partial;  // [nwarps][nsave][4]
+    unsigned long long* scatter;  // [4]
+};
+
+// Host launchers (one translation unit per precision).
+cudaError_t launch_fssh2_fp64(const FsshParams& p, cudaStream_t s);
+cudaError_t launch_fssh2_fp32(const FsshParams& p, cudaStream_t s);
+cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* out,
+                                   cudaStream_t s);
+
+}  // namespace nqcd

@@ -1,0 +1,543 @@
+// Ensemble kernels for two-state fewest-switches surface hopping.
+// One trajectory per thread, the whole time loop inside one launch.
+//
+//   fssh2_tully_kernel<R>     Tully models 1-3 (1 DoF): r, v, k, sigma and the
+//                             electronic cache live in registers.
+//   fssh2_spinboson_kernel<R> spin-boson (N bath modes): bath coordinates and
+//                             velocities in HBM as [mode][trajectory] (coalesced);
+//                             the 2x2 electronic problem in registers.
+//
+// R = double is the plain path (bit-identical to the oracle; its translation
+// unit is compiled with -fmad=false); R = float is the fast path.
+// Algorithm and reference citations: fssh2_traj.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <type_traits>
+
+#include "engine_params.h"
+#include "fssh2_traj.h"
+
+namespace nqcd {
+
+constexpr int kFsshBlock = 128;
+
+template <typename R>
+struct IsFast : std::integral_constant<bool, std::is_same<R, float>::value> {};
+
+// Per-warp partial sums of the diabatic population correlation at one save
+// point (TimeCorrelationFunctions.jl:61-88); reduced over warps afterwards in
+// a fixed order, so the ensemble mean is deterministic.
+__device__ __forceinline__ void warp_save_popcorr(const FsshParams& p, int isave, bool active, const double pop0[2],
+                                                  const double pop[2]) {
+    double c[4];
+    c[0] = active ? pop0[0] * pop[0] : 0.0;
+    c[1] = active ? pop0[0] * pop[1] : 0.0;
+    c[2] = active ? pop0[1] * pop[0] : 0.0;
+    c[3] = active ? pop0[1] * pop[1] : 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) c[q] += __shfl_xor_sync(0xffffffffu, c[q], off);
+    if ((threadIdx.x & 31) == 0 && isave < p.nsave) {
+        int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        double* dst = p.popcorr_partial + (warp * p.nsave + isave) * 4;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst[q] = c[q];
+    }
+}
+
+// diag(U sigma' U^T), sigma' = Re(sigma) with diagonal replaced by the
+// occupied state (fssh.jl:300-310).
+template <typename R>
+__device__ __forceinline__ void diabatic_pop2(const Sig2<R>& sg, int s, const R Z[4], double pop[2]) {
+    double sp00 = s == 0 ? 1.0 : 0.0, sp11 = s == 1 ? 1.0 : 0.0, sp01 = (double)sg.x;
+    double U00 = Z[0], U10 = Z[1], U01 = Z[2], U11 = Z[3];
+    double M00 = U00 * sp00 + U01 * sp01;
+    double M01 = U00 * sp01 + U01 * sp11;
+    double M10 = U10 * sp00 + U11 * sp01;
+    double M11 = U10 * sp01 + U11 * sp11;
+    pop[0] = M00 * U00 + M01 * U01;
+    pop[1] = M10 * U10 + M11 * U11;
+}
+
+// Initial electronic variables: adiabatic pure state, or a diabatic pure
+// state rotated to the adiabatic basis with the occupied state sampled from
+// its populations (fssh.jl:215-233; density_matrix_dynamics.jl:37-75).
+template <typename R>
+__device__ __forceinline__ void init_electronics2(const FsshParams& p, int64_t i, int64_t gid, const R Z[4],
+                                                  Sig2<R>& sg, int& state) {
+    if (p.init_kind == INIT_GIVEN) {
+        sg.p = (R)p.sigma[0 * p.ntraj + i];
+        sg.x = (R)p.sigma[2 * p.ntraj + i];
+        sg.y = (R)p.sigma[3 * p.ntraj + i];
+        sg.q = (R)p.sigma[6 * p.ntraj + i];
+        state = p.state[i];
+        return;
+    }
+    if (p.init_kind == INIT_ADIABATIC_PURE) {
+        sg.p = p.init_state == 0 ? R(1) : R(0);
+        sg.q = p.init_state == 1 ? R(1) : R(0);
+        sg.x = R(0);
+        sg.y = R(0);
+        state = p.init_state;
+        return;
+    }
+    // sigma = U^T rho U with rho = e_k e_k^T: sigma_ij = U_ki U_kj (evaluated as the oracle's products)
+    double U[2][2] = {{(double)Z[0], (double)Z[2]}, {(double)Z[1], (double)Z[3]}};
+    double rho[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    rho[p.init_state][p.init_state] = 1.0;
+    double T[2][2], S[2][2];
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) T[a][b] = U[0][a] * rho[0][b] + U[1][a] * rho[1][b];
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) S[a][b] = T[a][0] * U[0][b] + T[a][1] * U[1][b];
+    sg.p = (R)S[0][0];
+    sg.q = (R)S[1][1];
+    sg.x = (R)S[0][1];
+    sg.y = R(0);
+    double wsum = S[0][0] + S[1][1];
+    double tt = rng_uniform(p.seed, (uint64_t)gid, 0u, RNG_INIT_STATE) * wsum;
+    state = (S[0][0] < tt) ? 1 : 0;
+}
+
+// One electronic macro step: plain path in FP64; fast path in FP32 unless
+// the adiabatic gap is below gap_fp64.
+template <typename R>
+__device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>& buf, double t, double h,
+                                             R gap, Sig2<R>& sg) {
+    const double dtsub = p.dt / 5.0;
+    if constexpr (!IsFast<R>::value) {
+        Interp64 fn(buf);
+        electronic_macro_step2<double>(fn, t, h, dtsub, sg);
+    } else {
+        if (gap < p.gap_fp64) {
+            EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, buf.tc, buf.E0n, buf.E1n, buf.Dn, buf.tn};
+            Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
+            Interp64 fn(b64);
+            electronic_macro_step2<double>(fn, t, h, dtsub, s64);
+            sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
+        } else {
+            Interp32 fn(buf);
+            electronic_macro_step2<float>(fn, t, h, dtsub, sg);
+        }
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void write_sigma(const FsshParams& p, int64_t i, const Sig2<R>& sg) {
+    const int64_t N = p.ntraj;
+    p.sigma[0 * N + i] = sg.p;
+    p.sigma[1 * N + i] = 0.0;
+    p.sigma[2 * N + i] = sg.x;
+    p.sigma[3 * N + i] = sg.y;
+    p.sigma[4 * N + i] = sg.x;
+    p.sigma[5 * N + i] = -(double)sg.y;
+    p.sigma[6 * N + i] = sg.q;
+    p.sigma[7 * N + i] = 0.0;
+}
+
+__device__ __forceinline__ void log_hop(const FsshParams& p, bool active, int64_t i, int nh, int step, int from,
+                                        int to) {
+    if (active && p.hop_log && nh < p.max_hops) {
+        const int64_t N = p.ntraj;
+        p.hop_log[((int64_t)nh * 3 + 0) * N + i] = step;
+        p.hop_log[((int64_t)nh * 3 + 1) * N + i] = from;
+        p.hop_log[((int64_t)nh * 3 + 2) * N + i] = to;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tully models (1 DoF)
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParams p) {
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i0 < p.ntraj;
+    const int64_t i = active ? i0 : p.ntraj - 1;
+    const int64_t gid = p.traj_offset + i;
+
+    R mp[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) mp[q] = (R)p.mp[q];
+    const double mass = p.mass[0];
+    double x = p.r[i], v = p.v[i];
+
+    R Z[4] = {R(1), R(0), R(0), R(1)};
+    R w[2], A[3], nac;
+    auto update_cache = [&](double xx) {
+        R V[3], D[3], Zn[4];
+        tully_potential<R>(p.model, mp, (R)xx, V);
+        eigen2_phase<R>(V, Z, w, Zn);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Z[q] = Zn[q];
+        tully_derivative<R>(p.model, mp, (R)xx, D);
+        adiabatic_derivative2<R>(D, Z, A);
+        nac = A[1] / (w[1] - w[0]);
+    };
+    auto accel = [&](int s) -> double {
+        R a = s == 0 ? A[0] : A[2];
+        return (double)(-a / (R)mass);
+    };
+
+    update_cache(x);
+    Sig2<R> sg;
+    int state;
+    init_electronics2<R>(p, i, gid, Z, sg, state);
+    double k = accel(state);
+
+    double e0 = (0.0 + mass * (v * v)) / 2.0 + (double)w[state];
+    double pop0[2] = {0.0, 0.0};
+    int isave = 0;
+    if (p.save_stride > 0) {
+        diabatic_pop2<R>(sg, state, Z, pop0);
+        warp_save_popcorr(p, isave++, active, pop0, pop0);
+    }
+
+    EBuf<R> buf = {R(0), R(0), R(0), 0.0, R(0), R(0), R(0), 0.0};
+    int nh = 0, nf = 0, step = 0;
+    double t = p.t0;
+    while (t < p.t1) {
+        double h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
+        double half = h / 2.0;
+        double vtmp = v + half * k;
+        x = x + h * vtmp;
+        update_cache(x);
+        k = accel(state);
+        v = vtmp + half * k;
+        buf.E0c = buf.E0n;
+        buf.E1c = buf.E1n;
+        buf.Dc = buf.Dn;
+        buf.tc = buf.tn;
+        buf.E0n = w[0];
+        buf.E1n = w[1];
+        buf.Dn = R(0) + nac * (R)v;
+        buf.tn = t + h;
+        electronics2<R>(p, buf, t, h, w[1] - w[0], sg);
+        t = snap_time(t + h, p.t1);
+        step += 1;
+
+        // hop test
+        const int s = state;
+        R inv = R(1) / (s == 0 ? sg.p : sg.q);
+        R re = sg.x * inv;
+        R nsm = s == 0 ? nac : -nac;
+        R prob = clamp01<R>(R(0) + R(2) * (R)v * re * nsm * (R)p.dt);
+        double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
+        if ((double)prob > u) {
+            const int ns = 1 - s;
+            bool accept = true;
+            if (p.rescaling != RESCALE_OFF) {
+                double d = (double)(ns < s ? nac : -nac);
+                double aa = (0.0 + d * d / mass) / 2.0;
+                double bb = 0.0 + d * v;
+                double cc = (double)w[ns] - (double)w[s];
+                double disc = bb * bb - 4.0 * aa * cc;
+                if (disc < 0.0) {
+                    accept = false;
+                    if (p.rescaling == RESCALE_VINVERSION) {
+                        double nrm = sqrt(0.0 + d * d);
+                        double g = 0.0 + v * (d / nrm);
+                        v = v - 2.0 * g * (d / nrm);
+                    }
+                } else {
+                    double root = sqrt(disc);
+                    double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
+                    v = v - gamma * d / mass;
+                }
+            }
+            if (accept) {
+                log_hop(p, active, i, nh, step, s, ns);
+                nh += 1;
+                state = ns;
+            } else {
+                nf += 1;
+            }
+        }
+        if (p.save_stride > 0 && step % p.save_stride == 0) {
+            double pop[2];
+            diabatic_pop2<R>(sg, state, Z, pop);
+            warp_save_popcorr(p, isave++, active, pop0, pop);
+        }
+    }
+
+    if (!active) return;
+    p.r[i] = x;
+    p.v[i] = v;
+    write_sigma<R>(p, i, sg);
+    p.state[i] = state;
+    if (p.nhops) p.nhops[i] = nh;
+    if (p.nfrustrated) p.nfrustrated[i] = nf;
+    if (p.nsteps) p.nsteps[i] = step;
+    if (p.energy) {
+        p.energy[i] = e0;
+        p.energy[p.ntraj + i] = (0.0 + mass * (v * v)) / 2.0 + (double)w[state];
+    }
+    if (p.scatter) atomicAdd(p.scatter + (x > 0.0 ? 2 : 0) + state, 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Spin-boson (N bath modes, unit or given masses)
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshParams p) {
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i0 < p.ntraj;
+    const int64_t i = active ? i0 : p.ntraj - 1;
+    const int64_t gid = p.traj_offset + i;
+    const int64_t N = p.ntraj;
+    const int nd = p.ndof;
+    const double* __restrict__ cj = p.bath_c;
+    const double* __restrict__ w2j = p.bath_w2;
+    const double* __restrict__ mj = p.mass;
+    // inactive lanes (tail of the last warp) follow trajectory i on private
+    // copies only through registers: they never store to r or v.
+    double* __restrict__ r = p.r + i;
+    double* __restrict__ v = p.v + i;
+    double* __restrict__ nacs = p.scratch ? p.scratch + i : nullptr;
+    const R eps = (R)p.mp[0], Delta = (R)p.mp[1];
+
+    R Z[4] = {R(1), R(0), R(0), R(1)};
+    R w[2];
+    // Hamiltonian from the sums s0 = sum w2 r^2 and cr = c.r
+    auto set_eigen = [&](double s0, double cr) {
+        R V[3], Zn[4];
+        if constexpr (!IsFast<R>::value) {
+            double V0 = 0.5 * s0;
+            V[0] = (V0 + cr) + eps;
+            V[1] = Delta;
+            V[2] = (V0 - cr) - eps;
+        } else {
+            R V0 = (R)(0.5 * s0);
+            V[0] = (V0 + (R)cr) + eps;
+            V[1] = Delta;
+            V[2] = (V0 - (R)cr) - eps;
+        }
+        eigen2_phase<R>(V, Z, w, Zn);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Z[q] = Zn[q];
+    };
+    // (Z^T dH_I Z)_ss with dH_I = diag(w2 r + c, w2 r - c), oracle order
+    auto adi_ss = [&](const R Zk[4], int s, double rI, int I) -> R {
+        R d0 = (R)(w2j[I] * rI);
+        R d00 = d0 + (R)cj[I], d11 = d0 - (R)cj[I];
+        R z0 = Zk[2 * s], z1 = Zk[2 * s + 1];
+        return z0 * (d00 * z0) + z1 * (d11 * z1);
+    };
+
+    double s0 = 0.0, cr = 0.0, ke = 0.0;
+    for (int I = 0; I < nd; ++I) {
+        double rI = r[(int64_t)I * N];
+        double vI = v[(int64_t)I * N];
+        s0 = s0 + w2j[I] * (rI * rI);
+        cr = cr + cj[I] * rI;
+        ke = ke + mj[I] * (vI * vI);
+    }
+    set_eigen(s0, cr);
+    Sig2<R> sg;
+    int state;
+    init_electronics2<R>(p, i, gid, Z, sg, state);
+    double e0 = ke / 2.0 + (double)w[state];
+    R Zk[4] = {Z[0], Z[1], Z[2], Z[3]};  // eigenvectors the cached force was computed with
+    int sk = state;                      // state the cached force was computed for
+
+    double pop0[2] = {0.0, 0.0};
+    int isave = 0;
+    if (p.save_stride > 0) {
+        diabatic_pop2<R>(sg, state, Z, pop0);
+        warp_save_popcorr(p, isave++, active, pop0, pop0);
+    }
+
+    EBuf<R> buf = {R(0), R(0), R(0), 0.0, R(0), R(0), R(0), 0.0};
+    int nh = 0, nf = 0, step = 0;
+    double t = p.t0;
+    while (t < p.t1) {
+        double h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
+        double half = h / 2.0;
+        // B then A with the cached force (recomputed from r, Zk, sk)
+        s0 = 0.0;
+        cr = 0.0;
+        for (int I = 0; I < nd; ++I) {
+            double rI = r[(int64_t)I * N];
+            double vI = v[(int64_t)I * N];
+            double kI = (double)(-adi_ss(Zk, sk, rI, I) / (R)mj[I]);
+            double vt = vI + half * kI;
+            double rn = rI + h * vt;
+            if (active) {
+                r[(int64_t)I * N] = rn;
+                v[(int64_t)I * N] = vt;
+            }
+            s0 = s0 + w2j[I] * (rn * rn);
+            cr = cr + cj[I] * rn;
+        }
+        set_eigen(s0, cr);
+        const R gap = w[1] - w[0];
+        // B with the new force; couplings
+        R Dn;
+        double cv = 0.0;
+        R M01 = Z[0] * Z[2] - Z[1] * Z[3];
+        if constexpr (!IsFast<R>::value) {
+            double acc = 0.0;
+            for (int I = 0; I < nd; ++I) {
+                double rI = r[(int64_t)I * N];
+                double vt = v[(int64_t)I * N];
+                double d0 = w2j[I] * rI;
+                double d00 = d0 + cj[I], d11 = d0 - cj[I];
+                double ass = state == 0 ? Z[0] * (d00 * Z[0]) + Z[1] * (d11 * Z[1])
+                                        : Z[2] * (d00 * Z[2]) + Z[3] * (d11 * Z[3]);
+                double a01 = Z[0] * (d00 * Z[2]) + Z[1] * (d11 * Z[3]);
+                double kI = -ass / mj[I];
+                double vn = vt + half * kI;
+                double nI = a01 / (w[1] - w[0]);
+                if (active) {
+                    v[(int64_t)I * N] = vn;
+                    nacs[(int64_t)I * N] = nI;
+                }
+                acc = acc + nI * vn;
+            }
+            Dn = 0.0 + acc;
+        } else {
+            const float Mss = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];
+            for (int I = 0; I < nd; ++I) {
+                double rI = r[(int64_t)I * N];
+                double vt = v[(int64_t)I * N];
+                float kI = -((float)(w2j[I] * rI) + (float)cj[I] * Mss) / (float)mj[I];
+                double vn = vt + half * (double)kI;
+                if (active) v[(int64_t)I * N] = vn;
+                cv = cv + cj[I] * vn;
+            }
+            Dn = (float)cv * (M01 / gap);
+        }
+        Zk[0] = Z[0];
+        Zk[1] = Z[1];
+        Zk[2] = Z[2];
+        Zk[3] = Z[3];
+        sk = state;
+        buf.E0c = buf.E0n;
+        buf.E1c = buf.E1n;
+        buf.Dc = buf.Dn;
+        buf.tc = buf.tn;
+        buf.E0n = w[0];
+        buf.E1n = w[1];
+        buf.Dn = Dn;
+        buf.tn = t + h;
+        electronics2<R>(p, buf, t, h, gap, sg);
+        t = snap_time(t + h, p.t1);
+        step += 1;
+
+        // hop test
+        const int s = state;
+        R inv = R(1) / (s == 0 ? sg.p : sg.q);
+        R re = sg.x * inv;
+        R prob;
+        if constexpr (!IsFast<R>::value) {
+            double acc = 0.0;
+            for (int I = 0; I < nd; ++I) {
+                double nI = nacs[(int64_t)I * N];
+                double nsm = s == 0 ? nI : -nI;
+                acc = acc + 2.0 * v[(int64_t)I * N] * re * nsm * p.dt;
+            }
+            prob = clamp01<double>(acc);
+        } else {
+            float nsm = (s == 0 ? 1.0f : -1.0f) * (float)cv * (M01 / gap);
+            prob = clamp01<float>(2.0f * re * nsm * (float)p.dt);
+        }
+        double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
+        if ((double)prob > u) {
+            const int ns = 1 - s;
+            const double sgn = ns < s ? 1.0 : -1.0;  // d(new, old) = sgn * d01
+            bool accept = true;
+            if (p.rescaling != RESCALE_OFF) {
+                double aa = 0.0, bb = 0.0;
+                double dscale = (double)M01 / (double)gap;  // fast path: d_I = sgn * c_I * M01 / gap
+                if constexpr (!IsFast<R>::value) {
+                    for (int I = 0; I < nd; ++I) {
+                        double d = sgn * nacs[(int64_t)I * N];
+                        aa = aa + d * d / mj[I];
+                        bb = bb + d * v[(int64_t)I * N];
+                    }
+                } else {
+                    aa = dscale * dscale * p.sum_c2_over_m;
+                    bb = sgn * dscale * cv;
+                }
+                aa = aa / 2.0;
+                double cc = (double)w[ns] - (double)w[s];
+                double disc = bb * bb - 4.0 * aa * cc;
+                if (disc < 0.0) {
+                    accept = false;
+                    if (p.rescaling == RESCALE_VINVERSION) {
+                        double nrm = 0.0;
+                        for (int I = 0; I < nd; ++I) {
+                            double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                            nrm = nrm + d * d;
+                        }
+                        nrm = sqrt(nrm);
+                        double g = 0.0;
+                        for (int I = 0; I < nd; ++I) {
+                            double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                            g = g + v[(int64_t)I * N] * (d / nrm);
+                        }
+                        for (int I = 0; I < nd; ++I) {
+                            double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                            double vn = v[(int64_t)I * N] - 2.0 * g * (d / nrm);
+                            if (active) v[(int64_t)I * N] = vn;
+                        }
+                        if constexpr (IsFast<R>::value) {
+                            cv = 0.0;  // c.v is not reused after the hop test
+                        }
+                    }
+                } else {
+                    double root = sqrt(disc);
+                    double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
+                    for (int I = 0; I < nd; ++I) {
+                        double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                        double vn = v[(int64_t)I * N] - gamma * d / mj[I];
+                        if (active) v[(int64_t)I * N] = vn;
+                    }
+                }
+            }
+            if (accept) {
+                log_hop(p, active, i, nh, step, s, ns);
+                nh += 1;
+                state = ns;
+            } else {
+                nf += 1;
+            }
+        }
+        if (p.save_stride > 0 && step % p.save_stride == 0) {
+            double pop[2];
+            diabatic_pop2<R>(sg, state, Z, pop);
+            warp_save_popcorr(p, isave++, active, pop0, pop);
+        }
+    }
+
+    if (!active) return;
+    write_sigma<R>(p, i, sg);
+    p.state[i] = state;
+    if (p.nhops) p.nhops[i] = nh;
+    if (p.nfrustrated) p.nfrustrated[i] = nf;
+    if (p.nsteps) p.nsteps[i] = step;
+    if (p.energy) {
+        double ke1 = 0.0;
+        for (int I = 0; I < nd; ++I) {
+            double vI = v[(int64_t)I * N];
+            ke1 = ke1 + mj[I] * (vI * vI);
+        }
+        p.energy[i] = e0;
+        p.energy[N + i] = ke1 / 2.0 + (double)w[state];
+    }
+    if (p.scatter) atomicAdd(p.scatter + (r[0] > 0.0 ? 2 : 0) + state, 1ull);
+}
+
+template <typename R>
+cudaError_t launch_fssh2(const FsshParams& p, cudaStream_t s) {
+    if (p.ntraj <= 0) return cudaSuccess;
+    int64_t blocks = (p.ntraj + kFsshBlock - 1) / kFsshBlock;
+    if (p.model == MODEL_SPINBOSON)
+        fssh2_spinboson_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
+    else
+        fssh2_tully_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace nqcd

@@ -1,0 +1,641 @@
+// C ABI of the GB300 ensemble trajectory engine (declarations and contract:
+// include/nqcd_gpu.h).  Host-side runtime: handle and device-memory
+// ownership, host<->device staging with layout gathers, kernel dispatch,
+// deterministic reductions and CUDA-event timing on the engine stream.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <chrono>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/nqcd_gpu.h"
+#include "engine_params.h"
+#include "nqcd_math.h"
+#include "nqcd_models.h"
+
+using namespace nqcd;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// ---------------------------------------------------------------------------
+// Small device kernels: layout gathers and reductions
+// ---------------------------------------------------------------------------
+
+// AoS [n][m] -> SoA [m][n] (doubles), through a shared-memory tile so that
+// both the read and the write are coalesced.
+__global__ void transpose_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t n, int64_t m) {
+    __shared__ double tile[32][33];
+    int64_t bx = (int64_t)blockIdx.x * 32, by = (int64_t)blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        int64_t row = by + j, col = bx + threadIdx.x;
+        if (row < n && col < m) tile[j][threadIdx.x] = in[row * m + col];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        int64_t row = bx + j, col = by + threadIdx.x;  // out[row][col], row < m, col < n
+        if (row < m && col < n) out[row * n + col] = tile[threadIdx.x][j];
+    }
+}
+
+cudaError_t transpose(const double* in, double* out, int64_t n, int64_t m, cudaStream_t s) {
+    if (n == 0 || m == 0) return cudaSuccess;
+    dim3 block(32, 8);
+    dim3 grid((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
+    transpose_kernel<<<grid, block, 0, s>>>(in, out, n, m);
+    return cudaGetLastError();
+}
+
+__global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// out[k] = sum_p partial[p][k] in ascending p (deterministic).
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int64_t nparts, int64_t width,
+                                       double* __restrict__ out) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= width) return;
+    double acc = 0.0;
+    for (int64_t p = 0; p < nparts; ++p) acc += partial[p * width + k];
+    out[k] = acc;
+}
+
+// Run statistics: steps, hops, frustrated hops, non-finite trajectories.
+__global__ void stats_kernel(const int32_t* nsteps, const int32_t* nhops, const int32_t* nfrust,
+                             const double* r, const double* v, int64_t ndof, int64_t ntraj,
+                             unsigned long long* out) {
+    unsigned long long a = 0, b = 0, c = 0, d = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ntraj; i += (int64_t)gridDim.x * blockDim.x) {
+        a += (unsigned long long)nsteps[i];
+        b += (unsigned long long)nhops[i];
+        c += (unsigned long long)nfrust[i];
+        bool bad = false;
+        for (int64_t I = 0; I < ndof; ++I) bad |= !isfinite(r[I * ntraj + i]) || !isfinite(v[I * ntraj + i]);
+        d += bad ? 1ull : 0ull;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+        c += __shfl_xor_sync(0xffffffffu, c, off);
+        d += __shfl_xor_sync(0xffffffffu, d, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out + 0, a);
+        atomicAdd(out + 1, b);
+        atomicAdd(out + 2, c);
+        atomicAdd(out + 3, d);
+    }
+}
+
+// FMA throughput probe: 8 independent chains per thread, register resident.
+template <typename T>
+__global__ void fma_peak_kernel(T* sink, int iters, T seed) {
+    T a0 = seed + (T)threadIdx.x, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
+    T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+    const T b = (T)0.999999, c = (T)1e-7;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            a0 = fma(a0, b, c);
+            a1 = fma(a1, b, c);
+            a2 = fma(a2, b, c);
+            a3 = fma(a3, b, c);
+            a4 = fma(a4, b, c);
+            a5 = fma(a5, b, c);
+            a6 = fma(a6, b, c);
+            a7 = fma(a7, b, c);
+        }
+    }
+    T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == (T)-12345.0) sink[threadIdx.x] = s;  // never true; keeps the chains live
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Handle
+// ---------------------------------------------------------------------------
+struct nqcd_handle {
+    nqcd_config cfg;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+    int64_t cap = 0;
+    int64_t ntraj = 0;
+    int64_t ndof = 0;  // per trajectory (ndofs * natoms)
+    int nstates = 2;
+    std::vector<double> params;
+    double sum_c2_over_m = 0.0;
+    bool initial_set = false;
+    bool has_run = false;
+    int32_t nsave_last = 0;
+    // device buffers
+    double *d_mass = nullptr, *d_bath_c = nullptr, *d_bath_w2 = nullptr;
+    double *d_r0 = nullptr, *d_v0 = nullptr, *d_r = nullptr, *d_v = nullptr;
+    double *d_sig0 = nullptr, *d_sig = nullptr;
+    int32_t *d_state0 = nullptr, *d_state = nullptr;
+    double* d_scratch = nullptr;
+    int32_t *d_nhops = nullptr, *d_nfrust = nullptr, *d_nsteps = nullptr, *d_hoplog = nullptr;
+    double* d_energy = nullptr;
+    double* d_partial = nullptr;
+    int64_t partial_cap = 0;
+    double* d_popcorr = nullptr;
+    unsigned long long* d_counts = nullptr;  // [0..3] scatter, [4..7] stats
+    double* d_stage = nullptr;               // staging for layout gathers
+    int64_t stage_cap = 0;
+};
+
+namespace {
+
+int fail(nqcd_handle* h, int code, const std::string& msg) {
+    if (h)
+        h->err = msg;
+    else
+        g_create_error = msg;
+    return code;
+}
+
+int cuda_fail(nqcd_handle* h, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return fail(h, e == cudaErrorMemoryAllocation ? NQCD_ERR_OOM : NQCD_ERR_CUDA, m);
+}
+
+#define NQCD_CUDA(h, call)                                 \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, int64_t n) {
+    if (n <= 0) n = 1;
+    return cudaMalloc((void**)p, (size_t)n * sizeof(T));
+}
+
+void free_all(nqcd_handle* h) {
+    void* ptrs[] = {h->d_mass, h->d_bath_c, h->d_bath_w2, h->d_r0, h->d_v0, h->d_r, h->d_v, h->d_sig0,
+                    h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
+                    h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->evk0) cudaEventDestroy(h->evk0);
+    if (h->evk1) cudaEventDestroy(h->evk1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+int ensure_stage(nqcd_handle* h, int64_t n) {
+    if (n <= h->stage_cap) return NQCD_OK;
+    if (h->d_stage) cudaFree(h->d_stage);
+    h->d_stage = nullptr;
+    h->stage_cap = 0;
+    NQCD_CUDA(h, dalloc(&h->d_stage, n));
+    h->stage_cap = n;
+    return NQCD_OK;
+}
+
+int64_t count_steps(double t0, double t1, double dt) {
+    int64_t n = 0;
+    double t = t0;
+    while (t < t1 && n < (int64_t)1 << 40) {
+        double hh = (t1 - t) < dt ? (t1 - t) : dt;
+        t = snap_time(t + hh, t1);
+        ++n;
+    }
+    return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nqcd_version(void) { return NQCD_ABI_VERSION; }
+
+int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
+    if (!cfg || !out) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: null argument");
+    *out = nullptr;
+    if (cfg->method != NQCD_METHOD_FSSH)
+        return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: method not supported by this build");
+    const int model = cfg->model;
+    if (model != NQCD_MODEL_TULLY1 && model != NQCD_MODEL_TULLY2 && model != NQCD_MODEL_TULLY3 &&
+        model != NQCD_MODEL_SPINBOSON)
+        return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: unknown model");
+    if (cfg->nstates != 2) return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: only two-state models");
+    if (cfg->precision != NQCD_PREC_FP64 && cfg->precision != NQCD_PREC_FP32)
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown precision");
+    if (cfg->rescaling < 0 || cfg->rescaling > 2) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown rescaling");
+    if (cfg->ndofs <= 0 || cfg->natoms <= 0 || cfg->ntraj_max <= 0 || !cfg->masses)
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ndofs, natoms, ntraj_max and masses are required");
+    if (cfg->init_kind < 0 || cfg->init_kind > 2 || cfg->init_state < 0 || cfg->init_state >= cfg->nstates)
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bad initial electronic specification");
+    if (cfg->save_stride < 0 || cfg->max_hops < 0 || cfg->traj_offset < 0)
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: negative count");
+    const int64_t ndof = (int64_t)cfg->ndofs * cfg->natoms;
+    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : 4));
+    if (cfg->nparams < need_params || !cfg->params)
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: too few model parameters");
+    if (model == NQCD_MODEL_SPINBOSON) {
+        if (cfg->nbath != ndof || !cfg->bath_a || !cfg->bath_b)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: spin-boson needs nbath == ndofs*natoms couplings and frequencies");
+    } else if (ndof != 1) {
+        return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: Tully models have one degree of freedom");
+    }
+    for (int a = 0; a < cfg->natoms; ++a)
+        if (!(cfg->masses[a] > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: masses must be positive");
+
+    int dev_count = 0;
+    cudaError_t e = cudaGetDeviceCount(&dev_count);
+    if (e != cudaSuccess || dev_count == 0) {
+        cudaGetLastError();
+        return fail(nullptr, NQCD_ERR_CUDA, std::string("nqcd_create: no CUDA device (") + cudaGetErrorString(e) + ")");
+    }
+
+    nqcd_handle* h = new (std::nothrow) nqcd_handle();
+    if (!h) return fail(nullptr, NQCD_ERR_OOM, "nqcd_create: out of host memory");
+    h->cfg = *cfg;
+    h->cfg.params = nullptr;
+    h->cfg.bath_a = h->cfg.bath_b = h->cfg.masses = nullptr;
+    h->cap = cfg->ntraj_max;
+    h->ndof = ndof;
+    h->params.assign(cfg->params, cfg->params + cfg->nparams);
+    h->params.resize(8, 0.0);
+
+    auto bail = [&](cudaError_t ee, const char* what) {
+        std::string m = std::string("nqcd_create: ") + what + ": " + cudaGetErrorString(ee);
+        cudaGetLastError();
+        free_all(h);
+        delete h;
+        return fail(nullptr, ee == cudaErrorMemoryAllocation ? NQCD_ERR_OOM : NQCD_ERR_CUDA, m);
+    };
+#define NQCD_CREATE(call)                       \
+    do {                                        \
+        cudaError_t ee_ = (call);               \
+        if (ee_ != cudaSuccess) return bail(ee_, #call); \
+    } while (0)
+
+    NQCD_CREATE(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    NQCD_CREATE(cudaEventCreate(&h->ev0));
+    NQCD_CREATE(cudaEventCreate(&h->ev1));
+    NQCD_CREATE(cudaEventCreate(&h->evk0));
+    NQCD_CREATE(cudaEventCreate(&h->evk1));
+
+    std::vector<double> mass(ndof), bc(ndof, 0.0), bw2(ndof, 0.0);
+    for (int64_t I = 0; I < ndof; ++I) mass[I] = cfg->masses[I / cfg->ndofs];
+    if (model == NQCD_MODEL_SPINBOSON) {
+        for (int64_t I = 0; I < ndof; ++I) {
+            bc[I] = cfg->bath_a[I];
+            bw2[I] = cfg->bath_b[I] * cfg->bath_b[I];
+            h->sum_c2_over_m += bc[I] * bc[I] / mass[I];
+        }
+    }
+    const int64_t cap = h->cap;
+    NQCD_CREATE(dalloc(&h->d_mass, ndof));
+    NQCD_CREATE(dalloc(&h->d_bath_c, ndof));
+    NQCD_CREATE(dalloc(&h->d_bath_w2, ndof));
+    NQCD_CREATE(cudaMemcpy(h->d_mass, mass.data(), ndof * sizeof(double), cudaMemcpyHostToDevice));
+    NQCD_CREATE(cudaMemcpy(h->d_bath_c, bc.data(), ndof * sizeof(double), cudaMemcpyHostToDevice));
+    NQCD_CREATE(cudaMemcpy(h->d_bath_w2, bw2.data(), ndof * sizeof(double), cudaMemcpyHostToDevice));
+    NQCD_CREATE(dalloc(&h->d_r0, ndof * cap));
+    NQCD_CREATE(dalloc(&h->d_v0, ndof * cap));
+    NQCD_CREATE(dalloc(&h->d_r, ndof * cap));
+    NQCD_CREATE(dalloc(&h->d_v, ndof * cap));
+    NQCD_CREATE(dalloc(&h->d_sig0, 8 * cap));
+    NQCD_CREATE(dalloc(&h->d_sig, 8 * cap));
+    NQCD_CREATE(dalloc(&h->d_state0, cap));
+    NQCD_CREATE(dalloc(&h->d_state, cap));
+    if (model == NQCD_MODEL_SPINBOSON && cfg->precision == NQCD_PREC_FP64) NQCD_CREATE(dalloc(&h->d_scratch, ndof * cap));
+    NQCD_CREATE(dalloc(&h->d_nhops, cap));
+    NQCD_CREATE(dalloc(&h->d_nfrust, cap));
+    NQCD_CREATE(dalloc(&h->d_nsteps, cap));
+    if (cfg->max_hops > 0) NQCD_CREATE(dalloc(&h->d_hoplog, (int64_t)cfg->max_hops * 3 * cap));
+    NQCD_CREATE(dalloc(&h->d_energy, 2 * cap));
+    NQCD_CREATE(dalloc(&h->d_counts, 8));
+    NQCD_CREATE(cudaMemset(h->d_sig0, 0, 8 * cap * sizeof(double)));
+    NQCD_CREATE(cudaMemset(h->d_state0, 0, cap * sizeof(int32_t)));
+#undef NQCD_CREATE
+    *out = h;
+    return NQCD_OK;
+}
+
+static int set_initial_common(nqcd_handle* h, int64_t ntraj, const double* sig_re, const double* sig_im,
+                              const int32_t* state0, int64_t* h2d) {
+    const int64_t N = ntraj;
+    if (h->cfg.init_kind == NQCD_INIT_GIVEN) {
+        if (!sig_re || !state0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: sig_re and state0 required for NQCD_INIT_GIVEN");
+        // host (2,2,ntraj) column-major re/im -> device [8][ntraj]: component 2*(2*i+j)+{0,1}
+        std::vector<double> soa(8 * N);
+        for (int64_t t = 0; t < N; ++t)
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) {
+                    soa[(2 * (2 * i + j)) * N + t] = sig_re[t * 4 + i + 2 * j];
+                    soa[(2 * (2 * i + j) + 1) * N + t] = sig_im ? sig_im[t * 4 + i + 2 * j] : 0.0;
+                }
+        for (int64_t t = 0; t < N; ++t)
+            if (state0[t] < 0 || state0[t] >= h->nstates) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: state out of range");
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_sig0, soa.data(), 8 * N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_state0, state0, N * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+        *h2d += 8 * N * (int64_t)sizeof(double) + N * (int64_t)sizeof(int32_t);
+    }
+    h->ntraj = ntraj;
+    h->initial_set = true;
+    h->has_run = false;
+    return NQCD_OK;
+}
+
+int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, const double* sig_re,
+                     const double* sig_im, const int32_t* state0, const int32_t* nbeads) {
+    (void)nbeads;
+    if (!h) return NQCD_ERR_ARG;
+    if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: ntraj outside 1..ntraj_max");
+    if (!r0 || !v0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: r0 and v0 are required");
+    const int64_t n = ntraj * h->ndof;
+    int rc = ensure_stage(h, n);
+    if (rc) return rc;
+    int64_t h2d = 0;
+    // (ndof, ntraj) column-major host == AoS [ntraj][ndof]; gather to SoA [ndof][ntraj]
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_stage, r0, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    NQCD_CUDA(h, transpose(h->d_stage, h->d_r0, ntraj, h->ndof, h->stream));
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_stage, v0, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    NQCD_CUDA(h, transpose(h->d_stage, h->d_v0, ntraj, h->ndof, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    h2d += 2 * n * (int64_t)sizeof(double);
+    return set_initial_common(h, ntraj, sig_re, sig_im, state0, &h2d);
+}
+
+int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0, const double* d_v0,
+                            const int32_t* nbeads) {
+    (void)nbeads;
+    if (!h) return NQCD_ERR_ARG;
+    if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: ntraj outside 1..ntraj_max");
+    if (!d_r0 || !d_v0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: r0 and v0 are required");
+    if (h->cfg.init_kind == NQCD_INIT_GIVEN)
+        return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: NQCD_INIT_GIVEN needs nqcd_set_initial");
+    const int64_t n = ntraj * h->ndof;
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_r0, d_r0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_v0, d_v0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    int64_t h2d = 0;
+    return set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
+}
+
+int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out, nqcd_stats* stats) {
+    if (!h) return NQCD_ERR_ARG;
+    if (!h->initial_set) return fail(h, NQCD_ERR_STATE, "nqcd_run: call nqcd_set_initial first");
+    if (!(dt > 0.0) || !(t1 >= t0) || !isfinite(t0) || !isfinite(t1))
+        return fail(h, NQCD_ERR_ARG, "nqcd_run: need dt > 0 and finite t0 <= t1");
+    auto wall0 = std::chrono::steady_clock::now();
+    const int64_t N = h->ntraj;
+    const int64_t nsteps = count_steps(t0, t1, dt);
+    if (nsteps > 0x7fffffff) return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
+    const int stride = h->cfg.save_stride;
+    const int nsave = stride > 0 ? (int)(nsteps / stride + 1) : 0;
+    const int64_t blocks = (N + 127) / 128;
+    const int64_t nwarps = blocks * 4;
+    if (nsave > 0 && nwarps * nsave * 4 > h->partial_cap) {
+        if (h->d_partial) cudaFree(h->d_partial);
+        if (h->d_popcorr) cudaFree(h->d_popcorr);
+        h->d_partial = h->d_popcorr = nullptr;
+        h->partial_cap = 0;
+        NQCD_CUDA(h, dalloc(&h->d_partial, nwarps * nsave * 4));
+        NQCD_CUDA(h, dalloc(&h->d_popcorr, (int64_t)nsave * 4));
+        h->partial_cap = nwarps * nsave * 4;
+    }
+    cudaStream_t s = h->stream;
+    int launches = 0;
+    NQCD_CUDA(h, cudaEventRecord(h->ev0, s));
+    const int64_t nd = h->ndof;
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_r, h->d_r0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_v, h->d_v0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_sig, h->d_sig0, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_state, h->d_state0, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 8 * sizeof(unsigned long long), s));
+    if (h->d_hoplog) {
+        int64_t nl = (int64_t)h->cfg.max_hops * 3 * N;
+        fill_i32_kernel<<<(unsigned)((nl + 255) / 256 < 4096 ? (nl + 255) / 256 : 4096), 256, 0, s>>>(h->d_hoplog, nl, -1);
+        NQCD_CUDA(h, cudaGetLastError());
+        ++launches;
+    }
+
+    FsshParams p;
+    memset(&p, 0, sizeof(p));
+    p.model = h->cfg.model;
+    for (int q = 0; q < 8; ++q) p.mp[q] = h->params[q];
+    p.ndof = (int32_t)nd;
+    p.mass = h->d_mass;
+    p.bath_c = h->d_bath_c;
+    p.bath_w2 = h->d_bath_w2;
+    p.sum_c2_over_m = h->sum_c2_over_m;
+    p.rescaling = h->cfg.rescaling;
+    p.init_kind = h->cfg.init_kind;
+    p.init_state = h->cfg.init_state;
+    p.gap_fp64 = (float)h->cfg.gap_fp64;
+    p.ntraj = N;
+    p.traj_offset = h->cfg.traj_offset;
+    p.t0 = t0;
+    p.t1 = t1;
+    p.dt = dt;
+    p.seed = seed;
+    p.save_stride = stride;
+    p.nsave = nsave;
+    p.max_hops = h->cfg.max_hops;
+    p.r = h->d_r;
+    p.v = h->d_v;
+    p.scratch = h->d_scratch;
+    p.sigma = h->d_sig;
+    p.state = h->d_state;
+    p.nhops = h->d_nhops;
+    p.nfrustrated = h->d_nfrust;
+    p.nsteps = h->d_nsteps;
+    p.hop_log = h->d_hoplog;
+    p.energy = h->d_energy;
+    p.popcorr_partial = h->d_partial;
+    p.scatter = h->d_counts;
+    NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
+    cudaError_t e = h->cfg.precision == NQCD_PREC_FP64 ? launch_fssh2_fp64(p, s) : launch_fssh2_fp32(p, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_run: ensemble kernel launch");
+    NQCD_CUDA(h, cudaEventRecord(h->evk1, s));
+    ++launches;
+    if (nsave > 0) {
+        NQCD_CUDA(h, launch_reduce_partials(h->d_partial, nwarps, (int64_t)nsave * 4, h->d_popcorr, s));
+        ++launches;
+    }
+    stats_kernel<<<(unsigned)((N + 255) / 256 < 1024 ? (N + 255) / 256 : 1024), 256, 0, s>>>(
+        h->d_nsteps, h->d_nhops, h->d_nfrust, h->d_r, h->d_v, nd, N, h->d_counts + 4);
+    NQCD_CUDA(h, cudaGetLastError());
+    ++launches;
+    NQCD_CUDA(h, cudaEventRecord(h->ev1, s));
+
+    unsigned long long counts[8];
+    int64_t d2h = 0;
+    NQCD_CUDA(h, cudaMemcpyAsync(counts, h->d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
+    d2h += sizeof(counts);
+    std::vector<double> pc;
+    if (out && out->population_correlation && nsave > 0) {
+        pc.resize((size_t)nsave * 4);
+        NQCD_CUDA(h, cudaMemcpyAsync(pc.data(), h->d_popcorr, pc.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        d2h += (int64_t)pc.size() * sizeof(double);
+    }
+    NQCD_CUDA(h, cudaStreamSynchronize(s));
+    float ms = 0.0f, kms = 0.0f;
+    NQCD_CUDA(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    NQCD_CUDA(h, cudaEventElapsedTime(&kms, h->evk0, h->evk1));
+    if (out) {
+        out->nsave = nsave;
+        if (out->scattering)
+            for (int q = 0; q < 4; ++q) out->scattering[q] = (double)counts[q] / (double)N;
+        if (out->population_correlation && nsave > 0)
+            for (int k = 0; k < nsave * 4; ++k) out->population_correlation[k] = pc[k] / (double)N;
+    }
+    h->nsave_last = nsave;
+    h->has_run = true;
+    if (stats) {
+        stats->traj_steps = (int64_t)counts[4];
+        stats->hops = (int64_t)counts[5];
+        stats->frustrated = (int64_t)counts[6];
+        stats->flagged = (int64_t)counts[7];
+        stats->device_ms = ms;
+        stats->kernel_ms = kms;
+        stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+        stats->h2d_bytes = 0;
+        stats->d2h_bytes = d2h;
+        stats->kernel_launches = launches;
+    }
+    if (counts[7] > 0) return fail(h, NQCD_ERR_NAN, "nqcd_run: non-finite final positions or velocities");
+    return NQCD_OK;
+}
+
+int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double* sig_im, int32_t* state,
+                   int32_t* nhops, int32_t* nfrustrated, int32_t* nsteps, double* energy) {
+    if (!h) return NQCD_ERR_ARG;
+    if (!h->has_run) return fail(h, NQCD_ERR_STATE, "nqcd_get_final: no completed run");
+    const int64_t N = h->ntraj, nd = h->ndof;
+    cudaStream_t s = h->stream;
+    int rc = ensure_stage(h, std::max<int64_t>(nd * N, 8 * N));
+    if (rc) return rc;
+    double* pairs[2] = {r, v};
+    double* srcs[2] = {h->d_r, h->d_v};
+    for (int q = 0; q < 2; ++q) {
+        if (!pairs[q]) continue;
+        NQCD_CUDA(h, transpose(srcs[q], h->d_stage, nd, N, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(pairs[q], h->d_stage, nd * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+        NQCD_CUDA(h, cudaStreamSynchronize(s));
+    }
+    if (sig_re || sig_im) {
+        std::vector<double> soa(8 * N);
+        NQCD_CUDA(h, cudaMemcpyAsync(soa.data(), h->d_sig, 8 * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+        NQCD_CUDA(h, cudaStreamSynchronize(s));
+        for (int64_t t = 0; t < N; ++t)
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) {
+                    if (sig_re) sig_re[t * 4 + i + 2 * j] = soa[(2 * (2 * i + j)) * N + t];
+                    if (sig_im) sig_im[t * 4 + i + 2 * j] = soa[(2 * (2 * i + j) + 1) * N + t];
+                }
+    }
+    struct {
+        int32_t* dst;
+        int32_t* src;
+    } ints[4] = {{state, h->d_state}, {nhops, h->d_nhops}, {nfrustrated, h->d_nfrust}, {nsteps, h->d_nsteps}};
+    for (auto& q : ints)
+        if (q.dst) NQCD_CUDA(h, cudaMemcpyAsync(q.dst, q.src, N * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (energy) {
+        NQCD_CUDA(h, transpose(h->d_energy, h->d_stage, 2, N, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(energy, h->d_stage, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    NQCD_CUDA(h, cudaStreamSynchronize(s));
+    return NQCD_OK;
+}
+
+int nqcd_get_hop_log(nqcd_handle* h, int32_t* log) {
+    if (!h || !log) return NQCD_ERR_ARG;
+    if (!h->has_run) return fail(h, NQCD_ERR_STATE, "nqcd_get_hop_log: no completed run");
+    if (!h->d_hoplog) return fail(h, NQCD_ERR_STATE, "nqcd_get_hop_log: created with max_hops = 0");
+    const int64_t N = h->ntraj, w = (int64_t)h->cfg.max_hops * 3;
+    std::vector<int32_t> soa(w * N);
+    NQCD_CUDA(h, cudaMemcpyAsync(soa.data(), h->d_hoplog, soa.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int64_t t = 0; t < N; ++t)
+        for (int64_t c = 0; c < w; ++c) log[t * w + c] = soa[c * N + t];
+    return NQCD_OK;
+}
+
+const char* nqcd_last_error(const nqcd_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+void nqcd_destroy(nqcd_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+}
+
+int nqcd_pin_host(void* ptr, int64_t bytes) {
+    if (!ptr || bytes <= 0) return NQCD_ERR_ARG;
+    cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nqcd_pin_host");
+    return NQCD_OK;
+}
+
+int nqcd_unpin_host(void* ptr) {
+    if (!ptr) return NQCD_ERR_ARG;
+    cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nqcd_unpin_host");
+    return NQCD_OK;
+}
+
+int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
+    if (!fp64_tflops || !fp32_tflops) return NQCD_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return cuda_fail(nullptr, cudaGetLastError(), "nqcd_measure_fma_peaks");
+    double* sink64 = nullptr;
+    float* sink32 = nullptr;
+    cudaEvent_t a, b;
+    if (cudaMalloc(&sink64, 1024 * sizeof(double)) != cudaSuccess || cudaMalloc(&sink32, 1024 * sizeof(float)) != cudaSuccess)
+        return cuda_fail(nullptr, cudaGetLastError(), "nqcd_measure_fma_peaks: alloc");
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int threads = 256;
+    const int blocks = sms * 8;
+    auto run = [&](bool f64, int iters) -> double {
+        // warm-up then timed launch
+        for (int rep = 0; rep < 2; ++rep) {
+            cudaEventRecord(a);
+            if (f64)
+                fma_peak_kernel<double><<<blocks, threads>>>(sink64, iters, 1.0);
+            else
+                fma_peak_kernel<float><<<blocks, threads>>>(sink32, iters, 1.0f);
+            cudaEventRecord(b);
+            cudaEventSynchronize(b);
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        double flops = 2.0 * 8.0 * 16.0 * (double)iters * (double)threads * (double)blocks;
+        return flops / (ms * 1e-3) / 1e12;
+    };
+    *fp64_tflops = run(true, 256);
+    *fp32_tflops = run(false, 4096);
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink64);
+    cudaFree(sink32);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nqcd_measure_fma_peaks: kernel");
+    return NQCD_OK;
+}
+
+}  // extern "C"
+
+namespace nqcd {
+cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* out, cudaStream_t s) {
+    reduce_partials_kernel<<<(unsigned)((width + 127) / 128), 128, 0, s>>>(partial, nparts, width, out);
+    return cudaGetLastError();
+}
+}  // namespace nqcd

@@ -1,0 +1,38 @@
+"""GB300 ensemble trajectory engine for NQCDynamics.jl's FSSH / RPSH hot path.
+
+The compute runs in libnqcd_gb300.so (CUDA, sm_103a) behind the C ABI of
+include/nqcd_gpu.h; this package is the host-side mirror of the reference's
+ensemble interface (see api.py) plus the ctypes binding (_lib.py).
+"""
+from . import _lib
+from .api import (
+    Adiabatic,
+    Atoms,
+    Diabatic,
+    DynamicalDistribution,
+    EnsembleGB300,
+    EnsembleSerial,
+    EnsembleThreads,
+    FSSH,
+    MeanReduction,
+    OhmicSpectralDensity,
+    OutputFinal,
+    OutputStateResolvedScattering1D,
+    OutputSurfaceHops,
+    OutputTotalEnergy,
+    PopulationCorrelationFunction,
+    PositionHarmonicWigner,
+    PureState,
+    RingPolymerSimulation,
+    Simulation,
+    SpinBoson,
+    SumReduction,
+    TullyModelOne,
+    TullyModelThree,
+    TullyModelTwo,
+    VelocityHarmonicWigner,
+    run_dynamics,
+)
+from ._lib import EngineError, EngineUnavailable
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,240 @@
+"""ctypes binding of the engine's C ABI (include/nqcd_gpu.h).
+
+The engine has no CPU path: if libnqcd_gb300.so is missing or cannot be
+loaded, every call raises EngineUnavailable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libnqcd_gb300.so"
+
+NQCD_OK = 0
+ERRORS = {
+    -1: "NQCD_ERR_ARG",
+    -2: "NQCD_ERR_CUDA",
+    -3: "NQCD_ERR_OOM",
+    -4: "NQCD_ERR_TIMEOUT",
+    -5: "NQCD_ERR_NAN",
+    -6: "NQCD_ERR_UNSUPPORTED",
+    -7: "NQCD_ERR_STATE",
+}
+
+METHOD_FSSH, METHOD_RPSH, METHOD_IESH, METHOD_MDEF = 1, 2, 3, 4
+MODEL_TULLY1, MODEL_TULLY2, MODEL_TULLY3, MODEL_SPINBOSON = 1, 2, 3, 10
+PREC_FP64, PREC_FP32 = 0, 1
+RESCALE = {"standard": 0, "vinversion": 1, "off": 2}
+INIT_GIVEN, INIT_ADIABATIC_PURE, INIT_DIABATIC_PURE = 0, 1, 2
+
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int32)
+
+
+class nqcd_config(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32),
+        ("model", C.c_int32),
+        ("precision", C.c_int32),
+        ("rescaling", C.c_int32),
+        ("ndofs", C.c_int32),
+        ("natoms", C.c_int32),
+        ("nstates", C.c_int32),
+        ("nbeads_max", C.c_int32),
+        ("nparams", C.c_int32),
+        ("params", DP),
+        ("nbath", C.c_int32),
+        ("bath_a", DP),
+        ("bath_b", DP),
+        ("masses", DP),
+        ("beta", C.c_double),
+        ("ntraj_max", C.c_int64),
+        ("init_kind", C.c_int32),
+        ("init_state", C.c_int32),
+        ("save_stride", C.c_int32),
+        ("max_hops", C.c_int32),
+        ("terminate_x", C.c_double),
+        ("gap_fp64", C.c_double),
+        ("traj_offset", C.c_int64),
+        ("reserved", C.c_int32 * 6),
+    ]
+
+
+class nqcd_outputs(C.Structure):
+    _fields_ = [
+        ("scattering", DP),
+        ("population_correlation", DP),
+        ("nsave", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class nqcd_stats(C.Structure):
+    _fields_ = [
+        ("traj_steps", C.c_int64),
+        ("hops", C.c_int64),
+        ("frustrated", C.c_int64),
+        ("flagged", C.c_int64),
+        ("device_ms", C.c_double),
+        ("kernel_ms", C.c_double),
+        ("wall_ms", C.c_double),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
+        ("kernel_launches", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+EXPORTED = [
+    "nqcd_version",
+    "nqcd_create",
+    "nqcd_set_initial",
+    "nqcd_set_initial_device",
+    "nqcd_run",
+    "nqcd_get_final",
+    "nqcd_get_hop_log",
+    "nqcd_last_error",
+    "nqcd_destroy",
+    "nqcd_pin_host",
+    "nqcd_unpin_host",
+    "nqcd_measure_fma_peaks",
+]
+
+
+class EngineUnavailable(RuntimeError):
+    """The CUDA engine library is not built or cannot be loaded."""
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load the engine library (raises EngineUnavailable if absent)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise EngineUnavailable(f"{p} is not built; run __graft_entry__.build() (there is no CPU fallback)")
+    try:
+        lib = C.CDLL(str(p))
+    except OSError as e:  # pragma: no cover - depends on the CUDA runtime being present
+        raise EngineUnavailable(f"cannot load {p}: {e}") from e
+    lib.nqcd_version.restype = C.c_int
+    lib.nqcd_create.argtypes = [C.POINTER(nqcd_config), C.POINTER(C.c_void_p)]
+    lib.nqcd_set_initial.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP, DP, IP, IP]
+    lib.nqcd_set_initial_device.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, IP]
+    lib.nqcd_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                             C.POINTER(nqcd_outputs), C.POINTER(nqcd_stats)]
+    lib.nqcd_get_final.argtypes = [C.c_void_p, DP, DP, DP, DP, IP, IP, IP, IP, DP]
+    lib.nqcd_get_hop_log.argtypes = [C.c_void_p, IP]
+    lib.nqcd_last_error.restype = C.c_char_p
+    lib.nqcd_last_error.argtypes = [C.c_void_p]
+    lib.nqcd_destroy.argtypes = [C.c_void_p]
+    lib.nqcd_destroy.restype = None
+    lib.nqcd_pin_host.argtypes = [C.c_void_p, C.c_int64]
+    lib.nqcd_unpin_host.argtypes = [C.c_void_p]
+    lib.nqcd_measure_fma_peaks.argtypes = [DP, DP]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def dptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(DP)
+
+
+def iptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(IP)
+
+
+class Engine:
+    """Owns one nqcd_handle."""
+
+    def __init__(self, cfg: nqcd_config, keepalive=()):
+        self.lib = load()
+        self._keep = list(keepalive)
+        h = C.c_void_p()
+        rc = self.lib.nqcd_create(C.byref(cfg), C.byref(h))
+        if rc != NQCD_OK:
+            raise EngineError(rc, self.lib.nqcd_last_error(None).decode())
+        self.h = h
+        self.cfg = cfg
+
+    def _check(self, rc: int):
+        if rc != NQCD_OK:
+            raise EngineError(rc, self.lib.nqcd_last_error(self.h).decode())
+
+    def set_initial(self, r0, v0, sig_re=None, sig_im=None, state0=None, nbeads=None):
+        ntraj = r0.shape[0]
+        self._check(self.lib.nqcd_set_initial(self.h, ntraj, dptr(r0), dptr(v0), dptr(sig_re), dptr(sig_im),
+                                              iptr(state0), iptr(nbeads)))
+        self.ntraj = ntraj
+
+    def set_initial_device(self, ntraj: int, d_r0: int, d_v0: int):
+        self._check(self.lib.nqcd_set_initial_device(self.h, ntraj, C.c_void_p(d_r0), C.c_void_p(d_v0), None))
+        self.ntraj = ntraj
+
+    def run(self, t0, t1, dt, seed, scattering=None, popcorr=None):
+        out = nqcd_outputs()
+        out.scattering = dptr(scattering)
+        out.population_correlation = dptr(popcorr)
+        st = nqcd_stats()
+        self._check(self.lib.nqcd_run(self.h, t0, t1, dt, seed, C.byref(out), C.byref(st)))
+        return out, st
+
+    def get_final(self, ndof: int, nstates: int = 2):
+        n = self.ntraj
+        r = np.empty((n, ndof))
+        v = np.empty((n, ndof))
+        sre = np.empty((n, nstates, nstates))
+        sim = np.empty((n, nstates, nstates))
+        state = np.empty(n, np.int32)
+        nh = np.empty(n, np.int32)
+        nf = np.empty(n, np.int32)
+        ns = np.empty(n, np.int32)
+        en = np.empty((n, 2))
+        self._check(self.lib.nqcd_get_final(self.h, dptr(r), dptr(v), dptr(sre), dptr(sim), iptr(state),
+                                            iptr(nh), iptr(nf), iptr(ns), dptr(en)))
+        # (nstates, nstates) per trajectory arrive column-major: transpose to [i, j]
+        return dict(r=r, v=v, sig_re=sre.transpose(0, 2, 1).copy(), sig_im=sim.transpose(0, 2, 1).copy(),
+                    state=state, nhops=nh, nfrustrated=nf, nsteps=ns, energy=en)
+
+    def get_hop_log(self, max_hops: int):
+        log = np.empty((self.ntraj, max_hops, 3), np.int32)
+        self._check(self.lib.nqcd_get_hop_log(self.h, iptr(log)))
+        return log
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nqcd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def measure_fma_peaks() -> tuple[float, float]:
+    lib = load()
+    a, b = C.c_double(), C.c_double()
+    rc = lib.nqcd_measure_fma_peaks(C.byref(a), C.byref(b))
+    if rc != NQCD_OK:
+        raise EngineError(rc, lib.nqcd_last_error(None).decode())
+    return a.value, b.value

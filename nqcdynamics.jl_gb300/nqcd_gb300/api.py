@@ -1,0 +1,463 @@
+"""Host-side mirror of NQCDynamics.jl's ensemble interface for the GPU engine.
+
+Names, argument meanings and error behaviour follow the reference:
+
+  Atoms, TullyModelOne/Two/Three, SpinBoson + OhmicSpectralDensity   (NQCModels / NQCBase)
+  Simulation[FSSH](atoms, model; rescaling)       src/simulations.jl:12-44, fssh.jl:206-213
+  RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)   simulations.jl:46-73, rpsh.jl:5-7
+  PureState(state, Adiabatic()/Diabatic()), DynamicalDistribution,
+  PositionHarmonicWigner / VelocityHarmonicWigner           (NQCDistributions)
+  OutputStateResolvedScattering1D, OutputSurfaceHops, OutputFinal,
+  OutputTotalEnergy                                         src/DynamicsOutputs.jl
+  PopulationCorrelationFunction(sim, Diabatic())            src/TimeCorrelationFunctions.jl:61-88
+  MeanReduction, SumReduction                               src/Ensembles/reductions.jl:8-52
+  run_dynamics(sim, tspan, distribution; trajectories, output, reduction,
+               ensemble_algorithm, dt, saveat)              src/Ensembles/run_dynamics.jl:42-136
+
+States are 1-based here, as in Julia; the C ABI is 0-based.  The only
+ensemble algorithm is EnsembleGB300: SciMLBase's CPU algorithms raise,
+because this engine has no CPU path.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Any, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+# ---------------------------------------------------------------------------
+# Atoms and models
+# ---------------------------------------------------------------------------
+
+
+class Atoms:
+    """Atoms(masses) or Atoms(mass) for one atom (NQCBase.Atoms)."""
+
+    def __init__(self, masses):
+        m = np.atleast_1d(np.asarray(masses, dtype=np.float64))
+        if m.ndim != 1 or len(m) == 0 or np.any(m <= 0):
+            raise ValueError("masses must be a non-empty vector of positive numbers")
+        self.masses = m
+
+    def __len__(self):
+        return len(self.masses)
+
+
+class Model:
+    nstates = 2
+    ndofs = 1
+    kind: int
+    params: tuple
+
+
+@dataclass
+class TullyModelOne(Model):
+    a: float = 0.01
+    b: float = 1.6
+    c: float = 0.005
+    d: float = 1.0
+    kind = L.MODEL_TULLY1
+
+    @property
+    def params(self):
+        return (self.a, self.b, self.c, self.d)
+
+
+@dataclass
+class TullyModelTwo(Model):
+    a: float = 0.1
+    b: float = 0.28
+    c: float = 0.015
+    d: float = 0.06
+    e0: float = 0.05
+    kind = L.MODEL_TULLY2
+
+    @property
+    def params(self):
+        return (self.a, self.b, self.c, self.d, self.e0)
+
+
+@dataclass
+class TullyModelThree(Model):
+    a: float = 6e-4
+    b: float = 0.1
+    c: float = 0.9
+    kind = L.MODEL_TULLY3
+
+    @property
+    def params(self):
+        return (self.a, self.b, self.c)
+
+
+@dataclass
+class OhmicSpectralDensity:
+    """J(w) = pi/2 alpha w exp(-w/wc), discretised as
+    w_j = -wc ln(1 - j/(N+1)), c_j = sqrt(alpha wc/(N+1)) w_j
+    (docs/src/NQCModels/systembathmodels.md:45-59)."""
+
+    ωᶜ: float
+    α: float
+
+    def discretise(self, n: int):
+        j = np.arange(1, n + 1, dtype=np.float64)
+        w = -self.ωᶜ * np.log(1.0 - j / (1 + n))
+        c = np.sqrt(self.α * self.ωᶜ / (n + 1)) * w
+        return w, c
+
+
+class SpinBoson(Model):
+    """SpinBoson(density, N, ϵ, Δ): V = [[ϵ + c.R, Δ], [Δ, -ϵ - c.R]] + R^T Ω^2 R / 2."""
+
+    kind = L.MODEL_SPINBOSON
+
+    def __init__(self, density: OhmicSpectralDensity, N: int, ϵ: float, Δ: float):
+        self.density = density
+        self.N = int(N)
+        self.ϵ = float(ϵ)
+        self.Δ = float(Δ)
+        self.ωⱼ, self.cⱼ = density.discretise(self.N)
+
+    @property
+    def params(self):
+        return (self.ϵ, self.Δ)
+
+
+# ---------------------------------------------------------------------------
+# Methods and simulations
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class FSSH:
+    rescaling: str = "standard"
+
+    def __post_init__(self):
+        if self.rescaling not in L.RESCALE:
+            raise ValueError(f"rescaling {self.rescaling!r} not recognised (standard, vinversion, off)")
+
+
+class _MethodIndexed(type):
+    def __getitem__(cls, method):
+        def make(*args, **kwargs):
+            return cls(*args, method=method, **kwargs)
+
+        return make
+
+
+class Simulation(metaclass=_MethodIndexed):
+    """Simulation[FSSH](atoms, model; rescaling=:standard)."""
+
+    def __init__(self, atoms: Atoms, model: Model, method=FSSH, rescaling: str = "standard", temperature=0.0):
+        if method is not FSSH:
+            raise NotImplementedError(f"method {method} is not on the GPU path")
+        self.atoms = atoms
+        self.model = model
+        self.method = FSSH(rescaling)
+        self.temperature = float(temperature)
+        if isinstance(model, SpinBoson):
+            if len(atoms) != model.N:
+                raise ValueError("SpinBoson needs one atom per bath mode")
+        elif len(atoms) != 1:
+            raise ValueError("Tully models have one atom with one degree of freedom")
+
+    @property
+    def size(self):
+        return (self.model.ndofs, len(self.atoms))
+
+    @property
+    def ndof(self):
+        return self.model.ndofs * len(self.atoms)
+
+
+class RingPolymerSimulation(metaclass=_MethodIndexed):
+    """RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)."""
+
+    def __init__(self, atoms: Atoms, model: Model, n_beads, method=FSSH, rescaling: str = "standard",
+                 temperature: float = 0.0):
+        if method is not FSSH:
+            raise NotImplementedError(f"method {method} is not on the GPU path")
+        if isinstance(model, SpinBoson) or len(atoms) != 1:
+            raise NotImplementedError("ring-polymer surface hopping runs on the one-dimensional Tully models")
+        if not temperature > 0:
+            raise ValueError("ring polymers need a positive temperature")
+        self.atoms = atoms
+        self.model = model
+        self.method = FSSH(rescaling)
+        self.temperature = float(temperature)
+        self.n_beads = n_beads
+
+    @property
+    def beta(self):
+        return 1.0 / self.temperature
+
+
+# ---------------------------------------------------------------------------
+# Distributions
+# ---------------------------------------------------------------------------
+
+
+class Adiabatic:
+    pass
+
+
+class Diabatic:
+    pass
+
+
+@dataclass
+class PureState:
+    state: int
+    statetype: Any = field(default_factory=Diabatic)
+
+    def init_kind(self):
+        return L.INIT_ADIABATIC_PURE if isinstance(self.statetype, Adiabatic) else L.INIT_DIABATIC_PURE
+
+
+@dataclass
+class PositionHarmonicWigner:
+    """Wigner position distribution of a harmonic oscillator (hbar = 1)."""
+
+    ω: float
+    β: float
+    m: float
+
+    def sigma(self):
+        return math.sqrt(1.0 / (2.0 * self.m * self.ω * math.tanh(self.β * self.ω / 2.0)))
+
+
+@dataclass
+class VelocityHarmonicWigner:
+    ω: float
+    β: float
+    m: float
+
+    def sigma(self):
+        return math.sqrt(self.ω / (2.0 * self.m * math.tanh(self.β * self.ω / 2.0)))
+
+
+class DynamicalDistribution:
+    """DynamicalDistribution(velocity, position, size): each of velocity and
+    position is a scalar, an array of per-dof samplers/values, or a sequence
+    of explicit samples (one per trajectory)."""
+
+    def __init__(self, velocity, position, size):
+        self.velocity = velocity
+        self.position = position
+        self.size = tuple(size)
+
+    def __mul__(self, other):
+        return ProductDistribution(self, other)
+
+    def sample(self, which, ntraj, rng):
+        spec = self.velocity if which == "v" else self.position
+        n = int(np.prod(self.size))
+        if isinstance(spec, (list, tuple)) or (isinstance(spec, np.ndarray) and spec.dtype == object):
+            flat = list(np.asarray(spec, dtype=object).reshape(-1, order="F"))
+            if len(flat) == n and all(hasattr(s, "sigma") for s in flat):
+                sig = np.array([s.sigma() for s in flat])
+                return rng.standard_normal((ntraj, n)) * sig
+        arr = np.asarray(spec, dtype=np.float64)
+        if arr.size == 1:
+            return np.full((ntraj, n), float(arr))
+        if arr.shape == self.size or arr.size == n:
+            return np.broadcast_to(arr.reshape(-1, order="F"), (ntraj, n)).copy()
+        if arr.ndim >= 1 and arr.shape[0] == ntraj:
+            return arr.reshape(ntraj, -1).copy()
+        raise ValueError("cannot interpret distribution specification")
+
+
+@dataclass
+class ProductDistribution:
+    nuclear: DynamicalDistribution
+    electronic: PureState
+
+
+# ---------------------------------------------------------------------------
+# Outputs and reductions
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class OutputStateResolvedScattering1D:
+    sim: Any
+    type: str = "adiabatic"
+
+    def __post_init__(self):
+        if self.type not in ("adiabatic",):
+            raise ValueError(f"{self.type} not recognised: the GPU path evaluates adiabatic populations")
+
+
+@dataclass
+class PopulationCorrelationFunction:
+    sim: Any
+    statetype: Any = field(default_factory=Diabatic)
+
+    def __post_init__(self):
+        if not isinstance(self.statetype, Diabatic):
+            raise NotImplementedError("the GPU path evaluates the diabatic population correlation")
+
+
+class OutputFinal:
+    pass
+
+
+class OutputSurfaceHops:
+    pass
+
+
+class OutputTotalEnergy:
+    pass
+
+
+class MeanReduction:
+    pass
+
+
+class SumReduction:
+    pass
+
+
+class SortByTrajectoryReduction:
+    pass
+
+
+# ---------------------------------------------------------------------------
+# Ensemble algorithms
+# ---------------------------------------------------------------------------
+
+
+class EnsembleSerial:
+    pass
+
+
+class EnsembleThreads:
+    pass
+
+
+@dataclass
+class EnsembleGB300:
+    """GPU ensemble algorithm: precision 'fp64' (plain, bit-identical to the
+    FP64 reference integration) or 'fp32' (fast path)."""
+
+    precision: str = "fp64"
+    gap_fp64: float = 1e-3
+    max_hops: int = 16
+    seed: int = 20261203
+
+
+# ---------------------------------------------------------------------------
+# run_dynamics
+# ---------------------------------------------------------------------------
+
+
+def _output_name(o):
+    return o.__name__ if isinstance(o, type) else type(o).__name__
+
+
+def build_config(sim, electronic: PureState, ntraj: int, alg: EnsembleGB300, save_stride: int):
+    model = sim.model
+    cfg = L.nqcd_config()
+    cfg.method = L.METHOD_FSSH
+    cfg.model = model.kind
+    cfg.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[alg.precision]
+    cfg.rescaling = L.RESCALE[sim.method.rescaling]
+    cfg.ndofs = model.ndofs
+    cfg.natoms = len(sim.atoms)
+    cfg.nstates = model.nstates
+    params = np.asarray(model.params, dtype=np.float64)
+    masses = np.ascontiguousarray(sim.atoms.masses, dtype=np.float64)
+    keep = [params, masses]
+    cfg.nparams = len(params)
+    cfg.params = L.dptr(params)
+    if isinstance(model, SpinBoson):
+        c = np.ascontiguousarray(model.cⱼ)
+        w = np.ascontiguousarray(model.ωⱼ)
+        keep += [c, w]
+        cfg.nbath = model.N
+        cfg.bath_a = L.dptr(c)
+        cfg.bath_b = L.dptr(w)
+    cfg.masses = L.dptr(masses)
+    cfg.ntraj_max = ntraj
+    if not (1 <= electronic.state <= model.nstates):
+        raise ValueError("PureState index outside 1..nstates")
+    cfg.init_kind = electronic.init_kind()
+    cfg.init_state = electronic.state - 1
+    cfg.save_stride = save_stride
+    cfg.max_hops = alg.max_hops
+    cfg.gap_fp64 = alg.gap_fp64
+    return cfg, keep
+
+
+def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, reduction=None,
+                 ensemble_algorithm=None, dt: float = 1.0, saveat=None, seed: int | None = None,
+                 rng: np.random.Generator | None = None):
+    """Run an ensemble through the GPU engine and reduce the outputs.
+
+    Returns a dict keyed like the reference's MeanReduction Dictionary
+    (:Time plus one entry per output) or, for one trajectory, that
+    trajectory's outputs."""
+    alg = ensemble_algorithm if ensemble_algorithm is not None else EnsembleGB300()
+    if isinstance(alg, (EnsembleSerial, EnsembleThreads)) or alg in (EnsembleSerial, EnsembleThreads):
+        raise NotImplementedError("this engine has no CPU path: use ensemble_algorithm=EnsembleGB300()")
+    if not isinstance(alg, EnsembleGB300):
+        raise TypeError("ensemble_algorithm must be EnsembleGB300")
+    if isinstance(sim, RingPolymerSimulation):
+        raise NotImplementedError("ring-polymer ensembles run through run_ring_polymer_ensemble")
+    if not isinstance(distribution, ProductDistribution):
+        raise TypeError("distribution must be DynamicalDistribution * PureState")
+    outputs = output if isinstance(output, (tuple, list)) else (output,)
+    reduction = reduction if reduction is not None else MeanReduction()
+    if not isinstance(reduction, (MeanReduction, SumReduction)):
+        raise NotImplementedError("the GPU path reduces on the device: MeanReduction or SumReduction")
+    t0, t1 = float(tspan[0]), float(tspan[1])
+    save_stride = 0
+    for o in outputs:
+        if isinstance(o, PopulationCorrelationFunction):
+            if saveat is None:
+                raise ValueError("PopulationCorrelationFunction needs saveat")
+            stride = float(saveat) / dt
+            if abs(stride - round(stride)) > 1e-9 or round(stride) < 1:
+                raise ValueError("saveat must be a positive multiple of dt on the GPU path")
+            save_stride = int(round(stride))
+    ntraj = int(trajectories)
+    rng = rng if rng is not None else np.random.default_rng(alg.seed if seed is None else seed)
+    r0 = distribution.nuclear.sample("r", ntraj, rng)
+    v0 = distribution.nuclear.sample("v", ntraj, rng)
+    cfg, keep = build_config(sim, distribution.electronic, ntraj, alg, save_stride)
+    eng = L.Engine(cfg, keep)
+    try:
+        eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0))
+        sc = np.zeros(4)
+        pc = None
+        if save_stride:
+            nsteps = int(round((t1 - t0) / dt))
+            pc = np.zeros((nsteps // save_stride + 1) * 4 + 4)
+        out, stats = eng.run(t0, t1, dt, alg.seed if seed is None else seed, scattering=sc, popcorr=pc)
+        result: dict[str, Any] = {}
+        scale = ntraj if isinstance(reduction, SumReduction) else 1
+        final = None
+        for o in outputs:
+            name = _output_name(o)
+            if isinstance(o, OutputStateResolvedScattering1D):
+                result[name] = {"reflection": sc[:2] * scale, "transmission": sc[2:] * scale}
+            elif isinstance(o, PopulationCorrelationFunction):
+                result[name] = pc[: out.nsave * 4].reshape(out.nsave, 2, 2) * scale
+                result["Time"] = t0 + dt * save_stride * np.arange(out.nsave)
+            else:
+                if final is None:
+                    final = eng.get_final(sim.ndof)
+                if o is OutputFinal or isinstance(o, OutputFinal):
+                    result["OutputFinal"] = final
+                elif o is OutputTotalEnergy or isinstance(o, OutputTotalEnergy):
+                    result["OutputTotalEnergy"] = final["energy"]
+                elif o is OutputSurfaceHops or isinstance(o, OutputSurfaceHops):
+                    result["OutputSurfaceHops"] = final["nhops"]
+                else:
+                    raise NotImplementedError(f"output {name} is not available on the GPU path")
+        result["_stats"] = stats
+        return result
+    finally:
+        eng.close()

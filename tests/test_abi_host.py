@@ -1,0 +1,149 @@
+"""C-ABI library and host-side logic, without GPU compute.
+
+* the engine library loads and exports every function include/nqcd_gpu.h declares;
+* argument validation answers with the documented error codes before any
+  device work (and nqcd_create reports NQCD_ERR_CUDA when no GPU exists);
+* the host mirror of the reference API maps simulations to engine configs,
+  refuses CPU ensemble algorithms and samples initial conditions as specified.
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import nqcd_gb300 as N
+from nqcd_gb300 import _lib as L
+from nqcd_gb300 import api, workload
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    text = (ROOT / "include" / "nqcd_gpu.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(nqcd_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_expected_entry_points():
+    names = declared_functions()
+    assert set(L.EXPORTED) <= set(names), set(L.EXPORTED) - set(names)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = L.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert lib.nqcd_version() == 100
+
+
+def _cfg(**kw):
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = L.METHOD_FSSH, L.MODEL_TULLY1, L.PREC_FP64
+    cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 2
+    p = np.array([0.01, 1.6, 0.005, 1.0])
+    m = np.array([2000.0])
+    cfg.nparams, cfg.params, cfg.masses, cfg.ntraj_max = 4, L.dptr(p), L.dptr(m), 16
+    cfg.init_kind = L.INIT_ADIABATIC_PURE
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg, [p, m]
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("method", 99, -6), ("model", 77, -6), ("nstates", 3, -6), ("precision", 5, -1), ("rescaling", 7, -1),
+    ("ntraj_max", 0, -1), ("init_state", 2, -1), ("nparams", 2, -1), ("natoms", 2, -6), ("save_stride", -1, -1),
+])
+def test_create_validates_arguments(field, value, code):
+    cfg, keep = _cfg(**{field: value})
+    lib = L.load()
+    h = C.c_void_p()
+    rc = lib.nqcd_create(C.byref(cfg), C.byref(h))
+    assert rc == code, (field, rc, lib.nqcd_last_error(None))
+    assert not h.value
+    assert lib.nqcd_last_error(None)
+
+
+def test_create_without_gpu_or_with_gpu():
+    import torch
+
+    cfg, keep = _cfg()
+    lib = L.load()
+    h = C.c_void_p()
+    rc = lib.nqcd_create(C.byref(cfg), C.byref(h))
+    if torch.cuda.is_available():
+        assert rc == 0
+        lib.nqcd_destroy(h)
+    else:
+        assert rc == -2 and b"no CUDA device" in lib.nqcd_last_error(None)
+
+
+def test_null_arguments():
+    lib = L.load()
+    assert lib.nqcd_create(None, None) == -1
+    assert lib.nqcd_run(None, 0.0, 1.0, 1.0, 1, None, None) == -1
+    assert lib.nqcd_set_initial(None, 1, None, None, None, None, None, None) == -1
+    lib.nqcd_destroy(None)  # no-op
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(L.EngineUnavailable):
+        L.load(tmp_path / "absent.so")
+
+
+def test_ohmic_discretisation_matches_documentation():
+    # docs/src/NQCModels/systembathmodels.md:54-59
+    d = N.OhmicSpectralDensity(2.5, 0.1)
+    w, c = d.discretise(100)
+    j = np.arange(1, 101)
+    np.testing.assert_allclose(w, -2.5 * np.log(1 - j / 101))
+    np.testing.assert_allclose(c, np.sqrt(0.1 * 2.5 / 101) * w)
+    w2, c2, r0, v0 = workload.spin_boson_inputs(10, 100)
+    np.testing.assert_allclose(w2, w)
+    np.testing.assert_allclose(c2, c)
+
+
+def test_wigner_widths():
+    # harmonic Wigner distribution at beta: <x^2> = coth(beta w / 2) / (2 m w), <v^2> = w coth(beta w / 2) / (2 m)
+    p = N.PositionHarmonicWigner(1.3, 5.0, 1.0)
+    v = N.VelocityHarmonicWigner(1.3, 5.0, 1.0)
+    assert abs(p.sigma() ** 2 - 1 / (2 * 1.3 * np.tanh(5 * 1.3 / 2))) < 1e-14
+    assert abs(v.sigma() ** 2 - 1.3 / (2 * np.tanh(5 * 1.3 / 2))) < 1e-14
+    model = N.SpinBoson(N.OhmicSpectralDensity(2.5, 0.1), 4, 0.0, 1.0)
+    pos = [N.PositionHarmonicWigner(w, 5.0, 1.0) for w in model.ωⱼ]
+    vel = [N.VelocityHarmonicWigner(w, 5.0, 1.0) for w in model.ωⱼ]
+    dist = N.DynamicalDistribution(vel, pos, (1, 4))
+    x = dist.sample("r", 200000, np.random.default_rng(0))
+    np.testing.assert_allclose(x.std(axis=0), [q.sigma() for q in pos], rtol=0.01)
+
+
+def test_config_mapping_and_one_based_states():
+    sim = N.Simulation[N.FSSH](N.Atoms(2000.0), N.TullyModelTwo(), rescaling="vinversion")
+    cfg, keep = api.build_config(sim, N.PureState(2, N.Adiabatic()), 10, N.EnsembleGB300("fp32"), 0)
+    assert cfg.model == L.MODEL_TULLY2 and cfg.precision == L.PREC_FP32 and cfg.rescaling == 1
+    assert cfg.init_kind == L.INIT_ADIABATIC_PURE and cfg.init_state == 1
+    assert [cfg.params[i] for i in range(5)] == [0.1, 0.28, 0.015, 0.06, 0.05]
+    with pytest.raises(ValueError):
+        api.build_config(sim, N.PureState(3, N.Adiabatic()), 10, N.EnsembleGB300(), 0)
+    sb = N.SpinBoson(N.OhmicSpectralDensity(2.5, 0.1), 100, 0.0, 1.0)
+    sim2 = N.Simulation[N.FSSH](N.Atoms(np.ones(100)), sb)
+    cfg2, _ = api.build_config(sim2, N.PureState(1), 10, N.EnsembleGB300(), 2)
+    assert cfg2.init_kind == L.INIT_DIABATIC_PURE and cfg2.nbath == 100 and cfg2.save_stride == 2
+
+
+def test_cpu_ensemble_algorithms_are_refused():
+    sim = N.Simulation[N.FSSH](N.Atoms(2000.0), N.TullyModelOne())
+    dist = N.DynamicalDistribution(0.005, -10.0, (1, 1)) * N.PureState(1, N.Adiabatic())
+    for alg in (N.EnsembleThreads(), N.EnsembleSerial(), N.EnsembleThreads):
+        with pytest.raises(NotImplementedError):
+            N.run_dynamics(sim, (0.0, 10.0), dist, output=N.OutputStateResolvedScattering1D(sim, "adiabatic"),
+                           trajectories=4, ensemble_algorithm=alg)
+
+
+def test_unknown_rescaling_and_outputs_rejected():
+    # surface_hopping.jl:89-90 throws on an unknown rescaling mode
+    with pytest.raises(ValueError):
+        N.Simulation[N.FSSH](N.Atoms(2000.0), N.TullyModelOne(), rescaling="bogus")
+    with pytest.raises(ValueError):
+        N.OutputStateResolvedScattering1D(None, "sideways")

@@ -1,0 +1,202 @@
+"""Pin the CPU oracle against the reference's own known answers and invariants.
+
+The reference (NQCDynamics.jl) is pure Julia and cannot run here, so the
+oracle is checked against the golden vectors, known-answer tests and
+invariants its test suite and documentation hold for this path, and against
+published algorithm vectors (Philox4x32-10).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+TULLY = {1: (0.01, 1.6, 0.005, 1.0), 2: (0.1, 0.28, 0.015, 0.06, 0.05), 3: (6e-4, 0.1, 0.9)}
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32-10 (Salmon et al., SC'11)
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_uniform_stream_properties():
+    u = np.array([O.uniform(20261203, t, s, 1) for t in range(200) for s in range(50)])
+    assert u.min() >= 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 0.01 and abs(u.var() - 1 / 12) < 0.005
+    # distinct streams and counters give distinct draws
+    assert O.uniform(1, 5, 7, 1) != O.uniform(1, 5, 7, 2) != O.uniform(1, 6, 7, 1)
+
+
+def test_exp_error_bound():
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(-745, 709, 20000), rng.uniform(-30, 30, 20000), [0.0, 1e-300, -1e-300]])
+    for x in xs:
+        ref = math.exp(x)
+        if ref == 0.0 or not math.isfinite(ref):
+            continue
+        assert abs(O.exp(x) - ref) <= 2 * math.ulp(ref), x
+    assert O.exp(800.0) == math.inf and O.exp(-800.0) == 0.0 and math.isnan(O.exp(float("nan")))
+
+
+def test_normal_mode_transform_golden_vectors():
+    # docs/src/api/RingPolymerArrays/ringpolymerarrays.md:93-133 (n = 4)
+    U = O.nm_transform(4)
+    to = U.T @ np.ones(4)
+    np.testing.assert_allclose(to, [2.0, -8.65956e-17, 0.0, 2.59787e-16], atol=1e-21, rtol=1e-5)
+    frm = U @ np.ones(4)
+    np.testing.assert_allclose(frm, [1.70711, -0.707107, 0.292893, 0.707107], rtol=1e-5)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 8, 10, 16, 32])
+def test_normal_mode_transform_invariants(n):
+    # test/Core/ring_polymers.jl:22-27: U'U = I, |det U| = 1, U'SU diagonal with the normal-mode springs
+    U = O.nm_transform(n)
+    np.testing.assert_allclose(U.T @ U, np.eye(n), atol=1e-13)
+    assert abs(abs(np.linalg.det(U)) - 1) < 1e-12
+    wn = 2.0
+    if n == 1:
+        S = np.zeros((1, 1))
+    elif n == 2:
+        S = np.array([[2.0, -2.0], [-2.0, 2.0]])
+    else:
+        S = 2 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)
+        S[0, -1] = S[-1, 0] = -1
+    S = S * wn**2 / 2
+    lam = (2 * wn * np.sin(np.arange(n) * np.pi / n)) ** 2 / 2
+    np.testing.assert_allclose(U.T @ S @ U, np.diag(lam), atol=1e-12 * max(1, lam.max()))
+
+
+def test_cayley_half_squared_is_full():
+    # test/Core/ring_polymers.jl:30-32 and the definition in ring_polymer.jl:71-82
+    import scipy.linalg
+
+    for n, beta, dt in [(10, 1.0, 0.1), (4, 1024.0, 1.0), (32, 1024.0, 1.0)]:
+        full = O.cayley(n, beta, dt)
+        wn = n / beta
+        for k in range(n):
+            w = 2 * wn * np.sin(k * np.pi / n)
+            A = np.array([[0.0, 1.0], [-w * w, 0.0]])
+            ref = np.linalg.inv(np.eye(2) - dt * A / 2) @ (np.eye(2) + dt * A / 2)
+            np.testing.assert_allclose(full[k], ref, rtol=1e-13, atol=1e-15)
+            half = np.real(scipy.linalg.sqrtm(full[k]))
+            np.testing.assert_allclose(half @ half, full[k], rtol=1e-10, atol=1e-12)
+            # the free-ring-polymer propagator is symplectic: det = 1
+            assert abs(np.linalg.det(full[k]) - 1) < 1e-12
+
+
+def test_select_new_state_known_answers():
+    # test/Dynamics/fssh.jl:53-63 (1-based states there, 0-based here)
+    assert O.select_new_state([0.0, 1.0], 0, 0.5) == 1
+    assert O.select_new_state([0.0, 1.0], 1, 0.5) == 1
+    assert O.select_new_state([1.0, 0.0], 1, 0.5) == 0
+
+
+@pytest.mark.parametrize("kind", [1, 2, 3])
+def test_tully_derivative_finite_difference(kind):
+    # test/Dynamics/utils.jl:9-62 style consistency of V and dV/dx
+    for x in np.linspace(-6, 6, 37):
+        _, D = O.tully(kind, TULLY[kind], x)
+        h = 1e-6
+        Vp, _ = O.tully(kind, TULLY[kind], x + h)
+        Vm, _ = O.tully(kind, TULLY[kind], x - h)
+        # central differences: O(h^2) truncation, O(h) at Tully 1's x = 0 kink of d2V/dx2
+        np.testing.assert_allclose(D, (Vp - Vm) / (2 * h), atol=5e-8)
+
+
+def test_tully_closed_form_values():
+    # Tully, J. Chem. Phys. 93, 1061 (1990)
+    V, _ = O.tully(1, TULLY[1], 1.0)
+    assert np.allclose(V, [0.01 * (1 - np.exp(-1.6)), 0.005 * np.exp(-1.0), -0.01 * (1 - np.exp(-1.6))], rtol=1e-15)
+    V, _ = O.tully(2, TULLY[2], 0.5)
+    assert np.allclose(V, [0.0, 0.015 * np.exp(-0.06 * 0.25), -0.1 * np.exp(-0.28 * 0.25) + 0.05], rtol=1e-15)
+    V, _ = O.tully(3, TULLY[3], -1.0)
+    assert np.allclose(V, [6e-4, 0.1 * np.exp(-0.9), -6e-4], rtol=1e-15)
+
+
+def test_fssh_total_energy_conserved_tully2():
+    # test/Dynamics/fssh.jl:123-133: Tully 2, m = 2000, x = -10, v = 100/2000, dt = 0.1, rtol 1e-2
+    n = 64
+    r0 = np.full((n, 1), -10.0)
+    v0 = np.full((n, 1), 100 / 2000)
+    o = O.run_fssh(model=2, params=TULLY[2], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=500.0, dt=0.1, seed=3)
+    assert o["nhops"].sum() > 0
+    np.testing.assert_allclose(o["energy"][:, 1], o["energy"][:, 0], rtol=1e-2)
+
+
+def test_fssh_hop_rescaling_conserves_energy():
+    # test/Dynamics/fssh.jl:87-121: an accepted hop changes KE by -dE (rtol 1e-3)
+    # through a whole trajectory with hops: total energy drift stays at the integrator level
+    n = 256
+    r0 = np.full((n, 1), -10.0)
+    v0 = np.linspace(9.0, 25.0, n).reshape(n, 1) / 2000
+    o = O.run_fssh(model=1, params=TULLY[1], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=3000.0, dt=1.0, seed=11)
+    hopped = o["nhops"] > 0
+    assert hopped.sum() > 20
+    np.testing.assert_allclose(o["energy"][hopped, 1], o["energy"][hopped, 0], rtol=1e-2)
+
+
+def test_fssh_frustrated_hops_and_vinversion():
+    # test/Dynamics/fssh.jl:65-74: zero momentum -> frustrated, large momentum -> accepted
+    n = 128
+    r0 = np.full((n, 1), -4.0)
+    v0 = np.full((n, 1), 4.5 / 2000)  # too little energy to reach the upper state of Tully 2
+    std = O.run_fssh(model=2, params=TULLY[2], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=1500.0, dt=1.0, seed=5)
+    inv = O.run_fssh(model=2, params=TULLY[2], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=1500.0, dt=1.0, seed=5,
+                     rescaling=1)
+    off = O.run_fssh(model=2, params=TULLY[2], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=1500.0, dt=1.0, seed=5,
+                     rescaling=2)
+    assert std["nfrustrated"].sum() > 0 and std["nhops"].sum() == 0
+    assert inv["nfrustrated"].sum() > 0
+    assert off["nfrustrated"].sum() == 0 and off["nhops"].sum() > 0
+
+
+def test_spinboson_diabatic_population_at_symmetric_point():
+    # test/Dynamics/fssh.jl:47-51 analogue: symmetric two-level system at R = 0,
+    # adiabatic pure state -> diabatic populations 0.5 / 0.5
+    n, nm = 4, 10
+    w = np.linspace(0.5, 3, nm)
+    c = 0.1 * w
+    o = O.run_fssh(model=10, params=(0.0, 1.0), ndof=nm, mass=1.0, r0=np.zeros((n, nm)), v0=np.zeros((n, nm)),
+                   t0=0.0, t1=0.0, dt=0.1, seed=1, init_kind=1, init_state=0, bath_c=c, bath_w2=w * w, save_stride=1)
+    np.testing.assert_allclose(o["popcorr"][0], [0.25, 0.25, 0.25, 0.25], rtol=1e-14)
+
+
+def test_density_matrix_stays_hermitian_and_normalised():
+    n = 32
+    r0 = np.full((n, 1), -10.0)
+    v0 = np.full((n, 1), 15.0 / 2000)
+    o = O.run_fssh(model=1, params=TULLY[1], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=1200.0, dt=1.0, seed=2)
+    s = o["sigma"]
+    np.testing.assert_array_equal(s[:, 0, 1], np.conj(s[:, 1, 0]))
+    np.testing.assert_allclose(np.trace(s, axis1=1, axis2=2).real, 1.0, atol=1e-8)
+
+
+def test_rpsh_energy_and_termination():
+    # test/Dynamics/fssh.jl:210-233: RPSH on Tully 2 conserves the ring-polymer energy to rtol 1e-2
+    n, nb = 32, 5
+    rng = np.random.default_rng(1)
+    r = np.full((n, nb), -10.0) + 0.1 * rng.standard_normal((n, nb))
+    v = np.full((n, nb), 100 / 2000)
+    o = O.run_rpsh(model=2, params=TULLY[2], mass=2000.0, r0=r, v0=v, nbeads=np.full(n, nb, np.int32), beta=100.0,
+                   t0=0.0, t1=400.0, dt=0.1, seed=4)
+    np.testing.assert_allclose(o["energy"][:, 1], o["energy"][:, 0], rtol=1e-2)
+    # termination at |centroid| > 10
+    o2 = O.run_rpsh(model=1, params=TULLY[1], mass=2000.0, r0=np.full((n, 8), -9.5), v0=np.full((n, 8), 0.01),
+                    nbeads=np.full(n, 8, np.int32), beta=1024.0, t0=0.0, t1=20000.0, dt=1.0, seed=4, terminate_x=10.0)
+    assert np.all(o2["nsteps"] < 20000)
+    xc = o2["r"].mean(axis=1)
+    assert np.all(np.abs(xc) > 10.0)
+
+
+def test_rpsh_free_ring_polymer_centroid_moves_classically():
+    # without a potential gradient (Tully 3 far left, constant diabats) the centroid drifts at constant velocity
+    n, nb = 4, 8
+    r0 = np.full((n, nb), -30.0) + np.linspace(-0.1, 0.1, nb)
+    v0 = np.full((n, nb), 0.002)
+    o = O.run_rpsh(model=3, params=TULLY[3], mass=2000.0, r0=r0, v0=v0, nbeads=np.full(n, nb, np.int32), beta=1024.0,
+                   t0=0.0, t1=100.0, dt=1.0, seed=1)
+    np.testing.assert_allclose(o["r"].mean(axis=1), -30.0 + 0.2, rtol=1e-9)
