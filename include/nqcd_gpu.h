@@ -173,6 +173,37 @@ int nqcd_unpin_host(void* ptr);
  * (TFLOP/s, 2 flops per FMA) with a register-resident FMA chain kernel. */
 int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
 
+/* Allocation-free plain FP64 spin-boson FSSH ensemble.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory while
+ * they run (a Julia host whose CUDA.jl pool owns the device memory, a service
+ * that reserves all its memory at start-up, code that must not allocate while
+ * a stream is being captured).  It allocates nothing, on the device or the
+ * host: inputs and outputs are the caller's device buffers, and the per-mode
+ * coupling scratch is a fixed array of NQCD_NOALLOC_SCRATCH_DOUBLES doubles
+ * (8 MiB) built into the library, held by every GPU that loads it until exit.
+ *
+ * Same kernel and results as nqcd_run with NQCD_METHOD_FSSH,
+ * NQCD_MODEL_SPINBOSON, NQCD_PREC_FP64, NQCD_INIT_DIABATIC_PURE(diabatic_state).
+ *  d_bath_c, d_bath_omega2 (omega_j^2), d_mass: device [nmodes]
+ *  d_r, d_v: device [nmodes][ntraj] (trajectory fastest); initial conditions
+ *            in, final positions and velocities out
+ *  d_sigma: device [8][ntraj] out (re00 im00 re01 im01 re10 im10 re11 im11)
+ *  d_state: device [ntraj] out; d_nhops, d_nfrustrated, d_nsteps: device
+ *            [ntraj] out or NULL
+ *  stream: cudaStream_t (NULL = default stream); the call only enqueues.
+ * Returns NQCD_ERR_ARG (message in errbuf, if given) when nmodes * ntraj >
+ * NQCD_NOALLOC_SCRATCH_DOUBLES.  The first call on a device looks up the
+ * scratch array's device address (cudaGetSymbolAddress) and caches it: make
+ * that first call before any stream capture.  All calls share the scratch
+ * array, so calls whose kernels overlap on the GPU race. */
+#define NQCD_NOALLOC_SCRATCH_DOUBLES 1048576
+int nqcd_fssh_spinboson_fp64_noalloc(int64_t ntraj, int32_t nmodes, const double* d_bath_c,
+                                     const double* d_bath_omega2, const double* d_mass, double eps, double delta,
+                                     int32_t rescaling, int32_t diabatic_state, double* d_r, double* d_v,
+                                     double* d_sigma, int32_t* d_state, int32_t* d_nhops, int32_t* d_nfrustrated,
+                                     int32_t* d_nsteps, double t0, double t1, double dt, uint64_t seed, void* stream,
+                                     char* errbuf, int32_t errbuf_len);
+
 #ifdef __cplusplus
 }
 #endif

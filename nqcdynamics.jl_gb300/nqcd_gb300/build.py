@@ -31,6 +31,7 @@ ENGINE_UNITS = {
     "kernels_fp64.cu": ["-fmad=false"],
     "kernels_fp32.cu": [],
     "nqcd_abi.cu": [],
+    "noalloc.cu": [],
 }
 
 
