@@ -49,12 +49,17 @@ enum nqcd_model {
     NQCD_MODEL_TULLY1 = 1,    /* params: A, B, C, D */
     NQCD_MODEL_TULLY2 = 2,    /* params: A, B, C, D, E0 */
     NQCD_MODEL_TULLY3 = 3,    /* params: A, B, C */
-    NQCD_MODEL_SPINBOSON = 10 /* params: eps, Delta; bath_a = c_j, bath_b = omega_j */
+    NQCD_MODEL_SPINBOSON = 10, /* params: eps, Delta; bath_a = c_j, bath_b = omega_j */
+    NQCD_MODEL_NEWNS_ANDERSON = 20 /* AndersonHolstein with a displaced-harmonic impurity:
+                                      U0 = k x^2/2, U1 = k (x-g)^2/2 + delta; params: k, g, delta, mu, sigma
+                                      (Fermi level, Gaussian broadening width of the friction);
+                                      bath_a = bath levels e_k (ascending), bath_b = couplings V_k */
 };
 
 enum nqcd_precision {
-    NQCD_PREC_FP64 = 0, /* plain path: bit-identical to the FP64 reference integration */
-    NQCD_PREC_FP32 = 1  /* fast path: FP32 electronic structure, FP64 accumulation */
+    NQCD_PREC_FP64 = 0,      /* plain path: bit-identical to the FP64 reference integration */
+    NQCD_PREC_FP32 = 1,      /* fast path: FP32 electronic structure, FP64 position/velocity accumulation */
+    NQCD_PREC_FP32_KAHAN = 2 /* fast path with Kahan-compensated FP32 accumulation (no FP64 pipe work per mode) */
 };
 
 enum nqcd_rescaling { NQCD_RESCALE_STANDARD = 0, NQCD_RESCALE_VINVERSION = 1, NQCD_RESCALE_OFF = 2 };
@@ -89,13 +94,16 @@ typedef struct nqcd_config {
     double terminate_x;   /* ring polymer: stop a trajectory once |centroid x| > terminate_x (0 = off) */
     double gap_fp64;      /* fast path: propagate electronics in FP64 when the adiabatic gap is below this */
     int64_t traj_offset;  /* global index of trajectory 0 (Philox counter), for sharded ensembles */
-    int32_t reserved[6];
+    int32_t use_friction_surrogate; /* MDEF fast path: friction from the trained network inside its domain */
+    int32_t judge_every;  /* MDEF with surrogate: exact friction every judge_every steps (0 = never) */
+    int32_t reserved[4];
 } nqcd_config;
 
 typedef struct nqcd_outputs {
     /* Ensemble means (MeanReduction, src/Ensembles/reductions.jl:36-52).  Host pointers; NULL to skip. */
     double* scattering;             /* [2][nstates]: reflection, transmission (OutputStateResolvedScattering1D) */
     double* population_correlation; /* [nsave][nstates][nstates] (PopulationCorrelationFunction, Diabatic) */
+    double* observables;            /* MDEF: [nsave][4] means of x, x^2, kinetic energy, friction */
     int32_t nsave;                  /* out: save points written */
     int32_t reserved;
 } nqcd_outputs;
@@ -112,6 +120,9 @@ typedef struct nqcd_stats {
     int64_t d2h_bytes;      /* bytes copied device->host inside the call */
     int32_t kernel_launches;/* engine kernels launched by the call */
     int32_t reserved;
+    int64_t exact_friction_evals;     /* MDEF: electronic friction evaluations */
+    int64_t surrogate_friction_evals; /* MDEF: friction values taken from the surrogate network */
+    int64_t unconverged_roots;        /* MDEF: secular roots that hit the iteration cap */
 } nqcd_stats;
 
 typedef struct nqcd_handle nqcd_handle;
@@ -153,6 +164,43 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
  * total energy, DynamicsOutputs.OutputTotalEnergy). */
 int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double* sig_im, int32_t* state,
                    int32_t* nhops, int32_t* nfrustrated, int32_t* nsteps, double* energy);
+
+/* Ring polymers: per-trajectory Tully model (NQCD_MODEL_TULLY1..3, host array
+ * [ntraj]) for one batched launch that mixes the three models; the handle's
+ * own model keeps its parameters, the others use Tully's published values.
+ * Call after nqcd_set_initial.  No counterpart call in the reference, where one
+ * run_dynamics call has one Simulation and so one model: it lets the ensembles
+ * of several Simulations share a launch. */
+int nqcd_set_trajectory_models(nqcd_handle* h, const int32_t* models);
+
+/* MDEF: exact Fermi-weighted force and broadened friction of the model at n
+ * positions (host arrays), the quantities of DiabaticMDEF's acceleration! and
+ * friction! (src/DynamicsMethods/ClassicalMethods/mdef.jl:102-140), evaluated on
+ * the GPU with the handle's precision. */
+int nqcd_mdef_evaluate(nqcd_handle* h, int64_t n, const double* x, double* force, double* friction);
+
+/* MDEF friction surrogate (1-64-64-1 network, BF16 weights): generate npoints
+ * exact friction values at positions uniform in [x_lo, x_hi] with the engine,
+ * then train the network on the GPU (BF16 tensor-core kernels, FP32 master
+ * weights, Adam) for `epochs` passes of minibatches of `batch`.  The trained
+ * network serves runs with use_friction_surrogate inside [x_lo, x_hi].  No
+ * counterpart in the reference.  final_loss: mean squared error of the
+ * predicted Cholesky factor sqrt(Lambda) (may be NULL). */
+int nqcd_train_friction_mlp(nqcd_handle* h, double x_lo, double x_hi, int64_t npoints, int32_t epochs,
+                            int32_t batch, double learning_rate, uint64_t seed, double* final_loss);
+
+/* Surrogate network parameters as FP32, packed W1[64] b1[64] W2[64*64] b2[64]
+ * W3[64] b3[1] (4353 values): get from / set into the handle (set also fixes
+ * the input normalisation x -> (x - shift) * scale and the domain). */
+#define NQCD_MLP_NPARAMS 4353
+int nqcd_mlp_get(nqcd_handle* h, float* params, double* shift_scale_lo_hi);
+int nqcd_mlp_set(nqcd_handle* h, const float* params, const double* shift_scale_lo_hi);
+
+/* Loss and gradient of the surrogate on a host batch (x, target Cholesky
+ * factors), with the device training kernels: for checking them against a
+ * reference implementation.  grad: NQCD_MLP_NPARAMS values. */
+int nqcd_mlp_loss_grad(nqcd_handle* h, int64_t n, const double* x, const double* target_L, double* loss,
+                       float* grad);
 
 /* Accepted hops of the last run, [ntraj][max_hops][3] = (step, from, to), -1 padded
  * (DynamicsOutputs.OutputSurfaceHops, src/DynamicsOutputs.jl:235-243). */

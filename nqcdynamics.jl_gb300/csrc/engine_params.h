@@ -48,6 +48,13 @@ struct FsshParams {
 // Host launchers (one translation unit per precision).
 cudaError_t launch_fssh2_fp64(const FsshParams& p, cudaStream_t s);
 cudaError_t launch_fssh2_fp32(const FsshParams& p, cudaStream_t s);
+cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s);
+
+// Threads per trajectory of the kernel that runs (model, precision): the
+// fast spin-boson kernel spreads the bath over a group of 4 lanes.
+inline int fssh2_lanes_per_traj(int model, int precision) {
+    return (model == 10 /* MODEL_SPINBOSON */ && precision != 0 /* FP64 */) ? 4 : 1;
+}
 cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* out,
                                    cudaStream_t s);
 

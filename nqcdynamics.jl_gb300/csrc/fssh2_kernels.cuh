@@ -118,8 +118,8 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>&
             electronic_macro_step2<double>(fn, t, h, dtsub, s64);
             sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
         } else {
-            Interp32 fn(buf);
-            electronic_macro_step2<float>(fn, t, h, dtsub, sg);
+            InterpS32 fn(buf, t, h);
+            electronic_macro_step2_fast(fn, (float)h, (float)dtsub, sg);
         }
     }
 }

@@ -1,0 +1,296 @@
+// Fast spin-boson FSSH kernel: G lanes per trajectory, bath modes in registers.
+//
+// The spin-boson Hamiltonian V = [[eps + c.R, Delta], [Delta, -eps - c.R]]
+// + R^T W^2 R / 2 makes every per-mode quantity of the reference step a
+// function of two group sums (c.R, R^T W^2 R) and of the 2x2 eigenvectors:
+//   force on mode I on state s:  -(w_I^2 R_I + c_I M_ss) / m_I,
+//     M = Z^T diag(1, -1) Z  (the common part of Z^T dH_I Z),
+//   coupling d_I,01 = c_I M_01 / (E1 - E0),  so  D01 = (c.v) M_01 / gap,
+//   hop probability and momentum rescaling need only c.v and
+//   sum_I c_I^2 / m_I.
+// So each of the G lanes of a trajectory integrates ceil(N/G) modes in
+// registers, the group reduces three sums per step with shuffles, and all
+// G lanes carry the identical 2x2 electronic problem (FP32 Tsit5, FP64 below
+// the gap threshold).  Nothing per step touches HBM.
+//
+// Accumulation of positions and velocities (template Acc):
+//   AccF64  FP64 accumulators (one DFMA per update),
+//   AccKahan FP32 value + FP32 compensation (Kahan summation, four FP32 ops
+//            per update), used because the FP64 pipe of this GPU runs at
+//            1/73 of the FP32 rate (measured).
+// Reference algorithm: fssh2_traj.h (same steps, same random stream).
+#pragma once
+
+#include "fssh2_kernels.cuh"
+
+namespace nqcd {
+
+struct AccF64 {
+    double x;
+    __device__ __forceinline__ void load(double d) { x = d; }
+    __device__ __forceinline__ double get() const { return x; }
+    __device__ __forceinline__ float f() const { return (float)x; }
+    __device__ __forceinline__ void add(float inc) { x += (double)inc; }
+};
+
+struct AccKahan {
+    float s, c;  // value ~ s - c
+    __device__ __forceinline__ void load(double d) {
+        s = (float)d;
+        c = -(float)(d - (double)s);
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+    __device__ __forceinline__ float f() const { return s; }
+    __device__ __forceinline__ void add(float inc) {
+        float y = __fsub_rn(inc, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+
+template <int G>
+__device__ __forceinline__ float group_sum(float x) {
+#pragma unroll
+    for (int off = 1; off < G; off <<= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
+}
+
+constexpr int kSbFastBlock = 128;
+constexpr int kSbGroup = 4;
+
+template <typename Acc, int NPL>
+__global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshParams p) {
+    constexpr int G = kSbGroup;
+    extern __shared__ float4 bath[];  // (c, w2, 1/m, c^2/m) per mode
+    const int nd = p.ndof;
+    for (int I = threadIdx.x; I < G * NPL; I += blockDim.x) {
+        if (I < nd) {
+            double m = p.mass[I];
+            bath[I] = make_float4((float)p.bath_c[I], (float)p.bath_w2[I], (float)(1.0 / m),
+                                  (float)(p.bath_c[I] * p.bath_c[I] / m));
+        } else {
+            bath[I] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    __syncthreads();
+
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane_g = (int)(gt % G);
+    const int64_t i0 = gt / G;
+    const bool active = i0 < p.ntraj;
+    const int64_t i = active ? i0 : p.ntraj - 1;
+    const int64_t gid = p.traj_offset + i;
+    const int64_t N = p.ntraj;
+    const float eps = (float)p.mp[0], Delta = (float)p.mp[1];
+
+    // this lane's modes: I = lane_g + G * j
+    Acc r[NPL], v[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        int I = lane_g + G * j;
+        r[j].load(I < nd ? p.r[(int64_t)I * N + i] : 0.0);
+        v[j].load(I < nd ? p.v[(int64_t)I * N + i] : 0.0);
+    }
+
+    float Z[4] = {1.f, 0.f, 0.f, 1.f};
+    float w[2];
+    float vmean = 0.f;  // eigenvalue mean (energies are shifted by it for the electronics)
+    auto set_eigen = [&](float s0, float cr) {
+        float V0 = 0.5f * s0;
+        float Vs[3] = {(V0 + cr) + eps, Delta, (V0 - cr) - eps};
+        float Zn[4];
+        eigen2_phase<float>(Vs, Z, w, Zn);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Z[q] = Zn[q];
+        vmean = V0;
+    };
+
+    float s0 = 0.f, cr = 0.f, ke = 0.f;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        float4 b = bath[lane_g + G * j];
+        float x = r[j].f(), vv = v[j].f();
+        s0 += b.y * x * x;
+        cr += b.x * x;
+        ke += vv * vv / b.z;
+    }
+    s0 = group_sum<G>(s0);
+    cr = group_sum<G>(cr);
+    ke = group_sum<G>(ke);
+    set_eigen(s0, cr);
+    Sig2<float> sg;
+    int state;
+    init_electronics2<float>(p, i, gid, Z, sg, state);
+    double e0 = 0.5 * (double)ke + (double)w[state];
+    float Mk = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];  // M_ss of the cached force
+
+    double pop0[2] = {0.0, 0.0};
+    int isave = 0;
+    const bool lead = lane_g == 0;
+    if (p.save_stride > 0) {
+        diabatic_pop2<float>(sg, state, Z, pop0);
+        warp_save_popcorr(p, isave++, active && lead, pop0, pop0);
+    }
+
+    EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
+    int nh = 0, nf = 0, step = 0;
+    double t = p.t0;
+    float cv = 0.f;
+    while (t < p.t1) {
+        const double hd = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
+        const float h = (float)hd, half = 0.5f * h;
+        // B (cached force) and A
+        s0 = 0.f;
+        cr = 0.f;
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+            float4 b = bath[lane_g + G * j];
+            float x = r[j].f();
+            float k = -(b.y * x + b.x * Mk) * b.z;
+            v[j].add(half * k);
+            r[j].add(h * v[j].f());
+            float xn = r[j].f();
+            s0 += b.y * xn * xn;
+            cr += b.x * xn;
+        }
+        s0 = group_sum<G>(s0);
+        cr = group_sum<G>(cr);
+        float Eold0 = w[0], Eold1 = w[1];
+        (void)Eold0;
+        (void)Eold1;
+        set_eigen(s0, cr);
+        const float gap = w[1] - w[0];
+        const float M01 = Z[0] * Z[2] - Z[1] * Z[3];
+        Mk = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];
+        // B with the new force; c.v
+        cv = 0.f;
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+            float4 b = bath[lane_g + G * j];
+            float x = r[j].f();
+            float k = -(b.y * x + b.x * Mk) * b.z;
+            v[j].add(half * k);
+            cv += b.x * v[j].f();
+        }
+        cv = group_sum<G>(cv);
+        const float dscale = M01 / gap;  // d_I,01 = c_I * dscale
+        buf.E0c = buf.E0n;
+        buf.E1c = buf.E1n;
+        buf.Dc = buf.Dn;
+        buf.tc = buf.tn;
+        buf.E0n = w[0] - vmean;
+        buf.E1n = w[1] - vmean;
+        buf.Dn = cv * dscale;
+        buf.tn = t + hd;
+        electronics2<float>(p, buf, t, hd, gap, sg);
+        t = snap_time(t + hd, p.t1);
+        step += 1;
+
+        // hop test (identical in all G lanes of the group)
+        const int s = state;
+        float re = sg.x / (s == 0 ? sg.p : sg.q);
+        float nsm = (s == 0 ? 1.0f : -1.0f) * cv * dscale;
+        float prob = clamp01<float>(2.0f * re * nsm * (float)p.dt);
+        float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
+        if (prob > u) {
+            const int ns = 1 - s;
+            const float sgn = ns < s ? 1.0f : -1.0f;  // d(new, old) = sgn * c_I * dscale
+            bool accept = true;
+            if (p.rescaling != RESCALE_OFF) {
+                double aa = 0.5 * (double)dscale * (double)dscale * p.sum_c2_over_m;
+                double bb = (double)sgn * (double)dscale * (double)cv;
+                double cc = (double)w[ns] - (double)w[s];
+                double disc = bb * bb - 4.0 * aa * cc;
+                if (disc < 0.0) {
+                    accept = false;
+                    if (p.rescaling == RESCALE_VINVERSION) {
+                        // v -= 2 (v.n) n with n = d/|d|, |d|^2 = dscale^2 sum c^2; v.d = sgn dscale c.v
+                        double c2 = 0.0;
+                        for (int I = 0; I < nd; ++I) c2 += (double)bath[I].x * bath[I].x;
+                        float coef = (float)(2.0 * (double)cv / c2);  // 2 (v.d) d_I / |d|^2 = coef * c_I
+#pragma unroll
+                        for (int j = 0; j < NPL; ++j) v[j].add(-coef * bath[lane_g + G * j].x);
+                    }
+                } else {
+                    double root = sqrt(disc);
+                    double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
+                    float coef = (float)(gamma * (double)sgn * (double)dscale);  // gamma d_I / m_I = coef c_I / m_I
+#pragma unroll
+                    for (int j = 0; j < NPL; ++j) {
+                        float4 b = bath[lane_g + G * j];
+                        v[j].add(-coef * b.x * b.z);
+                    }
+                }
+            }
+            if (accept) {
+                log_hop(p, active && lead, i, nh, step, s, ns);
+                nh += 1;
+                state = ns;
+            } else {
+                nf += 1;
+            }
+        }
+        if (p.save_stride > 0 && step % p.save_stride == 0) {
+            double pop[2];
+            diabatic_pop2<float>(sg, state, Z, pop);
+            warp_save_popcorr(p, isave++, active && lead, pop0, pop);
+        }
+    }
+
+    // final state
+    ke = 0.f;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        float vv = v[j].f();
+        ke += vv * vv / bath[lane_g + G * j].z;
+    }
+    ke = group_sum<G>(ke);
+    if (!active) return;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        int I = lane_g + G * j;
+        if (I < nd) {
+            p.r[(int64_t)I * N + i] = r[j].get();
+            p.v[(int64_t)I * N + i] = v[j].get();
+        }
+    }
+    if (!lead) return;
+    write_sigma<float>(p, i, sg);
+    p.state[i] = state;
+    if (p.nhops) p.nhops[i] = nh;
+    if (p.nfrustrated) p.nfrustrated[i] = nf;
+    if (p.nsteps) p.nsteps[i] = step;
+    if (p.energy) {
+        p.energy[i] = e0;
+        p.energy[N + i] = 0.5 * (double)ke + (double)w[state];
+    }
+    if (p.scatter) atomicAdd(p.scatter + (p.r[i] > 0.0 ? 2 : 0) + state, 1ull);
+}
+
+template <typename Acc, int NPL>
+cudaError_t launch_sb_fast_npl(const FsshParams& p, cudaStream_t s) {
+    int64_t threads = p.ntraj * kSbGroup;
+    int64_t blocks = (threads + kSbFastBlock - 1) / kSbFastBlock;
+    size_t shmem = sizeof(float4) * kSbGroup * NPL;
+    fssh2_sb_fast_kernel<Acc, NPL><<<(unsigned)blocks, kSbFastBlock, shmem, s>>>(p);
+    return cudaGetLastError();
+}
+
+// modes per lane rounded up to an instantiated size
+template <typename Acc>
+cudaError_t launch_sb_fast(const FsshParams& p, cudaStream_t s) {
+    if (p.ntraj <= 0) return cudaSuccess;
+    int need = (p.ndof + kSbGroup - 1) / kSbGroup;
+    if (need <= 1) return launch_sb_fast_npl<Acc, 1>(p, s);
+    if (need <= 2) return launch_sb_fast_npl<Acc, 2>(p, s);
+    if (need <= 4) return launch_sb_fast_npl<Acc, 4>(p, s);
+    if (need <= 8) return launch_sb_fast_npl<Acc, 8>(p, s);
+    if (need <= 16) return launch_sb_fast_npl<Acc, 16>(p, s);
+    if (need <= 25) return launch_sb_fast_npl<Acc, 25>(p, s);
+    if (need <= 32) return launch_sb_fast_npl<Acc, 32>(p, s);
+    if (need <= 64) return launch_sb_fast_npl<Acc, 64>(p, s);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace nqcd

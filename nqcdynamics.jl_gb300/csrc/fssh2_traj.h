@@ -162,6 +162,95 @@ NQCD_HD void electronic_macro_step2(const F& fn, double t, double h, double dtsu
     }
 }
 
+// Fast path, FP32 only: the macro step [t, t + h] lies inside the DoubleBuffer
+// interval [tc, tn] (equal to it except in the first step of a run that does
+// not start at t = 0), so the interpolation parameter of a stage is
+// sa + sb * sigma with sigma in [0, 1] the position inside the macro step and
+// sa = (t - tc) / (tn - tc), sb = h / (tn - tc) formed once per macro step.
+// No FP64 work per stage.
+struct InterpS32 {
+    float E0c, E1c, Dc, dE0, dE1, dD, sa, sb;
+    NQCD_HD InterpS32(const EBuf<float>& b, double t, double h) : E0c(b.E0c), E1c(b.E1c), Dc(b.Dc),
+        dE0(b.E0n - b.E0c), dE1(b.E1n - b.E1c), dD(b.Dn - b.Dc) {
+        double den = b.tn - b.tc;
+        sa = den != 0.0 ? (float)((t - b.tc) / den) : 0.f;
+        sb = den != 0.0 ? (float)(h / den) : 0.f;
+    }
+    NQCD_HD Sig2<float> f(float sigma, const Sig2<float>& u) const {
+        float s = sa + sb * sigma;
+        float D = Dc + dD * s;
+        float E0 = E0c + dE0 * s;
+        float E1 = E1c + dE1 * s;
+        return rhs2<float>(E0, E1, D, u);
+    }
+};
+
+// Tsit5 step in macro-step coordinates: stage positions sigma0 + c * hr,
+// step length hr * h in time.
+template <typename F>
+NQCD_HD void tsit5_step2_s(const F& fn, float sigma0, float hr, float h, Sig2<float>& u, Sig2<float>& k1) {
+    typedef Tsit5 TS;
+    const float hs = hr * h;
+    Sig2<float> tmp, k2, k3, k4, k5, k6;
+#define NQCD_TS_COMB_S(dst, EXPR)              \
+    {                                          \
+        dst.p = u.p + hs * (EXPR(p));          \
+        dst.q = u.q + hs * (EXPR(q));          \
+        dst.x = u.x + hs * (EXPR(x));          \
+        dst.y = u.y + hs * (EXPR(y));          \
+    }
+#define E2(c) ((float)TS::a21 * k1.c)
+    NQCD_TS_COMB_S(tmp, E2);
+#undef E2
+    k2 = fn.f(sigma0 + (float)TS::c2 * hr, tmp);
+#define E3(c) ((float)TS::a31 * k1.c + (float)TS::a32 * k2.c)
+    NQCD_TS_COMB_S(tmp, E3);
+#undef E3
+    k3 = fn.f(sigma0 + (float)TS::c3 * hr, tmp);
+#define E4(c) ((float)TS::a41 * k1.c + (float)TS::a42 * k2.c + (float)TS::a43 * k3.c)
+    NQCD_TS_COMB_S(tmp, E4);
+#undef E4
+    k4 = fn.f(sigma0 + (float)TS::c4 * hr, tmp);
+#define E5(c) ((float)TS::a51 * k1.c + (float)TS::a52 * k2.c + (float)TS::a53 * k3.c + (float)TS::a54 * k4.c)
+    NQCD_TS_COMB_S(tmp, E5);
+#undef E5
+    k5 = fn.f(sigma0 + (float)TS::c5 * hr, tmp);
+#define E6(c)                                                                                                  \
+    ((float)TS::a61 * k1.c + (float)TS::a62 * k2.c + (float)TS::a63 * k3.c + (float)TS::a64 * k4.c + \
+     (float)TS::a65 * k5.c)
+    NQCD_TS_COMB_S(tmp, E6);
+#undef E6
+    k6 = fn.f(sigma0 + hr, tmp);
+#define E7(c)                                                                                                  \
+    ((float)TS::a71 * k1.c + (float)TS::a72 * k2.c + (float)TS::a73 * k3.c + (float)TS::a74 * k4.c + \
+     (float)TS::a75 * k5.c + (float)TS::a76 * k6.c)
+    NQCD_TS_COMB_S(tmp, E7);
+#undef E7
+#undef NQCD_TS_COMB_S
+    k1 = fn.f(sigma0 + hr, tmp);
+    u = tmp;
+}
+
+// Fast-path macro step: sub-steps of dtsub (the last one shortened), in FP32.
+NQCD_HD void electronic_macro_step2_fast(const InterpS32& fn, float h, float dtsub, Sig2<float>& u) {
+    const float fs = dtsub / h;
+    Sig2<float> k1 = fn.f(0.f, u);
+    float s0 = 0.f;
+    for (int guard = 0; s0 < 1.f && guard < 64; ++guard) {
+        float hr = (1.f - s0) < fs ? (1.f - s0) : fs;
+        tsit5_step2_s(fn, s0, hr, h, u, k1);
+        s0 = s0 + hr;
+        if (1.f - s0 < 1e-6f) s0 = 1.f;
+    }
+}
+
+// 24-bit uniform in [0, 1) from the same Philox block as rng_uniform (the
+// fast path compares in FP32; it differs from the 53-bit draw only below 2^-24).
+NQCD_HD float rng_uniform_f(uint64_t seed, uint64_t traj, uint32_t step, uint32_t stream) {
+    u32x4 b = rng_block(seed, traj, step, stream);
+    return (float)(b.x >> 8) * 0x1.0p-24f;
+}
+
 // clamp(x, 0, 1) with the reference's NaN propagation.
 template <typename R>
 NQCD_HD R clamp01(R x) {

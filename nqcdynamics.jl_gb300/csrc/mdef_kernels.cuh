@@ -1,0 +1,409 @@
+// MDEF (electronic-friction Langevin dynamics) on the Newns-Anderson model,
+// one warp per trajectory.
+//
+// Reference algorithm (NQCDynamics.jl):
+//   MDEF_BAOAB.perform_step!    src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:338-355
+//   step_O! (friction eigenbasis) src/DynamicsMethods/IntegrationAlgorithms/steps.jl:128-156
+//   DiabaticMDEF acceleration!  src/DynamicsMethods/ClassicalMethods/mdef.jl:102-124
+//   friction! (Lambda / sqrt(m)sqrt(m)^T) src/DynamicsMethods/ClassicalMethods/mdef.jl:131-140
+// The reference diagonalises the (1 + M)-state one-electron Hamiltonian
+//     H = [[h(x), V_k], [V_k, diag(e_k)]]     (AndersonHolstein)
+// with LAPACK at every force and friction evaluation.  This Hamiltonian is
+// an arrowhead matrix with x-independent border, so its eigenvalues are the
+// roots of the secular function
+//     f(l) = l - h - sum_k V_k^2 / (l - e_k),
+// one in each interval between consecutive bath levels plus one on each side,
+// and the impurity weights of the eigenvectors are z0_i^2 = 1 / f'(l_i).
+// Because dH/dx = h'(x) e0 e0^T, the Fermi-weighted force and the broadened
+// friction need only (l_i, z0_i^2):
+//     F = U0'(x) + h' sum_i z0_i^2 (f_i + f'_i l_i),
+//     Lambda = -pi h'^2 sum_nm z0_n^2 z0_m^2 g_sigma(l_n - l_m) f'(l_n).
+// So each of the 32 lanes owns roots i = lane, lane + 32, ... and solves them
+// by bracketed Newton measured from the nearer pole (accurate next to a pole),
+// warm-started from the previous evaluation.
+//
+// R = double: plain FP64 (all terms of the friction double sum).
+// R = float : fast path; Fermi factors below 1e-12 of their maximum and
+//             Gaussian factors beyond 8 sigma are skipped; optional friction
+//             surrogate network (BF16 weights, FP32 arithmetic) in place of the
+//             midpoint electronic evaluation.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "nqcd_math.h"
+
+namespace nqcd {
+
+constexpr int kMdefMaxBath = 512;
+constexpr int kMdefRootsPerLane = (kMdefMaxBath + 1 + 31) / 32;
+constexpr int kMdefWarps = 4;  // trajectories per block
+
+struct MlpWeights {
+    // 1-64-64-1 network, SiLU activations, output = softplus -> Cholesky factor L, Lambda = L^2
+    const __nv_bfloat16* W1;  // [64]
+    const __nv_bfloat16* b1;  // [64]
+    const __nv_bfloat16* W2;  // [64][64] row-major (out, in)
+    const __nv_bfloat16* b2;  // [64]
+    const __nv_bfloat16* W3;  // [64]
+    const __nv_bfloat16* b3;  // [1]
+    float x_shift, x_scale;   // input normalisation
+    float lo, hi;             // training domain (outside: exact friction)
+};
+
+struct MdefParams {
+    int32_t nbath;
+    const double* eps;   // [nbath] ascending
+    const double* V2;    // [nbath] V_k^2
+    double k, g, delta;  // impurity: U0 = k x^2/2, h = k g (g/2 - x) + delta
+    double mu, beta, sigma;
+    double mass;
+    int64_t ntraj, traj_offset;
+    double dt;
+    int32_t nsteps;
+    uint64_t seed;
+    int32_t save_stride, nsave;
+    int32_t use_mlp;        // fast path: friction from the surrogate inside its domain
+    int32_t judge_every;    // fast path with surrogate: exact friction every k steps (0 = never)
+    MlpWeights mlp;
+    double* x;              // [ntraj] in/out
+    double* v;              // [ntraj] in/out
+    double* energy;         // [2][ntraj] (initial, final) or null
+    double* obs_partial;    // [nwarps_total][nsave][4] (<x>, <x^2>, <KE>, <Lambda>)
+    unsigned long long* counters;  // [0] exact friction evaluations, [1] surrogate evaluations, [2] non-converged roots
+    double* friction_out;   // optional: exact friction at x (single evaluation mode), [ntraj]
+    double* force_out;      // optional: force at x, [ntraj]
+};
+
+template <typename R>
+struct MdefShared {
+    R eps[kMdefMaxBath];
+    R V2[kMdefMaxBath];
+    R lam[kMdefWarps][kMdefMaxBath + 1];
+    R z2[kMdefWarps][kMdefMaxBath + 1];
+};
+
+template <typename R>
+__device__ __forceinline__ R mdef_rcp(R d) {
+    if constexpr (std::is_same<R, float>::value)
+        return __frcp_rn(d);
+    else
+        return 1.0 / d;
+}
+
+template <typename R>
+__device__ __forceinline__ R mdef_exp(R x) {
+    if constexpr (std::is_same<R, float>::value)
+        return __expf(x);
+    else
+        return nqcd_exp(x);
+}
+
+// Fermi function and its derivative, f = 1/(1+e^{b(e-mu)}), f' = -b f (1-f).
+template <typename R>
+__device__ __forceinline__ void fermi_pair(R e, R mu, R beta, R& f, R& df) {
+    R z = beta * (e - mu);
+    if (z > R(0)) {
+        R ez = mdef_exp<R>(-z);
+        f = ez / (R(1) + ez);
+    } else {
+        R ez = mdef_exp<R>(z);
+        f = R(1) / (R(1) + ez);
+    }
+    df = -beta * f * (R(1) - f);
+}
+
+// Solve root i of the secular equation.  o = origin pole, d = offset from it,
+// (dlo, dhi) = bracket of d.  Returns l = o + d and z0^2 = 1/f'.
+template <typename R>
+__device__ __forceinline__ void secular_root(const MdefShared<R>& sh, int M, int i, R h, R Lbound, R& lam_io,
+                                             R& z2_out, unsigned long long* nonconv) {
+    // interval of root i
+    const bool first = i == 0, last = i == M;
+    R a = first ? sh.eps[0] : sh.eps[i - 1];
+    R b = last ? sh.eps[M - 1] : sh.eps[i];
+    int jo;  // origin pole index
+    R o, dlo, dhi;
+    if (first) {
+        jo = 0;
+        o = a;
+        dlo = -Lbound;
+        dhi = R(0);
+    } else if (last) {
+        jo = M - 1;
+        o = b;
+        dlo = R(0);
+        dhi = Lbound;
+    } else {
+        // which half: sign of f at the midpoint decides the nearer pole
+        R mid = a + R(0.5) * (b - a);
+        R s = R(0);
+        for (int k = 0; k < M; ++k) s += sh.V2[k] * mdef_rcp<R>(mid - sh.eps[k]);
+        R fm = mid - h - s;
+        if (fm > R(0)) {  // root in (a, mid): measure from a
+            jo = i - 1;
+            o = a;
+            dlo = R(0);
+            dhi = mid - a;
+        } else {
+            jo = i;
+            o = b;
+            dlo = mid - b;
+            dhi = R(0);
+        }
+    }
+    // warm start from the previous root if it lies in the bracket
+    R d = lam_io - o;
+    if (!(d > dlo && d < dhi)) d = R(0.5) * (dlo + dhi);
+    R fp = R(1);
+    bool conv = false;
+    for (int it = 0; it < 80; ++it) {
+        R s1 = R(0), s2 = R(0), sa = R(0);
+        for (int k = 0; k < M; ++k) {
+            R den = (k == jo) ? d : (o - sh.eps[k]) + d;
+            R t = mdef_rcp<R>(den);
+            R vt = sh.V2[k] * t;
+            s1 += vt;
+            s2 += vt * t;
+            sa += fabs(vt);
+        }
+        R f = (o + d) - h - s1;
+        fp = R(1) + s2;
+        if (f == R(0)) {  // exact root: keep d (a bisection here would leave it)
+            conv = true;
+            break;
+        }
+        if (f > R(0))
+            dhi = d;
+        else
+            dlo = d;
+        R dn = d - f / fp;
+        // the Newton point may equal the bracket end just set (a step below
+        // one ulp): that is convergence, not a reason to bisect
+        if (!(dn >= dlo && dn <= dhi)) dn = R(0.5) * (dlo + dhi);
+        R step = dn - d;
+        d = dn;
+        const R ulp = std::is_same<R, float>::value ? R(1.2e-7) : R(2.3e-16);
+        R tol = R(2) * ulp * (fabs(d) + fabs(o) * R(1e-3));
+        // f has reached the rounding error of its own evaluation: no further
+        // Newton step can be trusted (the secular-equation stopping test)
+        R ferr = ulp * (fabs(o + d) + fabs(h) + sa);
+        if (fabs(step) <= tol || dhi - dlo <= tol || fabs(f) <= ferr) {
+            conv = true;
+            break;
+        }
+    }
+    if (!conv && nonconv) atomicAdd(nonconv, 1ull);
+    lam_io = o + d;
+    z2_out = R(1) / fp;
+}
+
+// Electronic structure at x for the warp's trajectory: all roots, force and
+// (optionally) friction.  Roots and weights are also left in shared memory.
+template <typename R>
+__device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib, R lam[kMdefRootsPerLane],
+                                double x, bool want_friction, double& force, double& friction) {
+    const int lane = threadIdx.x & 31;
+    const int M = p.nbath;
+    const R h = (R)(p.k * p.g * (p.g / 2.0 - x) + p.delta);
+    const R dh = (R)(-p.k * p.g);
+    const R mu = (R)p.mu, beta = (R)p.beta;
+    R Lb = fabs(h) + R(2);
+    R accF = R(0);
+#pragma unroll
+    for (int q = 0; q < kMdefRootsPerLane; ++q) {
+        int i = lane + 32 * q;
+        if (i <= M) {
+            R z2;
+            secular_root<R>(sh, M, i, h, Lb, lam[q], z2, p.counters ? p.counters + 2 : nullptr);
+            R f, df;
+            fermi_pair<R>(lam[q], mu, beta, f, df);
+            accF += z2 * (f + df * lam[q]);
+            sh.lam[wib][i] = lam[q];
+            sh.z2[wib][i] = z2;
+        }
+    }
+    double sF = (double)accF;
+    for (int off = 16; off > 0; off >>= 1) sF += __shfl_xor_sync(0xffffffffu, sF, off);
+    force = p.k * x + (double)dh * sF;
+    friction = 0.0;
+    if (!want_friction) return;
+    __syncwarp();
+    const R inv_s2 = R(0.5) / (R)(p.sigma * p.sigma);
+    const R norm = R(1) / ((R)p.sigma * R(2.5066282746310002));  // 1/(sigma sqrt(2 pi))
+    R acc = R(0);
+    for (int n = lane; n <= M; n += 32) {
+        R ln = sh.lam[wib][n];
+        R f, df;
+        fermi_pair<R>(ln, mu, beta, f, df);
+        if constexpr (std::is_same<R, float>::value) {
+            if (fabsf(df) < 1e-12f * beta) continue;  // negligible Fermi derivative
+        }
+        R zn = sh.z2[wib][n];
+        R inner = R(0);
+        for (int m = 0; m <= M; ++m) {
+            R de = ln - sh.lam[wib][m];
+            if constexpr (std::is_same<R, float>::value) {
+                if (fabsf(de) > 8.0f * (float)p.sigma) continue;
+            }
+            inner += sh.z2[wib][m] * mdef_exp<R>(-de * de * inv_s2);
+        }
+        acc += zn * inner * df;
+    }
+    double sacc = (double)acc;
+    for (int off = 16; off > 0; off >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, off);
+    friction = -3.14159265358979323846 * (double)dh * (double)dh * (double)norm * sacc;
+    __syncwarp();
+}
+
+// Surrogate friction: 1-64-64-1 network, BF16 weights, FP32 arithmetic; each
+// lane computes two hidden units per layer.
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+
+__device__ inline float mlp_friction(const MlpWeights& w, float x) {
+    const int lane = threadIdx.x & 31;
+    float u = (x - w.x_shift) * w.x_scale;
+    // hidden layer 1 rounded to BF16, as the tensor-core training kernel sees it
+    float h1a = __bfloat162float(__float2bfloat16(silu(__bfloat162float(w.W1[lane]) * u + __bfloat162float(w.b1[lane]))));
+    float h1b = __bfloat162float(
+        __float2bfloat16(silu(__bfloat162float(w.W1[lane + 32]) * u + __bfloat162float(w.b1[lane + 32]))));
+    float za = __bfloat162float(w.b2[lane]), zb = __bfloat162float(w.b2[lane + 32]);
+#pragma unroll 8
+    for (int j = 0; j < 32; ++j) {
+        float hj0 = __shfl_sync(0xffffffffu, h1a, j);
+        float hj1 = __shfl_sync(0xffffffffu, h1b, j);
+        za += __bfloat162float(w.W2[lane * 64 + j]) * hj0 + __bfloat162float(w.W2[lane * 64 + 32 + j]) * hj1;
+        zb += __bfloat162float(w.W2[(lane + 32) * 64 + j]) * hj0 + __bfloat162float(w.W2[(lane + 32) * 64 + 32 + j]) * hj1;
+    }
+    float o = __bfloat162float(w.W3[lane]) * silu(za) + __bfloat162float(w.W3[lane + 32]) * silu(zb);
+    for (int off = 16; off > 0; off >>= 1) o += __shfl_xor_sync(0xffffffffu, o, off);
+    o += __bfloat162float(w.b3[0]);
+    float L = o > 20.f ? o : log1pf(__expf(o));  // softplus
+    return L * L;
+}
+
+// Standard normal of (trajectory, step): Box-Muller on one Philox block.
+__device__ __forceinline__ double noise_normal(uint64_t seed, uint64_t traj, uint32_t step) {
+    u32x4 b = rng_block(seed, traj, step, RNG_NOISE);
+    double u1 = 1.0 - u01_from_words(b.x, b.y);
+    double u2 = u01_from_words(b.z, b.w);
+    return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams p) {
+    __shared__ MdefShared<R> sh;
+    for (int k = threadIdx.x; k < p.nbath; k += blockDim.x) {
+        sh.eps[k] = (R)p.eps[k];
+        sh.V2[k] = (R)p.V2[k];
+    }
+    __syncthreads();
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t w0 = (int64_t)blockIdx.x * kMdefWarps + wib;
+    const bool active = w0 < p.ntraj;
+    const int64_t i = active ? w0 : p.ntraj - 1;
+    const uint64_t gid = (uint64_t)(p.traj_offset + i);
+    const int M = p.nbath;
+    R lam[kMdefRootsPerLane];
+#pragma unroll
+    for (int q = 0; q < kMdefRootsPerLane; ++q) {  // initial guesses: just above each pole
+        int idx = lane + 32 * q;
+        lam[q] = idx == 0 ? sh.eps[0] - R(1e-3) : (idx <= M ? sh.eps[idx - 1] + R(1e-9) : R(0));
+    }
+    double x = p.x[i], v = p.v[i];
+    const double m = p.mass, T = 1.0 / p.beta, dt = p.dt, half = 0.5;
+    double F, fr;
+    mdef_electronic<R>(p, sh, wib, lam, x, p.friction_out != nullptr, F, fr);
+    if (p.force_out || p.friction_out) {  // single-evaluation mode (force/friction tables, training data)
+        if (active && lane == 0) {
+            if (p.force_out) p.force_out[i] = F;
+            if (p.friction_out) p.friction_out[i] = fr;
+        }
+        return;
+    }
+    double k = -F / m;
+    // total energy with the potential of DiabaticMDEF, U0 + sum_i l_i f_i
+    // (mdef.jl:162-175), from the roots of the last electronic evaluation at x
+    auto total_energy = [&]() {
+        R acc = R(0);
+        for (int n = lane; n <= M; n += 32) {
+            R f, df;
+            fermi_pair<R>(sh.lam[wib][n], (R)p.mu, (R)p.beta, f, df);
+            acc += sh.lam[wib][n] * f;
+        }
+        double s = (double)acc;
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        return 0.5 * m * v * v + 0.5 * p.k * x * x + s;
+    };
+    const double e0 = p.energy ? total_energy() : 0.0;
+    int isave = 0;
+    auto save = [&](double lamv) {
+        if (p.save_stride <= 0) return;
+        if (lane == 0 && active && isave < p.nsave) {
+            double* dst = p.obs_partial + ((int64_t)(blockIdx.x * kMdefWarps + wib) * p.nsave + isave) * 4;
+            dst[0] = x;
+            dst[1] = x * x;
+            dst[2] = 0.5 * m * v * v;
+            dst[3] = lamv;
+        }
+        ++isave;
+    };
+    save(0.0);
+    unsigned long long n_exact = 0, n_mlp = 0;
+    for (int step = 1; step <= p.nsteps; ++step) {
+        v = v + (half * dt) * k;  // B
+        x = x + (half * dt) * v;  // A
+        double lamv;
+        bool use_net = false;
+        if constexpr (std::is_same<R, float>::value) {
+            use_net = p.use_mlp && (float)x >= p.mlp.lo && (float)x <= p.mlp.hi &&
+                      !(p.judge_every > 0 && step % p.judge_every == 0);
+        }
+        if (use_net) {
+            lamv = (double)mlp_friction(p.mlp, (float)x);
+            ++n_mlp;
+        } else {
+            double Fm;
+            mdef_electronic<R>(p, sh, wib, lam, x, true, Fm, lamv);
+            ++n_exact;
+        }
+        double gam = lamv / m;  // friction / (sqrt m sqrt m)
+        if (gam < 0.0) gam = 0.0;
+        double c1 = exp(-gam * dt);
+        double c2 = sqrt(1.0 - c1 * c1);
+        double xi = noise_normal(p.seed, gid, (uint32_t)step);
+        v = c1 * v + c2 * (sqrt(T / m) * xi);  // O
+        x = x + (half * dt) * v;                // A
+        double Fn, dummy;
+        mdef_electronic<R>(p, sh, wib, lam, x, false, Fn, dummy);
+        k = -Fn / m;
+        v = v + (half * dt) * k;  // B
+        if (p.save_stride > 0 && step % p.save_stride == 0) save(lamv);
+    }
+    const double e1 = p.energy ? total_energy() : 0.0;
+    if (!active || lane != 0) return;
+    p.x[i] = x;
+    p.v[i] = v;
+    if (p.energy) {
+        p.energy[i] = e0;
+        p.energy[p.ntraj + i] = e1;
+    }
+    if (p.counters) {
+        atomicAdd(p.counters + 0, n_exact);
+        atomicAdd(p.counters + 1, n_mlp);
+    }
+}
+
+template <typename R>
+cudaError_t launch_mdef(const MdefParams& p, cudaStream_t s) {
+    if (p.ntraj <= 0) return cudaSuccess;
+    if (p.nbath > kMdefMaxBath || p.nbath < 1) return cudaErrorInvalidValue;
+    int64_t blocks = (p.ntraj + kMdefWarps - 1) / kMdefWarps;
+    mdef_kernel<R><<<(unsigned)blocks, 32 * kMdefWarps, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace nqcd

@@ -16,10 +16,27 @@
 #include "engine_params.h"
 #include "nqcd_math.h"
 #include "nqcd_models.h"
+#include "mlp.h"
+#include "ring_polymer.h"
+#include "rpsh_kernels.cuh"
 
 using namespace nqcd;
 
+namespace nqcd {
+int rpsh_grid_fp64();
+int rpsh_grid_fp32();
+cudaError_t launch_rpsh_fp64(const RpshParams& p, int blocks, cudaStream_t s);
+cudaError_t launch_rpsh_fp32(const RpshParams& p, int blocks, cudaStream_t s);
+cudaError_t launch_mdef_fp64(const MdefParams& p, cudaStream_t s);
+cudaError_t launch_mdef_fp32(const MdefParams& p, cudaStream_t s);
+}  // namespace nqcd
+
 namespace {
+
+// bead counts with an instantiated ring-polymer kernel
+constexpr int kRpCounts[] = {1, 2, 4, 5, 8, 10, 16, 32};
+constexpr int kNumRpCounts = 8;
+constexpr int kMaxRpGrid = 8192;
 
 thread_local std::string g_create_error;
 
@@ -131,6 +148,7 @@ struct nqcd_handle {
     int64_t ndof = 0;  // per trajectory (ndofs * natoms)
     int nstates = 2;
     std::vector<double> params;
+    double mass0 = 0.0;  // mass of the first atom (ring polymers: the one atom)
     double sum_c2_over_m = 0.0;
     bool initial_set = false;
     bool has_run = false;
@@ -149,6 +167,21 @@ struct nqcd_handle {
     unsigned long long* d_counts = nullptr;  // [0..3] scatter, [4..7] stats
     double* d_stage = nullptr;               // staging for layout gathers
     int64_t stage_cap = 0;
+    // ring polymers: normal-mode tables per instantiated bead count, bead-count classes
+    int64_t rp_U_off[kNumRpCounts] = {0};
+    double *d_rpU = nullptr, *d_rpcay = nullptr;
+    float *d_rpUf = nullptr, *d_rpcayf = nullptr;
+    int32_t *d_nbeads = nullptr, *d_class_traj = nullptr, *d_block_class = nullptr;
+    unsigned long long* d_queue = nullptr;
+    int nclass = 0;
+    int class_beads[kRpshMaxClasses] = {0};
+    int class_slot[kRpshMaxClasses] = {0};  // index into kRpCounts
+    int class_model[kRpshMaxClasses] = {0};
+    int64_t class_begin[kRpshMaxClasses + 1] = {0};
+    std::vector<int32_t> traj_beads, traj_models;  // host copies (ring polymers)
+    // MDEF: bath levels and squared couplings; friction surrogate
+    double *d_eps = nullptr, *d_V2 = nullptr;
+    MlpState mlp;
 };
 
 namespace {
@@ -182,9 +215,12 @@ cudaError_t dalloc(T** p, int64_t n) {
 void free_all(nqcd_handle* h) {
     void* ptrs[] = {h->d_mass, h->d_bath_c, h->d_bath_w2, h->d_r0, h->d_v0, h->d_r, h->d_v, h->d_sig0,
                     h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
-                    h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage};
+                    h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
+                    h->d_rpU, h->d_rpcay, h->d_rpUf, h->d_rpcayf, h->d_nbeads, h->d_class_traj,
+                    h->d_block_class, h->d_queue, h->d_eps, h->d_V2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    mlp_free(h->mlp);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->evk0) cudaEventDestroy(h->evk0);
@@ -213,6 +249,38 @@ int64_t count_steps(double t0, double t1, double dt) {
     return n;
 }
 
+// MDEF launch parameters of a handle (device pointers of the handle).
+MdefParams mdef_params(nqcd_handle* h, int64_t N, double dt, int32_t nsteps, uint64_t seed, int stride, int nsave) {
+    MdefParams m;
+    memset(&m, 0, sizeof(m));
+    m.nbath = h->cfg.nbath;
+    m.eps = h->d_eps;
+    m.V2 = h->d_V2;
+    m.k = h->params[0];
+    m.g = h->params[1];
+    m.delta = h->params[2];
+    m.mu = h->params[3];
+    m.sigma = h->params[4];
+    m.beta = h->cfg.beta;
+    m.mass = h->mass0;
+    m.ntraj = N;
+    m.traj_offset = h->cfg.traj_offset;
+    m.dt = dt;
+    m.nsteps = nsteps;
+    m.seed = seed;
+    m.save_stride = stride;
+    m.nsave = nsave;
+    m.use_mlp = (h->cfg.use_friction_surrogate && h->cfg.precision != NQCD_PREC_FP64) ? 1 : 0;
+    m.judge_every = h->cfg.judge_every;
+    m.mlp = mlp_view(h->mlp);
+    m.x = h->d_r;
+    m.v = h->d_v;
+    m.energy = h->d_energy;
+    m.obs_partial = h->d_partial;
+    m.counters = h->d_counts + 8;
+    return m;
+}
+
 }  // namespace
 
 extern "C" {
@@ -222,14 +290,35 @@ int nqcd_version(void) { return NQCD_ABI_VERSION; }
 int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     if (!cfg || !out) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: null argument");
     *out = nullptr;
-    if (cfg->method != NQCD_METHOD_FSSH)
+    if (cfg->method != NQCD_METHOD_FSSH && cfg->method != NQCD_METHOD_RPSH && cfg->method != NQCD_METHOD_MDEF)
         return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: method not supported by this build");
+    const bool rp = cfg->method == NQCD_METHOD_RPSH;
+    const bool mdef = cfg->method == NQCD_METHOD_MDEF;
     const int model = cfg->model;
-    if (model != NQCD_MODEL_TULLY1 && model != NQCD_MODEL_TULLY2 && model != NQCD_MODEL_TULLY3 &&
-        model != NQCD_MODEL_SPINBOSON)
-        return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: unknown model");
-    if (cfg->nstates != 2) return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: only two-state models");
-    if (cfg->precision != NQCD_PREC_FP64 && cfg->precision != NQCD_PREC_FP32)
+    if (mdef) {
+        if (model != NQCD_MODEL_NEWNS_ANDERSON)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs on the Newns-Anderson model");
+        if (cfg->ndofs * cfg->natoms != 1)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs one adsorbate degree of freedom");
+        if (cfg->nbath < 1 || cfg->nbath > kMdefMaxBath || !cfg->bath_a || !cfg->bath_b)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: MDEF needs 1..512 bath levels and couplings");
+        for (int k = 1; k < cfg->nbath; ++k)
+            if (!(cfg->bath_a[k] > cfg->bath_a[k - 1]))
+                return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bath levels must be strictly ascending");
+        for (int k = 0; k < cfg->nbath; ++k)
+            if (cfg->bath_b[k] == 0.0) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bath couplings must be nonzero");
+        if (cfg->nparams < 5 || !cfg->params || !(cfg->params[4] > 0.0))
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: Newns-Anderson needs k, g, delta, mu, sigma > 0");
+        if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: MDEF needs beta > 0");
+        if (!cfg->masses || !(cfg->masses[0] > 0.0) || cfg->ntraj_max <= 0 || cfg->save_stride < 0)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: mass, ntraj_max and save_stride are required");
+    } else {
+        if (model != NQCD_MODEL_TULLY1 && model != NQCD_MODEL_TULLY2 && model != NQCD_MODEL_TULLY3 &&
+            model != NQCD_MODEL_SPINBOSON)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: unknown model");
+        if (cfg->nstates != 2) return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: only two-state models");
+    }
+    if (cfg->precision != NQCD_PREC_FP64 && cfg->precision != NQCD_PREC_FP32 && cfg->precision != NQCD_PREC_FP32_KAHAN)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown precision");
     if (cfg->rescaling < 0 || cfg->rescaling > 2) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown rescaling");
     if (cfg->ndofs <= 0 || cfg->natoms <= 0 || cfg->ntraj_max <= 0 || !cfg->masses)
@@ -238,14 +327,28 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bad initial electronic specification");
     if (cfg->save_stride < 0 || cfg->max_hops < 0 || cfg->traj_offset < 0)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: negative count");
-    const int64_t ndof = (int64_t)cfg->ndofs * cfg->natoms;
-    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : 4));
+    if (rp) {
+        if (model == NQCD_MODEL_SPINBOSON || cfg->ndofs * cfg->natoms != 1)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring-polymer surface hopping runs on one-dimensional Tully models");
+        if (cfg->nbeads_max < 1 || cfg->nbeads_max > 32)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: nbeads_max must be 1..32");
+        if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ring polymers need beta > 0");
+        if (cfg->init_kind == NQCD_INIT_DIABATIC_PURE)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring-polymer runs start from an adiabatic state");
+        if (cfg->save_stride != 0)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring-polymer runs report final-state outputs only");
+        if (!(cfg->terminate_x >= 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: terminate_x must be >= 0");
+    }
+    const int64_t ndof = rp ? (int64_t)cfg->nbeads_max : (int64_t)cfg->ndofs * cfg->natoms;
+    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? 5 : 4)));
     if (cfg->nparams < need_params || !cfg->params)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: too few model parameters");
-    if (model == NQCD_MODEL_SPINBOSON) {
+    if (mdef) {
+        // validated above
+    } else if (model == NQCD_MODEL_SPINBOSON) {
         if (cfg->nbath != ndof || !cfg->bath_a || !cfg->bath_b)
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: spin-boson needs nbath == ndofs*natoms couplings and frequencies");
-    } else if (ndof != 1) {
+    } else if (!rp && ndof != 1) {
         return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: Tully models have one degree of freedom");
     }
     for (int a = 0; a < cfg->natoms; ++a)
@@ -267,6 +370,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     h->ndof = ndof;
     h->params.assign(cfg->params, cfg->params + cfg->nparams);
     h->params.resize(8, 0.0);
+    h->mass0 = cfg->masses[0];
 
     auto bail = [&](cudaError_t ee, const char* what) {
         std::string m = std::string("nqcd_create: ") + what + ": " + cudaGetErrorString(ee);
@@ -288,7 +392,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     NQCD_CREATE(cudaEventCreate(&h->evk1));
 
     std::vector<double> mass(ndof), bc(ndof, 0.0), bw2(ndof, 0.0);
-    for (int64_t I = 0; I < ndof; ++I) mass[I] = cfg->masses[I / cfg->ndofs];
+    for (int64_t I = 0; I < ndof; ++I) mass[I] = rp ? cfg->masses[0] : cfg->masses[I / cfg->ndofs];
     if (model == NQCD_MODEL_SPINBOSON) {
         for (int64_t I = 0; I < ndof; ++I) {
             bc[I] = cfg->bath_a[I];
@@ -317,18 +421,104 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     NQCD_CREATE(dalloc(&h->d_nsteps, cap));
     if (cfg->max_hops > 0) NQCD_CREATE(dalloc(&h->d_hoplog, (int64_t)cfg->max_hops * 3 * cap));
     NQCD_CREATE(dalloc(&h->d_energy, 2 * cap));
-    NQCD_CREATE(dalloc(&h->d_counts, 8));
+    NQCD_CREATE(dalloc(&h->d_counts, 16));
+    if (mdef) {
+        std::vector<double> eps(cfg->bath_a, cfg->bath_a + cfg->nbath), V2(cfg->nbath);
+        for (int k = 0; k < cfg->nbath; ++k) V2[k] = cfg->bath_b[k] * cfg->bath_b[k];
+        NQCD_CREATE(dalloc(&h->d_eps, cfg->nbath));
+        NQCD_CREATE(dalloc(&h->d_V2, cfg->nbath));
+        NQCD_CREATE(cudaMemcpy(h->d_eps, eps.data(), eps.size() * sizeof(double), cudaMemcpyHostToDevice));
+        NQCD_CREATE(cudaMemcpy(h->d_V2, V2.data(), V2.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     NQCD_CREATE(cudaMemset(h->d_sig0, 0, 8 * cap * sizeof(double)));
     NQCD_CREATE(cudaMemset(h->d_state0, 0, cap * sizeof(int32_t)));
+    if (rp) {
+        // normal-mode matrices of every instantiated bead count (dt-independent)
+        int64_t off = 0;
+        for (int c = 0; c < kNumRpCounts; ++c) {
+            h->rp_U_off[c] = off;
+            off += (int64_t)kRpCounts[c] * kRpCounts[c];
+        }
+        std::vector<double> U(off);
+        std::vector<float> Uf(off);
+        for (int c = 0; c < kNumRpCounts; ++c) nm_transform_matrix(kRpCounts[c], U.data() + h->rp_U_off[c]);
+        for (int64_t q = 0; q < off; ++q) Uf[q] = (float)U[q];
+        NQCD_CREATE(dalloc(&h->d_rpU, off));
+        NQCD_CREATE(dalloc(&h->d_rpUf, off));
+        NQCD_CREATE(cudaMemcpy(h->d_rpU, U.data(), off * sizeof(double), cudaMemcpyHostToDevice));
+        NQCD_CREATE(cudaMemcpy(h->d_rpUf, Uf.data(), off * sizeof(float), cudaMemcpyHostToDevice));
+        NQCD_CREATE(dalloc(&h->d_rpcay, 4 * 32 * kNumRpCounts));
+        NQCD_CREATE(dalloc(&h->d_rpcayf, 4 * 32 * kNumRpCounts));
+        NQCD_CREATE(dalloc(&h->d_nbeads, cap));
+        NQCD_CREATE(dalloc(&h->d_class_traj, cap));
+        NQCD_CREATE(dalloc(&h->d_queue, kRpshMaxClasses));
+        NQCD_CREATE(dalloc(&h->d_block_class, kMaxRpGrid));
+    }
 #undef NQCD_CREATE
     *out = h;
     return NQCD_OK;
 }
 
+// Ring polymers: group trajectories by (Tully model, bead count) into the
+// classes served by the persistent kernel, from the host copies of the
+// per-trajectory bead counts and models.
+static int build_rp_classes(nqcd_handle* h, int64_t* h2d) {
+    const int64_t ntraj = (int64_t)h->traj_beads.size();
+    constexpr int nkey = 3 * kNumRpCounts;
+    std::vector<int64_t> count(nkey, 0);
+    std::vector<int> key_of(ntraj);
+    for (int64_t t = 0; t < ntraj; ++t) {
+        int b = h->traj_beads[t], slot = -1;
+        for (int c = 0; c < kNumRpCounts; ++c)
+            if (kRpCounts[c] == b) slot = c;
+        key_of[t] = (h->traj_models[t] - NQCD_MODEL_TULLY1) * kNumRpCounts + slot;
+        count[key_of[t]] += 1;
+    }
+    h->nclass = 0;
+    h->class_begin[0] = 0;
+    std::vector<int64_t> fillpos(nkey, 0);
+    for (int key = 0; key < nkey; ++key) {
+        if (!count[key]) continue;
+        const int k = h->nclass;
+        h->class_slot[k] = key % kNumRpCounts;
+        h->class_beads[k] = kRpCounts[key % kNumRpCounts];
+        h->class_model[k] = NQCD_MODEL_TULLY1 + key / kNumRpCounts;
+        fillpos[key] = h->class_begin[k];
+        h->class_begin[k + 1] = h->class_begin[k] + count[key];
+        h->nclass += 1;
+    }
+    std::vector<int32_t> order(ntraj);
+    for (int64_t t = 0; t < ntraj; ++t) order[fillpos[key_of[t]]++] = (int32_t)t;
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_class_traj, order.data(), ntraj * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    *h2d += ntraj * (int64_t)sizeof(int32_t);
+    return NQCD_OK;
+}
+
+// Per-trajectory bead counts (host array nbeads, NULL = nbeads_max for all);
+// every trajectory starts on the handle's model.
+static int set_bead_classes(nqcd_handle* h, int64_t ntraj, const int32_t* nbeads, int64_t* h2d) {
+    if (h->cfg.method != NQCD_METHOD_RPSH) return NQCD_OK;
+    h->traj_beads.assign(ntraj, h->cfg.nbeads_max);
+    h->traj_models.assign(ntraj, h->cfg.model);
+    for (int64_t t = 0; t < ntraj; ++t) {
+        int b = nbeads ? nbeads[t] : h->cfg.nbeads_max;
+        bool known = false;
+        for (int c = 0; c < kNumRpCounts; ++c) known |= kRpCounts[c] == b;
+        if (!known || b > h->cfg.nbeads_max)
+            return fail(h, NQCD_ERR_UNSUPPORTED,
+                        "nqcd_set_initial: bead counts must be one of 1, 2, 4, 5, 8, 10, 16, 32 and <= nbeads_max");
+        h->traj_beads[t] = b;
+    }
+    return build_rp_classes(h, h2d);
+}
+
 static int set_initial_common(nqcd_handle* h, int64_t ntraj, const double* sig_re, const double* sig_im,
                               const int32_t* state0, int64_t* h2d) {
     const int64_t N = ntraj;
-    if (h->cfg.init_kind == NQCD_INIT_GIVEN) {
+    // MDEF carries no electronic state: only FSSH and RPSH read sigma and state0
+    const bool two_state = h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH;
+    if (two_state && h->cfg.init_kind == NQCD_INIT_GIVEN) {
         if (!sig_re || !state0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: sig_re and state0 required for NQCD_INIT_GIVEN");
         // host (2,2,ntraj) column-major re/im -> device [8][ntraj]: component 2*(2*i+j)+{0,1}
         std::vector<double> soa(8 * N);
@@ -353,7 +543,6 @@ static int set_initial_common(nqcd_handle* h, int64_t ntraj, const double* sig_r
 
 int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, const double* sig_re,
                      const double* sig_im, const int32_t* state0, const int32_t* nbeads) {
-    (void)nbeads;
     if (!h) return NQCD_ERR_ARG;
     if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: ntraj outside 1..ntraj_max");
     if (!r0 || !v0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: r0 and v0 are required");
@@ -368,22 +557,25 @@ int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const doub
     NQCD_CUDA(h, transpose(h->d_stage, h->d_v0, ntraj, h->ndof, h->stream));
     NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
     h2d += 2 * n * (int64_t)sizeof(double);
+    rc = set_bead_classes(h, ntraj, nbeads, &h2d);
+    if (rc) return rc;
     return set_initial_common(h, ntraj, sig_re, sig_im, state0, &h2d);
 }
 
 int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0, const double* d_v0,
                             const int32_t* nbeads) {
-    (void)nbeads;
     if (!h) return NQCD_ERR_ARG;
     if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: ntraj outside 1..ntraj_max");
     if (!d_r0 || !d_v0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: r0 and v0 are required");
-    if (h->cfg.init_kind == NQCD_INIT_GIVEN)
+    if ((h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH) && h->cfg.init_kind == NQCD_INIT_GIVEN)
         return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: NQCD_INIT_GIVEN needs nqcd_set_initial");
     const int64_t n = ntraj * h->ndof;
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_r0, d_r0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_v0, d_v0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
     int64_t h2d = 0;
+    int rc = set_bead_classes(h, ntraj, nbeads, &h2d);
+    if (rc) return rc;
     return set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
 }
 
@@ -398,7 +590,11 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     if (nsteps > 0x7fffffff) return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
     const int stride = h->cfg.save_stride;
     const int nsave = stride > 0 ? (int)(nsteps / stride + 1) : 0;
-    const int64_t blocks = (N + 127) / 128;
+    const bool mdef = h->cfg.method == NQCD_METHOD_MDEF;
+    if (mdef && fabs((double)nsteps * dt - (t1 - t0)) > 1e-9 * (fabs(t1 - t0) + dt))
+        return fail(h, NQCD_ERR_ARG, "nqcd_run: MDEF needs t1 - t0 to be a whole number of steps");
+    const int64_t lanes = mdef ? 32 : fssh2_lanes_per_traj(h->cfg.model, h->cfg.precision);
+    const int64_t blocks = (N * lanes + 127) / 128;
     const int64_t nwarps = blocks * 4;
     if (nsave > 0 && nwarps * nsave * 4 > h->partial_cap) {
         if (h->d_partial) cudaFree(h->d_partial);
@@ -417,7 +613,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_v, h->d_v0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_sig, h->d_sig0, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_state, h->d_state0, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
-    NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 8 * sizeof(unsigned long long), s));
+    NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 16 * sizeof(unsigned long long), s));
     if (h->d_hoplog) {
         int64_t nl = (int64_t)h->cfg.max_hops * 3 * N;
         fill_i32_kernel<<<(unsigned)((nl + 255) / 256 < 4096 ? (nl + 255) / 256 : 4096), 256, 0, s>>>(h->d_hoplog, nl, -1);
@@ -459,8 +655,110 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.energy = h->d_energy;
     p.popcorr_partial = h->d_partial;
     p.scatter = h->d_counts;
-    NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
-    cudaError_t e = h->cfg.precision == NQCD_PREC_FP64 ? launch_fssh2_fp64(p, s) : launch_fssh2_fp32(p, s);
+    cudaError_t e = cudaSuccess;
+    int64_t h2d = 0;
+    if (h->cfg.method == NQCD_METHOD_RPSH) {
+        // Cayley propagators for this dt, one slot of 32 modes per instantiated bead count
+        const bool plain = h->cfg.precision == NQCD_PREC_FP64;
+        std::vector<double> cay(4 * 32 * kNumRpCounts, 0.0);
+        std::vector<float> cayf(cay.size(), 0.0f);
+        RpshParams rq;
+        memset(&rq, 0, sizeof(rq));
+        for (int k = 0; k < h->nclass; ++k) {
+            const int slot = h->class_slot[k], n = h->class_beads[k];
+            cayley_matrices(n, h->cfg.beta, dt, cay.data() + 4 * 32 * slot);
+            rq.class_beads[k] = n;
+            rq.U[k] = h->d_rpU + h->rp_U_off[slot];
+            rq.Uf[k] = h->d_rpUf + h->rp_U_off[slot];
+            rq.cay[k] = h->d_rpcay + 4 * 32 * slot;
+            rq.cayf[k] = h->d_rpcayf + 4 * 32 * slot;
+        }
+        for (size_t q = 0; q < cay.size(); ++q) cayf[q] = (float)cay[q];
+        // persistent grid; blocks start on classes in proportion to their estimated work
+        int grid = plain ? rpsh_grid_fp64() : rpsh_grid_fp32();
+        if (grid > kMaxRpGrid) grid = kMaxRpGrid;
+        if (grid < 1) grid = 1;
+        std::vector<double> cost(h->nclass);
+        double total = 0.0;
+        for (int k = 0; k < h->nclass; ++k) {
+            double b = h->class_beads[k];
+            cost[k] = (double)(h->class_begin[k + 1] - h->class_begin[k]) * (2000.0 + 60.0 * b + 4.0 * b * b);
+            total += cost[k];
+        }
+        std::vector<int32_t> bc(grid, 0);
+        {
+            int pos = 0;
+            for (int k = 0; k < h->nclass; ++k) {
+                int nb = (int)(grid * cost[k] / (total > 0 ? total : 1.0));
+                if (nb < 1) nb = 1;
+                for (int q = 0; q < nb && pos < grid; ++q) bc[pos++] = k;
+            }
+            for (; pos < grid; ++pos) bc[pos] = h->nclass - 1;
+        }
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpcay, cay.data(), cay.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpcayf, cayf.data(), cayf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_block_class, bc.data(), grid * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        NQCD_CUDA(h, cudaMemsetAsync(h->d_queue, 0, kRpshMaxClasses * sizeof(unsigned long long), s));
+        h2d += (int64_t)(cay.size() * sizeof(double) + cayf.size() * sizeof(float) + grid * sizeof(int32_t));
+        for (int k = 0; k < h->nclass; ++k) {
+            // the handle's model uses its parameters; the other Tully models their published defaults
+            static const double kTullyDefaults[3][8] = {{0.01, 1.6, 0.005, 1.0, 0, 0, 0, 0},
+                                                        {0.1, 0.28, 0.015, 0.06, 0.05, 0, 0, 0},
+                                                        {6e-4, 0.1, 0.9, 0, 0, 0, 0, 0}};
+            rq.class_model[k] = h->class_model[k];
+            for (int q = 0; q < 8; ++q)
+                rq.class_mp[k][q] = h->class_model[k] == h->cfg.model
+                                        ? h->params[q]
+                                        : kTullyDefaults[h->class_model[k] - NQCD_MODEL_TULLY1][q];
+        }
+        rq.mass = h->mass0;
+        rq.beta = h->cfg.beta;
+        rq.rescaling = h->cfg.rescaling;
+        rq.init_kind = h->cfg.init_kind;
+        rq.init_state = h->cfg.init_state;
+        rq.gap_fp64 = (float)h->cfg.gap_fp64;
+        rq.ntraj = N;
+        rq.traj_offset = h->cfg.traj_offset;
+        rq.t0 = t0;
+        rq.t1 = t1;
+        rq.dt = dt;
+        rq.seed = seed;
+        rq.terminate_x = h->cfg.terminate_x;
+        rq.max_hops = h->cfg.max_hops;
+        rq.nclass = h->nclass;
+        for (int k = 0; k <= h->nclass; ++k) rq.class_begin[k] = h->class_begin[k];
+        rq.class_traj = h->d_class_traj;
+        rq.queue = h->d_queue;
+        rq.block_class = h->d_block_class;
+        rq.r = h->d_r;
+        rq.v = h->d_v;
+        rq.sigma = h->d_sig;
+        rq.state = h->d_state;
+        rq.nhops = h->d_nhops;
+        rq.nfrustrated = h->d_nfrust;
+        rq.nsteps = h->d_nsteps;
+        rq.hop_log = h->d_hoplog;
+        rq.energy = h->d_energy;
+        rq.scatter = h->d_counts;
+        NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
+        e = plain ? launch_rpsh_fp64(rq, grid, s) : launch_rpsh_fp32(rq, grid, s);
+    } else if (mdef) {
+        MdefParams mp = mdef_params(h, N, dt, (int32_t)nsteps, seed, stride, nsave);
+        if (mp.use_mlp && !h->mlp.trained)
+            return fail(h, NQCD_ERR_STATE, "nqcd_run: use_friction_surrogate needs nqcd_train_friction_mlp or nqcd_mlp_set");
+        // steps and hop counters are not written by MDEF; observables need zeroed partials
+        NQCD_CUDA(h, cudaMemsetAsync(h->d_nsteps, 0, N * sizeof(int32_t), s));
+        NQCD_CUDA(h, cudaMemsetAsync(h->d_nhops, 0, N * sizeof(int32_t), s));
+        NQCD_CUDA(h, cudaMemsetAsync(h->d_nfrust, 0, N * sizeof(int32_t), s));
+        if (nsave > 0) NQCD_CUDA(h, cudaMemsetAsync(h->d_partial, 0, nwarps * nsave * 4 * sizeof(double), s));
+        NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
+        e = h->cfg.precision == NQCD_PREC_FP64 ? launch_mdef_fp64(mp, s) : launch_mdef_fp32(mp, s);
+    } else {
+        NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
+        e = h->cfg.precision == NQCD_PREC_FP64   ? launch_fssh2_fp64(p, s)
+            : h->cfg.precision == NQCD_PREC_FP32 ? launch_fssh2_fp32(p, s)
+                                                 : launch_fssh2_fp32_kahan(p, s);
+    }
     if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_run: ensemble kernel launch");
     NQCD_CUDA(h, cudaEventRecord(h->evk1, s));
     ++launches;
@@ -474,12 +772,12 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     ++launches;
     NQCD_CUDA(h, cudaEventRecord(h->ev1, s));
 
-    unsigned long long counts[8];
+    unsigned long long counts[16];
     int64_t d2h = 0;
     NQCD_CUDA(h, cudaMemcpyAsync(counts, h->d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
     d2h += sizeof(counts);
     std::vector<double> pc;
-    if (out && out->population_correlation && nsave > 0) {
+    if (out && (mdef ? out->observables : out->population_correlation) && nsave > 0) {
         pc.resize((size_t)nsave * 4);
         NQCD_CUDA(h, cudaMemcpyAsync(pc.data(), h->d_popcorr, pc.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         d2h += (int64_t)pc.size() * sizeof(double);
@@ -492,20 +790,24 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         out->nsave = nsave;
         if (out->scattering)
             for (int q = 0; q < 4; ++q) out->scattering[q] = (double)counts[q] / (double)N;
-        if (out->population_correlation && nsave > 0)
-            for (int k = 0; k < nsave * 4; ++k) out->population_correlation[k] = pc[k] / (double)N;
+        double* dst = mdef ? out->observables : out->population_correlation;
+        if (dst && nsave > 0)
+            for (int k = 0; k < nsave * 4; ++k) dst[k] = pc[k] / (double)N;
     }
     h->nsave_last = nsave;
     h->has_run = true;
     if (stats) {
-        stats->traj_steps = (int64_t)counts[4];
+        stats->traj_steps = mdef ? N * nsteps : (int64_t)counts[4];
+        stats->exact_friction_evals = (int64_t)counts[8];
+        stats->surrogate_friction_evals = (int64_t)counts[9];
+        stats->unconverged_roots = (int64_t)counts[10];
         stats->hops = (int64_t)counts[5];
         stats->frustrated = (int64_t)counts[6];
         stats->flagged = (int64_t)counts[7];
         stats->device_ms = ms;
         stats->kernel_ms = kms;
         stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
-        stats->h2d_bytes = 0;
+        stats->h2d_bytes = h2d;
         stats->d2h_bytes = d2h;
         stats->kernel_launches = launches;
     }
@@ -552,6 +854,166 @@ int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double*
     }
     NQCD_CUDA(h, cudaStreamSynchronize(s));
     return NQCD_OK;
+}
+
+// Exact force and friction at n host positions, in chunks of the handle's capacity.
+static int mdef_eval_device(nqcd_handle* h, const double* d_x, int64_t n, double* d_force, double* d_fric) {
+    MdefParams m = mdef_params(h, n, 1.0, 0, 0, 0, 0);
+    m.x = const_cast<double*>(d_x);
+    m.v = d_fric;  // unused in evaluation mode
+    m.energy = nullptr;
+    m.obs_partial = nullptr;
+    m.use_mlp = 0;
+    m.force_out = d_force;
+    m.friction_out = d_fric;
+    cudaError_t e = h->cfg.precision == NQCD_PREC_FP64 ? launch_mdef_fp64(m, h->stream) : launch_mdef_fp32(m, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "MDEF evaluation kernel");
+    return NQCD_OK;
+}
+
+int nqcd_mdef_evaluate(nqcd_handle* h, int64_t n, const double* x, double* force, double* friction) {
+    if (!h || !x || n <= 0) return NQCD_ERR_ARG;
+    if (h->cfg.method != NQCD_METHOD_MDEF) return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_mdef_evaluate: MDEF handles only");
+    int rc = ensure_stage(h, 3 * n);
+    if (rc) return rc;
+    double *dx = h->d_stage, *dF = h->d_stage + n, *dG = h->d_stage + 2 * n;
+    NQCD_CUDA(h, cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    rc = mdef_eval_device(h, dx, n, dF, dG);
+    if (rc) return rc;
+    if (force) NQCD_CUDA(h, cudaMemcpyAsync(force, dF, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (friction) NQCD_CUDA(h, cudaMemcpyAsync(friction, dG, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    return NQCD_OK;
+}
+
+__global__ void uniform_positions_kernel(double* x, int64_t n, double lo, double hi, uint64_t seed) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = lo + (hi - lo) * rng_uniform(seed, (uint64_t)i, 0u, 9u);
+}
+
+__global__ void cholesky_target_kernel(const double* fric, double* L, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) L[i] = sqrt(fric[i] > 0.0 ? fric[i] : 0.0);
+}
+
+int nqcd_train_friction_mlp(nqcd_handle* h, double x_lo, double x_hi, int64_t npoints, int32_t epochs, int32_t batch,
+                            double learning_rate, uint64_t seed, double* final_loss) {
+    if (!h) return NQCD_ERR_ARG;
+    if (h->cfg.method != NQCD_METHOD_MDEF)
+        return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_train_friction_mlp: MDEF handles only");
+    if (!(x_hi > x_lo) || npoints < 16 || epochs < 1 || batch < 16 || batch > 65536 || !(learning_rate > 0))
+        return fail(h, NQCD_ERR_ARG, "nqcd_train_friction_mlp: bad domain, sizes or learning rate");
+    cudaStream_t s = h->stream;
+    if (!h->mlp.master) {
+        cudaError_t e = mlp_alloc(h->mlp, 65536);
+        if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_train_friction_mlp: allocation");
+    }
+    double *dx = nullptr, *dF = nullptr, *dG = nullptr, *dL = nullptr;
+    NQCD_CUDA(h, dalloc(&dx, npoints));
+    NQCD_CUDA(h, dalloc(&dF, npoints));
+    NQCD_CUDA(h, dalloc(&dG, npoints));
+    NQCD_CUDA(h, dalloc(&dL, npoints));
+    auto release = [&]() {
+        cudaFree(dx);
+        cudaFree(dF);
+        cudaFree(dG);
+        cudaFree(dL);
+    };
+    uniform_positions_kernel<<<(unsigned)((npoints + 255) / 256), 256, 0, s>>>(dx, npoints, x_lo, x_hi, seed);
+    int rc = mdef_eval_device(h, dx, npoints, dF, dG);  // training data from the method itself
+    if (rc) {
+        release();
+        return rc;
+    }
+    cholesky_target_kernel<<<(unsigned)((npoints + 255) / 256), 256, 0, s>>>(dG, dL, npoints);
+    // output bias starts at the mean target so that training starts near the data
+    std::vector<double> Lh(npoints);
+    cudaError_t e = cudaMemcpyAsync(Lh.data(), dL, npoints * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        release();
+        return cuda_fail(h, e, "nqcd_train_friction_mlp: targets");
+    }
+    double mean = 0.0;
+    for (double v : Lh) mean += v;
+    mean /= (double)npoints;
+    float bias = (float)(mean > 20.0 ? mean : log(expm1(mean > 1e-6 ? mean : 1e-6)));  // inverse softplus
+    h->mlp.shift = 0.5 * (x_lo + x_hi);
+    h->mlp.scale = 2.0 / (x_hi - x_lo);
+    h->mlp.lo = x_lo;
+    h->mlp.hi = x_hi;
+    e = mlp_init_weights(h->mlp, seed, bias, s);
+    if (e == cudaSuccess) {
+        int64_t nsteps = (int64_t)epochs * ((npoints + batch - 1) / batch);
+        e = mlp_train_device(h->mlp, dx, dL, npoints, nsteps, batch, (float)learning_rate, seed, s, final_loss);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    release();
+    if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_train_friction_mlp: training");
+    h->mlp.trained = true;
+    return NQCD_OK;
+}
+
+int nqcd_mlp_get(nqcd_handle* h, float* params, double* meta) {
+    if (!h || !params) return NQCD_ERR_ARG;
+    if (!h->mlp.master) return fail(h, NQCD_ERR_STATE, "nqcd_mlp_get: no network");
+    NQCD_CUDA(h, cudaMemcpyAsync(params, h->mlp.master, kMlpN * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (meta) {
+        meta[0] = h->mlp.shift;
+        meta[1] = h->mlp.scale;
+        meta[2] = h->mlp.lo;
+        meta[3] = h->mlp.hi;
+    }
+    return NQCD_OK;
+}
+
+int nqcd_mlp_set(nqcd_handle* h, const float* params, const double* meta) {
+    if (!h || !params || !meta) return NQCD_ERR_ARG;
+    if (h->cfg.method != NQCD_METHOD_MDEF) return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_mlp_set: MDEF handles only");
+    if (!h->mlp.master) {
+        cudaError_t e = mlp_alloc(h->mlp, 65536);
+        if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_mlp_set: allocation");
+    }
+    NQCD_CUDA(h, cudaMemcpyAsync(h->mlp.master, params, kMlpN * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    NQCD_CUDA(h, mlp_sync_bf16(h->mlp, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->mlp.shift = meta[0];
+    h->mlp.scale = meta[1];
+    h->mlp.lo = meta[2];
+    h->mlp.hi = meta[3];
+    h->mlp.trained = true;
+    return NQCD_OK;
+}
+
+int nqcd_mlp_loss_grad(nqcd_handle* h, int64_t n, const double* x, const double* target_L, double* loss, float* grad) {
+    if (!h || !x || !target_L || n <= 0 || n > 65536) return NQCD_ERR_ARG;
+    if (!h->mlp.master) return fail(h, NQCD_ERR_STATE, "nqcd_mlp_loss_grad: no network");
+    int rc = ensure_stage(h, 2 * n);
+    if (rc) return rc;
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_stage, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_stage + n, target_L, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    NQCD_CUDA(h, mlp_loss_grad_device(h->mlp, h->d_stage, h->d_stage + n, (int)n, h->stream));
+    std::vector<float> g(kMlpN + 1);
+    NQCD_CUDA(h, cudaMemcpyAsync(g.data(), h->mlp.grad, g.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (grad) memcpy(grad, g.data(), kMlpN * sizeof(float));
+    if (loss) *loss = g[kMlpN];
+    return NQCD_OK;
+}
+
+int nqcd_set_trajectory_models(nqcd_handle* h, const int32_t* models) {
+    if (!h || !models) return NQCD_ERR_ARG;
+    if (h->cfg.method != NQCD_METHOD_RPSH)
+        return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_set_trajectory_models: ring-polymer handles only");
+    if (!h->initial_set) return fail(h, NQCD_ERR_STATE, "nqcd_set_trajectory_models: call nqcd_set_initial first");
+    for (int64_t t = 0; t < h->ntraj; ++t)
+        if (models[t] < NQCD_MODEL_TULLY1 || models[t] > NQCD_MODEL_TULLY3)
+            return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_set_trajectory_models: Tully models 1-3 only");
+    h->traj_models.assign(models, models + h->ntraj);
+    int64_t h2d = 0;
+    h->has_run = false;
+    return build_rp_classes(h, &h2d);
 }
 
 int nqcd_get_hop_log(nqcd_handle* h, int32_t* log) {

@@ -24,8 +24,9 @@ ERRORS = {
 }
 
 METHOD_FSSH, METHOD_RPSH, METHOD_IESH, METHOD_MDEF = 1, 2, 3, 4
-MODEL_TULLY1, MODEL_TULLY2, MODEL_TULLY3, MODEL_SPINBOSON = 1, 2, 3, 10
-PREC_FP64, PREC_FP32 = 0, 1
+MODEL_TULLY1, MODEL_TULLY2, MODEL_TULLY3, MODEL_SPINBOSON, MODEL_NEWNS_ANDERSON = 1, 2, 3, 10, 20
+MLP_NPARAMS = 4353
+PREC_FP64, PREC_FP32, PREC_FP32_KAHAN = 0, 1, 2
 RESCALE = {"standard": 0, "vinversion": 1, "off": 2}
 INIT_GIVEN, INIT_ADIABATIC_PURE, INIT_DIABATIC_PURE = 0, 1, 2
 
@@ -58,7 +59,9 @@ class nqcd_config(C.Structure):
         ("terminate_x", C.c_double),
         ("gap_fp64", C.c_double),
         ("traj_offset", C.c_int64),
-        ("reserved", C.c_int32 * 6),
+        ("use_friction_surrogate", C.c_int32),
+        ("judge_every", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -66,6 +69,7 @@ class nqcd_outputs(C.Structure):
     _fields_ = [
         ("scattering", DP),
         ("population_correlation", DP),
+        ("observables", DP),
         ("nsave", C.c_int32),
         ("reserved", C.c_int32),
     ]
@@ -84,6 +88,9 @@ class nqcd_stats(C.Structure):
         ("d2h_bytes", C.c_int64),
         ("kernel_launches", C.c_int32),
         ("reserved", C.c_int32),
+        ("exact_friction_evals", C.c_int64),
+        ("surrogate_friction_evals", C.c_int64),
+        ("unconverged_roots", C.c_int64),
     ]
 
 
@@ -95,6 +102,12 @@ EXPORTED = [
     "nqcd_run",
     "nqcd_get_final",
     "nqcd_get_hop_log",
+    "nqcd_set_trajectory_models",
+    "nqcd_mdef_evaluate",
+    "nqcd_train_friction_mlp",
+    "nqcd_mlp_get",
+    "nqcd_mlp_set",
+    "nqcd_mlp_loss_grad",
     "nqcd_last_error",
     "nqcd_destroy",
     "nqcd_pin_host",
@@ -136,6 +149,14 @@ def load(path: Path | str | None = None) -> C.CDLL:
                              C.POINTER(nqcd_outputs), C.POINTER(nqcd_stats)]
     lib.nqcd_get_final.argtypes = [C.c_void_p, DP, DP, DP, DP, IP, IP, IP, IP, DP]
     lib.nqcd_get_hop_log.argtypes = [C.c_void_p, IP]
+    lib.nqcd_set_trajectory_models.argtypes = [C.c_void_p, IP]
+    lib.nqcd_mdef_evaluate.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP]
+    lib.nqcd_train_friction_mlp.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32, C.c_int32,
+                                            C.c_double, C.c_uint64, DP]
+    FP = C.POINTER(C.c_float)
+    lib.nqcd_mlp_get.argtypes = [C.c_void_p, FP, DP]
+    lib.nqcd_mlp_set.argtypes = [C.c_void_p, FP, DP]
+    lib.nqcd_mlp_loss_grad.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP, FP]
     lib.nqcd_last_error.restype = C.c_char_p
     lib.nqcd_last_error.argtypes = [C.c_void_p]
     lib.nqcd_destroy.argtypes = [C.c_void_p]
@@ -189,10 +210,11 @@ class Engine:
         self._check(self.lib.nqcd_set_initial_device(self.h, ntraj, C.c_void_p(d_r0), C.c_void_p(d_v0), None))
         self.ntraj = ntraj
 
-    def run(self, t0, t1, dt, seed, scattering=None, popcorr=None):
+    def run(self, t0, t1, dt, seed, scattering=None, popcorr=None, observables=None):
         out = nqcd_outputs()
         out.scattering = dptr(scattering)
         out.population_correlation = dptr(popcorr)
+        out.observables = dptr(observables)
         st = nqcd_stats()
         self._check(self.lib.nqcd_run(self.h, t0, t1, dt, seed, C.byref(out), C.byref(st)))
         return out, st
@@ -213,6 +235,42 @@ class Engine:
         # (nstates, nstates) per trajectory arrive column-major: transpose to [i, j]
         return dict(r=r, v=v, sig_re=sre.transpose(0, 2, 1).copy(), sig_im=sim.transpose(0, 2, 1).copy(),
                     state=state, nhops=nh, nfrustrated=nf, nsteps=ns, energy=en)
+
+    def mdef_evaluate(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        F = np.empty_like(x)
+        G = np.empty_like(x)
+        self._check(self.lib.nqcd_mdef_evaluate(self.h, len(x), dptr(x), dptr(F), dptr(G)))
+        return F, G
+
+    def train_friction_mlp(self, lo, hi, npoints, epochs, batch, lr, seed):
+        loss = C.c_double()
+        self._check(self.lib.nqcd_train_friction_mlp(self.h, lo, hi, npoints, epochs, batch, lr, seed,
+                                                     C.byref(loss)))
+        return loss.value
+
+    def mlp_get(self):
+        w = np.empty(MLP_NPARAMS, np.float32)
+        meta = np.empty(4)
+        self._check(self.lib.nqcd_mlp_get(self.h, w.ctypes.data_as(C.POINTER(C.c_float)), dptr(meta)))
+        return w, meta
+
+    def mlp_set(self, w, meta):
+        w = np.ascontiguousarray(w, np.float32)
+        meta = np.ascontiguousarray(meta, np.float64)
+        self._check(self.lib.nqcd_mlp_set(self.h, w.ctypes.data_as(C.POINTER(C.c_float)), dptr(meta)))
+
+    def mlp_loss_grad(self, x, target):
+        x = np.ascontiguousarray(x, np.float64)
+        t = np.ascontiguousarray(target, np.float64)
+        loss = C.c_double()
+        g = np.empty(MLP_NPARAMS, np.float32)
+        self._check(self.lib.nqcd_mlp_loss_grad(self.h, len(x), dptr(x), dptr(t), C.byref(loss),
+                                                g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
+    def set_trajectory_models(self, models):
+        self._check(self.lib.nqcd_set_trajectory_models(self.h, iptr(np.ascontiguousarray(models, np.int32))))
 
     def get_hop_log(self, max_hops: int):
         log = np.empty((self.ntraj, max_hops, 3), np.int32)

@@ -340,7 +340,9 @@ class EnsembleThreads:
 @dataclass
 class EnsembleGB300:
     """GPU ensemble algorithm: precision 'fp64' (plain, bit-identical to the
-    FP64 reference integration) or 'fp32' (fast path)."""
+    FP64 reference integration), 'fp32' (fast path, FP64 accumulation of
+    positions and velocities) or 'fp32_kahan' (fast path, compensated FP32
+    accumulation)."""
 
     precision: str = "fp64"
     gap_fp64: float = 1e-3
@@ -362,7 +364,7 @@ def build_config(sim, electronic: PureState, ntraj: int, alg: EnsembleGB300, sav
     cfg = L.nqcd_config()
     cfg.method = L.METHOD_FSSH
     cfg.model = model.kind
-    cfg.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[alg.precision]
+    cfg.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32, "fp32_kahan": L.PREC_FP32_KAHAN}[alg.precision]
     cfg.rescaling = L.RESCALE[sim.method.rescaling]
     cfg.ndofs = model.ndofs
     cfg.natoms = len(sim.atoms)

@@ -32,6 +32,7 @@ ENGINE_UNITS = {
     "kernels_fp32.cu": [],
     "nqcd_abi.cu": [],
     "noalloc.cu": [],
+    "mlp.cu": [],
 }
 
 

@@ -32,6 +32,42 @@ def spin_boson_inputs(ntraj: int, nmodes: int = 100, *, wc: float = 2.5, alpha: 
     return w, c, r0, v0
 
 
+AU_PER_FS = 41.341373335
+KELVIN_AU = 3.166811563e-6
+
+
+def shenvi_gauss_legendre(M: int, a: float, b: float, ef: float = 0.0):
+    """Bath levels and weights of the ShenviGaussLegendre discretisation
+    (docs/src/NQCModels/systembathmodels.md:241-256): Gauss-Legendre halves
+    below and above the Fermi level (upper shift (ef + b)/2, which maps the
+    knots into [ef, b])."""
+    x, w = np.polynomial.legendre.leggauss(M // 2)
+    lo = 0.5 * (ef - a) * x + 0.5 * (a + ef)
+    hi = 0.5 * (b - ef) * x + 0.5 * (ef + b)
+    return np.concatenate([lo, hi]), np.concatenate([0.5 * (ef - a) * w, 0.5 * (b - ef) * w])
+
+
+def newns_anderson_mdef(ntraj: int, *, M: int = 200, coupling: float = 0.02, mass: float = 1837.0,
+                        omega: float = 0.004, g: float = 1.0, sigma: float = 0.01, temperature_K: float = 300.0,
+                        hot: float = 10.0, seed: int = SEED, traj_offset: int = 0):
+    """Electronic-friction workload: one adsorbate degree of freedom (hydrogen
+    mass) on a displaced-harmonic impurity coupled to a metal band of M
+    Gauss-Legendre states on [-0.5, 0.5] Hartree with V_k = coupling sqrt(w_k),
+    Fermi level 0, electronic temperature 300 K.  The impurity level
+    h(x) = k g (g/2 - x) + delta with delta = -k g^2 / 2 crosses the Fermi
+    level at x = 0.  Initial conditions are thermal at `hot` times the
+    electronic temperature (a vibrationally hot adsorbate that the friction
+    cools).  Returns the model parameters and initial positions/velocities."""
+    eps, w = shenvi_gauss_legendre(M, -0.5, 0.5, 0.0)
+    k = mass * omega**2
+    T = temperature_K * KELVIN_AU
+    rng = np.random.default_rng([seed, traj_offset, 4])
+    x0 = rng.standard_normal(ntraj) * np.sqrt(hot * T / k)
+    v0 = rng.standard_normal(ntraj) * np.sqrt(hot * T / mass)
+    return dict(eps=eps, weights=w, V=coupling * np.sqrt(w), k=k, g=g, delta=-0.5 * k * g * g, mu=0.0, sigma=sigma,
+                beta=1.0 / T, mass=mass, x0=x0, v0=v0, dt=0.1 * AU_PER_FS)
+
+
 # ---------------------------------------------------------------------------
 # Algorithmic work of the reference algorithm per nuclear step of one
 # trajectory (two electronic states), counted operation by operation from

@@ -1,0 +1,222 @@
+"""IESH oracle -- TEST INFRASTRUCTURE ONLY.
+
+numpy FP64 restatement of NQCDynamics.jl's independent-electron surface
+hopping on a Newns-Anderson (AndersonHolstein) metal:
+
+  VerletwithElectronics.perform_step!   src/DynamicsMethods/IntegrationAlgorithms/verlet_with_electronics.jl:42-69
+  propagate_wavefunction! /
+  get_quantum_propagator                src/DynamicsUtils/wavefunction_dynamics.jl:15-58
+  IESH acceleration!                    src/DynamicsMethods/SurfaceHoppingMethods/iesh.jl:190-207
+  evaluate_hopping_probability!         iesh.jl:231-283 (with the estimate screen :251-254)
+  evaluate_v_dot_d!, calculate_Akj,
+  compute_overlap!                      iesh.jl:285-316
+  select_new_state                      iesh.jl:318-335
+  iesh_check_hop! / iesh_execute_hop!   iesh.jl:390-407
+  rescale_velocity!                     surface_hopping.jl:64-99
+  sample_fermi_dirac_distribution       src/DynamicsUtils/DynamicsUtils.jl:407-421
+  set_unoccupied_states!                DynamicsUtils.jl:375-384
+
+Electronic structure as the reference's cache computes it: dense
+eigen-decomposition (LAPACK) with eigenvector signs fixed by continuity with
+the previous step (identity first), Z^T dH Z, couplings A_ij / (l_j - l_i).
+The propagator is the exact U exp(-i mu dt) U^H of the effective
+Hamiltonian (LAPACK eigh of the Hermitian matrix), determinants by LU.
+
+Random numbers: the engine's Philox4x32-10 stream; one 53-bit uniform per
+trajectory and step for the hop test (stream HOP), three per Metropolis
+iteration of the initial occupations (stream FERMI_DIRAC).
+
+Model (AndersonHolstein with a 3-D impurity): one atom, coordinates
+(x, y, z); U0 = k_xy (x^2 + y^2)/2 + A exp(-a z);
+h = U1 - U0 = delta - B exp(-b z); constant couplings V_k; bath levels e_k.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from mdef_oracle import philox
+
+RNG_HOP = 1
+RNG_INIT_FD = 4
+
+
+def u53(w0, w1):
+    a = ((np.asarray(w0).astype(np.uint64) << np.uint64(32)) | np.asarray(w1).astype(np.uint64)) >> np.uint64(11)
+    return a.astype(np.float64) * 2.0**-53
+
+
+def uniform(seed, traj, step, stream):
+    traj = np.asarray(traj, dtype=np.uint64)
+    w = philox((traj & np.uint64(0xFFFFFFFF)).astype(np.uint32), (traj >> np.uint64(32)).astype(np.uint32),
+               np.full(traj.shape, step, np.uint32), np.full(traj.shape, stream, np.uint32), seed & 0xFFFFFFFF,
+               (seed >> 32) & 0xFFFFFFFF)
+    return w
+
+
+class Metal3D:
+    def __init__(self, *, kxy, A, a, delta, B, b, eps, V):
+        self.kxy, self.A, self.a, self.delta, self.B, self.b = kxy, A, a, delta, B, b
+        self.eps = np.asarray(eps, np.float64)
+        self.V = np.asarray(V, np.float64)
+        self.nstates = 1 + len(self.eps)
+
+    def h(self, r):
+        return self.delta - self.B * np.exp(-self.b * r[..., 2])
+
+    def grad_h(self, r):
+        g = np.zeros_like(r)
+        g[..., 2] = self.B * self.b * np.exp(-self.b * r[..., 2])
+        return g
+
+    def grad_U0(self, r):
+        g = np.zeros_like(r)
+        g[..., 0] = self.kxy * r[..., 0]
+        g[..., 1] = self.kxy * r[..., 1]
+        g[..., 2] = -self.A * self.a * np.exp(-self.a * r[..., 2])
+        return g
+
+    def U0(self, r):
+        return 0.5 * self.kxy * (r[..., 0] ** 2 + r[..., 1] ** 2) + self.A * np.exp(-self.a * r[..., 2])
+
+    def hamiltonian(self, r):
+        n = r.shape[0]
+        N = self.nstates
+        H = np.zeros((n, N, N))
+        H[:, 0, 0] = self.h(r)
+        H[:, 0, 1:] = self.V
+        H[:, 1:, 0] = self.V
+        idx = np.arange(1, N)
+        H[:, idx, idx] = self.eps
+        return H
+
+
+def eigen_continuous(model, r, Zprev):
+    w, Z = np.linalg.eigh(model.hamiltonian(r))
+    sgn = np.where(np.einsum("tki,tki->ti", Z, Zprev) < 0, -1.0, 1.0)
+    return w, Z * sgn[:, None, :]
+
+
+def sample_fermi_dirac(energies, ne, beta, seed, traj_ids):
+    """Metropolis occupations: Ne electrons in N states (DynamicsUtils.jl:407-421)."""
+    n, N = energies.shape
+    states = np.tile(np.arange(ne), (n, 1))
+    for it in range(N * ne):
+        wa = uniform(seed, traj_ids, it, RNG_INIT_FD)
+        wb = uniform(seed, traj_ids, it, RNG_INIT_FD + 16)
+        ua, ub, uc = u53(wa[0], wa[1]), u53(wa[2], wa[3]), u53(wb[0], wb[1])
+        for t in range(n):
+            ci = min(int(ua[t] * ne), ne - 1)
+            occ = set(states[t].tolist())
+            unocc = [s for s in range(N) if s not in occ]
+            j = unocc[min(int(ub[t] * len(unocc)), len(unocc) - 1)]
+            i = states[t, ci]
+            prob = np.exp(-beta * (energies[t, j] - energies[t, i]))
+            if prob > uc[t]:
+                states[t, ci] = j
+    return np.sort(states, axis=1)
+
+
+def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, max_hops=16):
+    n = r0.shape[0]
+    N = model.nstates
+    traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
+    r = np.asarray(r0, np.float64).copy()
+    v = np.asarray(v0, np.float64).copy()
+    Z = np.tile(np.eye(N), (n, 1, 1))
+    w, Z = eigen_continuous(model, r, Z)
+    states = sample_fermi_dirac(w, ne, beta, seed, traj)
+    psi = np.zeros((n, N, ne), np.complex128)
+    for t in range(n):
+        psi[t, states[t], np.arange(ne)] = 1.0
+    state = states.copy()
+    hops = [[] for _ in range(n)]
+    nfr = np.zeros(n, np.int32)
+
+    def accel(w, Z, r, state):
+        gh = model.grad_h(r)
+        z0 = Z[:, 0, :]
+        occ = np.take_along_axis(z0, state, axis=1) ** 2
+        return -(model.grad_U0(r) + gh * occ.sum(1)[:, None]) / mass
+
+    k = accel(w, Z, r, state)
+    for step in range(1, nsteps + 1):
+        vt = v + (dt / 2) * k
+        r = r + dt * vt
+        w, Z = eigen_continuous(model, r, Z)
+        k = accel(w, Z, r, state)
+        v = vt + (dt / 2) * k
+        gh = model.grad_h(r)
+        z0 = Z[:, 0, :]
+        lam_diff = w[:, None, :] - w[:, :, None]  # l_j - l_i
+        with np.errstate(divide="ignore", invalid="ignore"):
+            base = z0[:, :, None] * z0[:, None, :] / lam_diff
+        idx = np.arange(N)
+        base[:, idx, idx] = 0.0
+        vdh = np.einsum("ta,ta->t", v, gh)  # sum_alpha v_alpha dh/dq_alpha
+        vd = vdh[:, None, None] * base  # sum_alpha v_alpha d_alpha
+        Heff = np.zeros((n, N, N), np.complex128)
+        Heff[:, idx, idx] = w
+        Heff -= 1j * vd
+        mu, U = np.linalg.eigh(Heff)
+        P = np.einsum("tij,tj,tkj->tik", U, np.exp(-1j * mu * dt), U.conj())
+        psi = P @ psi
+        # hopping
+        wh = uniform(seed, traj, step, RNG_HOP)
+        rnd = u53(wh[0], wh[1])
+        for t in range(n):
+            st = state[t]
+            unocc = np.array([s for s in range(N) if s not in set(st.tolist())])
+            S = psi[t][st, :]
+            detS = np.linalg.det(S)
+            Akk = abs(detS) ** 2
+            pref = 2 * dt / Akk
+            vdd = np.zeros((N, ne))
+            for nn in range(ne):
+                vdd[unocc, nn] -= vd[t][unocc, st[nn]]
+            estimate = pref * np.abs(vdd).sum() * (abs(detS.real) + abs(detS.imag))
+            if estimate < rnd[t]:
+                continue
+            prob = np.zeros((N, ne))
+            for nn in range(ne):
+                for m in unocc:
+                    s2 = st.copy()
+                    s2[nn] = m
+                    det2 = np.linalg.det(psi[t][s2, :])
+                    prob[m, nn] = pref * (detS * np.conj(det2)).real * vdd[m, nn]
+            prob = np.clip(prob, 0, 1)
+            cum = 0.0
+            new = None
+            for nn in range(ne):
+                for m in unocc:
+                    cum += prob[m, nn]
+                    if rnd[t] < cum:
+                        new = (nn, m)
+                        break
+                if new:
+                    break
+            if new is None:
+                continue
+            nn, m = new
+            old = st[nn]
+            accept = True
+            if rescaling != 2:
+                d = gh[t] * z0[t, m] * z0[t, old] / (w[t, old] - w[t, m])  # d_alpha[m, old]
+                aa = np.sum(d * d / mass) / 2
+                bb = np.dot(d, v[t])
+                cc = w[t, m] - w[t, old]
+                disc = bb * bb - 4 * aa * cc
+                if disc < 0:
+                    accept = False
+                    if rescaling == 1:
+                        dn = d / np.linalg.norm(d)
+                        v[t] = v[t] - 2 * np.dot(v[t], dn) * dn
+                else:
+                    root = np.sqrt(disc)
+                    gam = (bb + root) / (2 * aa) if bb < 0 else (bb - root) / (2 * aa)
+                    v[t] = v[t] - gam * d / mass
+            if accept:
+                state[t, nn] = m
+                hops[t].append((step, int(old), int(m)))
+            else:
+                nfr[t] += 1
+    return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, Z=Z, w=w, initial_state=states)

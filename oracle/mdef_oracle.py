@@ -1,0 +1,174 @@
+"""MDEF oracle -- TEST INFRASTRUCTURE ONLY.
+
+A numpy FP64 restatement of NQCDynamics.jl's electronic-friction Langevin
+dynamics on the Newns-Anderson (AndersonHolstein) model:
+
+  MDEF_BAOAB.perform_step!   src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:338-355
+  step_O!                    src/DynamicsMethods/IntegrationAlgorithms/steps.jl:128-156
+  DiabaticMDEF acceleration! src/DynamicsMethods/ClassicalMethods/mdef.jl:102-124
+  friction!                  src/DynamicsMethods/ClassicalMethods/mdef.jl:131-140
+
+The electronic structure is evaluated the way the reference's cache does it:
+dense eigen-decomposition of the (1 + M) x (1 + M) one-electron Hamiltonian
+(numpy.linalg.eigh, LAPACK), adiabatic derivative Z^T dH Z, Fermi-weighted
+force, and the Gaussian-broadened friction
+    Lambda = sum_nm -pi dH_nm dH_mn g_sigma(e_n - e_m) f'(e_n)
+(the GaussianBroadening form of the reference's calculator package, which
+is not vendored; its normalisation is restated here, parity unpinned).
+
+Noise: one standard normal per degree of freedom and step from the engine's
+Philox4x32-10 stream (key = seed, counter = (trajectory, step, NOISE stream,
+0)), Box-Muller on the block's two 53-bit uniforms, restated in numpy, so the
+oracle and the GPU integrate the same Wiener increments.
+
+Model (restated from the AndersonHolstein definition: impurity level
+h = U1 - U0, couplings V_k = V sqrt(w_k), bath levels e_k, state-independent
+potential U0): a displaced-harmonic impurity
+    U0(x) = k x^2 / 2,   U1(x) = k (x - g)^2 / 2 + Delta,   V constant,
+and the bath of ShenviGaussLegendre(M, a, b) around the Fermi level mu.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+M0 = np.uint64(0xD2511F53)
+M1 = np.uint64(0xCD9E8D57)
+W0 = np.uint32(0x9E3779B9)
+W1 = np.uint32(0xBB67AE85)
+RNG_NOISE = 3
+
+
+def philox(c0, c1, c2, c3, k0, k1):
+    """Vectorised Philox4x32-10 (uint32 arrays)."""
+    c0, c1, c2, c3 = (np.asarray(c, dtype=np.uint32) for c in (c0, c1, c2, c3))
+    k0 = np.uint32(k0)
+    k1 = np.uint32(k1)
+    mask = np.uint64(0xFFFFFFFF)
+    for _ in range(10):
+        p0 = c0.astype(np.uint64) * M0
+        p1 = c2.astype(np.uint64) * M1
+        hi0 = (p0 >> np.uint64(32)).astype(np.uint32)
+        lo0 = (p0 & mask).astype(np.uint32)
+        hi1 = (p1 >> np.uint64(32)).astype(np.uint32)
+        lo1 = (p1 & mask).astype(np.uint32)
+        c0, c1, c2, c3 = hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0
+        k0 = np.uint32((int(k0) + int(W0)) & 0xFFFFFFFF)
+        k1 = np.uint32((int(k1) + int(W1)) & 0xFFFFFFFF)
+    return c0, c1, c2, c3
+
+
+def normal(seed: int, traj: np.ndarray, step: int, dof: int = 0) -> np.ndarray:
+    """Standard normal per trajectory: Box-Muller on one Philox block,
+    u1 = 1 - U53(w0, w1) in (0, 1], u2 = U53(w2, w3)."""
+    traj = np.asarray(traj, dtype=np.uint64)
+    w = philox((traj & np.uint64(0xFFFFFFFF)).astype(np.uint32), (traj >> np.uint64(32)).astype(np.uint32),
+               np.full(traj.shape, step, np.uint32), np.full(traj.shape, RNG_NOISE + 16 * dof, np.uint32),
+               seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
+    a = ((w[0].astype(np.uint64) << np.uint64(32)) | w[1].astype(np.uint64)) >> np.uint64(11)
+    b = ((w[2].astype(np.uint64) << np.uint64(32)) | w[3].astype(np.uint64)) >> np.uint64(11)
+    u1 = 1.0 - a.astype(np.float64) * 2.0**-53
+    u2 = b.astype(np.float64) * 2.0**-53
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def shenvi_gauss_legendre(M: int, a: float, b: float, ef: float = 0.0):
+    """Bath levels and weights (docs/src/NQCModels/systembathmodels.md:241-256):
+    Gauss-Legendre halves below and above the Fermi level.  The upper half's
+    shift is taken as (ef + b)/2, which maps the knots into [ef, b]."""
+    x, w = np.polynomial.legendre.leggauss(M // 2)
+    lo = 0.5 * (ef - a) * x + 0.5 * (a + ef)
+    hi = 0.5 * (b - ef) * x + 0.5 * (ef + b)
+    return np.concatenate([lo, hi]), np.concatenate([0.5 * (ef - a) * w, 0.5 * (b - ef) * w])
+
+
+class NewnsAnderson:
+    def __init__(self, *, k, g, delta, V, eps, weights, mu=0.0):
+        self.k, self.g, self.delta, self.V, self.mu = k, g, delta, V, mu
+        self.eps = np.asarray(eps, np.float64)
+        self.Vk = V * np.sqrt(np.asarray(weights, np.float64))
+        self.nstates = 1 + len(self.eps)
+
+    def h(self, x):
+        return self.k * self.g * (self.g / 2 - x) + self.delta
+
+    def dh(self, x):
+        return -self.k * self.g * np.ones_like(x)
+
+    def dU0(self, x):
+        return self.k * x
+
+    def U0(self, x):
+        return 0.5 * self.k * x * x
+
+    def hamiltonian(self, x):
+        n = len(x)
+        N = self.nstates
+        H = np.zeros((n, N, N))
+        H[:, 0, 0] = self.h(x)
+        H[:, 0, 1:] = self.Vk
+        H[:, 1:, 0] = self.Vk
+        idx = np.arange(1, N)
+        H[:, idx, idx] = self.eps
+        return H
+
+
+def fermi(e, mu, beta):
+    return 0.5 * (1.0 - np.tanh(0.5 * beta * (e - mu)))
+
+
+def dfermi(e, mu, beta):
+    f = fermi(e, mu, beta)
+    return -beta * f * (1.0 - f)
+
+
+def electronic(model, x, beta, sigma, want_friction=True):
+    """Eigenvalues, Fermi-weighted force and broadened friction at x (vectorised)."""
+    w, Z = np.linalg.eigh(model.hamiltonian(x))
+    dh = model.dh(x)
+    z0 = Z[:, 0, :]
+    deps = dh[:, None] * z0 * z0  # (Z^T dH Z)_ii
+    f = fermi(w, model.mu, beta)
+    df = dfermi(w, model.mu, beta)
+    F = model.dU0(x) + np.sum(deps * f + df * deps * w, axis=1)
+    out = {"w": w, "F": F, "z0sq": z0 * z0}
+    if want_friction:
+        dH = dh[:, None, None] * z0[:, :, None] * z0[:, None, :]  # (Z^T dH Z)_nm
+        de = w[:, :, None] - w[:, None, :]
+        g = np.exp(-0.5 * de * de / sigma**2) / (sigma * np.sqrt(2 * np.pi))
+        lam = np.sum(-np.pi * dH * dH * g * df[:, :, None], axis=(1, 2))
+        out["friction"] = lam
+    return out
+
+
+def run_mdef(model: NewnsAnderson, *, mass, beta, sigma, x0, v0, dt, nsteps, seed, traj_offset=0,
+             friction_fn=None):
+    """BAOAB with friction in the tensor's eigenbasis (1 DoF: a scalar).
+    friction_fn(x) may replace the exact friction (surrogate runs)."""
+    x = np.asarray(x0, np.float64).copy()
+    v = np.asarray(v0, np.float64).copy()
+    traj = np.arange(len(x), dtype=np.uint64) + np.uint64(traj_offset)
+    T = 1.0 / beta
+    half = 0.5
+    k = -electronic(model, x, beta, sigma, want_friction=False)["F"] / mass
+    for step in range(1, nsteps + 1):
+        v = v + (half * dt) * k                         # B
+        x = x + (half * dt) * v                         # A
+        if friction_fn is None:
+            lam = electronic(model, x, beta, sigma)["friction"]
+        else:
+            lam = friction_fn(x)
+        gam = np.maximum(lam / mass, 0.0)               # Lambda / (sqrt m sqrt m), clamp(gamma, 0, Inf)
+        c1 = np.exp(-gam * dt)
+        c2 = np.sqrt(1.0 - c1 * c1)
+        noise = np.sqrt(T / mass) * normal(seed, traj, step)
+        v = c1 * v + c2 * noise                         # O
+        x = x + (half * dt) * v                         # A
+        k = -electronic(model, x, beta, sigma, want_friction=False)["F"] / mass
+        v = v + (half * dt) * k                         # B
+    return x, v
+
+
+def energy(model, x, v, mass, beta):
+    """Classical potential of DiabaticMDEF (mdef.jl:162-175) plus kinetic energy."""
+    w, _ = np.linalg.eigh(model.hamiltonian(x))
+    return 0.5 * mass * v * v + model.U0(x) + np.sum(w * fermi(w, model.mu, beta), axis=1)

@@ -1,0 +1,157 @@
+"""GPU parity of the MDEF kernels and of the friction surrogate network.
+
+The engine solves the Newns-Anderson electronic structure through the
+secular equation of its arrowhead Hamiltonian; the oracle diagonalises the
+dense matrix as the reference does (LAPACK).  Agreement is therefore to
+floating-point tolerance, not bitwise:
+  FP64 path: force and friction to 1e-9 relative, trajectories with the
+             same Wiener increments to 1e-8 relative over 100 steps;
+  FP32 path: force and friction to 2e-3 relative, ensemble energy
+             relaxation within 2 % of the FP64 path.
+Surrogate: device gradients equal the float64 reference of the same BF16
+network to 2e-3; a trained network replaces most exact friction
+evaluations while the relaxation curve stays within 2 %.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import mdef_oracle as MO
+import mlp_oracle as MLP
+from nqcd_gb300 import _lib as L
+from nqcd_gb300 import workload as WL
+
+pytestmark = pytest.mark.gpu
+
+
+def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, judge_every=0):
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON, precision
+    cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 1 + len(wl["eps"])
+    params = np.array([wl["k"], wl["g"], wl["delta"], wl["mu"], wl["sigma"]])
+    masses = np.array([wl["mass"]])
+    eps = np.ascontiguousarray(wl["eps"])
+    V = np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 5, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta = wl["beta"]
+    cfg.ntraj_max = ntraj
+    cfg.save_stride = save_stride
+    cfg.use_friction_surrogate = int(surrogate)
+    cfg.judge_every = judge_every
+    return L.Engine(cfg, [params, masses, eps, V])
+
+
+def oracle_model(wl):
+    return MO.NewnsAnderson(k=wl["k"], g=wl["g"], delta=wl["delta"], V=1.0, eps=wl["eps"],
+                            weights=wl["V"] ** 2, mu=wl["mu"])
+
+
+@pytest.mark.parametrize("M", [40, 200])
+def test_mdef_electronic_structure(M):
+    wl = WL.newns_anderson_mdef(8, M=M)
+    x = np.linspace(-0.8, 0.8, 97)
+    ref = MO.electronic(oracle_model(wl), x, wl["beta"], wl["sigma"])
+    for prec, rtol in ((L.PREC_FP64, 1e-9), (L.PREC_FP32, 2e-3)):
+        eng = make_mdef(wl, 8, prec)
+        try:
+            F, G = eng.mdef_evaluate(x)
+        finally:
+            eng.close()
+        np.testing.assert_allclose(F, ref["F"], rtol=rtol, atol=rtol * np.abs(ref["F"]).max())
+        np.testing.assert_allclose(G, ref["friction"], rtol=rtol, atol=rtol * np.abs(ref["friction"]).max())
+    assert ref["friction"].max() > 0
+
+
+def test_mdef_fp64_trajectories_match_oracle():
+    n, nsteps = 32, 100
+    wl = WL.newns_anderson_mdef(n, M=80)
+    eng = make_mdef(wl, n)
+    try:
+        eng.set_initial(wl["x0"].reshape(n, 1).copy(), wl["v0"].reshape(n, 1).copy())
+        _, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 99)
+        fin = eng.get_final(1)
+    finally:
+        eng.close()
+    assert st.unconverged_roots == 0
+    x, v = MO.run_mdef(oracle_model(wl), mass=wl["mass"], beta=wl["beta"], sigma=wl["sigma"], x0=wl["x0"],
+                       v0=wl["v0"], dt=wl["dt"], nsteps=nsteps, seed=99)
+    np.testing.assert_allclose(fin["r"][:, 0], x, rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(fin["v"][:, 0], v, rtol=1e-8, atol=1e-12)
+
+
+def run_relax(wl, n, prec, nsteps, stride, surrogate=False, judge_every=0, mlp=None):
+    eng = make_mdef(wl, n, prec, save_stride=stride, surrogate=surrogate, judge_every=judge_every)
+    try:
+        if mlp is not None:
+            eng.mlp_set(*mlp)
+        eng.set_initial(wl["x0"].reshape(n, 1).copy(), wl["v0"].reshape(n, 1).copy())
+        obs = np.zeros((nsteps // stride + 1) * 4)
+        t0 = time.perf_counter()
+        out, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 5, observables=obs)
+        wall = time.perf_counter() - t0
+        return obs[: out.nsave * 4].reshape(out.nsave, 4), st, wall
+    finally:
+        eng.close()
+
+
+def test_mdef_fp32_relaxation_matches_fp64():
+    n, nsteps, stride = 2048, 400, 20
+    wl = WL.newns_anderson_mdef(n, M=200)
+    a, _, _ = run_relax(wl, n, L.PREC_FP64, nsteps, stride)
+    b, st, _ = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
+    assert st.unconverged_roots == 0
+    ke_a, ke_b = a[:, 2], b[:, 2]
+    assert ke_a[-1] < 0.8 * ke_a[0]  # friction cools the hot adsorbate
+    np.testing.assert_allclose(ke_b, ke_a, rtol=0.02)
+
+
+def test_mlp_gradient_matches_reference():
+    wl = WL.newns_anderson_mdef(4, M=40)
+    eng = make_mdef(wl, 4, L.PREC_FP32)
+    try:
+        rng = np.random.default_rng(3)
+        p = np.zeros(MLP.NP, np.float32)
+        p[0:64] = rng.uniform(-3, 3, 64)
+        p[64:128] = rng.uniform(-3, 3, 64)
+        p[128:128 + 4096] = rng.uniform(-0.2, 0.2, 4096)
+        p[4224:4288] = rng.uniform(-0.1, 0.1, 64)
+        p[4288:4352] = rng.uniform(-0.2, 0.2, 64)
+        p[4352] = 0.3
+        meta = np.array([0.0, 2.0, -0.5, 0.5])
+        eng.mlp_set(p, meta)
+        x = rng.uniform(-0.5, 0.5, 1000)
+        t = rng.uniform(0.0, 1.0, 1000)
+        loss, g = eng.mlp_loss_grad(x, t)
+        w, meta2 = eng.mlp_get()
+    finally:
+        eng.close()
+    np.testing.assert_array_equal(w, p)
+    ref_loss, ref_g = MLP.loss_grad(p.astype(np.float64), x, t, meta[0], meta[1])
+    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    np.testing.assert_allclose(g, ref_g, rtol=2e-3, atol=2e-3 * np.abs(ref_g).max())
+
+
+def test_friction_surrogate_trains_and_serves():
+    n, nsteps, stride = 2048, 400, 20
+    wl = WL.newns_anderson_mdef(n, M=200)
+    lo, hi = -1.2, 1.2
+    eng = make_mdef(wl, 8, L.PREC_FP32)
+    try:
+        loss = eng.train_friction_mlp(lo, hi, 20000, 30, 1024, 2e-3, 11)
+        mlp = eng.mlp_get()
+        xs = np.linspace(lo, hi, 201)
+        _, G = eng.mdef_evaluate(xs)
+    finally:
+        eng.close()
+    pred = MLP.predict_friction(mlp[0].astype(np.float64), xs, mlp[1][0], mlp[1][1])
+    # the network reproduces the exact friction over its domain
+    assert np.max(np.abs(pred - G)) < 0.05 * G.max(), (loss, np.max(np.abs(pred - G)), G.max())
+    exact, st_e, t_e = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
+    surr, st_s, t_s = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, judge_every=50, mlp=mlp)
+    assert st_s.surrogate_friction_evals > 0.9 * n * nsteps * 0.9
+    assert st_s.exact_friction_evals < 0.1 * n * nsteps
+    np.testing.assert_allclose(surr[:, 2], exact[:, 2], rtol=0.02)
+    # gain: the surrogate removes the midpoint electronic-structure evaluation
+    assert st_s.kernel_ms < 0.8 * st_e.kernel_ms, (st_s.kernel_ms, st_e.kernel_ms)

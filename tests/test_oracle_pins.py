@@ -200,3 +200,51 @@ def test_rpsh_free_ring_polymer_centroid_moves_classically():
     o = O.run_rpsh(model=3, params=TULLY[3], mass=2000.0, r0=r0, v0=v0, nbeads=np.full(n, nb, np.int32), beta=1024.0,
                    t0=0.0, t1=100.0, dt=1.0, seed=1)
     np.testing.assert_allclose(o["r"].mean(axis=1), -30.0 + 0.2, rtol=1e-9)
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    # the surrogate network's reference gradient, without BF16 rounding, against central differences
+    import mlp_oracle as MLP
+
+    rng = np.random.default_rng(0)
+    p = np.zeros(MLP.NP)
+    p[0:64] = rng.uniform(-2, 2, 64)
+    p[64:128] = rng.uniform(-2, 2, 64)
+    p[128:4224] = rng.uniform(-0.2, 0.2, 4096)
+    p[4224:4288] = rng.uniform(-0.1, 0.1, 64)
+    p[4288:4352] = rng.uniform(-0.2, 0.2, 64)
+    p[4352] = 0.3
+    x = rng.uniform(-0.5, 0.5, 50)
+    t = rng.uniform(0.0, 1.0, 50)
+    _, g = MLP.loss_grad(p, x, t, 0.0, 2.0, rounding=False)
+    for i in list(rng.choice(MLP.NP, 40, replace=False)) + [4352, 0, 64, 4224, 4288]:
+        e = np.zeros(MLP.NP)
+        e[i] = 1e-6
+        lp, _ = MLP.loss_grad(p + e, x, t, 0.0, 2.0, rounding=False)
+        lm, _ = MLP.loss_grad(p - e, x, t, 0.0, 2.0, rounding=False)
+        assert abs((lp - lm) / 2e-6 - g[i]) <= 1e-6 + 1e-5 * abs(g[i]), i
+
+
+def test_mdef_oracle_friction_and_force_consistency():
+    # force = dE/dx of the Fermi-weighted band energy (finite differences), friction >= 0,
+    # Philox normals have unit variance
+    import mdef_oracle as MO
+    from nqcd_gb300 import workload as WL
+
+    wl = WL.newns_anderson_mdef(4, M=40)
+    model = MO.NewnsAnderson(k=wl["k"], g=wl["g"], delta=wl["delta"], V=1.0, eps=wl["eps"], weights=wl["V"] ** 2)
+    x = np.linspace(-0.5, 0.5, 21)
+    out = MO.electronic(model, x, wl["beta"], wl["sigma"])
+
+    def energy(xx):
+        w, _ = np.linalg.eigh(model.hamiltonian(xx))
+        f = MO.fermi(w, 0.0, wl["beta"])
+        return model.U0(xx) + np.sum(w * f, axis=1)
+
+    h = 1e-6
+    fd = (energy(x + h) - energy(x - h)) / (2 * h)
+    # dE/dx = U0' + sum (d eps_i) (f_i + f'_i eps_i) at fixed mu: the reference force
+    np.testing.assert_allclose(out["F"], fd, rtol=1e-5, atol=1e-8)
+    assert np.all(out["friction"] >= -1e-15)
+    z = MO.normal(7, np.arange(20000), 3)
+    assert abs(z.mean()) < 0.03 and abs(z.std() - 1) < 0.03
