@@ -182,7 +182,9 @@ int nqcd_mdef_evaluate(nqcd_handle* h, int64_t n, const double* x, double* force
 /* MDEF friction surrogate (1-64-64-1 network, BF16 weights): generate npoints
  * exact friction values at positions uniform in [x_lo, x_hi] with the engine,
  * then train the network on the GPU (BF16 tensor-core kernels, FP32 master
- * weights, Adam) for `epochs` passes of minibatches of `batch`.  The trained
+ * weights, Adam with the step size decaying from learning_rate to
+ * learning_rate / 100 on a cosine) for `epochs` passes of minibatches of
+ * `batch`.  The trained
  * network serves runs with use_friction_surrogate inside [x_lo, x_hi].  No
  * counterpart in the reference.  final_loss: mean squared error of the
  * predicted Cholesky factor sqrt(Lambda) (may be NULL). */

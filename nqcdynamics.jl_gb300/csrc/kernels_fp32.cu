@@ -19,7 +19,7 @@ cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s) {
     return launch_fssh2<float>(p, s);
 }
 
-// See kernels_fp64.cu: the per-thread stack must cover the bead arrays.
+// The per-thread stack limit must cover the kernel's spilled bead arrays.
 static cudaError_t ensure_rpsh_stack_fp32() {
     cudaFuncAttributes a;
     cudaError_t e = cudaFuncGetAttributes(&a, rpsh_persistent_kernel<float>);
@@ -27,7 +27,7 @@ static cudaError_t ensure_rpsh_stack_fp32() {
     size_t cur = 0;
     e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
     if (e != cudaSuccess) return e;
-    size_t need = a.localSizeBytes + 8192;
+    size_t need = a.localSizeBytes;
     if (cur < need) e = cudaDeviceSetLimit(cudaLimitStackSize, need);
     return e;
 }

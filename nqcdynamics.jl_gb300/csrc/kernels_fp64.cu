@@ -9,9 +9,9 @@ namespace nqcd {
 
 cudaError_t launch_fssh2_fp64(const FsshParams& p, cudaStream_t s) { return launch_fssh2<double>(p, s); }
 
-// The ring-polymer trajectories of the larger bead counts keep their bead
-// arrays on the per-thread stack; make sure this context's stack limit covers
-// the kernel's requirement (the default is 1 KiB).
+// The persistent ring-polymer kernel calls non-inlined per-bead-count
+// trajectory functions; make sure this context's stack limit covers the
+// kernel's local-memory requirement (the default is 1 KiB).
 static cudaError_t ensure_rpsh_stack_fp64() {
     cudaFuncAttributes a;
     cudaError_t e = cudaFuncGetAttributes(&a, rpsh_persistent_kernel<double>);
@@ -19,7 +19,7 @@ static cudaError_t ensure_rpsh_stack_fp64() {
     size_t cur = 0;
     e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
     if (e != cudaSuccess) return e;
-    size_t need = a.localSizeBytes + 8192;
+    size_t need = a.localSizeBytes;
     if (cur < need) e = cudaDeviceSetLimit(cudaLimitStackSize, need);
     return e;
 }

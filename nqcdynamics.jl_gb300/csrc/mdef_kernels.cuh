@@ -189,8 +189,12 @@ __device__ __forceinline__ void secular_root(const MdefShared<R>& sh, int M, int
         const R ulp = std::is_same<R, float>::value ? R(1.2e-7) : R(2.3e-16);
         R tol = R(2) * ulp * (fabs(d) + fabs(o) * R(1e-3));
         // f has reached the rounding error of its own evaluation: no further
-        // Newton step can be trusted (the secular-equation stopping test)
+        // Newton step can be trusted (the secular-equation stopping test).
+        // The summed error of the M terms can exceed ulp * sum|terms| by about
+        // sqrt(M); after the first iterations accept the bound used by LAPACK's
+        // secular solver, 8 ulp * sum|terms|.
         R ferr = ulp * (fabs(o + d) + fabs(h) + sa);
+        if (it >= 16) ferr *= R(8);
         if (fabs(step) <= tol || dhi - dlo <= tol || fabs(f) <= ferr) {
             conv = true;
             break;

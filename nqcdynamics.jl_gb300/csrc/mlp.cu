@@ -236,11 +236,14 @@ __global__ void mlp_tick_kernel(unsigned long long* counter) { *counter += 1ull;
 
 __global__ void mlp_adam_kernel(float* __restrict__ w, float* __restrict__ m1, float* __restrict__ m2,
                                 const float* __restrict__ g, __nv_bfloat16* __restrict__ bf,
-                                const unsigned long long* counter, float lr) {
+                                const unsigned long long* counter, float lr0, float total_steps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kMlpN) return;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     float t = (float)*counter;
+    // cosine decay from lr0 to lr0 / 100 over the run
+    float frac = total_steps > 1.f ? fminf((t - 1.f) / total_steps, 1.f) : 0.f;
+    float lr = lr0 * (0.01f + 0.495f * (1.f + cospif(frac)));
     float gi = g[i];
     float a = b1 * m1[i] + (1.f - b1) * gi;
     float b = b2 * m2[i] + (1.f - b2) * gi * gi;
@@ -343,7 +346,8 @@ cudaError_t mlp_train_device(MlpState& s, const double* d_x, const double* d_t, 
     mlp_fwd_bwd_kernel<<<nb, 128, train_smem(), st>>>(s.bf, d_x, d_t, s.batch_index, batch, (float)batch,
                                                       (float)s.shift, (float)s.scale, s.partial);
     mlp_reduce_kernel<<<(kMlpN + 1 + 255) / 256, 256, 0, st>>>(s.partial, nb, s.grad);
-    mlp_adam_kernel<<<(kMlpN + 255) / 256, 256, 0, st>>>(s.master, s.m1, s.m2, s.grad, s.bf, s.step_counter, lr);
+    mlp_adam_kernel<<<(kMlpN + 255) / 256, 256, 0, st>>>(s.master, s.m1, s.m2, s.grad, s.bf, s.step_counter, lr,
+                                                         (float)nsteps);
     e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) return e;
     e = cudaGraphInstantiate(&exec, graph, 0);

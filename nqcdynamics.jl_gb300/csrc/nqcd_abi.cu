@@ -173,6 +173,8 @@ struct nqcd_handle {
     float *d_rpUf = nullptr, *d_rpcayf = nullptr;
     int32_t *d_nbeads = nullptr, *d_class_traj = nullptr, *d_block_class = nullptr;
     unsigned long long* d_queue = nullptr;
+    double* d_rpscratch = nullptr;  // plain path bead arrays, grown on demand
+    int64_t rpscratch_cap = 0;
     int nclass = 0;
     int class_beads[kRpshMaxClasses] = {0};
     int class_slot[kRpshMaxClasses] = {0};  // index into kRpCounts
@@ -217,7 +219,7 @@ void free_all(nqcd_handle* h) {
                     h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
                     h->d_rpU, h->d_rpcay, h->d_rpUf, h->d_rpcayf, h->d_nbeads, h->d_class_traj,
-                    h->d_block_class, h->d_queue, h->d_eps, h->d_V2};
+                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mlp_free(h->mlp);
@@ -740,6 +742,21 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         rq.hop_log = h->d_hoplog;
         rq.energy = h->d_energy;
         rq.scatter = h->d_counts;
+        if (plain) {
+            int maxb = 1;
+            for (int k = 0; k < h->nclass; ++k) maxb = h->class_beads[k] > maxb ? h->class_beads[k] : maxb;
+            const int64_t threads = (int64_t)grid * kRpshBlock, need = 6 * (int64_t)maxb * threads;
+            if (need > h->rpscratch_cap) {
+                NQCD_CUDA(h, cudaStreamSynchronize(s));
+                if (h->d_rpscratch) cudaFree(h->d_rpscratch);
+                h->d_rpscratch = nullptr;
+                h->rpscratch_cap = 0;
+                NQCD_CUDA(h, dalloc(&h->d_rpscratch, need));
+                h->rpscratch_cap = need;
+            }
+            rq.scratch = h->d_rpscratch;
+            rq.scratch_stride = threads;
+        }
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         e = plain ? launch_rpsh_fp64(rq, grid, s) : launch_rpsh_fp32(rq, grid, s);
     } else if (mdef) {

@@ -72,6 +72,9 @@ struct RpshParams {
     int32_t* hop_log;  // [max_hops][3][ntraj]
     double* energy;    // [2][ntraj]
     unsigned long long* scatter;  // [4]
+    // plain path: bead-array scratch, [6 * bead count][scratch_stride] doubles
+    double* scratch;
+    int64_t scratch_stride;  // threads in the launch
 };
 
 __device__ __forceinline__ void rp_log_hop(const RpshParams& p, int64_t i, int nh, int step, int from, int to) {
@@ -145,6 +148,20 @@ __device__ __forceinline__ R rp_bead_accel(int model, const R* mp, R x, int s, R
 // ---------------------------------------------------------------------------
 // plain FP64 trajectory (oracle order)
 // ---------------------------------------------------------------------------
+// One column of the launch's scratch block: element j of a per-thread bead
+// array, stride = threads in the launch (coalesced across a warp).
+struct BeadCol {
+    double* base;
+    int64_t stride;
+    __device__ __forceinline__ double& operator[](int j) const { return base[(int64_t)j * stride]; }
+};
+
+// The six bead arrays of a plain trajectory (r, v, k, vt and the normal-mode
+// q, p) live in the launch's global scratch block, one column per thread,
+// instead of in per-thread local arrays: with 16 and 32 beads the local-array
+// form of this FP64 code gave wrong results on sm_103a while the identical
+// source compiled for the host reproduces the oracle bit for bit (cause not
+// identified).  The arithmetic and its order are unchanged.
 template <int B>
 __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64_t i) {
     const int64_t N = p.ntraj;
@@ -156,15 +173,16 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
     double mp[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) mp[q] = p.class_mp[cls][q];
-    double r[B], v[B], k[B], vt[B], qm[B], pm[B];
-#pragma unroll
+    const int64_t T = p.scratch_stride;
+    double* col = p.scratch + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const BeadCol r{col, T}, v{col + (int64_t)B * T, T}, k{col + (int64_t)2 * B * T, T},
+        vt{col + (int64_t)3 * B * T, T}, qm{col + (int64_t)4 * B * T, T}, pm{col + (int64_t)5 * B * T, T};
     for (int j = 0; j < B; ++j) {
         r[j] = p.r[(int64_t)j * N + i];
         v[j] = p.v[(int64_t)j * N + i];
     }
-    auto centroid = [&](const double* x) {
+    auto centroid = [&](const BeadCol& x) {
         double acc = 0.0;
-#pragma unroll
         for (int j = 0; j < B; ++j) acc = acc + x[j];
         return acc / B;
     };
@@ -184,12 +202,10 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
         double spring = 0.0;
         if (B > 1) {
             spring = spring + mass * ((r[B - 1] - r[0]) * (r[B - 1] - r[0]));
-#pragma unroll
             for (int j = 0; j < B - 1; ++j) spring = spring + mass * ((r[j] - r[j + 1]) * (r[j] - r[j + 1]));
         }
         spring = spring * (wn * wn) / 2.0;
         double ke = 0.0, pe = 0.0;
-#pragma unroll
         for (int j = 0; j < B; ++j) ke = ke + mass * (v[j] * v[j]);
         for (int j = 0; j < B; ++j) {
             double ws;
@@ -214,15 +230,10 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
     while (t < p.t1) {
         double h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
         double half = h / 2.0;
-#pragma unroll
         for (int j = 0; j < B; ++j) vt[j] = v[j] + half * k[j];
-        // to normal modes: q_k = sum_j U[j,k] x_j.  The transform loops are
-        // kept rolled: fully unrolled at 16 and 32 beads this FP64 code was
-        // miscompiled (wrong results on the device, exact on the host).
-#pragma unroll 1
+        // to normal modes: q_k = sum_j U[j,k] x_j
         for (int kk = 0; kk < B; ++kk) {
             double a = U[0 + B * kk] * r[0], b = U[0 + B * kk] * vt[0];
-#pragma unroll 1
             for (int j = 1; j < B; ++j) {
                 a = a + U[j + B * kk] * r[j];
                 b = b + U[j + B * kk] * vt[j];
@@ -230,7 +241,6 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
             qm[kk] = a;
             pm[kk] = b;
         }
-#pragma unroll 1
         for (int kk = 0; kk < B; ++kk) {  // step_C!
             const double* c = cay + 4 * kk;
             double rn = c[0] * qm[kk] + c[1] * pm[kk];
@@ -239,10 +249,8 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
             pm[kk] = vn;
         }
         // from normal modes: x_j = sum_k U[j,k] q_k
-#pragma unroll 1
         for (int j = 0; j < B; ++j) {
             double a = U[j] * qm[0], b = U[j] * pm[0];
-#pragma unroll 1
             for (int kk = 1; kk < B; ++kk) {
                 a = a + U[j + B * kk] * qm[kk];
                 b = b + U[j + B * kk] * pm[kk];
@@ -251,7 +259,6 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
             vt[j] = b;
         }
         for (int j = 0; j < B; ++j) k[j] = rp_bead_accel<double>(model, mp, r[j], state, mass, nullptr);
-#pragma unroll
         for (int j = 0; j < B; ++j) v[j] = vt[j] + half * k[j];
         xc = centroid(r);
         update_centroid(xc);
@@ -292,18 +299,15 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
                         double nrm = sqrt(0.0 + d * d);
                         double dn = d / nrm;
                         double vcom = 0.0;
-#pragma unroll
                         for (int j = 0; j < B; ++j) vcom = vcom + v[j];
                         vcom = vcom / B;
                         double g = 0.0 + vcom * dn;
-#pragma unroll
                         for (int j = 0; j < B; ++j) v[j] = v[j] - 2.0 * g * dn;
                     }
                 } else {
                     double root = sqrt(disc);
                     double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
                     double dv = gamma * d / mass;
-#pragma unroll
                     for (int j = 0; j < B; ++j) v[j] = v[j] - dv;
                 }
             }
@@ -317,7 +321,6 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
         }
         if (p.terminate_x > 0.0 && fabs(centroid(r)) > p.terminate_x) break;
     }
-#pragma unroll
     for (int j = 0; j < B; ++j) {
         p.r[(int64_t)j * N + i] = r[j];
         p.v[(int64_t)j * N + i] = v[j];

@@ -12,8 +12,6 @@ Surrogate: device gradients equal the float64 reference of the same BF16
 network to 2e-3; a trained network replaces most exact friction
 evaluations while the relaxation curve stays within 2 %.
 """
-import time
-
 import numpy as np
 import pytest
 
@@ -88,23 +86,34 @@ def run_relax(wl, n, prec, nsteps, stride, surrogate=False, judge_every=0, mlp=N
             eng.mlp_set(*mlp)
         eng.set_initial(wl["x0"].reshape(n, 1).copy(), wl["v0"].reshape(n, 1).copy())
         obs = np.zeros((nsteps // stride + 1) * 4)
-        t0 = time.perf_counter()
         out, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 5, observables=obs)
-        wall = time.perf_counter() - t0
-        return obs[: out.nsave * 4].reshape(out.nsave, 4), st, wall
+        fin = eng.get_final(1)
+        return obs[: out.nsave * 4].reshape(out.nsave, 4), st, fin["energy"]
     finally:
         eng.close()
 
 
+def energy_drop(energy):
+    """Mean and standard error of the total-energy change per trajectory."""
+    d = energy[:, 1] - energy[:, 0]
+    return d.mean(), d.std() / np.sqrt(len(d))
+
+
 def test_mdef_fp32_relaxation_matches_fp64():
+    # the hot ensemble (10x the electronic temperature) loses energy to the
+    # electrons; the kinetic energy alone oscillates (the potential minimum
+    # is displaced from the initial distribution), the total energy falls
     n, nsteps, stride = 2048, 400, 20
     wl = WL.newns_anderson_mdef(n, M=200)
-    a, _, _ = run_relax(wl, n, L.PREC_FP64, nsteps, stride)
-    b, st, _ = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
-    assert st.unconverged_roots == 0
-    ke_a, ke_b = a[:, 2], b[:, 2]
-    assert ke_a[-1] < 0.8 * ke_a[0]  # friction cools the hot adsorbate
-    np.testing.assert_allclose(ke_b, ke_a, rtol=0.02)
+    a, st_a, e_a = run_relax(wl, n, L.PREC_FP64, nsteps, stride)
+    b, st_b, e_b = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
+    assert st_a.unconverged_roots == 0 and st_b.unconverged_roots == 0
+    da, sa = energy_drop(e_a)
+    db, sb = energy_drop(e_b)
+    assert da < -5 * sa  # friction removes energy
+    assert abs(db - da) <= 0.02 * abs(da) + 2 * sa, (da, db, sa)
+    np.testing.assert_allclose(b[:, 2], a[:, 2], rtol=0.02)  # <KE>(t)
+    np.testing.assert_allclose(b[:, 0], a[:, 0], rtol=0.02, atol=0.01)  # <x>(t)
 
 
 def test_mlp_gradient_matches_reference():
@@ -134,12 +143,14 @@ def test_mlp_gradient_matches_reference():
 
 
 def test_friction_surrogate_trains_and_serves():
+    # the domain covers where the hot ensemble goes (its potential minimum is
+    # near x = 0.9); outside it the kernel falls back to the exact friction
     n, nsteps, stride = 2048, 400, 20
     wl = WL.newns_anderson_mdef(n, M=200)
-    lo, hi = -1.2, 1.2
+    lo, hi = -1.5, 2.5
     eng = make_mdef(wl, 8, L.PREC_FP32)
     try:
-        loss = eng.train_friction_mlp(lo, hi, 20000, 30, 1024, 2e-3, 11)
+        loss = eng.train_friction_mlp(lo, hi, 20000, 150, 1024, 3e-3, 11)
         mlp = eng.mlp_get()
         xs = np.linspace(lo, hi, 201)
         _, G = eng.mdef_evaluate(xs)
@@ -147,11 +158,15 @@ def test_friction_surrogate_trains_and_serves():
         eng.close()
     pred = MLP.predict_friction(mlp[0].astype(np.float64), xs, mlp[1][0], mlp[1][1])
     # the network reproduces the exact friction over its domain
-    assert np.max(np.abs(pred - G)) < 0.05 * G.max(), (loss, np.max(np.abs(pred - G)), G.max())
-    exact, st_e, t_e = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
-    surr, st_s, t_s = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, judge_every=50, mlp=mlp)
-    assert st_s.surrogate_friction_evals > 0.9 * n * nsteps * 0.9
-    assert st_s.exact_friction_evals < 0.1 * n * nsteps
+    assert np.max(np.abs(pred - G)) < 0.02 * G.max(), (loss, np.max(np.abs(pred - G)), G.max())
+    exact, st_e, e_e = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
+    surr, st_s, e_s = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, judge_every=50, mlp=mlp)
+    total = n * nsteps
+    assert st_s.surrogate_friction_evals + st_s.exact_friction_evals == total
+    assert st_s.surrogate_friction_evals > 0.9 * total
+    de, se = energy_drop(e_e)
+    ds, ss = energy_drop(e_s)
+    assert abs(ds - de) <= 0.03 * abs(de) + 2 * se, (de, ds, se)
     np.testing.assert_allclose(surr[:, 2], exact[:, 2], rtol=0.02)
     # gain: the surrogate removes the midpoint electronic-structure evaluation
     assert st_s.kernel_ms < 0.8 * st_e.kernel_ms, (st_s.kernel_ms, st_e.kernel_ms)

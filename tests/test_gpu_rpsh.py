@@ -120,7 +120,10 @@ def test_rpsh_fast_observables():
     sig = np.sqrt(np.maximum(p * (1 - p), 1e-4) / ntraj)
     assert np.all(np.abs(a["scatter"] - b["scatter"]) <= 3 * sig + 1e-12), (a["scatter"], b["scatter"])
     assert np.mean(a["state"] == b["state"]) > 0.95
-    assert np.all(b["nsteps"] < 20000)
+    # a few slow trajectories that hop up without rescaling crawl on the upper
+    # surface past t1 in both precisions; the unterminated fractions agree
+    assert np.mean(a["nsteps"] >= 20000) < 0.005
+    assert abs(np.mean(a["nsteps"] >= 20000) - np.mean(b["nsteps"] >= 20000)) <= 0.002
     # termination time agrees to a few steps for trajectories with the same hop history
     same = (a["nhops"] == b["nhops"]) & (a["state"] == b["state"])
     assert np.mean(np.abs(a["nsteps"][same] - b["nsteps"][same]) <= 2) > 0.95
