@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 100
+#define NQCD_ABI_VERSION 101
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -50,10 +50,14 @@ enum nqcd_model {
     NQCD_MODEL_TULLY2 = 2,    /* params: A, B, C, D, E0 */
     NQCD_MODEL_TULLY3 = 3,    /* params: A, B, C */
     NQCD_MODEL_SPINBOSON = 10, /* params: eps, Delta; bath_a = c_j, bath_b = omega_j */
-    NQCD_MODEL_NEWNS_ANDERSON = 20 /* AndersonHolstein with a displaced-harmonic impurity:
+    NQCD_MODEL_NEWNS_ANDERSON = 20, /* AndersonHolstein with a displaced-harmonic impurity:
                                       U0 = k x^2/2, U1 = k (x-g)^2/2 + delta; params: k, g, delta, mu, sigma
                                       (Fermi level, Gaussian broadening width of the friction);
                                       bath_a = bath levels e_k (ascending), bath_b = couplings V_k */
+    NQCD_MODEL_NEWNS_ANDERSON_3D = 21 /* AndersonHolstein, one atom (x, y, z) above the metal:
+                                      U0 = kxy (x^2+y^2)/2 + A exp(-a z), h = U1 - U0 = delta - B exp(-b z);
+                                      params: kxy, A, a, delta, B, b; bath_a = e_k (ascending),
+                                      bath_b = V_k; nstates = nbath + 1 */
 };
 
 enum nqcd_precision {
@@ -67,7 +71,9 @@ enum nqcd_rescaling { NQCD_RESCALE_STANDARD = 0, NQCD_RESCALE_VINVERSION = 1, NQ
 enum nqcd_init {
     NQCD_INIT_GIVEN = 0,          /* density matrix and state from nqcd_set_initial */
     NQCD_INIT_ADIABATIC_PURE = 1, /* PureState(init_state, Adiabatic()) */
-    NQCD_INIT_DIABATIC_PURE = 2   /* PureState(init_state, Diabatic()): rotated, state sampled */
+    NQCD_INIT_DIABATIC_PURE = 2,  /* PureState(init_state, Diabatic()): rotated, state sampled */
+    NQCD_INIT_FERMI_DIRAC = 3     /* IESH: FermiDiracState(mu, 1/beta, Adiabatic()), occupations sampled
+                                     (src/DynamicsUtils/DynamicsUtils.jl:194-208); NQCD_INIT_GIVEN reads them */
 };
 
 typedef struct nqcd_config {
@@ -96,14 +102,18 @@ typedef struct nqcd_config {
     int64_t traj_offset;  /* global index of trajectory 0 (Philox counter), for sharded ensembles */
     int32_t use_friction_surrogate; /* MDEF fast path: friction from the trained network inside its domain */
     int32_t judge_every;  /* MDEF with surrogate: exact friction every judge_every steps (0 = never) */
-    int32_t reserved[4];
+    int32_t nelectrons;   /* IESH: electrons (occupied one-electron states) */
+    int32_t exact_hop_probability; /* IESH: 1 = no estimate screen (estimate_probability = false) */
+    int32_t reserved[2];
 } nqcd_config;
 
 typedef struct nqcd_outputs {
     /* Ensemble means (MeanReduction, src/Ensembles/reductions.jl:36-52).  Host pointers; NULL to skip. */
     double* scattering;             /* [2][nstates]: reflection, transmission (OutputStateResolvedScattering1D) */
     double* population_correlation; /* [nsave][nstates][nstates] (PopulationCorrelationFunction, Diabatic) */
-    double* observables;            /* MDEF: [nsave][4] means of x, x^2, kinetic energy, friction */
+    double* observables;            /* MDEF: [nsave][4] means of x, x^2, kinetic energy, friction;
+                                       IESH: [nsave][4] means of z, kinetic energy, impurity (diabatic)
+                                       population (iesh.jl:351-369), potential energy (iesh.jl:380-388) */
     int32_t nsave;                  /* out: save points written */
     int32_t reserved;
 } nqcd_outputs;
@@ -122,7 +132,9 @@ typedef struct nqcd_stats {
     int32_t reserved;
     int64_t exact_friction_evals;     /* MDEF: electronic friction evaluations */
     int64_t surrogate_friction_evals; /* MDEF: friction values taken from the surrogate network */
-    int64_t unconverged_roots;        /* MDEF: secular roots that hit the iteration cap */
+    int64_t unconverged_roots;        /* MDEF, IESH: secular roots that hit the iteration cap */
+    int64_t hop_evaluations;          /* IESH: steps whose hop probabilities were evaluated in full */
+    int64_t propagator_terms;         /* IESH: Chebyshev terms summed over trajectory steps */
 } nqcd_stats;
 
 typedef struct nqcd_handle nqcd_handle;
@@ -140,6 +152,9 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out);
  * sample_distribution, src/Ensembles/selections.jl:70-99, and
  * DynamicsVariables, fssh.jl:215-233).  r0, v0: (ndofs, natoms[, nbeads], ntraj).
  * sig_re/sig_im/state0 are read only for NQCD_INIT_GIVEN (else may be NULL).
+ * IESH: state0 holds the occupied states (nelectrons, ntraj), 0-based and
+ * distinct, the orbitals start as unit vectors on them (iesh.jl:89-97);
+ * sig_re/sig_im are not read.
  * nbeads: per-trajectory bead counts for ring polymers (NULL = nbeads_max). */
 int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, const double* sig_re,
                      const double* sig_im, const int32_t* state0, const int32_t* nbeads);
@@ -151,8 +166,10 @@ int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0_so
 
 /* Run the ensemble from t0 to t1 with step dt (reference: the ensemble solve,
  * src/Ensembles/run_dynamics.jl:91-97, with the method's integrator,
- * src/DynamicsMethods/IntegrationAlgorithms/bab_electronics.jl:61-91 or
- * bcb_electronics.jl:53-97, and hopping callback surface_hopping.jl:2-16).
+ * src/DynamicsMethods/IntegrationAlgorithms/bab_electronics.jl:61-91,
+ * bcb_electronics.jl:53-97, verlet_with_electronics.jl:42-69 (IESH) or
+ * mdef_baoab.jl:163-180 (MDEF), and hopping callbacks surface_hopping.jl:2-16,
+ * iesh.jl:390-411).
  * Every run starts from the initial conditions last set.  Random numbers are
  * Philox4x32-10 keyed by `seed` with counter (trajectory, step, stream). */
 int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out,
@@ -161,7 +178,9 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
 /* Final per-trajectory state of the last run (any pointer may be NULL):
  * r, v as in nqcd_set_initial; sig_re/sig_im (nstates, nstates, ntraj);
  * state, nhops, nfrustrated, nsteps [ntraj]; energy [ntraj][2] (initial, final
- * total energy, DynamicsOutputs.OutputTotalEnergy). */
+ * total energy, DynamicsOutputs.OutputTotalEnergy).
+ * IESH: sig_re/sig_im receive the orbitals psi (nstates, nelectrons, ntraj)
+ * and state the occupations (nelectrons, ntraj) in electron order. */
 int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double* sig_im, int32_t* state,
                    int32_t* nhops, int32_t* nfrustrated, int32_t* nsteps, double* energy);
 

@@ -1,0 +1,808 @@
+// IESH (independent-electron surface hopping) ensemble kernel on a
+// three-dimensional Newns-Anderson adsorbate; one CTA per trajectory.
+//
+// Reference algorithm (NQCDynamics.jl):
+//   VerletwithElectronics.perform_step!  src/DynamicsMethods/IntegrationAlgorithms/verlet_with_electronics.jl:42-69
+//   IESH acceleration!                   src/DynamicsMethods/SurfaceHoppingMethods/iesh.jl:190-207
+//   get_quantum_propagator,
+//   propagate_wavefunction!              src/DynamicsUtils/wavefunction_dynamics.jl:15-58
+//   evaluate_hopping_probability!        iesh.jl:231-283 (estimate screen :251-254)
+//   evaluate_v_dot_d!, calculate_Akj,
+//   compute_overlap!                     iesh.jl:285-316
+//   select_new_state                     iesh.jl:318-335
+//   iesh_check_hop!, iesh_execute_hop!   iesh.jl:390-411
+//   rescale_velocity!                    src/DynamicsMethods/SurfaceHoppingMethods/surface_hopping.jl:64-168
+//   FermiDiracState{Adiabatic} start     iesh.jl:99-128 with sample_fermi_dirac_distribution
+//                                        src/DynamicsUtils/DynamicsUtils.jl:194-208
+//   iesh_diabatic_population             iesh.jl:351-369
+//   classical_potential_energy           iesh.jl:380-388
+//
+// Model: one atom (x, y, z) above a metal band, AndersonHolstein form
+//     U0 = kxy (x^2 + y^2) / 2 + A exp(-a z),   h = U1 - U0 = delta - B exp(-b z),
+//     H  = [[h, V_k], [V_k, diag(e_k)]]          (N = M + 1 one-electron states).
+// The reference diagonalises H (LAPACK) every step.  H is an arrowhead matrix
+// whose derivative is dh e0 e0^T, so the eigenvalues l_i are the roots of the
+// secular equation (secular.h), the adiabatic derivative is
+// (Z^T dH Z)_ij = dh z0_i z0_j and the couplings are d_ij = dh A_ij with
+// A_ij = z0_i z0_j / (l_j - l_i): O(N^2) per step instead of O(N^3).
+//
+// Propagator: the reference forms H_eff = diag(l) - i (v . grad h) A, takes its
+// full Hermitian eigendecomposition and applies U exp(-i mu dt) U^H to the
+// N x Ne orbital matrix psi.  Here exp(-i H_eff dt) psi is applied directly as
+// a Chebyshev series (Tal-Ezer and Kosloff, J. Chem. Phys. 81, 3967 (1984)):
+//     exp(-i H dt) = exp(-i c dt) sum_k (2 - delta_k0) (-i)^k J_k(alpha) T_k(Ht),
+//     Ht = (H - c) / w,  alpha = w dt,
+// with [c - w, c + w] a Gershgorin enclosure of the spectrum and the series cut
+// where |J_k(alpha)| falls below the tolerance (1e-17 on the plain path, so
+// the result equals the eigendecomposition to rounding).  Each term is one
+// product of the real N x N matrix A with the complex N x Ne block, done with
+// 4 x 4 register tiles per thread.
+//
+// Hop probabilities: S = psi[state, :] (Ne x Ne) is LU-factorised once per
+// step for det S and the estimate screen.  Where the screen does not reject,
+// the reference evaluates the determinant of every row-replaced S' (1600 LU
+// factorisations for 40 electrons in 80 states); by the matrix determinant
+// lemma det S' = det S (psi[m, :] S^-1)_n, so all of them follow from one
+// solve S^T Y = psi[unocc, :]^T, and
+//     p_mn = 2 dt Re(Y_nm) (v.d)_mn = prefactor Re(det S conj(det S')) (v.d)_mn.
+//
+// R = double: plain path.  R = float: fast path (FP32 electronic structure,
+// propagation and hop linear algebra; positions, velocities and the hop
+// decision's scalar logic in FP64; initial occupations from FP64 roots).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "fssh2_traj.h"
+#include "nqcd_math.h"
+#include "secular.h"
+
+namespace nqcd {
+
+constexpr int kIeshBlock = 256;
+constexpr int kIeshMaxStates = 128;
+constexpr int kIeshMaxTerms = 128;  // Chebyshev terms (Bessel recurrence starts at kIeshMaxTerms - 1)
+
+enum IeshInit : int32_t { IESH_INIT_GIVEN = 0, IESH_INIT_FERMI_DIRAC = 3 };
+
+struct IeshParams {
+    int32_t nbath, nstates, nelec;  // nstates = nbath + 1
+    const double* eps;              // [nbath] ascending bath levels
+    const double* V2;               // [nbath] V_k^2
+    double sumV2;
+    double kxy, A, a, delta, B, b;  // model, see above
+    double beta;                    // electronic inverse temperature (Fermi-Dirac start)
+    double mass;
+    int32_t rescaling;
+    int32_t init_kind;
+    int32_t exact_probability;      // 1: every step evaluates all probabilities (estimate_probability = false)
+    int32_t save_stride, nsave, max_hops;
+    int64_t ntraj, traj_offset;
+    double dt;
+    int32_t nsteps;
+    uint64_t seed;
+    double cheb_tol;                // truncation of the Chebyshev series
+    double* r;                      // [3][ntraj] in/out
+    double* v;                      // [3][ntraj] in/out
+    const int32_t* occ0;            // [nelec][ntraj] given initial occupations (IESH_INIT_GIVEN)
+    int32_t* occ;                   // [nelec][ntraj] final occupations (electron order)
+    double* psi_re;                 // [ntraj][nelec][nstates] final orbitals, or null
+    double* psi_im;
+    int32_t* nhops;
+    int32_t* nfrustrated;
+    int32_t* nsteps_out;
+    int32_t* hop_log;               // [max_hops][3][ntraj]: step, from, to
+    double* energy;                 // [2][ntraj] total energy at start and end, or null
+    double* obs_partial;            // [ntraj][nsave][4]: z, kinetic, impurity population, potential
+    unsigned long long* counters;   // [0] full hop evaluations, [1] Chebyshev terms, [2] unconverged roots
+};
+
+template <typename R>
+struct alignas(2 * sizeof(R)) Cx {
+    R re, im;
+};
+
+// Dynamic shared memory layout of one CTA (identical on host and device).
+struct IeshLayout {
+    int N, Ne, Nu, Np, Nep;
+    size_t o_eps, o_V2, o_lam, o_z2, o_z0, o_lam64, o_At, o_phiA, o_phiB, o_J, o_occ, o_unocc, o_piv, o_red,
+        o_misc, bytes;
+};
+
+NQCD_HD size_t iesh_take(size_t& o, size_t bytes) {
+    size_t at = o;
+    o += (bytes + 15) & ~(size_t)15;
+    return at;
+}
+
+template <typename R>
+NQCD_HD IeshLayout iesh_layout(int N, int Ne) {
+    IeshLayout L;
+    L.N = N;
+    L.Ne = Ne;
+    L.Nu = N - Ne;
+    L.Np = (N + 3) & ~3;
+    L.Nep = (Ne + 3) & ~3;
+    size_t o = 0;
+    L.o_eps = iesh_take(o, sizeof(R) * L.Np);
+    L.o_V2 = iesh_take(o, sizeof(R) * L.Np);
+    L.o_lam = iesh_take(o, sizeof(R) * L.Np);
+    L.o_z2 = iesh_take(o, sizeof(R) * L.Np);
+    L.o_z0 = iesh_take(o, sizeof(R) * L.Np);
+    L.o_lam64 = iesh_take(o, sizeof(double) * L.Np);
+    L.o_At = iesh_take(o, sizeof(R) * L.Np * L.Np);
+    L.o_phiA = iesh_take(o, 2 * sizeof(R) * L.Np * L.Nep);
+    const size_t pb = 2 * sizeof(R) * (size_t)L.Np * L.Nep;
+    const size_t lu = 2 * sizeof(R) * (size_t)L.Nep * (L.Nep + L.Nu);  // S^T and the right-hand sides
+    L.o_phiB = iesh_take(o, lu > pb ? lu : pb);
+    L.o_J = iesh_take(o, sizeof(double) * kIeshMaxTerms);
+    L.o_occ = iesh_take(o, sizeof(int) * L.Nep);
+    L.o_unocc = iesh_take(o, sizeof(int) * L.Np);
+    L.o_piv = iesh_take(o, sizeof(int) * L.Nep);
+    L.o_red = iesh_take(o, sizeof(double) * 72);
+    L.o_misc = iesh_take(o, sizeof(double) * 32);
+    L.bytes = o;
+    return L;
+}
+
+// Register tiles of the A * phi products: 4 rows x 4 orbitals per thread.
+NQCD_HD int iesh_tiles(int N, int Ne) { return (((N + 3) & ~3) / 4) * (((Ne + 3) & ~3) / 4); }
+
+// Bessel functions J_k(alpha), k = 0 .. kIeshMaxTerms-1, by Miller's backward
+// recurrence J_{k-1} = (2k / alpha) J_k - J_{k+1} from order kIeshMaxTerms + 20,
+// normalised with J_0 + 2 sum_{k>=1} J_{2k} = 1.  Returns the last order K
+// with |J_K| >= tol (the series uses terms 0..K), or -1 if the tail is not
+// below tol within kIeshMaxTerms terms.
+__device__ inline int iesh_bessel(double alpha, double tol, double* J) {
+    const int top = kIeshMaxTerms + 20;
+    double jp1 = 0.0, jk = 1e-280, sum = 0.0;
+    for (int k = top; k > 0; --k) {
+        const double jm1 = (2.0 * k / alpha) * jk - jp1;
+        jp1 = jk;
+        jk = jm1;  // J_{k-1}
+        if (k - 1 < kIeshMaxTerms) J[k - 1] = jk;
+        if (k - 1 > 0 && ((k - 1) & 1) == 0) sum += 2.0 * jk;
+        if (fabs(jk) > 1e250) {  // rescale the recurrence
+            jk *= 1e-250;
+            jp1 *= 1e-250;
+            sum *= 1e-250;
+            for (int q = k - 1; q < kIeshMaxTerms; ++q) J[q] *= 1e-250;
+        }
+    }
+    const double norm = 1.0 / (sum + jk);
+    for (int q = 0; q < kIeshMaxTerms; ++q) J[q] *= norm;
+    int K = kIeshMaxTerms - 1;
+    while (K > 0 && fabs(J[K]) < tol) --K;
+    if (K >= kIeshMaxTerms - 2) return -1;
+    return K;
+}
+
+// k-th (0-based) unset bit among bits [0, n) of a 128-bit mask.
+__device__ inline int iesh_nth_unset(const unsigned long long* m, int n, int k) {
+    for (int w = 0; w < 2; ++w) {
+        const int lo = 64 * w;
+        if (lo >= n) break;
+        const int nb = n - lo < 64 ? n - lo : 64;
+        const unsigned long long valid = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
+        unsigned long long z = ~m[w] & valid;
+        const int c = __popcll(z);
+        if (k < c) {
+            for (int q = 0; q < k; ++q) z &= z - 1ull;
+            return lo + __ffsll((long long)z) - 1;
+        }
+        k -= c;
+    }
+    return -1;
+}
+
+// Deterministic block reductions (fixed order), result broadcast to all threads.
+__device__ inline double iesh_block_sum(double x, double* red) {
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) red[w] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double s = l < nw ? red[l] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (l == 0) red[64] = s;
+    }
+    __syncthreads();
+    return red[64];
+}
+
+__device__ inline void iesh_block_minmax(double& lo, double& hi, double* red) {
+    for (int off = 16; off > 0; off >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) {
+        red[w] = lo;
+        red[32 + w] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double a = l < nw ? red[l] : 1e300, b = l < nw ? red[32 + l] : -1e300;
+        for (int off = 16; off > 0; off >>= 1) {
+            a = fmin(a, __shfl_xor_sync(0xffffffffu, a, off));
+            b = fmax(b, __shfl_xor_sync(0xffffffffu, b, off));
+        }
+        if (l == 0) {
+            red[64] = a;
+            red[65] = b;
+        }
+    }
+    __syncthreads();
+    lo = red[64];
+    hi = red[65];
+}
+
+template <typename R>
+__device__ inline Cx<R> cx_div(Cx<R> a, Cx<R> b) {
+    const R d = b.re * b.re + b.im * b.im;
+    return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+
+template <typename R>
+__device__ inline Cx<R> cx_mul(Cx<R> a, Cx<R> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+
+template <typename R>
+constexpr int iesh_min_blocks() {
+    return std::is_same<R, float>::value ? 2 : 1;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(const IeshParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec);
+    R* eps = (R*)(smem + L.o_eps);
+    R* V2 = (R*)(smem + L.o_V2);
+    R* lam = (R*)(smem + L.o_lam);
+    R* z2 = (R*)(smem + L.o_z2);
+    R* z0 = (R*)(smem + L.o_z0);
+    double* lam64 = (double*)(smem + L.o_lam64);
+    R* At = (R*)(smem + L.o_At);
+    Cx<R>* phiA = (Cx<R>*)(smem + L.o_phiA);
+    Cx<R>* phiB = (Cx<R>*)(smem + L.o_phiB);
+    double* Jc = (double*)(smem + L.o_J);
+    int* occ = (int*)(smem + L.o_occ);
+    int* unocc = (int*)(smem + L.o_unocc);
+    int* piv = (int*)(smem + L.o_piv);
+    double* red = (double*)(smem + L.o_red);
+    double* misc = (double*)(smem + L.o_misc);
+
+    const int N = L.N, Ne = L.Ne, Nu = L.Nu, Np = L.Np, Nep = L.Nep, M = p.nbath;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int64_t ti = blockIdx.x;
+    const int64_t NT = p.ntraj;
+    const uint64_t gid = (uint64_t)(p.traj_offset + ti);
+    const double mass = p.mass, dt = p.dt, half = dt / 2.0;
+    unsigned long long* nonconv = p.counters ? p.counters + 2 : nullptr;
+
+    for (int k = tid; k < Np; k += nthr) {
+        eps[k] = k < M ? (R)p.eps[k] : R(0);
+        V2[k] = k < M ? (R)p.V2[k] : R(0);
+        lam[k] = R(0);
+        z2[k] = R(0);
+        z0[k] = R(0);
+    }
+    for (int q = tid; q < Np * Np; q += nthr) At[q] = R(0);
+    for (int q = tid; q < Np * Nep; q += nthr) {
+        phiA[q] = {R(0), R(0)};
+        phiB[q] = {R(0), R(0)};
+    }
+    __syncthreads();
+
+    double r[3], v[3], k[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r[d] = p.r[d * NT + ti];
+        v[d] = p.v[d * NT + ti];
+    }
+    const double Lpad = fabs(p.eps[0]) + fabs(p.eps[M - 1]) + 1.0 + p.sumV2;
+    // thread i < N owns root i and warm-starts it from the previous step
+    R lam_own = tid == 0 ? eps[0] - R(1e-3) : (tid <= M ? eps[tid - 1] + R(1e-9) : R(0));
+    double hz = 0.0, dhz = 0.0;
+    auto electronic = [&](double zpos) {
+        const double ebz = nqcd_exp(-p.b * zpos);
+        hz = p.delta - p.B * ebz;
+        dhz = p.B * p.b * ebz;
+        if (tid < N) {
+            R zz;
+            secular_root<R>(eps, V2, M, tid, (R)hz, (R)(fabs(hz) + Lpad), lam_own, zz, nonconv);
+            lam[tid] = lam_own;
+            z2[tid] = zz;
+            z0[tid] = sqrt(zz);
+        }
+        __syncthreads();
+    };
+    auto accel = [&]() {
+        double occsum = 0.0;
+        for (int jj = 0; jj < Ne; ++jj) occsum += (double)z2[occ[jj]];
+        const double eaz = nqcd_exp(-p.a * r[2]);
+        k[0] = -(p.kxy * r[0]) / mass;
+        k[1] = -(p.kxy * r[1]) / mass;
+        k[2] = -(-p.A * p.a * eaz + dhz * occsum) / mass;
+    };
+    auto potential = [&]() {
+        double s = 0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) + p.A * nqcd_exp(-p.a * r[2]);
+        for (int jj = 0; jj < Ne; ++jj) s += (double)lam[occ[jj]];
+        return s;
+    };
+    auto kinetic = [&]() { return 0.5 * mass * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+    auto rebuild_unocc = [&]() {  // ascending, as set_unoccupied_states! (DynamicsUtils.jl:162-171)
+        unsigned long long m2[2] = {0ull, 0ull};
+        for (int jj = 0; jj < Ne; ++jj) m2[occ[jj] >> 6] |= 1ull << (occ[jj] & 63);
+        int u = 0;
+        for (int s = 0; s < N; ++s)
+            if (!((m2[s >> 6] >> (s & 63)) & 1ull)) unocc[u++] = s;
+    };
+
+    // ---- initial electronic structure and occupations ----
+    electronic(r[2]);
+    if (p.init_kind == IESH_INIT_FERMI_DIRAC) {
+        // the Metropolis acceptance uses FP64 eigenvalues on both paths
+        if (tid < N) {
+            if constexpr (std::is_same<R, double>::value) {
+                lam64[tid] = (double)lam[tid];
+            } else {  // FP64 roots from the global FP64 bath arrays
+                double l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9, zz;
+                secular_root<double>(p.eps, p.V2, M, tid, hz, fabs(hz) + Lpad, l64, zz, nonconv);
+                lam64[tid] = l64;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            unsigned long long m2[2] = {0ull, 0ull};
+            for (int jj = 0; jj < Ne; ++jj) {
+                occ[jj] = jj;
+                m2[jj >> 6] |= 1ull << (jj & 63);
+            }
+            for (int it = 0; it < N * Ne; ++it) {
+                const u32x4 wa = rng_block(p.seed, gid, (uint32_t)it, RNG_INIT_FD);
+                const u32x4 wb = rng_block(p.seed, gid, (uint32_t)it, RNG_INIT_FD + 16);
+                const double ua = u01_from_words(wa.x, wa.y), ub = u01_from_words(wa.z, wa.w);
+                const double uc = u01_from_words(wb.x, wb.y);
+                int ci = (int)(ua * Ne);
+                if (ci > Ne - 1) ci = Ne - 1;
+                int pick = (int)(ub * Nu);
+                if (pick > Nu - 1) pick = Nu - 1;
+                const int j = iesh_nth_unset(m2, N, pick);
+                const int i = occ[ci];
+                const double prob = nqcd_exp(-p.beta * (lam64[j] - lam64[i]));
+                if (prob > uc) {
+                    m2[i >> 6] &= ~(1ull << (i & 63));
+                    m2[j >> 6] |= 1ull << (j & 63);
+                    occ[ci] = j;
+                }
+            }
+            for (int a = 1; a < Ne; ++a) {  // sort!(state)
+                const int x = occ[a];
+                int b = a - 1;
+                while (b >= 0 && occ[b] > x) {
+                    occ[b + 1] = occ[b];
+                    --b;
+                }
+                occ[b + 1] = x;
+            }
+            rebuild_unocc();
+        }
+    } else if (tid == 0) {
+        for (int jj = 0; jj < Ne; ++jj) occ[jj] = p.occ0[(int64_t)jj * NT + ti];
+        rebuild_unocc();
+    }
+    __syncthreads();
+    for (int jj = tid; jj < Ne; jj += nthr) phiA[occ[jj] * Nep + jj] = {R(1), R(0)};
+    __syncthreads();
+    accel();
+    const double e0 = p.energy ? kinetic() + potential() : 0.0;
+
+    // matrix-product tiles
+    const int ncg = Nep >> 2;
+    const int ntile = (Np >> 2) * ncg;
+    const bool tile_on = tid < ntile;
+    const int i0 = tile_on ? (tid / ncg) * 4 : 0;
+    const int c0 = tile_on ? (tid % ncg) * 4 : 0;
+
+    auto save = [&](int isave) {
+        // impurity population (iesh_diabatic_population, row 0 of Z rho Z^T)
+        double contrib = 0.0;
+        if (tid < Ne) {
+            double ar = 0.0, ai = 0.0, sq = 0.0;
+            for (int a = 0; a < N; ++a) {
+                const Cx<R> c = phiA[a * Nep + tid];
+                const double za = (double)z0[a];
+                ar += za * (double)c.re;
+                ai += za * (double)c.im;
+                sq += (double)z2[a] * ((double)c.re * (double)c.re + (double)c.im * (double)c.im);
+            }
+            contrib = ar * ar + ai * ai - sq + (double)z2[occ[tid]];
+        }
+        const double nimp = iesh_block_sum(contrib, red);
+        if (tid == 0 && isave < p.nsave) {
+            double* dst = p.obs_partial + (ti * p.nsave + isave) * 4;
+            dst[0] = r[2];
+            dst[1] = kinetic();
+            dst[2] = nimp;
+            dst[3] = potential();
+        }
+        __syncthreads();  // the next step rewrites the roots thread 0 just read
+    };
+    int isave = 0;
+    if (p.save_stride > 0 && p.obs_partial) save(isave++);
+
+    int nh = 0, nf = 0;
+    unsigned long long nfull = 0, nterms = 0;
+    for (int step = 1; step <= p.nsteps; ++step) {
+        // ---- velocity Verlet (verlet_with_electronics.jl:55-63) ----
+        double vt[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vt[d] = v[d] + half * k[d];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) r[d] = r[d] + dt * vt[d];
+        electronic(r[2]);
+        accel();
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = vt[d] + half * k[d];
+        const double w = v[2] * dhz;  // v . grad h: the couplings are d_alpha = dh/dalpha A
+
+        // ---- propagator (wavefunction_dynamics.jl:15-58) ----
+        for (int q = tid; q < N * N; q += nthr) {
+            const int j = q / N, i = q - j * N;
+            At[j * Np + i] = i == j ? R(0) : z0[i] * z0[j] / (lam[j] - lam[i]);
+        }
+        __syncthreads();
+        double elo = 1e300, ehi = -1e300;
+        if (tid < N) {
+            R sacc = R(0);
+            for (int j = 0; j < N; ++j) sacc += fabs(At[j * Np + tid]);
+            const double rad = fabs(w) * (double)sacc;
+            elo = (double)lam[tid] - rad;
+            ehi = (double)lam[tid] + rad;
+        }
+        iesh_block_minmax(elo, ehi, red);
+        const double cen = 0.5 * (ehi + elo);
+        const double hw = 0.5 * (ehi - elo) * (1.0 + 1e-12) + 1e-300;
+        if (tid == 0) misc[0] = (double)iesh_bessel(hw * dt, p.cheb_tol, Jc);
+        __syncthreads();
+        const int K = (int)misc[0];
+        if (K < 0) {  // step too long for the series: leave psi unchanged, count as unconverged
+            if (tid == 0 && nonconv) atomicAdd(nonconv, 1ull);
+        } else {
+            nterms += (unsigned long long)K;
+            const R s = (R)(w / hw);
+            R dl[4];
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) dl[rr] = (R)(((double)lam[i0 + rr] - cen) / hw);
+            Cx<R> prev[4][4], out[4][4];
+            if (tile_on) {
+                const R j0 = (R)Jc[0];
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const Cx<R> x = phiA[(i0 + rr) * Nep + c0 + cc];
+                        out[rr][cc] = {j0 * x.re, j0 * x.im};
+                        prev[rr][cc] = {R(0), R(0)};
+                    }
+            }
+            for (int kk = 1; kk <= K; ++kk) {
+                const Cx<R>* src = (kk & 1) ? phiA : phiB;
+                Cx<R>* dst = (kk & 1) ? phiB : phiA;
+                __syncthreads();
+                if (tile_on) {
+                    R ar[4][4], ai[4][4];
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) ar[rr][cc] = ai[rr][cc] = R(0);
+                    for (int j = 0; j < N; ++j) {
+                        const R* aj = At + j * Np + i0;
+                        const Cx<R>* pj = src + j * Nep + c0;
+                        R av[4];
+                        Cx<R> pv[4];
+#pragma unroll
+                        for (int rr = 0; rr < 4; ++rr) av[rr] = aj[rr];
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) pv[cc] = pj[cc];
+#pragma unroll
+                        for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                            for (int cc = 0; cc < 4; ++cc) {
+                                ar[rr][cc] += av[rr] * pv[cc].re;
+                                ai[rr][cc] += av[rr] * pv[cc].im;
+                            }
+                    }
+                    const R jk = (R)(2.0 * Jc[kk]);
+                    const int ph = kk & 3;
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) {
+                            const Cx<R> cur = src[(i0 + rr) * Nep + c0 + cc];
+                            // Ht phi = dl phi - i s (A phi)
+                            const R hre = dl[rr] * cur.re + s * ai[rr][cc];
+                            const R him = dl[rr] * cur.im - s * ar[rr][cc];
+                            Cx<R> nw;
+                            if (kk == 1)
+                                nw = {hre, him};
+                            else
+                                nw = {R(2) * hre - prev[rr][cc].re, R(2) * him - prev[rr][cc].im};
+                            prev[rr][cc] = cur;
+                            dst[(i0 + rr) * Nep + c0 + cc] = nw;
+                            Cx<R>& o = out[rr][cc];
+                            if (ph == 0) {
+                                o.re += jk * nw.re;
+                                o.im += jk * nw.im;
+                            } else if (ph == 1) {  // (-i) nw
+                                o.re += jk * nw.im;
+                                o.im -= jk * nw.re;
+                            } else if (ph == 2) {
+                                o.re -= jk * nw.re;
+                                o.im -= jk * nw.im;
+                            } else {  // (+i) nw
+                                o.re -= jk * nw.im;
+                                o.im += jk * nw.re;
+                            }
+                        }
+                }
+            }
+            __syncthreads();
+            double sn, cs;
+            sincos(cen * dt, &sn, &cs);  // exp(-i c dt) = cs - i sn
+            const R csr = (R)cs, snr = (R)sn;
+            if (tile_on) {
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const Cx<R> o = out[rr][cc];
+                        phiA[(i0 + rr) * Nep + c0 + cc] = {o.re * csr + o.im * snr, o.im * csr - o.re * snr};
+                    }
+            }
+            __syncthreads();
+        }
+
+        // ---- hop test (iesh.jl:231-335, 390-411) ----
+        Cx<R>* Sm = phiB;              // S^T, [Nep][Nep]
+        Cx<R>* Rh = phiB + Nep * Nep;  // right-hand sides psi[unocc, :]^T, [Nep][Nu]
+        for (int q = tid; q < Ne * Ne; q += nthr) {
+            const int c = q / Ne, j = q - c * Ne;
+            Sm[c * Nep + j] = phiA[occ[j] * Nep + c];
+        }
+        __syncthreads();
+        bool singular = false;
+        for (int col = 0; col < Ne; ++col) {
+            if (tid < 32) {
+                double best = -1.0;
+                int bi = col;
+                for (int rr = col + tid; rr < Ne; rr += 32) {
+                    const Cx<R> x = Sm[rr * Nep + col];
+                    const double mg = fabs((double)x.re) + fabs((double)x.im);
+                    if (mg > best) {
+                        best = mg;
+                        bi = rr;
+                    }
+                }
+                for (int off = 16; off > 0; off >>= 1) {
+                    const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                    if (ob > best || (ob == best && oi < bi)) {
+                        best = ob;
+                        bi = oi;
+                    }
+                }
+                if (tid == 0) {
+                    piv[col] = bi;
+                    misc[1] = best;
+                }
+            }
+            __syncthreads();
+            if (!(misc[1] > 0.0)) {
+                singular = true;
+                break;
+            }
+            const int pr = piv[col];
+            if (pr != col)
+                for (int q = tid; q < Ne; q += nthr) {
+                    const Cx<R> t = Sm[col * Nep + q];
+                    Sm[col * Nep + q] = Sm[pr * Nep + q];
+                    Sm[pr * Nep + q] = t;
+                }
+            __syncthreads();
+            const Cx<R> pv = Sm[col * Nep + col];
+            for (int rr = col + 1 + tid; rr < Ne; rr += nthr) Sm[rr * Nep + col] = cx_div<R>(Sm[rr * Nep + col], pv);
+            __syncthreads();
+            const int nt = Ne - col - 1;
+            for (int q = tid; q < nt * nt; q += nthr) {
+                const int rr = col + 1 + q / nt, cc = col + 1 + q % nt;
+                const Cx<R> l = Sm[rr * Nep + col], u = Sm[col * Nep + cc];
+                Cx<R>& t = Sm[rr * Nep + cc];
+                t.re -= l.re * u.re - l.im * u.im;
+                t.im -= l.re * u.im + l.im * u.re;
+            }
+            __syncthreads();
+        }
+        const double u = std::is_same<R, double>::value
+                             ? rng_uniform(p.seed, gid, (uint32_t)step, RNG_HOP)
+                             : (double)rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP);
+        // sum |v.d| over unoccupied rows and electrons (the estimate's sum(abs, v_dot_d))
+        double sabs = 0.0;
+        for (int q = tid; q < Nu * Ne; q += nthr) {
+            const int mm = q / Ne, n = q - mm * Ne;
+            sabs += fabs(w * (double)At[occ[n] * Np + unocc[mm]]);
+        }
+        sabs = iesh_block_sum(sabs, red);
+        if (tid == 0) {
+            int full = 0;
+            if (!singular) {
+                // det S with a running power-of-two exponent
+                double dr = 1.0, di = 0.0;
+                int de = 0, swaps = 0;
+                for (int q = 0; q < Ne; ++q) {
+                    const Cx<R> d = Sm[q * Nep + q];
+                    const double nr = dr * (double)d.re - di * (double)d.im;
+                    const double ni = dr * (double)d.im + di * (double)d.re;
+                    int ex;
+                    const double mg = frexp(fabs(nr) + fabs(ni), &ex);
+                    (void)mg;
+                    dr = ldexp(nr, -ex);
+                    di = ldexp(ni, -ex);
+                    de += ex;
+                    if (piv[q] != q) ++swaps;
+                }
+                if (swaps & 1) {
+                    dr = -dr;
+                    di = -di;
+                }
+                // estimate = 2 dt / |det|^2 * sum|v.d| * (|Re det| + |Im det|)
+                const double est = 2.0 * dt * sabs * ldexp((fabs(dr) + fabs(di)) / (dr * dr + di * di), -de);
+                full = (p.exact_probability || !(est < u)) ? 1 : 0;
+            }
+            misc[2] = full;
+        }
+        __syncthreads();
+        if (misc[2] != 0.0) {
+            ++nfull;
+            for (int q = tid; q < Ne * Nu; q += nthr) {
+                const int c = q / Nu, mm = q - c * Nu;
+                Rh[c * Nu + mm] = phiA[unocc[mm] * Nep + c];
+            }
+            __syncthreads();
+            if (tid < Nu) {  // one right-hand side per thread: P, L, U solves
+                const int mm = tid;
+                for (int q = 0; q < Ne; ++q) {
+                    const int pq = piv[q];
+                    if (pq != q) {
+                        const Cx<R> t = Rh[q * Nu + mm];
+                        Rh[q * Nu + mm] = Rh[pq * Nu + mm];
+                        Rh[pq * Nu + mm] = t;
+                    }
+                }
+                for (int rr = 1; rr < Ne; ++rr) {
+                    Cx<R> y = Rh[rr * Nu + mm];
+                    for (int q = 0; q < rr; ++q) {
+                        const Cx<R> l = Sm[rr * Nep + q], x = Rh[q * Nu + mm];
+                        y.re -= l.re * x.re - l.im * x.im;
+                        y.im -= l.re * x.im + l.im * x.re;
+                    }
+                    Rh[rr * Nu + mm] = y;
+                }
+                for (int rr = Ne - 1; rr >= 0; --rr) {
+                    Cx<R> y = Rh[rr * Nu + mm];
+                    for (int q = rr + 1; q < Ne; ++q) {
+                        const Cx<R> a = Sm[rr * Nep + q], x = Rh[q * Nu + mm];
+                        y.re -= a.re * x.re - a.im * x.im;
+                        y.im -= a.re * x.im + a.im * x.re;
+                    }
+                    Rh[rr * Nu + mm] = cx_div<R>(y, Sm[rr * Nep + rr]);
+                }
+                // p_mn = 2 dt Re(Y_nm) (v.d)_mn, (v.d)_mn = -w A[m][state n]
+                const int m = unocc[mm];
+                for (int n = 0; n < Ne; ++n) {
+                    const double vdd = -w * (double)At[occ[n] * Np + m];
+                    const double pr = clamp01<double>(2.0 * dt * (double)Rh[n * Nu + mm].re * vdd);
+                    Rh[n * Nu + mm].re = (R)pr;
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                int sel_n = -1, sel_m = -1;
+                double cum = 0.0;
+                for (int n = 0; n < Ne && sel_n < 0; ++n)
+                    for (int mm = 0; mm < Nu; ++mm) {
+                        cum += (double)Rh[n * Nu + mm].re;
+                        if (u < cum) {
+                            sel_n = n;
+                            sel_m = unocc[mm];
+                            break;
+                        }
+                    }
+                if (sel_n >= 0) {
+                    const int old = occ[sel_n], nw = sel_m;
+                    bool accept = true;
+                    if (p.rescaling != RESCALE_OFF) {
+                        // d[new, old] = dh A[new][old]; only its z component is nonzero
+                        const double dz = dhz * (double)z0[nw] * (double)z0[old] / ((double)lam[old] - (double)lam[nw]);
+                        const double aa = (dz * dz / mass) / 2.0;
+                        const double bb = dz * v[2];
+                        const double cc = (double)lam[nw] - (double)lam[old];
+                        const double disc = bb * bb - 4.0 * aa * cc;
+                        if (disc < 0.0) {
+                            accept = false;
+                            if (p.rescaling == RESCALE_VINVERSION) v[2] = -v[2];
+                        } else {
+                            const double root = sqrt(disc);
+                            const double gam = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
+                            v[2] = v[2] - gam * dz / mass;
+                        }
+                    }
+                    if (accept) {
+                        if (p.hop_log && nh < p.max_hops) {
+                            p.hop_log[((int64_t)nh * 3 + 0) * NT + ti] = step;
+                            p.hop_log[((int64_t)nh * 3 + 1) * NT + ti] = old;
+                            p.hop_log[((int64_t)nh * 3 + 2) * NT + ti] = nw;
+                        }
+                        ++nh;
+                        occ[sel_n] = nw;
+                        rebuild_unocc();
+                    } else {
+                        ++nf;
+                    }
+                }
+                misc[3] = v[2];
+            }
+            __syncthreads();
+            v[2] = misc[3];  // hop counts live in thread 0, which writes them out
+        }
+        if (p.save_stride > 0 && p.obs_partial && step % p.save_stride == 0) save(isave++);
+    }
+
+    const double e1 = p.energy ? kinetic() + potential() : 0.0;
+    // final orbitals: (nstates, nelectrons) column-major per trajectory
+    if (p.psi_re)
+        for (int q = tid; q < N * Ne; q += nthr) {
+            const int c = q / N, i = q - c * N;
+            const Cx<R> x = phiA[i * Nep + c];
+            p.psi_re[(ti * Ne + c) * N + i] = (double)x.re;
+            p.psi_im[(ti * Ne + c) * N + i] = (double)x.im;
+        }
+    for (int jj = tid; jj < Ne; jj += nthr) p.occ[(int64_t)jj * NT + ti] = occ[jj];
+    if (tid == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            p.r[d * NT + ti] = r[d];
+            p.v[d * NT + ti] = v[d];
+        }
+        if (p.nhops) p.nhops[ti] = nh;
+        if (p.nfrustrated) p.nfrustrated[ti] = nf;
+        if (p.nsteps_out) p.nsteps_out[ti] = p.nsteps;
+        if (p.energy) {
+            p.energy[ti] = e0;
+            p.energy[NT + ti] = e1;
+        }
+        if (p.counters) {
+            atomicAdd(p.counters + 0, nfull);
+            atomicAdd(p.counters + 1, nterms);
+        }
+    }
+}
+
+template <typename R>
+cudaError_t launch_iesh(const IeshParams& p, cudaStream_t s) {
+    if (p.ntraj <= 0) return cudaSuccess;
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec);
+    cudaError_t e = cudaFuncSetAttribute(iesh_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
+    if (e != cudaSuccess) return e;
+    iesh_kernel<R><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace nqcd

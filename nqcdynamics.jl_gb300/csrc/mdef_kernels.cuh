@@ -2,8 +2,8 @@
 // one warp per trajectory.
 //
 // Reference algorithm (NQCDynamics.jl):
-//   MDEF_BAOAB.perform_step!    src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:338-355
-//   step_O! (friction eigenbasis) src/DynamicsMethods/IntegrationAlgorithms/steps.jl:128-156
+//   MDEF_BAOAB.perform_step!    src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:163-180
+//   step_O! (friction eigenbasis) src/DynamicsMethods/IntegrationAlgorithms/steps.jl:41-69
 //   DiabaticMDEF acceleration!  src/DynamicsMethods/ClassicalMethods/mdef.jl:102-124
 //   friction! (Lambda / sqrt(m)sqrt(m)^T) src/DynamicsMethods/ClassicalMethods/mdef.jl:131-140
 // The reference diagonalises the (1 + M)-state one-electron Hamiltonian
@@ -35,6 +35,7 @@
 #include <type_traits>
 
 #include "nqcd_math.h"
+#include "secular.h"
 
 namespace nqcd {
 
@@ -87,14 +88,6 @@ struct MdefShared {
 };
 
 template <typename R>
-__device__ __forceinline__ R mdef_rcp(R d) {
-    if constexpr (std::is_same<R, float>::value)
-        return __frcp_rn(d);
-    else
-        return 1.0 / d;
-}
-
-template <typename R>
 __device__ __forceinline__ R mdef_exp(R x) {
     if constexpr (std::is_same<R, float>::value)
         return __expf(x);
@@ -116,95 +109,6 @@ __device__ __forceinline__ void fermi_pair(R e, R mu, R beta, R& f, R& df) {
     df = -beta * f * (R(1) - f);
 }
 
-// Solve root i of the secular equation.  o = origin pole, d = offset from it,
-// (dlo, dhi) = bracket of d.  Returns l = o + d and z0^2 = 1/f'.
-template <typename R>
-__device__ __forceinline__ void secular_root(const MdefShared<R>& sh, int M, int i, R h, R Lbound, R& lam_io,
-                                             R& z2_out, unsigned long long* nonconv) {
-    // interval of root i
-    const bool first = i == 0, last = i == M;
-    R a = first ? sh.eps[0] : sh.eps[i - 1];
-    R b = last ? sh.eps[M - 1] : sh.eps[i];
-    int jo;  // origin pole index
-    R o, dlo, dhi;
-    if (first) {
-        jo = 0;
-        o = a;
-        dlo = -Lbound;
-        dhi = R(0);
-    } else if (last) {
-        jo = M - 1;
-        o = b;
-        dlo = R(0);
-        dhi = Lbound;
-    } else {
-        // which half: sign of f at the midpoint decides the nearer pole
-        R mid = a + R(0.5) * (b - a);
-        R s = R(0);
-        for (int k = 0; k < M; ++k) s += sh.V2[k] * mdef_rcp<R>(mid - sh.eps[k]);
-        R fm = mid - h - s;
-        if (fm > R(0)) {  // root in (a, mid): measure from a
-            jo = i - 1;
-            o = a;
-            dlo = R(0);
-            dhi = mid - a;
-        } else {
-            jo = i;
-            o = b;
-            dlo = mid - b;
-            dhi = R(0);
-        }
-    }
-    // warm start from the previous root if it lies in the bracket
-    R d = lam_io - o;
-    if (!(d > dlo && d < dhi)) d = R(0.5) * (dlo + dhi);
-    R fp = R(1);
-    bool conv = false;
-    for (int it = 0; it < 80; ++it) {
-        R s1 = R(0), s2 = R(0), sa = R(0);
-        for (int k = 0; k < M; ++k) {
-            R den = (k == jo) ? d : (o - sh.eps[k]) + d;
-            R t = mdef_rcp<R>(den);
-            R vt = sh.V2[k] * t;
-            s1 += vt;
-            s2 += vt * t;
-            sa += fabs(vt);
-        }
-        R f = (o + d) - h - s1;
-        fp = R(1) + s2;
-        if (f == R(0)) {  // exact root: keep d (a bisection here would leave it)
-            conv = true;
-            break;
-        }
-        if (f > R(0))
-            dhi = d;
-        else
-            dlo = d;
-        R dn = d - f / fp;
-        // the Newton point may equal the bracket end just set (a step below
-        // one ulp): that is convergence, not a reason to bisect
-        if (!(dn >= dlo && dn <= dhi)) dn = R(0.5) * (dlo + dhi);
-        R step = dn - d;
-        d = dn;
-        const R ulp = std::is_same<R, float>::value ? R(1.2e-7) : R(2.3e-16);
-        R tol = R(2) * ulp * (fabs(d) + fabs(o) * R(1e-3));
-        // f has reached the rounding error of its own evaluation: no further
-        // Newton step can be trusted (the secular-equation stopping test).
-        // The summed error of the M terms can exceed ulp * sum|terms| by about
-        // sqrt(M); after the first iterations accept the bound used by LAPACK's
-        // secular solver, 8 ulp * sum|terms|.
-        R ferr = ulp * (fabs(o + d) + fabs(h) + sa);
-        if (it >= 16) ferr *= R(8);
-        if (fabs(step) <= tol || dhi - dlo <= tol || fabs(f) <= ferr) {
-            conv = true;
-            break;
-        }
-    }
-    if (!conv && nonconv) atomicAdd(nonconv, 1ull);
-    lam_io = o + d;
-    z2_out = R(1) / fp;
-}
-
 // Electronic structure at x for the warp's trajectory: all roots, force and
 // (optionally) friction.  Roots and weights are also left in shared memory.
 template <typename R>
@@ -222,7 +126,7 @@ __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib,
         int i = lane + 32 * q;
         if (i <= M) {
             R z2;
-            secular_root<R>(sh, M, i, h, Lb, lam[q], z2, p.counters ? p.counters + 2 : nullptr);
+            secular_root<R>(sh.eps, sh.V2, M, i, h, Lb, lam[q], z2, p.counters ? p.counters + 2 : nullptr);
             R f, df;
             fermi_pair<R>(lam[q], mu, beta, f, df);
             accF += z2 * (f + df * lam[q]);

@@ -19,6 +19,7 @@
 #include "mlp.h"
 #include "ring_polymer.h"
 #include "rpsh_kernels.cuh"
+#include "iesh_kernels.cuh"
 
 using namespace nqcd;
 
@@ -29,6 +30,8 @@ cudaError_t launch_rpsh_fp64(const RpshParams& p, int blocks, cudaStream_t s);
 cudaError_t launch_rpsh_fp32(const RpshParams& p, int blocks, cudaStream_t s);
 cudaError_t launch_mdef_fp64(const MdefParams& p, cudaStream_t s);
 cudaError_t launch_mdef_fp32(const MdefParams& p, cudaStream_t s);
+cudaError_t launch_iesh_fp64(const IeshParams& p, cudaStream_t s);
+cudaError_t launch_iesh_fp32(const IeshParams& p, cudaStream_t s);
 }  // namespace nqcd
 
 namespace {
@@ -184,6 +187,11 @@ struct nqcd_handle {
     // MDEF: bath levels and squared couplings; friction surrogate
     double *d_eps = nullptr, *d_V2 = nullptr;
     MlpState mlp;
+    // IESH: occupations [nelec][traj] (given initial, final) and final orbitals [traj][nelec][nstates]
+    int32_t *d_occ0 = nullptr, *d_occ = nullptr;
+    double *d_psi_re = nullptr, *d_psi_im = nullptr;
+    int nelec = 0;
+    double sumV2 = 0.0;
 };
 
 namespace {
@@ -219,7 +227,8 @@ void free_all(nqcd_handle* h) {
                     h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
                     h->d_rpU, h->d_rpcay, h->d_rpUf, h->d_rpcayf, h->d_nbeads, h->d_class_traj,
-                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2};
+                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2,
+                    h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mlp_free(h->mlp);
@@ -292,12 +301,44 @@ int nqcd_version(void) { return NQCD_ABI_VERSION; }
 int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     if (!cfg || !out) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: null argument");
     *out = nullptr;
-    if (cfg->method != NQCD_METHOD_FSSH && cfg->method != NQCD_METHOD_RPSH && cfg->method != NQCD_METHOD_MDEF)
+    if (cfg->method != NQCD_METHOD_FSSH && cfg->method != NQCD_METHOD_RPSH && cfg->method != NQCD_METHOD_MDEF &&
+        cfg->method != NQCD_METHOD_IESH)
         return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: method not supported by this build");
     const bool rp = cfg->method == NQCD_METHOD_RPSH;
     const bool mdef = cfg->method == NQCD_METHOD_MDEF;
+    const bool iesh = cfg->method == NQCD_METHOD_IESH;
     const int model = cfg->model;
-    if (mdef) {
+    if (iesh) {
+        if (model != NQCD_MODEL_NEWNS_ANDERSON_3D)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: IESH runs on the three-dimensional Newns-Anderson model");
+        if (cfg->natoms != 1 || cfg->ndofs != 3)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: IESH runs one atom with three degrees of freedom");
+        if (cfg->nbath < 2 || !cfg->bath_a || !cfg->bath_b)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: IESH needs bath levels and couplings");
+        if (cfg->nstates != cfg->nbath + 1 || cfg->nstates > kIeshMaxStates)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: IESH needs nstates == nbath + 1 <= 128");
+        for (int k = 1; k < cfg->nbath; ++k)
+            if (!(cfg->bath_a[k] > cfg->bath_a[k - 1]))
+                return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bath levels must be strictly ascending");
+        for (int k = 0; k < cfg->nbath; ++k)
+            if (cfg->bath_b[k] == 0.0) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bath couplings must be nonzero");
+        if (cfg->nelectrons < 1 || cfg->nelectrons >= cfg->nstates)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: IESH needs 1 <= nelectrons < nstates");
+        if (iesh_tiles(cfg->nstates, cfg->nelectrons) > kIeshBlock)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED,
+                        "nqcd_create: IESH needs ceil(nstates/4) * ceil(nelectrons/4) <= 256");
+        const size_t smem = cfg->precision == NQCD_PREC_FP64 ? iesh_layout<double>(cfg->nstates, cfg->nelectrons).bytes
+                                                             : iesh_layout<float>(cfg->nstates, cfg->nelectrons).bytes;
+        if (smem > 227 * 1024) return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: IESH system too large for one CTA");
+        if (cfg->nparams < 6 || !cfg->params)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: IESH model needs kxy, A, a, delta, B, b");
+        if (cfg->init_kind != NQCD_INIT_GIVEN && cfg->init_kind != NQCD_INIT_FERMI_DIRAC)
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: IESH starts from given or Fermi-Dirac occupations");
+        if (cfg->init_kind == NQCD_INIT_FERMI_DIRAC && !(cfg->beta > 0.0))
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: Fermi-Dirac occupations need beta > 0");
+        if (cfg->precision == NQCD_PREC_FP32_KAHAN)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: IESH runs NQCD_PREC_FP64 or NQCD_PREC_FP32");
+    } else if (mdef) {
         if (model != NQCD_MODEL_NEWNS_ANDERSON)
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs on the Newns-Anderson model");
         if (cfg->ndofs * cfg->natoms != 1)
@@ -314,7 +355,8 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
         if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: MDEF needs beta > 0");
         if (!cfg->masses || !(cfg->masses[0] > 0.0) || cfg->ntraj_max <= 0 || cfg->save_stride < 0)
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: mass, ntraj_max and save_stride are required");
-    } else {
+    }
+    if (!mdef && !iesh) {
         if (model != NQCD_MODEL_TULLY1 && model != NQCD_MODEL_TULLY2 && model != NQCD_MODEL_TULLY3 &&
             model != NQCD_MODEL_SPINBOSON)
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: unknown model");
@@ -325,7 +367,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     if (cfg->rescaling < 0 || cfg->rescaling > 2) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown rescaling");
     if (cfg->ndofs <= 0 || cfg->natoms <= 0 || cfg->ntraj_max <= 0 || !cfg->masses)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ndofs, natoms, ntraj_max and masses are required");
-    if (cfg->init_kind < 0 || cfg->init_kind > 2 || cfg->init_state < 0 || cfg->init_state >= cfg->nstates)
+    if (!iesh && (cfg->init_kind < 0 || cfg->init_kind > 2 || cfg->init_state < 0 || cfg->init_state >= cfg->nstates))
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bad initial electronic specification");
     if (cfg->save_stride < 0 || cfg->max_hops < 0 || cfg->traj_offset < 0)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: negative count");
@@ -342,10 +384,10 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
         if (!(cfg->terminate_x >= 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: terminate_x must be >= 0");
     }
     const int64_t ndof = rp ? (int64_t)cfg->nbeads_max : (int64_t)cfg->ndofs * cfg->natoms;
-    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? 5 : 4)));
+    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? 5 : (iesh ? 6 : 4))));
     if (cfg->nparams < need_params || !cfg->params)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: too few model parameters");
-    if (mdef) {
+    if (mdef || iesh) {
         // validated above
     } else if (model == NQCD_MODEL_SPINBOSON) {
         if (cfg->nbath != ndof || !cfg->bath_a || !cfg->bath_b)
@@ -373,6 +415,10 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     h->params.assign(cfg->params, cfg->params + cfg->nparams);
     h->params.resize(8, 0.0);
     h->mass0 = cfg->masses[0];
+    if (iesh) {
+        h->nstates = cfg->nstates;
+        h->nelec = cfg->nelectrons;
+    }
 
     auto bail = [&](cudaError_t ee, const char* what) {
         std::string m = std::string("nqcd_create: ") + what + ": " + cudaGetErrorString(ee);
@@ -424,13 +470,22 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     if (cfg->max_hops > 0) NQCD_CREATE(dalloc(&h->d_hoplog, (int64_t)cfg->max_hops * 3 * cap));
     NQCD_CREATE(dalloc(&h->d_energy, 2 * cap));
     NQCD_CREATE(dalloc(&h->d_counts, 16));
-    if (mdef) {
+    if (mdef || iesh) {
         std::vector<double> eps(cfg->bath_a, cfg->bath_a + cfg->nbath), V2(cfg->nbath);
         for (int k = 0; k < cfg->nbath; ++k) V2[k] = cfg->bath_b[k] * cfg->bath_b[k];
+        for (int k = 0; k < cfg->nbath; ++k) h->sumV2 += V2[k];
         NQCD_CREATE(dalloc(&h->d_eps, cfg->nbath));
         NQCD_CREATE(dalloc(&h->d_V2, cfg->nbath));
         NQCD_CREATE(cudaMemcpy(h->d_eps, eps.data(), eps.size() * sizeof(double), cudaMemcpyHostToDevice));
         NQCD_CREATE(cudaMemcpy(h->d_V2, V2.data(), V2.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (iesh) {
+        const int64_t ne = cfg->nelectrons, ns = cfg->nstates;
+        NQCD_CREATE(dalloc(&h->d_occ0, ne * cap));
+        NQCD_CREATE(dalloc(&h->d_occ, ne * cap));
+        NQCD_CREATE(dalloc(&h->d_psi_re, ne * ns * cap));
+        NQCD_CREATE(dalloc(&h->d_psi_im, ne * ns * cap));
+        NQCD_CREATE(cudaMemset(h->d_occ0, 0, ne * cap * sizeof(int32_t)));
     }
     NQCD_CREATE(cudaMemset(h->d_sig0, 0, 8 * cap * sizeof(double)));
     NQCD_CREATE(cudaMemset(h->d_state0, 0, cap * sizeof(int32_t)));
@@ -520,6 +575,25 @@ static int set_initial_common(nqcd_handle* h, int64_t ntraj, const double* sig_r
     const int64_t N = ntraj;
     // MDEF carries no electronic state: only FSSH and RPSH read sigma and state0
     const bool two_state = h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH;
+    if (h->cfg.method == NQCD_METHOD_IESH && h->cfg.init_kind == NQCD_INIT_GIVEN) {
+        // occupations (nelectrons, ntraj) column-major -> device [electron][trajectory]
+        if (!state0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: IESH with NQCD_INIT_GIVEN needs the occupations in state0");
+        const int ne = h->nelec, ns = h->nstates;
+        std::vector<int32_t> soa((size_t)ne * N);
+        for (int64_t t = 0; t < N; ++t) {
+            unsigned long long m2[2] = {0ull, 0ull};
+            for (int j = 0; j < ne; ++j) {
+                const int32_t s = state0[t * ne + j];
+                if (s < 0 || s >= ns || ((m2[s >> 6] >> (s & 63)) & 1ull))
+                    return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: occupations must be distinct states in 0..nstates-1");
+                m2[s >> 6] |= 1ull << (s & 63);
+                soa[(size_t)j * N + t] = s;
+            }
+        }
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_occ0, soa.data(), soa.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+        *h2d += (int64_t)(soa.size() * sizeof(int32_t));
+    }
     if (two_state && h->cfg.init_kind == NQCD_INIT_GIVEN) {
         if (!sig_re || !state0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: sig_re and state0 required for NQCD_INIT_GIVEN");
         // host (2,2,ntraj) column-major re/im -> device [8][ntraj]: component 2*(2*i+j)+{0,1}
@@ -569,7 +643,7 @@ int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0, c
     if (!h) return NQCD_ERR_ARG;
     if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: ntraj outside 1..ntraj_max");
     if (!d_r0 || !d_v0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: r0 and v0 are required");
-    if ((h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH) && h->cfg.init_kind == NQCD_INIT_GIVEN)
+    if (h->cfg.method != NQCD_METHOD_MDEF && h->cfg.init_kind == NQCD_INIT_GIVEN)
         return fail(h, NQCD_ERR_ARG, "nqcd_set_initial_device: NQCD_INIT_GIVEN needs nqcd_set_initial");
     const int64_t n = ntraj * h->ndof;
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_r0, d_r0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -588,16 +662,23 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         return fail(h, NQCD_ERR_ARG, "nqcd_run: need dt > 0 and finite t0 <= t1");
     auto wall0 = std::chrono::steady_clock::now();
     const int64_t N = h->ntraj;
-    const int64_t nsteps = count_steps(t0, t1, dt);
+    const bool mdef = h->cfg.method == NQCD_METHOD_MDEF;
+    const bool iesh = h->cfg.method == NQCD_METHOD_IESH;
+    // FSSH and RPSH step like the reference's integrator (a last partial step
+    // up to t1); MDEF and IESH take whole steps of dt only
+    const double span = (t1 - t0) / dt;
+    if ((mdef || iesh) && !(span < 2147483647.0))
+        return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
+    const int64_t nsteps = (mdef || iesh) ? (int64_t)llround(span) : count_steps(t0, t1, dt);
     if (nsteps > 0x7fffffff) return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
     const int stride = h->cfg.save_stride;
     const int nsave = stride > 0 ? (int)(nsteps / stride + 1) : 0;
-    const bool mdef = h->cfg.method == NQCD_METHOD_MDEF;
-    if (mdef && fabs((double)nsteps * dt - (t1 - t0)) > 1e-9 * (fabs(t1 - t0) + dt))
-        return fail(h, NQCD_ERR_ARG, "nqcd_run: MDEF needs t1 - t0 to be a whole number of steps");
-    const int64_t lanes = mdef ? 32 : fssh2_lanes_per_traj(h->cfg.model, h->cfg.precision);
+    if ((mdef || iesh) && fabs((double)nsteps * dt - (t1 - t0)) > 1e-9 * (fabs(t1 - t0) + dt))
+        return fail(h, NQCD_ERR_ARG, "nqcd_run: MDEF and IESH need t1 - t0 to be a whole number of steps");
+    const int64_t lanes = mdef ? 32 : (iesh ? 1 : fssh2_lanes_per_traj(h->cfg.model, h->cfg.precision));
     const int64_t blocks = (N * lanes + 127) / 128;
-    const int64_t nwarps = blocks * 4;
+    // rows of observable partial sums: one per warp (FSSH, MDEF) or per trajectory (IESH)
+    const int64_t nwarps = iesh ? N : blocks * 4;
     if (nsave > 0 && nwarps * nsave * 4 > h->partial_cap) {
         if (h->d_partial) cudaFree(h->d_partial);
         if (h->d_popcorr) cudaFree(h->d_popcorr);
@@ -759,6 +840,51 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         }
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         e = plain ? launch_rpsh_fp64(rq, grid, s) : launch_rpsh_fp32(rq, grid, s);
+    } else if (iesh) {
+        IeshParams q;
+        memset(&q, 0, sizeof(q));
+        q.nbath = h->cfg.nbath;
+        q.nstates = h->nstates;
+        q.nelec = h->nelec;
+        q.eps = h->d_eps;
+        q.V2 = h->d_V2;
+        q.sumV2 = h->sumV2;
+        q.kxy = h->params[0];
+        q.A = h->params[1];
+        q.a = h->params[2];
+        q.delta = h->params[3];
+        q.B = h->params[4];
+        q.b = h->params[5];
+        q.beta = h->cfg.beta;
+        q.mass = h->mass0;
+        q.rescaling = h->cfg.rescaling;
+        q.init_kind = h->cfg.init_kind;
+        q.exact_probability = h->cfg.exact_hop_probability ? 1 : 0;
+        q.save_stride = stride;
+        q.nsave = nsave;
+        q.max_hops = h->cfg.max_hops;
+        q.ntraj = N;
+        q.traj_offset = h->cfg.traj_offset;
+        q.dt = dt;
+        q.nsteps = (int32_t)nsteps;
+        q.seed = seed;
+        // series tail below the rounding of each path's arithmetic
+        q.cheb_tol = h->cfg.precision == NQCD_PREC_FP64 ? 1e-17 : 1e-8;
+        q.r = h->d_r;
+        q.v = h->d_v;
+        q.occ0 = h->d_occ0;
+        q.occ = h->d_occ;
+        q.psi_re = h->d_psi_re;
+        q.psi_im = h->d_psi_im;
+        q.nhops = h->d_nhops;
+        q.nfrustrated = h->d_nfrust;
+        q.nsteps_out = h->d_nsteps;
+        q.hop_log = h->d_hoplog;
+        q.energy = h->d_energy;
+        q.obs_partial = nsave > 0 ? h->d_partial : nullptr;
+        q.counters = h->d_counts + 8;
+        NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
+        e = h->cfg.precision == NQCD_PREC_FP64 ? launch_iesh_fp64(q, s) : launch_iesh_fp32(q, s);
     } else if (mdef) {
         MdefParams mp = mdef_params(h, N, dt, (int32_t)nsteps, seed, stride, nsave);
         if (mp.use_mlp && !h->mlp.trained)
@@ -794,7 +920,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     NQCD_CUDA(h, cudaMemcpyAsync(counts, h->d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
     d2h += sizeof(counts);
     std::vector<double> pc;
-    if (out && (mdef ? out->observables : out->population_correlation) && nsave > 0) {
+    if (out && ((mdef || iesh) ? out->observables : out->population_correlation) && nsave > 0) {
         pc.resize((size_t)nsave * 4);
         NQCD_CUDA(h, cudaMemcpyAsync(pc.data(), h->d_popcorr, pc.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         d2h += (int64_t)pc.size() * sizeof(double);
@@ -807,7 +933,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         out->nsave = nsave;
         if (out->scattering)
             for (int q = 0; q < 4; ++q) out->scattering[q] = (double)counts[q] / (double)N;
-        double* dst = mdef ? out->observables : out->population_correlation;
+        double* dst = (mdef || iesh) ? out->observables : out->population_correlation;
         if (dst && nsave > 0)
             for (int k = 0; k < nsave * 4; ++k) dst[k] = pc[k] / (double)N;
     }
@@ -815,9 +941,11 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     h->has_run = true;
     if (stats) {
         stats->traj_steps = mdef ? N * nsteps : (int64_t)counts[4];
-        stats->exact_friction_evals = (int64_t)counts[8];
-        stats->surrogate_friction_evals = (int64_t)counts[9];
+        stats->exact_friction_evals = mdef ? (int64_t)counts[8] : 0;
+        stats->surrogate_friction_evals = mdef ? (int64_t)counts[9] : 0;
         stats->unconverged_roots = (int64_t)counts[10];
+        stats->hop_evaluations = iesh ? (int64_t)counts[8] : 0;
+        stats->propagator_terms = iesh ? (int64_t)counts[9] : 0;
         stats->hops = (int64_t)counts[5];
         stats->frustrated = (int64_t)counts[6];
         stats->flagged = (int64_t)counts[7];
@@ -847,6 +975,20 @@ int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double*
         NQCD_CUDA(h, transpose(srcs[q], h->d_stage, nd, N, s));
         NQCD_CUDA(h, cudaMemcpyAsync(pairs[q], h->d_stage, nd * N * sizeof(double), cudaMemcpyDeviceToHost, s));
         NQCD_CUDA(h, cudaStreamSynchronize(s));
+    }
+    if (h->cfg.method == NQCD_METHOD_IESH) {
+        const int64_t ne = h->nelec, ns = h->nstates;
+        if (sig_re) NQCD_CUDA(h, cudaMemcpyAsync(sig_re, h->d_psi_re, ne * ns * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (sig_im) NQCD_CUDA(h, cudaMemcpyAsync(sig_im, h->d_psi_im, ne * ns * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (state) {
+            std::vector<int32_t> soa((size_t)(ne * N));
+            NQCD_CUDA(h, cudaMemcpyAsync(soa.data(), h->d_occ, soa.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            NQCD_CUDA(h, cudaStreamSynchronize(s));
+            for (int64_t t = 0; t < N; ++t)
+                for (int64_t j = 0; j < ne; ++j) state[t * ne + j] = soa[(size_t)(j * N + t)];
+            state = nullptr;  // written
+        }
+        sig_re = sig_im = nullptr;
     }
     if (sig_re || sig_im) {
         std::vector<double> soa(8 * N);

@@ -25,10 +25,11 @@ ERRORS = {
 
 METHOD_FSSH, METHOD_RPSH, METHOD_IESH, METHOD_MDEF = 1, 2, 3, 4
 MODEL_TULLY1, MODEL_TULLY2, MODEL_TULLY3, MODEL_SPINBOSON, MODEL_NEWNS_ANDERSON = 1, 2, 3, 10, 20
+MODEL_NEWNS_ANDERSON_3D = 21
 MLP_NPARAMS = 4353
 PREC_FP64, PREC_FP32, PREC_FP32_KAHAN = 0, 1, 2
 RESCALE = {"standard": 0, "vinversion": 1, "off": 2}
-INIT_GIVEN, INIT_ADIABATIC_PURE, INIT_DIABATIC_PURE = 0, 1, 2
+INIT_GIVEN, INIT_ADIABATIC_PURE, INIT_DIABATIC_PURE, INIT_FERMI_DIRAC = 0, 1, 2, 3
 
 DP = C.POINTER(C.c_double)
 IP = C.POINTER(C.c_int32)
@@ -61,7 +62,9 @@ class nqcd_config(C.Structure):
         ("traj_offset", C.c_int64),
         ("use_friction_surrogate", C.c_int32),
         ("judge_every", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("nelectrons", C.c_int32),
+        ("exact_hop_probability", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -91,6 +94,8 @@ class nqcd_stats(C.Structure):
         ("exact_friction_evals", C.c_int64),
         ("surrogate_friction_evals", C.c_int64),
         ("unconverged_roots", C.c_int64),
+        ("hop_evaluations", C.c_int64),
+        ("propagator_terms", C.c_int64),
     ]
 
 
@@ -235,6 +240,24 @@ class Engine:
         # (nstates, nstates) per trajectory arrive column-major: transpose to [i, j]
         return dict(r=r, v=v, sig_re=sre.transpose(0, 2, 1).copy(), sig_im=sim.transpose(0, 2, 1).copy(),
                     state=state, nhops=nh, nfrustrated=nf, nsteps=ns, energy=en)
+
+    def get_final_iesh(self, nstates: int, nelectrons: int):
+        """IESH final state: orbitals psi (ntraj, nstates, nelectrons) and
+        occupations (ntraj, nelectrons) in electron order."""
+        n = self.ntraj
+        r = np.empty((n, 3))
+        v = np.empty((n, 3))
+        pre = np.empty((n, nelectrons, nstates))
+        pim = np.empty((n, nelectrons, nstates))
+        occ = np.empty((n, nelectrons), np.int32)
+        nh = np.empty(n, np.int32)
+        nf = np.empty(n, np.int32)
+        ns = np.empty(n, np.int32)
+        en = np.empty((n, 2))
+        self._check(self.lib.nqcd_get_final(self.h, dptr(r), dptr(v), dptr(pre), dptr(pim), iptr(occ),
+                                            iptr(nh), iptr(nf), iptr(ns), dptr(en)))
+        psi = (pre + 1j * pim).transpose(0, 2, 1).copy()
+        return dict(r=r, v=v, psi=psi, state=occ, nhops=nh, nfrustrated=nf, nsteps=ns, energy=en)
 
     def mdef_evaluate(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

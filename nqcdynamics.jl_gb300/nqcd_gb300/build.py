@@ -33,6 +33,7 @@ ENGINE_UNITS = {
     "nqcd_abi.cu": [],
     "noalloc.cu": [],
     "mlp.cu": [],
+    "kernels_iesh.cu": [],
 }
 
 

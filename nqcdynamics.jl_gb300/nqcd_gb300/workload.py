@@ -68,6 +68,52 @@ def newns_anderson_mdef(ntraj: int, *, M: int = 200, coupling: float = 0.02, mas
                 beta=1.0 / T, mass=mass, x0=x0, v0=v0, dt=0.1 * AU_PER_FS)
 
 
+EV_AU = 1.0 / 27.211386245988
+AMU_AU = 1822.888486
+
+
+def trapezoidal_rule(M: int, a: float, b: float):
+    """Bath levels and squared-coupling weights of TrapezoidalRule
+    (docs/src/NQCModels/systembathmodels.md:204-214): M evenly spaced levels
+    on [a, b], |V_n|^2 = |V(e)|^2 (b - a) / (M - 1)."""
+    eps = a + np.arange(M) * (b - a) / (M - 1)
+    return eps, np.full(M, (b - a) / (M - 1))
+
+
+def newns_anderson_iesh(ntraj: int, *, nstates: int = 80, nelectrons: int = 40, coupling: float = 0.04,
+                        mass_amu: float = 1.008, energy_eV: float = 0.5, z0: float = 12.0,
+                        temperature_K: float = 300.0, seed: int = SEED, traj_offset: int = 0):
+    """IESH scattering workload: one hydrogen atom with three degrees of
+    freedom approaching a metal along -z at energy_eV translational energy.
+    The metal band has nstates - 1 evenly spaced levels on [-0.5, 0.5] Hartree
+    with V_k = coupling sqrt(de) (TrapezoidalRule), Fermi level 0, electronic
+    temperature 300 K, nelectrons electrons.  Impurity:
+    U0 = kxy (x^2 + y^2)/2 + A exp(-a z), a repulsive wall with its turning
+    point near z = 2 at 0.5 eV, and h = delta - B exp(-b z), an affinity level
+    2.2 eV above the Fermi level far from the surface that crosses it at
+    z = 2.2, so the atom charges up and excites electron-hole pairs at the
+    turning point.  Initial p_z Gaussian around -sqrt(2 m E) (5 % spread),
+    lateral momenta and positions thermal at 300 K, occupations Fermi-Dirac
+    sampled by the engine.  dt = 0.1 fs; 1 ps is 10 000 steps."""
+    M = nstates - 1
+    eps, w = trapezoidal_rule(M, -0.5, 0.5)
+    mass = mass_amu * AMU_AU
+    T = temperature_K * KELVIN_AU
+    omega_xy = 0.002
+    kxy = mass * omega_xy**2
+    params = dict(kxy=kxy, A=0.2, a=1.2, delta=0.08, B=0.3, b=0.6)
+    rng = np.random.default_rng([seed, traj_offset, 5])
+    p0 = np.sqrt(2.0 * mass * energy_eV * EV_AU)
+    r0 = np.zeros((ntraj, 3))
+    v0 = np.zeros((ntraj, 3))
+    r0[:, 0:2] = rng.standard_normal((ntraj, 2)) * np.sqrt(T / kxy)
+    r0[:, 2] = z0
+    v0[:, 0:2] = rng.standard_normal((ntraj, 2)) * np.sqrt(T / mass)
+    v0[:, 2] = -(p0 + 0.05 * p0 * rng.standard_normal(ntraj)) / mass
+    return dict(eps=eps, V=coupling * np.sqrt(w), params=params, mass=mass, beta=1.0 / T, nstates=nstates,
+                nelectrons=nelectrons, r0=r0, v0=v0, dt=0.1 * AU_PER_FS)
+
+
 # ---------------------------------------------------------------------------
 # Algorithmic work of the reference algorithm per nuclear step of one
 # trajectory (two electronic states), counted operation by operation from

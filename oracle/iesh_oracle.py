@@ -116,7 +116,23 @@ def sample_fermi_dirac(energies, ne, beta, seed, traj_ids):
     return np.sort(states, axis=1)
 
 
-def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, max_hops=16):
+def total_energy(model, r, v, w, state, mass):
+    """KE + U0 + sum of occupied eigenvalues (iesh.jl:380-388)."""
+    return 0.5 * mass * np.sum(v * v, axis=1) + model.U0(r) + np.take_along_axis(w, state, axis=1).sum(1)
+
+
+def impurity_population(psi, Z, state):
+    """Row 0 of iesh_diabatic_population (iesh.jl:351-369) per trajectory."""
+    z0 = Z[:, 0, :]
+    amp = np.einsum("ta,tan->tn", z0, psi)
+    sq = np.einsum("ta,tan->tn", z0 * z0, np.abs(psi) ** 2)
+    return (np.abs(amp) ** 2 - sq).sum(1) + (np.take_along_axis(z0, state, axis=1) ** 2).sum(1)
+
+
+def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, max_hops=16,
+             estimate=True, initial_state=None):
+    """estimate: the reference's estimate_probability screen (iesh.jl:251-254).
+    initial_state: given occupations (ntraj, ne) instead of Fermi-Dirac sampling."""
     n = r0.shape[0]
     N = model.nstates
     traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
@@ -124,7 +140,7 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
     v = np.asarray(v0, np.float64).copy()
     Z = np.tile(np.eye(N), (n, 1, 1))
     w, Z = eigen_continuous(model, r, Z)
-    states = sample_fermi_dirac(w, ne, beta, seed, traj)
+    states = sample_fermi_dirac(w, ne, beta, seed, traj) if initial_state is None else np.array(initial_state)
     psi = np.zeros((n, N, ne), np.complex128)
     for t in range(n):
         psi[t, states[t], np.arange(ne)] = 1.0
@@ -139,6 +155,8 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
         return -(model.grad_U0(r) + gh * occ.sum(1)[:, None]) / mass
 
     k = accel(w, Z, r, state)
+    e0 = total_energy(model, r, v, w, state, mass)
+    nfull = 0
     for step in range(1, nsteps + 1):
         vt = v + (dt / 2) * k
         r = r + dt * vt
@@ -173,9 +191,10 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
             vdd = np.zeros((N, ne))
             for nn in range(ne):
                 vdd[unocc, nn] -= vd[t][unocc, st[nn]]
-            estimate = pref * np.abs(vdd).sum() * (abs(detS.real) + abs(detS.imag))
-            if estimate < rnd[t]:
+            est = pref * np.abs(vdd).sum() * (abs(detS.real) + abs(detS.imag))
+            if estimate and est < rnd[t]:
                 continue
+            nfull += 1
             prob = np.zeros((N, ne))
             for nn in range(ne):
                 for m in unocc:
@@ -219,4 +238,6 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
                 hops[t].append((step, int(old), int(m)))
             else:
                 nfr[t] += 1
-    return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, Z=Z, w=w, initial_state=states)
+    e1 = total_energy(model, r, v, w, state, mass)
+    return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, Z=Z, w=w, initial_state=states,
+                energy=np.stack([e0, e1], axis=1), nimp=impurity_population(psi, Z, state), nfull=nfull)

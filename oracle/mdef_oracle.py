@@ -3,8 +3,8 @@
 A numpy FP64 restatement of NQCDynamics.jl's electronic-friction Langevin
 dynamics on the Newns-Anderson (AndersonHolstein) model:
 
-  MDEF_BAOAB.perform_step!   src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:338-355
-  step_O!                    src/DynamicsMethods/IntegrationAlgorithms/steps.jl:128-156
+  MDEF_BAOAB.perform_step!   src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:163-180
+  step_O!                    src/DynamicsMethods/IntegrationAlgorithms/steps.jl:41-69
   DiabaticMDEF acceleration! src/DynamicsMethods/ClassicalMethods/mdef.jl:102-124
   friction!                  src/DynamicsMethods/ClassicalMethods/mdef.jl:131-140
 

@@ -1,0 +1,145 @@
+"""GPU parity of the IESH kernel (independent-electron surface hopping on the
+three-dimensional Newns-Anderson adsorbate).
+
+The oracle follows the reference's algorithm with dense LAPACK
+eigendecompositions, the exact propagator U exp(-i mu dt) U^H and explicit
+determinants for every hop candidate; the engine uses the secular roots of
+the arrowhead Hamiltonian, a Chebyshev propagator converged to 1e-17 and the
+determinant lemma.  Agreement is to rounding, not bitwise:
+  plain FP64 path: identical Fermi-Dirac occupations, hop sequences and
+      frustrated-hop counts; positions, velocities and orbitals to 1e-8;
+  fast FP32 path: ensemble observables within their sampling error.
+The estimate screen of the reference (iesh.jl:251-254) never changes a
+result: runs with and without it are bitwise equal.
+"""
+import numpy as np
+import pytest
+
+import iesh_oracle as IO
+from nqcd_gb300 import _lib as L
+from nqcd_gb300 import workload as WL
+
+pytestmark = pytest.mark.gpu
+
+
+def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_DIRAC, max_hops=32, save_stride=0,
+              exact=0):
+    P = wl["params"]
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_IESH, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
+    cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nelectrons = 3, 1, wl["nstates"], wl["nelectrons"]
+    params = np.array([P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"]])
+    masses = np.array([wl["mass"]])
+    eps = np.ascontiguousarray(wl["eps"])
+    V = np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 6, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta = wl["beta"]
+    cfg.ntraj_max = ntraj
+    cfg.init_kind = init
+    cfg.max_hops = max_hops
+    cfg.save_stride = save_stride
+    cfg.exact_hop_probability = exact
+    return L.Engine(cfg, [params, masses, eps, V])
+
+
+def oracle_model(wl):
+    P = wl["params"]
+    return IO.Metal3D(kxy=P["kxy"], A=P["A"], a=P["a"], delta=P["delta"], B=P["B"], b=P["b"], eps=wl["eps"],
+                      V=wl["V"])
+
+
+def run_engine(wl, n, nsteps, seed, state0_arr=None, **kw):
+    eng = make_iesh(wl, n, **kw)
+    try:
+        eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]), state0=state0_arr)
+        _, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], seed)
+        fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+        fin["hop_log"] = eng.get_hop_log(eng.cfg.max_hops)
+        fin["stats"] = st
+        return fin
+    finally:
+        eng.close()
+
+
+def compare_with_oracle(fin, o, n):
+    for t in range(n):
+        log = [tuple(x) for x in fin["hop_log"][t] if x[0] >= 0]
+        assert log == [tuple(h) for h in o["hops"][t]], (t, log, o["hops"][t])
+    np.testing.assert_array_equal(fin["nfrustrated"], o["nfrustrated"])
+    np.testing.assert_array_equal(fin["state"], o["state"])
+    np.testing.assert_allclose(fin["r"], o["r"], rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(fin["v"], o["v"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(fin["psi"], o["psi"], atol=1e-8)
+    np.testing.assert_allclose(fin["energy"], o["energy"], rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("nstates,nelectrons,n,nsteps,z0", [(20, 10, 12, 500, 3.5), (80, 40, 4, 300, 3.0)])
+def test_iesh_fp64_matches_oracle(nstates, nelectrons, n, nsteps, z0):
+    wl = WL.newns_anderson_iesh(n, nstates=nstates, nelectrons=nelectrons, z0=z0)
+    fin = run_engine(wl, n, nsteps, 3)
+    assert fin["stats"].unconverged_roots == 0
+    o = IO.run_iesh(oracle_model(wl), mass=wl["mass"], ne=nelectrons, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"],
+                    dt=wl["dt"], nsteps=nsteps, seed=3)
+    compare_with_oracle(fin, o, n)
+    if nstates == 80:
+        assert sum(len(h) for h in o["hops"]) > 0  # the case exercises hops
+
+
+def test_iesh_given_occupations_and_rescaling_modes():
+    n, nsteps = 4, 300
+    wl = WL.newns_anderson_iesh(n, nstates=40, nelectrons=20, z0=3.0)
+    occ0 = np.tile(np.arange(20, dtype=np.int32)[::-1], (n, 1)).copy()  # ground state, reversed electron order
+    for rescaling in (1, 2):
+        fin = run_engine(wl, n, nsteps, 5, rescaling=rescaling, init=L.INIT_GIVEN, state0_arr=occ0)
+        o = IO.run_iesh(oracle_model(wl), mass=wl["mass"], ne=20, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"],
+                        dt=wl["dt"], nsteps=nsteps, seed=5, rescaling=rescaling, initial_state=occ0)
+        compare_with_oracle(fin, o, n)
+
+
+@pytest.mark.parametrize("precision", [L.PREC_FP64, L.PREC_FP32])
+def test_iesh_estimate_screen_never_changes_results(precision):
+    n, nsteps = 16, 400
+    wl = WL.newns_anderson_iesh(n, z0=3.5)
+    a = run_engine(wl, n, nsteps, 7, precision=precision)
+    b = run_engine(wl, n, nsteps, 7, precision=precision, exact=1)
+    for key in ("r", "v", "psi", "state", "nhops", "nfrustrated", "hop_log", "energy"):
+        np.testing.assert_array_equal(a[key], b[key], err_msg=key)
+    assert b["stats"].hop_evaluations == n * nsteps
+    assert a["stats"].hop_evaluations < b["stats"].hop_evaluations
+
+
+@pytest.mark.parametrize("precision,tol", [(L.PREC_FP64, 1e-10), (L.PREC_FP32, 2e-4)])
+def test_iesh_orbitals_stay_orthonormal(precision, tol):
+    n, nsteps = 8, 1000
+    wl = WL.newns_anderson_iesh(n, z0=4.0)
+    fin = run_engine(wl, n, nsteps, 11, precision=precision)
+    for t in range(n):
+        g = fin["psi"][t].conj().T @ fin["psi"][t]
+        assert np.abs(g - np.eye(wl["nelectrons"])).max() < tol
+
+
+def test_iesh_fast_path_observables():
+    n, nsteps, stride = 1024, 1500, 100
+    wl = WL.newns_anderson_iesh(n, z0=5.0)
+    res = {}
+    for prec in (L.PREC_FP64, L.PREC_FP32):
+        eng = make_iesh(wl, n, precision=prec, save_stride=stride)
+        try:
+            eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]))
+            obs = np.zeros((nsteps // stride + 1) * 4)
+            out, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 13, observables=obs)
+            fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+            res[prec] = (obs.reshape(-1, 4), fin, st)
+        finally:
+            eng.close()
+    (oa, fa, sa), (ob, fb, sb) = res[L.PREC_FP64], res[L.PREC_FP32]
+    assert sa.hops > 0
+    # same Fermi-Dirac start (FP64 roots on both paths)
+    np.testing.assert_allclose(ob[0], oa[0], rtol=1e-5, atol=1e-6)
+    # ensemble means along the run: height, kinetic energy, impurity population
+    np.testing.assert_allclose(ob[:, 0], oa[:, 0], rtol=0.01)
+    np.testing.assert_allclose(ob[:, 1], oa[:, 1], rtol=0.01)
+    se = fa["nhops"].std() / np.sqrt(n)
+    assert abs(fb["nhops"].mean() - fa["nhops"].mean()) <= 3 * se + 0.01
+    assert np.mean(fa["nhops"] == fb["nhops"]) > 0.9
