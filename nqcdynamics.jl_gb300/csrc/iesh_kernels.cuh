@@ -64,7 +64,9 @@ namespace nqcd {
 
 constexpr int kIeshBlock = 256;
 constexpr int kIeshMaxStates = 128;
-constexpr int kIeshMaxTerms = 128;  // Chebyshev terms (Bessel recurrence starts at kIeshMaxTerms - 1)
+constexpr int kIeshMaxTerms = 128;  // Chebyshev terms
+constexpr int kIeshInv = 192;       // table of 1/n for the Bessel power series
+constexpr int kIeshFdChunk = 256;   // Metropolis iterations whose random numbers are drawn together
 
 enum IeshInit : int32_t { IESH_INIT_GIVEN = 0, IESH_INIT_FERMI_DIRAC = 3 };
 
@@ -108,8 +110,8 @@ struct alignas(2 * sizeof(R)) Cx {
 // Dynamic shared memory layout of one CTA (identical on host and device).
 struct IeshLayout {
     int N, Ne, Nu, Np, Nep;
-    size_t o_eps, o_V2, o_lam, o_z2, o_z0, o_lam64, o_At, o_phiA, o_phiB, o_J, o_occ, o_unocc, o_piv, o_red,
-        o_misc, bytes;
+    size_t o_eps, o_V2, o_lam, o_z2, o_z0, o_w64, o_At, o_phiA, o_phiB, o_out, o_J, o_Jr, o_inv, o_fdu, o_fdi, o_occ,
+        o_unocc, o_piv, o_red, o_misc, bytes;
 };
 
 NQCD_HD size_t iesh_take(size_t& o, size_t bytes) {
@@ -132,13 +134,18 @@ NQCD_HD IeshLayout iesh_layout(int N, int Ne) {
     L.o_lam = iesh_take(o, sizeof(R) * L.Np);
     L.o_z2 = iesh_take(o, sizeof(R) * L.Np);
     L.o_z0 = iesh_take(o, sizeof(R) * L.Np);
-    L.o_lam64 = iesh_take(o, sizeof(double) * L.Np);
+    L.o_w64 = iesh_take(o, sizeof(double) * L.Np);
     L.o_At = iesh_take(o, sizeof(R) * L.Np * L.Np);
     L.o_phiA = iesh_take(o, 2 * sizeof(R) * L.Np * L.Nep);
     const size_t pb = 2 * sizeof(R) * (size_t)L.Np * L.Nep;
     const size_t lu = 2 * sizeof(R) * (size_t)L.Nep * (L.Nep + L.Nu);  // S^T and the right-hand sides
     L.o_phiB = iesh_take(o, lu > pb ? lu : pb);
+    L.o_out = iesh_take(o, 2 * sizeof(R) * L.Np * L.Nep);
     L.o_J = iesh_take(o, sizeof(double) * kIeshMaxTerms);
+    L.o_Jr = iesh_take(o, sizeof(R) * kIeshMaxTerms);
+    L.o_inv = iesh_take(o, sizeof(double) * kIeshInv);
+    L.o_fdu = iesh_take(o, sizeof(double) * kIeshFdChunk);
+    L.o_fdi = iesh_take(o, 2 * kIeshFdChunk);
     L.o_occ = iesh_take(o, sizeof(int) * L.Nep);
     L.o_unocc = iesh_take(o, sizeof(int) * L.Np);
     L.o_piv = iesh_take(o, sizeof(int) * L.Nep);
@@ -148,36 +155,61 @@ NQCD_HD IeshLayout iesh_layout(int N, int Ne) {
     return L;
 }
 
-// Register tiles of the A * phi products: 4 rows x 4 orbitals per thread.
+// Register tiles of the A * phi products: 4 rows x 4 orbitals per thread,
+// interleaved (rows rt + RG rr, orbitals ct + CG cc with RG = Np/4, CG = Nep/4)
+// so that the lanes of a warp address consecutive shared-memory banks.
 NQCD_HD int iesh_tiles(int N, int Ne) { return (((N + 3) & ~3) / 4) * (((Ne + 3) & ~3) / 4); }
 
-// Bessel functions J_k(alpha), k = 0 .. kIeshMaxTerms-1, by Miller's backward
-// recurrence J_{k-1} = (2k / alpha) J_k - J_{k+1} from order kIeshMaxTerms + 20,
-// normalised with J_0 + 2 sum_{k>=1} J_{2k} = 1.  Returns the last order K
-// with |J_K| >= tol (the series uses terms 0..K), or -1 if the tail is not
-// below tol within kIeshMaxTerms terms.
-__device__ inline int iesh_bessel(double alpha, double tol, double* J) {
-    const int top = kIeshMaxTerms + 20;
-    double jp1 = 0.0, jk = 1e-280, sum = 0.0;
-    for (int k = top; k > 0; --k) {
-        const double jm1 = (2.0 * k / alpha) * jk - jp1;
-        jp1 = jk;
-        jk = jm1;  // J_{k-1}
-        if (k - 1 < kIeshMaxTerms) J[k - 1] = jk;
-        if (k - 1 > 0 && ((k - 1) & 1) == 0) sum += 2.0 * jk;
-        if (fabs(jk) > 1e250) {  // rescale the recurrence
-            jk *= 1e-250;
-            jp1 *= 1e-250;
-            sum *= 1e-250;
-            for (int q = k - 1; q < kIeshMaxTerms; ++q) J[q] *= 1e-250;
+// Chebyshev coefficients J_k(alpha), k = 0 .. kIeshMaxTerms-1, computed by one
+// warp.  For alpha <= 4 each lane sums the power series
+//     J_k(x) = sum_m (-1)^m (x/2)^(2m+k) / (m! (m+k)!)
+// for its orders (terms at most e^4 / 2 in size, so the sum keeps 1e-14
+// relative accuracy); larger alpha use Miller's backward recurrence
+// J_{k-1} = (2k/alpha) J_k - J_{k+1} on lane 0, normalised with
+// J_0 + 2 sum J_2k = 1.  Returns the last order K with |J_K| >= tol (the
+// series uses terms 0..K), or -1 if the tail does not fall below tol.
+__device__ inline int iesh_bessel_warp(double alpha, double tol, double* J, const double* inv) {
+    const int lane = threadIdx.x & 31;
+    if (alpha <= 4.0) {
+        // orders 0..31 (J_k(4) < 1e-25 beyond), 24 series terms ((x/2)^2m / (m! (m+k)!) < 1e-20 beyond)
+        const double x = 0.5 * alpha, mx2 = -x * x;
+        const int k = lane;
+        double t = 1.0;
+        for (int q = 1; q <= k; ++q) t *= x * inv[q];  // x^k / k!
+        double s = t;
+#pragma unroll 4
+        for (int m = 1; m <= 24; ++m) {
+            t *= mx2 * (inv[m] * inv[m + k]);
+            s += t;
         }
+        J[k] = s;
+        for (int q = 32 + lane; q < kIeshMaxTerms; q += 32) J[q] = 0.0;
+    } else if (lane == 0) {
+        const double ia = 1.0 / alpha;
+        const int top = kIeshMaxTerms + 20;
+        double jp1 = 0.0, jk = 1e-280, sum = 0.0;
+        for (int k = top; k > 0; --k) {
+            const double jm1 = (2.0 * k * ia) * jk - jp1;
+            jp1 = jk;
+            jk = jm1;  // J_{k-1}
+            if (k - 1 < kIeshMaxTerms) J[k - 1] = jk;
+            if (k - 1 > 0 && ((k - 1) & 1) == 0) sum += 2.0 * jk;
+            if (fabs(jk) > 1e250) {
+                jk *= 1e-250;
+                jp1 *= 1e-250;
+                sum *= 1e-250;
+                for (int q = k - 1; q < kIeshMaxTerms; ++q) J[q] *= 1e-250;
+            }
+        }
+        const double norm = 1.0 / (sum + jk);
+        for (int q = 0; q < kIeshMaxTerms; ++q) J[q] *= norm;
     }
-    const double norm = 1.0 / (sum + jk);
-    for (int q = 0; q < kIeshMaxTerms; ++q) J[q] *= norm;
-    int K = kIeshMaxTerms - 1;
-    while (K > 0 && fabs(J[K]) < tol) --K;
-    if (K >= kIeshMaxTerms - 2) return -1;
-    return K;
+    __syncwarp();
+    int K = -1;
+    for (int k = lane; k < kIeshMaxTerms; k += 32)
+        if (fabs(J[k]) >= tol) K = k;
+    for (int off = 16; off > 0; off >>= 1) K = max(K, __shfl_xor_sync(0xffffffffu, K, off));
+    return K >= kIeshMaxTerms - 2 ? -1 : K;
 }
 
 // k-th (0-based) unset bit among bits [0, n) of a 128-bit mask.
@@ -187,11 +219,13 @@ __device__ inline int iesh_nth_unset(const unsigned long long* m, int n, int k) 
         if (lo >= n) break;
         const int nb = n - lo < 64 ? n - lo : 64;
         const unsigned long long valid = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
-        unsigned long long z = ~m[w] & valid;
+        const unsigned long long z = ~m[w] & valid;
         const int c = __popcll(z);
         if (k < c) {
-            for (int q = 0; q < k; ++q) z &= z - 1ull;
-            return lo + __ffsll((long long)z) - 1;
+            const unsigned lo32 = (unsigned)z, hi32 = (unsigned)(z >> 32);
+            const int c32 = __popc(lo32);
+            if (k < c32) return lo + (int)__fns(lo32, 0, k + 1);
+            return lo + 32 + (int)__fns(hi32, 0, k - c32 + 1);
         }
         k -= c;
     }
@@ -243,14 +277,26 @@ __device__ inline void iesh_block_minmax(double& lo, double& hi, double* red) {
 }
 
 template <typename R>
+__device__ inline R warp_sum(R x) {
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
+}
+
+template <typename R>
 __device__ inline Cx<R> cx_div(Cx<R> a, Cx<R> b) {
     const R d = b.re * b.re + b.im * b.im;
     return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
 }
 
-template <typename R>
-__device__ inline Cx<R> cx_mul(Cx<R> a, Cx<R> b) {
-    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+// (re, im) * 2^e with |re| + |im| kept in [0.5, 1): products of many pivots
+// without overflow or underflow.
+__device__ inline void scaled_mul(double& re, double& im, int& e, double br, double bi, int be) {
+    const double nr = re * br - im * bi, ni = re * bi + im * br;
+    int ex;
+    frexp(fabs(nr) + fabs(ni), &ex);
+    re = ldexp(nr, -ex);
+    im = ldexp(ni, -ex);
+    e += be + ex;
 }
 
 template <typename R>
@@ -258,6 +304,32 @@ constexpr int iesh_min_blocks() {
     return std::is_same<R, float>::value ? 2 : 1;
 }
 
+// Model functions at height z: h, dh/dz (FP32 on the fast path).
+template <typename R>
+__device__ inline void iesh_level(const IeshParams& p, double z, double& h, double& dh) {
+    if constexpr (std::is_same<R, float>::value) {
+        const float e = expf(-(float)p.b * (float)z);
+        h = (double)((float)p.delta - (float)p.B * e);
+        dh = (double)((float)p.B * (float)p.b * e);
+    } else {
+        const double e = nqcd_exp(-p.b * z);
+        h = p.delta - p.B * e;
+        dh = p.B * p.b * e;
+    }
+}
+
+template <typename R>
+__device__ inline double iesh_wall(const IeshParams& p, double z) {  // exp(-a z)
+    if constexpr (std::is_same<R, float>::value)
+        return (double)expf(-(float)p.a * (float)z);
+    else
+        return nqcd_exp(-p.a * z);
+}
+
+// One CTA integrates one trajectory.  Warp 0 owns the nuclear state (every
+// lane holds the same copy) and the serial FP64 work; it publishes h, dh/dz
+// and v . grad h through shared memory.  All threads share the root solve,
+// the coupling matrix, the propagator and the hop linear algebra.
 template <typename R>
 __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(const IeshParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -267,23 +339,30 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     R* lam = (R*)(smem + L.o_lam);
     R* z2 = (R*)(smem + L.o_z2);
     R* z0 = (R*)(smem + L.o_z0);
-    double* lam64 = (double*)(smem + L.o_lam64);
+    double* w64 = (double*)(smem + L.o_w64);
     R* At = (R*)(smem + L.o_At);
     Cx<R>* phiA = (Cx<R>*)(smem + L.o_phiA);
     Cx<R>* phiB = (Cx<R>*)(smem + L.o_phiB);
+    Cx<R>* outb = (Cx<R>*)(smem + L.o_out);
     double* Jc = (double*)(smem + L.o_J);
+    R* Jr = (R*)(smem + L.o_Jr);  // 2 J_k in the working precision
+    double* inv = (double*)(smem + L.o_inv);
+    double* fdu = (double*)(smem + L.o_fdu);
+    unsigned char* fdi = (unsigned char*)(smem + L.o_fdi);
     int* occ = (int*)(smem + L.o_occ);
     int* unocc = (int*)(smem + L.o_unocc);
     int* piv = (int*)(smem + L.o_piv);
     double* red = (double*)(smem + L.o_red);
+    // misc: [0] K [1] sin(c dt) [2] cos(c dt), then the full-evaluation flag [3] v_z [4] h [5] dh/dz
+    //       [6] v . grad h [7] singular S [8] c [9] 1/hw [10] w/hw [11] J_0
     double* misc = (double*)(smem + L.o_misc);
 
     const int N = L.N, Ne = L.Ne, Nu = L.Nu, Np = L.Np, Nep = L.Nep, M = p.nbath;
-    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int64_t ti = blockIdx.x;
     const int64_t NT = p.ntraj;
     const uint64_t gid = (uint64_t)(p.traj_offset + ti);
-    const double mass = p.mass, dt = p.dt, half = dt / 2.0;
+    const double mass = p.mass, inv_mass = 1.0 / p.mass, dt = p.dt, half = dt / 2.0;
     unsigned long long* nonconv = p.counters ? p.counters + 2 : nullptr;
 
     for (int k = tid; k < Np; k += nthr) {
@@ -297,23 +376,22 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     for (int q = tid; q < Np * Nep; q += nthr) {
         phiA[q] = {R(0), R(0)};
         phiB[q] = {R(0), R(0)};
+        outb[q] = {R(0), R(0)};
     }
-    __syncthreads();
+    for (int q = tid; q < kIeshInv; q += nthr) inv[q] = q ? 1.0 / q : 0.0;
 
-    double r[3], v[3], k[3];
+    double r[3], v[3], k[3];  // meaningful in warp 0
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         r[d] = p.r[d * NT + ti];
         v[d] = p.v[d * NT + ti];
+        k[d] = 0.0;
     }
     const double Lpad = fabs(p.eps[0]) + fabs(p.eps[M - 1]) + 1.0 + p.sumV2;
     // thread i < N owns root i and warm-starts it from the previous step
-    R lam_own = tid == 0 ? eps[0] - R(1e-3) : (tid <= M ? eps[tid - 1] + R(1e-9) : R(0));
-    double hz = 0.0, dhz = 0.0;
-    auto electronic = [&](double zpos) {
-        const double ebz = nqcd_exp(-p.b * zpos);
-        hz = p.delta - p.B * ebz;
-        dhz = p.B * p.b * ebz;
+    R lam_own = R(0);
+    auto roots = [&]() {  // after a barrier that published misc[4] = h
+        const double hz = misc[4];
         if (tid < N) {
             R zz;
             secular_root<R>(eps, V2, M, tid, (R)hz, (R)(fabs(hz) + Lpad), lam_own, zz, nonconv);
@@ -323,18 +401,19 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         }
         __syncthreads();
     };
-    auto accel = [&]() {
-        double occsum = 0.0;
-        for (int jj = 0; jj < Ne; ++jj) occsum += (double)z2[occ[jj]];
-        const double eaz = nqcd_exp(-p.a * r[2]);
-        k[0] = -(p.kxy * r[0]) / mass;
-        k[1] = -(p.kxy * r[1]) / mass;
-        k[2] = -(-p.A * p.a * eaz + dhz * occsum) / mass;
+    auto accel = [&](double dh) {  // warp 0
+        R acc = R(0);
+        for (int jj = lane; jj < Ne; jj += 32) acc += z2[occ[jj]];
+        const double occsum = (double)warp_sum<R>(acc);
+        const double eaz = iesh_wall<R>(p, r[2]);
+        k[0] = -(p.kxy * r[0]) * inv_mass;
+        k[1] = -(p.kxy * r[1]) * inv_mass;
+        k[2] = -(-p.A * p.a * eaz + dh * occsum) * inv_mass;
     };
-    auto potential = [&]() {
-        double s = 0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) + p.A * nqcd_exp(-p.a * r[2]);
-        for (int jj = 0; jj < Ne; ++jj) s += (double)lam[occ[jj]];
-        return s;
+    auto potential = [&]() {  // warp 0: U0 + sum of occupied eigenvalues (iesh.jl:380-388)
+        R acc = R(0);
+        for (int jj = lane; jj < Ne; jj += 32) acc += lam[occ[jj]];
+        return 0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) + p.A * iesh_wall<R>(p, r[2]) + (double)warp_sum<R>(acc);
     };
     auto kinetic = [&]() { return 0.5 * mass * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
     auto rebuild_unocc = [&]() {  // ascending, as set_unoccupied_states! (DynamicsUtils.jl:162-171)
@@ -346,43 +425,89 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     };
 
     // ---- initial electronic structure and occupations ----
-    electronic(r[2]);
+    lam_own = tid == 0 ? eps[0] - R(1e-3) : (tid <= M ? eps[tid - 1] + R(1e-9) : R(0));
+    double hz = 0.0, dhz = 0.0;
+    if (warp == 0) {
+        iesh_level<R>(p, r[2], hz, dhz);
+        if (lane == 0) {
+            misc[4] = hz;
+            misc[5] = dhz;
+        }
+    }
+    __syncthreads();
+    roots();
     if (p.init_kind == IESH_INIT_FERMI_DIRAC) {
-        // the Metropolis acceptance uses FP64 eigenvalues on both paths
+        // Metropolis over occupations with the Boltzmann ratio (DynamicsUtils.jl:194-208).
+        // Acceptance exp(-beta (e_j - e_i)) > u is tested as w_j > u w_i with
+        // w_s = exp(-beta (e_s - e_ref)); FP64 eigenvalues on both paths.
+        __shared__ int bad_weight;
+        if (tid == 0) bad_weight = 0;
+        __syncthreads();
+        const double eref = 0.5 * (p.eps[0] + p.eps[M - 1]);
         if (tid < N) {
+            double l64;
             if constexpr (std::is_same<R, double>::value) {
-                lam64[tid] = (double)lam[tid];
-            } else {  // FP64 roots from the global FP64 bath arrays
-                double l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9, zz;
-                secular_root<double>(p.eps, p.V2, M, tid, hz, fabs(hz) + Lpad, l64, zz, nonconv);
-                lam64[tid] = l64;
+                l64 = lam[tid];
+            } else {
+                const double h64 = p.delta - p.B * nqcd_exp(-p.b * r[2]);
+                double zz;
+                l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9;
+                secular_root<double>(p.eps, p.V2, M, tid, h64, fabs(h64) + Lpad, l64, zz, nonconv);
             }
+            const double wt = nqcd_exp(-p.beta * (l64 - eref));
+            w64[tid] = l64;
+            if (!(wt > 0.0 && wt < 1e300)) bad_weight = 1;
+            else w64[tid] = wt;
         }
         __syncthreads();
-        if (tid == 0) {
-            unsigned long long m2[2] = {0ull, 0ull};
+        const bool direct = bad_weight != 0;  // weights out of range: exponentiate each difference
+        if (direct && tid < N) {               // w64 must hold the eigenvalues then
+            if constexpr (std::is_same<R, double>::value) {
+                w64[tid] = lam[tid];
+            } else {
+                const double h64 = p.delta - p.B * nqcd_exp(-p.b * r[2]);
+                double zz, l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9;
+                secular_root<double>(p.eps, p.V2, M, tid, h64, fabs(h64) + Lpad, l64, zz, nullptr);
+                w64[tid] = l64;
+            }
+        }
+        unsigned long long m2[2] = {0ull, 0ull};
+        if (tid == 0)
             for (int jj = 0; jj < Ne; ++jj) {
                 occ[jj] = jj;
                 m2[jj >> 6] |= 1ull << (jj & 63);
             }
-            for (int it = 0; it < N * Ne; ++it) {
+        const int total = N * Ne;
+        for (int base = 0; base < total; base += kIeshFdChunk) {
+            const int cnt = total - base < kIeshFdChunk ? total - base : kIeshFdChunk;
+            __syncthreads();
+            for (int q = tid; q < cnt; q += nthr) {
+                const int it = base + q;
                 const u32x4 wa = rng_block(p.seed, gid, (uint32_t)it, RNG_INIT_FD);
                 const u32x4 wb = rng_block(p.seed, gid, (uint32_t)it, RNG_INIT_FD + 16);
-                const double ua = u01_from_words(wa.x, wa.y), ub = u01_from_words(wa.z, wa.w);
-                const double uc = u01_from_words(wb.x, wb.y);
-                int ci = (int)(ua * Ne);
+                int ci = (int)(u01_from_words(wa.x, wa.y) * Ne);
                 if (ci > Ne - 1) ci = Ne - 1;
-                int pick = (int)(ub * Nu);
+                int pick = (int)(u01_from_words(wa.z, wa.w) * Nu);
                 if (pick > Nu - 1) pick = Nu - 1;
-                const int j = iesh_nth_unset(m2, N, pick);
-                const int i = occ[ci];
-                const double prob = nqcd_exp(-p.beta * (lam64[j] - lam64[i]));
-                if (prob > uc) {
-                    m2[i >> 6] &= ~(1ull << (i & 63));
-                    m2[j >> 6] |= 1ull << (j & 63);
-                    occ[ci] = j;
-                }
+                fdi[2 * q] = (unsigned char)ci;
+                fdi[2 * q + 1] = (unsigned char)pick;
+                fdu[q] = u01_from_words(wb.x, wb.y);
             }
+            __syncthreads();
+            if (tid == 0)
+                for (int q = 0; q < cnt; ++q) {
+                    const int ci = fdi[2 * q];
+                    const int j = iesh_nth_unset(m2, N, fdi[2 * q + 1]);
+                    const int i = occ[ci];
+                    const bool acc = direct ? nqcd_exp(-p.beta * (w64[j] - w64[i])) > fdu[q] : w64[j] > fdu[q] * w64[i];
+                    if (acc) {
+                        m2[i >> 6] &= ~(1ull << (i & 63));
+                        m2[j >> 6] |= 1ull << (j & 63);
+                        occ[ci] = j;
+                    }
+                }
+        }
+        if (tid == 0) {
             for (int a = 1; a < Ne; ++a) {  // sort!(state)
                 const int x = occ[a];
                 int b = a - 1;
@@ -400,40 +525,46 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     }
     __syncthreads();
     for (int jj = tid; jj < Ne; jj += nthr) phiA[occ[jj] * Nep + jj] = {R(1), R(0)};
+    double e0 = 0.0;
+    if (warp == 0) {
+        accel(dhz);
+        const double pe = potential();
+        e0 = kinetic() + pe;
+    }
     __syncthreads();
-    accel();
-    const double e0 = p.energy ? kinetic() + potential() : 0.0;
 
     // matrix-product tiles
-    const int ncg = Nep >> 2;
-    const int ntile = (Np >> 2) * ncg;
+    const int CG = Nep >> 2, RG = Np >> 2;
+    const int ntile = RG * CG;
     const bool tile_on = tid < ntile;
-    const int i0 = tile_on ? (tid / ncg) * 4 : 0;
-    const int c0 = tile_on ? (tid % ncg) * 4 : 0;
+    const int i0 = tile_on ? tid / CG : 0;  // rows i0 + RG rr
+    const int c0 = tile_on ? tid % CG : 0;  // orbitals c0 + CG cc
 
     auto save = [&](int isave) {
         // impurity population (iesh_diabatic_population, row 0 of Z rho Z^T)
         double contrib = 0.0;
         if (tid < Ne) {
-            double ar = 0.0, ai = 0.0, sq = 0.0;
+            R ar = R(0), ai = R(0), sq = R(0);
             for (int a = 0; a < N; ++a) {
                 const Cx<R> c = phiA[a * Nep + tid];
-                const double za = (double)z0[a];
-                ar += za * (double)c.re;
-                ai += za * (double)c.im;
-                sq += (double)z2[a] * ((double)c.re * (double)c.re + (double)c.im * (double)c.im);
+                ar += z0[a] * c.re;
+                ai += z0[a] * c.im;
+                sq += z2[a] * (c.re * c.re + c.im * c.im);
             }
-            contrib = ar * ar + ai * ai - sq + (double)z2[occ[tid]];
+            contrib = (double)ar * (double)ar + (double)ai * (double)ai - (double)sq + (double)z2[occ[tid]];
         }
         const double nimp = iesh_block_sum(contrib, red);
-        if (tid == 0 && isave < p.nsave) {
-            double* dst = p.obs_partial + (ti * p.nsave + isave) * 4;
-            dst[0] = r[2];
-            dst[1] = kinetic();
-            dst[2] = nimp;
-            dst[3] = potential();
+        if (warp == 0) {
+            const double pe = potential();
+            if (lane == 0 && isave < p.nsave) {
+                double* dst = p.obs_partial + (ti * p.nsave + isave) * 4;
+                dst[0] = r[2];
+                dst[1] = kinetic();
+                dst[2] = nimp;
+                dst[3] = pe;
+            }
         }
-        __syncthreads();  // the next step rewrites the roots thread 0 just read
+        __syncthreads();  // the next step rewrites the roots warp 0 just read
     };
     int isave = 0;
     if (p.save_stride > 0 && p.obs_partial) save(isave++);
@@ -443,22 +574,32 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     for (int step = 1; step <= p.nsteps; ++step) {
         // ---- velocity Verlet (verlet_with_electronics.jl:55-63) ----
         double vt[3];
+        if (warp == 0) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) vt[d] = v[d] + half * k[d];
+            for (int d = 0; d < 3; ++d) vt[d] = v[d] + half * k[d];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) r[d] = r[d] + dt * vt[d];
-        electronic(r[2]);
-        accel();
+            for (int d = 0; d < 3; ++d) r[d] = r[d] + dt * vt[d];
+            iesh_level<R>(p, r[2], hz, dhz);
+            if (lane == 0) {
+                misc[4] = hz;
+                misc[5] = dhz;
+            }
+        }
+        __syncthreads();
+        roots();
+        if (warp == 0) {
+            accel(dhz);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) v[d] = vt[d] + half * k[d];
-        const double w = v[2] * dhz;  // v . grad h: the couplings are d_alpha = dh/dalpha A
-
+            for (int d = 0; d < 3; ++d) v[d] = vt[d] + half * k[d];
+            if (lane == 0) misc[6] = v[2] * dhz;  // v . grad h: the couplings are d_alpha = dh/dalpha A
+        }
         // ---- propagator (wavefunction_dynamics.jl:15-58) ----
         for (int q = tid; q < N * N; q += nthr) {
             const int j = q / N, i = q - j * N;
             At[j * Np + i] = i == j ? R(0) : z0[i] * z0[j] / (lam[j] - lam[i]);
         }
         __syncthreads();
+        const double w = misc[6];
         double elo = 1e300, ehi = -1e300;
         if (tid < N) {
             R sacc = R(0);
@@ -468,32 +609,50 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             ehi = (double)lam[tid] + rad;
         }
         iesh_block_minmax(elo, ehi, red);
-        const double cen = 0.5 * (ehi + elo);
-        const double hw = 0.5 * (ehi - elo) * (1.0 + 1e-12) + 1e-300;
-        if (tid == 0) misc[0] = (double)iesh_bessel(hw * dt, p.cheb_tol, Jc);
+        if (warp == 0) {
+            // enclosure [c - hw, c + hw] of the spectrum, widened by a margin that
+            // covers the rounding of the bound in the working precision
+            const double cen = 0.5 * (ehi + elo);
+            const double hw = 0.5 * (ehi - elo) * (1.0 + (std::is_same<R, float>::value ? 1e-5 : 1e-12)) + 1e-300;
+            const int K = iesh_bessel_warp(hw * dt, p.cheb_tol, Jc, inv);
+            for (int q = lane; q < kIeshMaxTerms; q += 32) Jr[q] = (R)(2.0 * Jc[q]);
+            if (lane == 0) {
+                double sn, cs;
+                sincos(cen * dt, &sn, &cs);  // exp(-i c dt) = cs - i sn
+                misc[0] = (double)K;
+                misc[1] = sn;
+                misc[2] = cs;
+                misc[8] = cen;
+                misc[9] = 1.0 / hw;
+                misc[10] = w / hw;
+                misc[11] = Jc[0];
+            }
+        }
         __syncthreads();
         const int K = (int)misc[0];
         if (K < 0) {  // step too long for the series: leave psi unchanged, count as unconverged
             if (tid == 0 && nonconv) atomicAdd(nonconv, 1ull);
         } else {
             nterms += (unsigned long long)K;
-            const R s = (R)(w / hw);
+            const R s = (R)misc[10];
+            const R cenr = (R)misc[8], ihwr = (R)misc[9];
             R dl[4];
 #pragma unroll
-            for (int rr = 0; rr < 4; ++rr) dl[rr] = (R)(((double)lam[i0 + rr] - cen) / hw);
-            Cx<R> prev[4][4], out[4][4];
+            for (int rr = 0; rr < 4; ++rr) dl[rr] = (lam[i0 + RG * rr] - cenr) * ihwr;
             if (tile_on) {
-                const R j0 = (R)Jc[0];
+                const R j0 = (R)misc[11];
 #pragma unroll
                 for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc) {
-                        const Cx<R> x = phiA[(i0 + rr) * Nep + c0 + cc];
-                        out[rr][cc] = {j0 * x.re, j0 * x.im};
-                        prev[rr][cc] = {R(0), R(0)};
+                        const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
+                        const Cx<R> x = phiA[ix];
+                        outb[ix] = {j0 * x.re, j0 * x.im};
                     }
             }
             for (int kk = 1; kk <= K; ++kk) {
+                // phi_k = 2 Ht phi_{k-1} - phi_{k-2}: dst holds phi_{k-2} on entry and
+                // each thread reads back only its own tile before overwriting it
                 const Cx<R>* src = (kk & 1) ? phiA : phiB;
                 Cx<R>* dst = (kk & 1) ? phiB : phiA;
                 __syncthreads();
@@ -509,9 +668,9 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                         R av[4];
                         Cx<R> pv[4];
 #pragma unroll
-                        for (int rr = 0; rr < 4; ++rr) av[rr] = aj[rr];
+                        for (int rr = 0; rr < 4; ++rr) av[rr] = aj[RG * rr];
 #pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) pv[cc] = pj[cc];
+                        for (int cc = 0; cc < 4; ++cc) pv[cc] = pj[CG * cc];
 #pragma unroll
                         for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
@@ -520,24 +679,26 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                                 ai[rr][cc] += av[rr] * pv[cc].im;
                             }
                     }
-                    const R jk = (R)(2.0 * Jc[kk]);
+                    const R jk = Jr[kk];
                     const int ph = kk & 3;
 #pragma unroll
                     for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
                         for (int cc = 0; cc < 4; ++cc) {
-                            const Cx<R> cur = src[(i0 + rr) * Nep + c0 + cc];
+                            const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
+                            const Cx<R> cur = src[ix];
                             // Ht phi = dl phi - i s (A phi)
                             const R hre = dl[rr] * cur.re + s * ai[rr][cc];
                             const R him = dl[rr] * cur.im - s * ar[rr][cc];
                             Cx<R> nw;
-                            if (kk == 1)
+                            if (kk == 1) {
                                 nw = {hre, him};
-                            else
-                                nw = {R(2) * hre - prev[rr][cc].re, R(2) * him - prev[rr][cc].im};
-                            prev[rr][cc] = cur;
-                            dst[(i0 + rr) * Nep + c0 + cc] = nw;
-                            Cx<R>& o = out[rr][cc];
+                            } else {
+                                const Cx<R> pr = dst[ix];
+                                nw = {R(2) * hre - pr.re, R(2) * him - pr.im};
+                            }
+                            dst[ix] = nw;
+                            Cx<R> o = outb[ix];
                             if (ph == 0) {
                                 o.re += jk * nw.re;
                                 o.im += jk * nw.im;
@@ -551,20 +712,20 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                                 o.re -= jk * nw.im;
                                 o.im += jk * nw.re;
                             }
+                            outb[ix] = o;
                         }
                 }
             }
             __syncthreads();
-            double sn, cs;
-            sincos(cen * dt, &sn, &cs);  // exp(-i c dt) = cs - i sn
-            const R csr = (R)cs, snr = (R)sn;
+            const R snr = (R)misc[1], csr = (R)misc[2];
             if (tile_on) {
 #pragma unroll
                 for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc) {
-                        const Cx<R> o = out[rr][cc];
-                        phiA[(i0 + rr) * Nep + c0 + cc] = {o.re * csr + o.im * snr, o.im * csr - o.re * snr};
+                        const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
+                        const Cx<R> o = outb[ix];
+                        phiA[ix] = {o.re * csr + o.im * snr, o.im * csr - o.re * snr};
                     }
             }
             __syncthreads();
@@ -578,92 +739,107 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             Sm[c * Nep + j] = phiA[occ[j] * Nep + c];
         }
         __syncthreads();
+        double det_r = 0.0, det_i = 0.0;
+        int det_e = 0;
+        // LU with partial pivoting of S^T: warp 0 picks the pivot, swaps and
+        // scales the pivot column; all warps share the trailing update (rows
+        // by warp, columns by lane); two barriers per column.
         bool singular = false;
+        const int nwarp = nthr >> 5;
         for (int col = 0; col < Ne; ++col) {
-            if (tid < 32) {
-                double best = -1.0;
+            if (warp == 0) {
+                R best = R(-1);
                 int bi = col;
-                for (int rr = col + tid; rr < Ne; rr += 32) {
+                for (int rr = col + lane; rr < Ne; rr += 32) {
                     const Cx<R> x = Sm[rr * Nep + col];
-                    const double mg = fabs((double)x.re) + fabs((double)x.im);
+                    const R mg = fabs(x.re) + fabs(x.im);
                     if (mg > best) {
                         best = mg;
                         bi = rr;
                     }
                 }
                 for (int off = 16; off > 0; off >>= 1) {
-                    const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+                    const R ob = __shfl_xor_sync(0xffffffffu, best, off);
                     const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
                     if (ob > best || (ob == best && oi < bi)) {
                         best = ob;
                         bi = oi;
                     }
                 }
-                if (tid == 0) {
+                if (best > R(0)) {
+                    if (bi != col)
+                        for (int q = lane; q < Ne; q += 32) {
+                            const Cx<R> t = Sm[col * Nep + q];
+                            Sm[col * Nep + q] = Sm[bi * Nep + q];
+                            Sm[bi * Nep + q] = t;
+                        }
+                    __syncwarp();
+                    const Cx<R> pv = Sm[col * Nep + col];
+                    for (int rr = col + 1 + lane; rr < Ne; rr += 32) Sm[rr * Nep + col] = cx_div<R>(Sm[rr * Nep + col], pv);
+                }
+                if (lane == 0) {
                     piv[col] = bi;
-                    misc[1] = best;
+                    misc[7] = best > R(0) ? 0.0 : 1.0;
                 }
             }
             __syncthreads();
-            if (!(misc[1] > 0.0)) {
+            if (misc[7] != 0.0) {
                 singular = true;
                 break;
             }
-            const int pr = piv[col];
-            if (pr != col)
-                for (int q = tid; q < Ne; q += nthr) {
-                    const Cx<R> t = Sm[col * Nep + q];
-                    Sm[col * Nep + q] = Sm[pr * Nep + q];
-                    Sm[pr * Nep + q] = t;
+            for (int rr = col + 1 + warp; rr < Ne; rr += nwarp) {
+                const Cx<R> l = Sm[rr * Nep + col];
+                for (int cc = col + 1 + lane; cc < Ne; cc += 32) {
+                    const Cx<R> u = Sm[col * Nep + cc];
+                    Cx<R>& t = Sm[rr * Nep + cc];
+                    t.re -= l.re * u.re - l.im * u.im;
+                    t.im -= l.re * u.im + l.im * u.re;
                 }
-            __syncthreads();
-            const Cx<R> pv = Sm[col * Nep + col];
-            for (int rr = col + 1 + tid; rr < Ne; rr += nthr) Sm[rr * Nep + col] = cx_div<R>(Sm[rr * Nep + col], pv);
-            __syncthreads();
-            const int nt = Ne - col - 1;
-            for (int q = tid; q < nt * nt; q += nthr) {
-                const int rr = col + 1 + q / nt, cc = col + 1 + q % nt;
-                const Cx<R> l = Sm[rr * Nep + col], u = Sm[col * Nep + cc];
-                Cx<R>& t = Sm[rr * Nep + cc];
-                t.re -= l.re * u.re - l.im * u.im;
-                t.im -= l.re * u.im + l.im * u.re;
             }
             __syncthreads();
         }
-        const double u = std::is_same<R, double>::value
-                             ? rng_uniform(p.seed, gid, (uint32_t)step, RNG_HOP)
-                             : (double)rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP);
-        // sum |v.d| over unoccupied rows and electrons (the estimate's sum(abs, v_dot_d))
-        double sabs = 0.0;
-        for (int q = tid; q < Nu * Ne; q += nthr) {
-            const int mm = q / Ne, n = q - mm * Ne;
-            sabs += fabs(w * (double)At[occ[n] * Np + unocc[mm]]);
-        }
-        sabs = iesh_block_sum(sabs, red);
-        if (tid == 0) {
-            int full = 0;
-            if (!singular) {
-                // det S with a running power-of-two exponent
+        R sabs = R(0);
+        if (warp == 0) {
+            if (!singular) {  // det S on lane 0
                 double dr = 1.0, di = 0.0;
                 int de = 0, swaps = 0;
-                for (int q = 0; q < Ne; ++q) {
+                for (int q = lane; q < Ne; q += 32) {
                     const Cx<R> d = Sm[q * Nep + q];
-                    const double nr = dr * (double)d.re - di * (double)d.im;
-                    const double ni = dr * (double)d.im + di * (double)d.re;
-                    int ex;
-                    const double mg = frexp(fabs(nr) + fabs(ni), &ex);
-                    (void)mg;
-                    dr = ldexp(nr, -ex);
-                    di = ldexp(ni, -ex);
-                    de += ex;
+                    scaled_mul(dr, di, de, (double)d.re, (double)d.im, 0);
                     if (piv[q] != q) ++swaps;
+                }
+                for (int off = 16; off > 0; off >>= 1) {
+                    const double orr = __shfl_xor_sync(0xffffffffu, dr, off);
+                    const double oii = __shfl_xor_sync(0xffffffffu, di, off);
+                    const int oe = __shfl_xor_sync(0xffffffffu, de, off);
+                    scaled_mul(dr, di, de, orr, oii, oe);
+                    swaps += __shfl_xor_sync(0xffffffffu, swaps, off);
                 }
                 if (swaps & 1) {
                     dr = -dr;
                     di = -di;
                 }
+                det_r = dr;
+                det_i = di;
+                det_e = de;
+            }
+        } else {
+            // sum |v.d| over unoccupied rows and electrons (the estimate's sum(abs, v_dot_d))
+            for (int q = tid - 32; q < Nu * Ne; q += nthr - 32) {
+                const int mm = q / Ne, n = q - mm * Ne;
+                sabs += fabs(At[occ[n] * Np + unocc[mm]]);
+            }
+        }
+        const double sumabs = fabs(w) * iesh_block_sum((double)sabs, red);
+        const double u = std::is_same<R, double>::value
+                             ? rng_uniform(p.seed, gid, (uint32_t)step, RNG_HOP)
+                             : (double)rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP);
+        if (tid == 0) {
+            int full = 0;
+            if (!singular) {
                 // estimate = 2 dt / |det|^2 * sum|v.d| * (|Re det| + |Im det|)
-                const double est = 2.0 * dt * sabs * ldexp((fabs(dr) + fabs(di)) / (dr * dr + di * di), -de);
+                const double est =
+                    2.0 * dt * sumabs * ldexp((fabs(det_r) + fabs(det_i)) / (det_r * det_r + det_i * det_i), -det_e);
                 full = (p.exact_probability || !(est < u)) ? 1 : 0;
             }
             misc[2] = full;
@@ -760,12 +936,16 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                 misc[3] = v[2];
             }
             __syncthreads();
-            v[2] = misc[3];  // hop counts live in thread 0, which writes them out
+            if (warp == 0) v[2] = misc[3];  // hop counts live in thread 0, which writes them out
         }
         if (p.save_stride > 0 && p.obs_partial && step % p.save_stride == 0) save(isave++);
     }
 
-    const double e1 = p.energy ? kinetic() + potential() : 0.0;
+    double e1 = 0.0;
+    if (warp == 0 && p.energy) {
+        const double pe = potential();
+        e1 = kinetic() + pe;
+    }
     // final orbitals: (nstates, nelectrons) column-major per trajectory
     if (p.psi_re)
         for (int q = tid; q < N * Ne; q += nthr) {

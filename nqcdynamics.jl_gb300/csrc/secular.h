@@ -50,6 +50,7 @@ __device__ __forceinline__ void secular_root(const R* __restrict__ eps, const R*
         // which half: sign of f at the midpoint decides the nearer pole
         R mid = a + R(0.5) * (b - a);
         R s = R(0);
+#pragma unroll 4
         for (int k = 0; k < M; ++k) s += V2[k] * secular_rcp<R>(mid - eps[k]);
         R fm = mid - h - s;
         if (fm > R(0)) {  // root in (a, mid): measure from a
@@ -71,6 +72,7 @@ __device__ __forceinline__ void secular_root(const R* __restrict__ eps, const R*
     bool conv = false;
     for (int it = 0; it < 80; ++it) {
         R s1 = R(0), s2 = R(0), sa = R(0);
+#pragma unroll 4
         for (int k = 0; k < M; ++k) {
             R den = (k == jo) ? d : (o - eps[k]) + d;
             R t = secular_rcp<R>(den);
