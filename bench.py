@@ -17,6 +17,12 @@ configuration's shapes (nqcd_gb300/workload.py).
 
 --impl reference times the CPU restatement of the reference integration on
 the host cores (the reference itself is Julia and cannot run here).
+
+--workload tully1|rpsh|mdef|iesh measures the other benchmark configurations
+(C1, C3, C4, C5; nqcd_gb300/configs.py) the same way: the chosen fast path on
+the full ensemble, the plain FP64 path, and the observable error between the
+two on a common subset.  These are records for the design notes; the default
+run is the headline configuration.
 Multi-GPU (torchrun): each rank runs an independent replica shard of
 trajectories (global trajectory ids offset by rank); no collective on the
 data path, only a barrier and a max over ranks of the timings.
@@ -56,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="spinboson", choices=["spinboson", "tully1", "rpsh", "mdef", "iesh"])
+    ap.add_argument("--nsteps", type=int, default=0, help="secondary workloads: nuclear steps of the fast path")
     return ap.parse_args()
 
 
@@ -222,6 +230,8 @@ def main():
 
     if args.impl == "reference":
         return reference_arm(args, dist, B, WL)
+    if args.workload != "spinboson":
+        return secondary(args, dist)
 
     B.build_all()
     from nqcd_gb300 import _lib as L
@@ -332,6 +342,176 @@ def main():
     }
     if dist.rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args, w, c, r0, v0, os.cpu_count() or 1)
+    if dist.rank == 0:
+        print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# secondary configurations (C1, C3, C4, C5)
+# ---------------------------------------------------------------------------
+def _timed(eng, run, warmup, steps, dist):
+    """Device time of `steps` calls of run() after `warmup` calls."""
+    for _ in range(warmup):
+        run()
+    dist.barrier()
+    dev, ker, ts, launches = 0.0, [], 0, 0
+    for _ in range(steps):
+        _, st = run()
+        dev += st.device_ms
+        ker.append(st.kernel_ms)
+        ts += st.traj_steps
+        launches += st.kernel_launches
+    dist.barrier()
+    dev_s = dist.max(dev / 1e3)
+    return dict(value=dist.sum(ts) / dev_s, ms_per_step=dev_s * 1e3 / steps, kernel_ms=float(np.mean(ker)),
+                traj_steps=ts // steps, launches=launches, st=st)
+
+
+def secondary(args, dist):
+    from nqcd_gb300 import build as B
+    from nqcd_gb300 import configs as C
+    from nqcd_gb300 import workload as WL
+
+    B.build_all()
+    from nqcd_gb300 import _lib as L
+
+    fp64_peak, fp32_peak = L.measure_fma_peaks()
+    wk, seed, steps, warm = args.workload, WL.SEED, max(1, args.steps), max(1, args.warmup)
+    rank_off = dist.rank
+    res = {}
+    with ClockSampler(dist.local) as clk:
+        if wk == "tully1":
+            n = args.ntraj if args.ntraj != 100_000 else 10_000
+            r0, v0 = C.tully_inputs(n)
+            sc = {}
+            for name, prec in (("fp64", L.PREC_FP64), ("fp32", L.PREC_FP32)):
+                eng = C.tully_fssh(L, n, prec, traj_offset=rank_off * n)
+                eng.set_initial(r0, v0)
+                sc[name] = np.zeros(4)
+                res[name] = _timed(eng, lambda: eng.run(0.0, 3000.0, 1.0, seed, scattering=sc[name]), warm, steps, dist)
+                eng.close()
+            p = np.maximum(sc["fp64"], 1.0 / n)
+            sig = np.sqrt(p * (1 - p) / n)
+            obs = {"quantity": "state-resolved transmission/reflection probabilities, fast - plain FP64",
+                   "value": float(np.max(np.abs(sc["fp32"] - sc["fp64"]))), "tolerance": float(3 * sig.max()),
+                   "plain": sc["fp64"].tolist(), "fast": sc["fp32"].tolist()}
+            cfg = {"workload": "fssh_tully1_x-10_p10_traj10k_dt1_t3000", "ntraj_per_gpu": n, "nsteps": 3000}
+            ref_flops = WL.ref_flops_per_traj_step(1)
+            kname = "fssh2_tully_kernel<float>"
+        elif wk == "rpsh":
+            n = args.ntraj if args.ntraj != 100_000 else 200_000
+            nsub = min(n, 20_000)
+            r0, v0, nb, models = C.rpsh_inputs(n, traj_offset=rank_off * n)
+            sc = {}
+            for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
+                eng = C.rpsh_tully(L, nt, prec, traj_offset=rank_off * n)
+                eng.set_initial(np.ascontiguousarray(r0[:nt]), np.ascontiguousarray(v0[:nt]),
+                                nbeads=np.ascontiguousarray(nb[:nt]))
+                eng.set_trajectory_models(np.ascontiguousarray(models[:nt]))
+                sc[name] = np.zeros(4)
+                st_steps = 1 if name == "fp32_sub" else steps
+                res[name] = _timed(eng, lambda: eng.run(0.0, 20000.0, 1.0, seed, scattering=sc[name]),
+                                   1 if name != "fp32" else warm, st_steps, dist)
+                fin = eng.get_final(32)
+                res[name]["bead_steps"] = int(np.sum(fin["nsteps"].astype(np.int64) * nb[:nt]))
+                eng.close()
+            p = np.maximum(sc["fp64"], 1.0 / nsub)
+            sig = np.sqrt(p * (1 - p) / nsub)
+            obs = {"quantity": "state-resolved scattering probabilities on the first 20 000 trajectories, fast - plain",
+                   "value": float(np.max(np.abs(sc["fp32_sub"] - sc["fp64"]))), "tolerance": float(3 * sig.max())}
+            f = res["fp32"]
+            f["bead_steps_per_s"] = f["bead_steps"] / (f["ms_per_step"] / 1e3)
+            cfg = {"workload": "rpsh_tully123_beads4-32_beta1024_traj200k_dt1_tmax20000_term10", "ntraj_per_gpu": n,
+                   "traj_steps_per_step": f["traj_steps"], "bead_steps_per_step": f["bead_steps"]}
+            nbar = f["bead_steps"] / max(1, f["traj_steps"])
+            ref_flops = 6600 + 100 * nbar + 8 * nbar * nbar + 6 * nbar
+            kname = "rpsh_persistent_kernel<float>"
+        elif wk == "mdef":
+            n = args.ntraj if args.ntraj != 100_000 else 50_000
+            nsteps = args.nsteps or 2000
+            nsub, nsub_steps, stride = min(n, 4096), 400, 20
+            wl = WL.newns_anderson_mdef(n, M=200, traj_offset=rank_off * n)
+            x0, v0 = wl["x0"].reshape(n, 1).copy(), wl["v0"].reshape(n, 1).copy()
+            t_train = time.perf_counter()
+            teng = C.mdef_newns_anderson(L, wl, 8, L.PREC_FP32)
+            loss = teng.train_friction_mlp(-1.5, 2.5, 200_000, 150, 1024, 3e-3, 11)
+            mlp = teng.mlp_get()
+            teng.close()
+            t_train = time.perf_counter() - t_train
+            obsv = {}
+            for name, prec, nt, ns, sur in (("fp64", L.PREC_FP64, nsub, nsub_steps, False),
+                                            ("fp32_sub", L.PREC_FP32, nsub, nsub_steps, False),
+                                            ("surrogate_sub", L.PREC_FP32, nsub, nsub_steps, True),
+                                            ("fp32", L.PREC_FP32, n, nsteps, False),
+                                            ("surrogate", L.PREC_FP32, n, nsteps, True)):
+                eng = C.mdef_newns_anderson(L, wl, nt, prec, surrogate=sur, judge_every=50 if sur else 0,
+                                            save_stride=stride, traj_offset=rank_off * n)
+                if sur:
+                    eng.mlp_set(*mlp)
+                eng.set_initial(np.ascontiguousarray(x0[:nt]), np.ascontiguousarray(v0[:nt]))
+                ob = np.zeros((ns // stride + 1) * 4)
+                sub = name.endswith("_sub") or name == "fp64"
+                res[name] = _timed(eng, lambda: eng.run(0.0, ns * wl["dt"], wl["dt"], seed, observables=ob),
+                                   1 if sub else warm, 1 if sub else steps, dist)
+                obsv[name] = ob.reshape(-1, 4).copy()
+                eng.close()
+            ke = obsv["fp64"][:, 2]
+            obs = {"quantity": "max_t relative error of <KE>(t) on 4096 trajectories x 400 steps vs plain FP64",
+                   "value": float(np.max(np.abs(obsv["surrogate_sub"][:, 2] - ke) / ke)),
+                   "fp32_exact": float(np.max(np.abs(obsv["fp32_sub"][:, 2] - ke) / ke)), "tolerance": 0.02,
+                   "surrogate_training": {"points": 200_000, "epochs": 150, "final_loss": loss, "seconds": t_train}}
+            st = res["surrogate"]["st"]
+            cfg = {"workload": "mdef_newns_anderson_M200_traj50k_dt0.1fs", "ntraj_per_gpu": n, "nsteps": nsteps,
+                   "surrogate_friction_evals": st.surrogate_friction_evals, "exact_friction_evals": st.exact_friction_evals}
+            ref_flops = 9 * 201**3 + 10 * 201**2
+            kname = "mdef_kernel<float>"
+        else:  # iesh
+            n = args.ntraj if args.ntraj != 100_000 else 20_000
+            nsteps = args.nsteps or 500
+            nsub, stride = 608, 100
+            wl = WL.newns_anderson_iesh(n, traj_offset=rank_off * n)
+            obsv = {}
+            for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
+                eng = C.iesh_newns_anderson(L, wl, nt, prec, save_stride=stride, traj_offset=rank_off * n)
+                eng.set_initial(np.ascontiguousarray(wl["r0"][:nt]), np.ascontiguousarray(wl["v0"][:nt]))
+                ob = np.zeros((nsteps // stride + 1) * 4)
+                sub = name != "fp32"
+                res[name] = _timed(eng, lambda: eng.run(0.0, nsteps * wl["dt"], wl["dt"], seed, observables=ob),
+                                   1 if sub else warm, 1 if sub else steps, dist)
+                obsv[name] = ob.reshape(-1, 4).copy()
+                eng.close()
+            a, b = obsv["fp64"], obsv["fp32_sub"]
+            obs = {"quantity": "max_t relative error of <z>(t), <KE>(t) on 608 trajectories vs plain FP64",
+                   "value": float(max(np.max(np.abs(b[:, 0] - a[:, 0]) / np.abs(a[:, 0])),
+                                      np.max(np.abs(b[:, 1] - a[:, 1]) / np.abs(a[:, 1])))),
+                   "impurity_population_abs_error": float(np.max(np.abs(b[:, 2] - a[:, 2]))), "tolerance": 0.01}
+            st = res["fp32"]["st"]
+            terms = st.propagator_terms / max(1, st.traj_steps)
+            cfg = {"workload": "iesh_newns_anderson_80states_40e_3dof_traj20k_dt0.1fs", "ntraj_per_gpu": n,
+                   "nsteps": nsteps, "chebyshev_terms_per_step": terms,
+                   "full_hop_evaluations_per_step": st.hop_evaluations / max(1, st.traj_steps)}
+            ref_flops = 3.5e7
+            kname = "iesh_kernel<float>"
+    fast = res["fp32"]
+    plain = res["fp64"]
+    line = {
+        "metric": METRIC, "workload": wk, "value": fast["value"], "unit": UNIT, "n_gpus": dist.world, "steps": steps,
+        "warmup": warm, "ms_per_step": fast["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+fp64acc", "data": "synthetic", "chosen_path": "fp32", "config": cfg,
+        "plain_fp64": {"value": plain["value"], "unit": UNIT, "speedup_chosen_vs_plain": fast["value"] / plain["value"]},
+        "observable_error": obs,
+        "reference_equivalent": {"flops_per_traj_step": ref_flops,
+                                 "tflops": ref_flops * fast["value"] / 1e12,
+                                 "note": "FP64 work of the reference's algorithm per trajectory step, at the measured rate"},
+        "kernel": kname, "kernel_ms": fast["kernel_ms"],
+        "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
+        "clocks": clk.summary(), "gpu_launches": fast["launches"],
+    }
+    if "bead_steps_per_s" in fast:
+        line["bead_steps_per_s"] = fast["bead_steps_per_s"]
+    if wk == "mdef":
+        line["surrogate_path"] = {"value": res["surrogate"]["value"],
+                                  "speedup_vs_plain": res["surrogate"]["value"] / plain["value"]}
     if dist.rank == 0:
         print(json.dumps(line))
 

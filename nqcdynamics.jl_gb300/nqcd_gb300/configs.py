@@ -1,0 +1,111 @@
+"""Engines for the benchmark configurations (C1-C5 of the reference's
+headline benchmark), built from the synthetic workloads in workload.py.
+
+C1  FSSH, Tully single avoided crossing, 10 000 trajectories
+C2  FSSH, Ohmic spin-boson (100 modes), 100 000 trajectories   (bench.py default)
+C3  RPSH, Tully 1-3 mixed, bead counts {4, 8, 16, 32}, 200 000 trajectories
+C4  MDEF, Newns-Anderson, 200 band states, 50 000 trajectories
+C5  IESH, Newns-Anderson, 40 electrons in 80 states, 20 000 trajectories
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import workload as WL
+
+TULLY_PARAMS = {1: (0.01, 1.6, 0.005, 1.0), 2: (0.1, 0.28, 0.015, 0.06, 0.05), 3: (6e-4, 0.1, 0.9)}
+
+
+def tully_fssh(L, ntraj, precision, model=1, mass=2000.0, rescaling=0, max_hops=0, traj_offset=0):
+    """C1: FSSH on a Tully model, one degree of freedom, adiabatic state 1."""
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_FSSH, model, precision, rescaling
+    cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 2
+    p = np.asarray(TULLY_PARAMS[model], np.float64)
+    m = np.array([mass])
+    cfg.nparams, cfg.params, cfg.masses = len(p), L.dptr(p), L.dptr(m)
+    cfg.ntraj_max = ntraj
+    cfg.init_kind, cfg.init_state = L.INIT_ADIABATIC_PURE, 0
+    cfg.max_hops = max_hops
+    cfg.gap_fp64 = 1e-3
+    cfg.traj_offset = traj_offset
+    return L.Engine(cfg, [p, m])
+
+
+def tully_inputs(ntraj, x0=-10.0, p0=10.0, mass=2000.0):
+    return np.full((ntraj, 1), x0), np.full((ntraj, 1), p0 / mass)
+
+
+def rpsh_tully(L, ntraj, precision, bmax=32, beta=1024.0, mass=2000.0, terminate_x=10.0, rescaling=0, max_hops=0,
+               traj_offset=0):
+    """C3: ring-polymer surface hopping on Tully models (the handle's model is
+    Tully 1; per-trajectory models come from nqcd_set_trajectory_models)."""
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_RPSH, 1, precision, rescaling
+    cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nbeads_max = 1, 1, 2, bmax
+    p = np.asarray(TULLY_PARAMS[1], np.float64)
+    m = np.array([mass])
+    cfg.nparams, cfg.params, cfg.masses = len(p), L.dptr(p), L.dptr(m)
+    cfg.beta = beta
+    cfg.ntraj_max = ntraj
+    cfg.init_kind, cfg.init_state = L.INIT_ADIABATIC_PURE, 0
+    cfg.max_hops = max_hops
+    cfg.terminate_x = terminate_x
+    cfg.gap_fp64 = 1e-3
+    cfg.traj_offset = traj_offset
+    return L.Engine(cfg, [p, m])
+
+
+def rpsh_inputs(ntraj, bmax=32, mass=2000.0, x0=-9.5, seed=WL.SEED, traj_offset=0):
+    """Models 1-3 round robin, bead counts uniform in {4, 8, 16, 32}, p0
+    uniform in [8, 30], all beads at the centroid x0."""
+    rng = np.random.default_rng([seed, traj_offset, 3])
+    nb = rng.choice(np.array([4, 8, 16, 32], np.int32), ntraj).astype(np.int32)
+    p0 = rng.uniform(8.0, 30.0, ntraj)
+    r0 = np.full((ntraj, bmax), x0)
+    v0 = np.repeat((p0 / mass)[:, None], bmax, axis=1)
+    models = (1 + (np.arange(ntraj) + traj_offset) % 3).astype(np.int32)
+    return r0, v0, nb, models
+
+
+def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0, save_stride=0, traj_offset=0):
+    """C4: MDEF (electronic-friction Langevin) on the Newns-Anderson model."""
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON, precision
+    cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 1 + len(wl["eps"])
+    params = np.array([wl["k"], wl["g"], wl["delta"], wl["mu"], wl["sigma"]])
+    masses = np.array([wl["mass"]])
+    eps = np.ascontiguousarray(wl["eps"])
+    V = np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 5, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta = wl["beta"]
+    cfg.ntraj_max = ntraj
+    cfg.save_stride = save_stride
+    cfg.use_friction_surrogate = int(surrogate)
+    cfg.judge_every = judge_every
+    cfg.traj_offset = traj_offset
+    return L.Engine(cfg, [params, masses, eps, V])
+
+
+def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max_hops=0, exact=0, traj_offset=0):
+    """C5: IESH on the three-dimensional Newns-Anderson adsorbate, Fermi-Dirac
+    initial occupations."""
+    P = wl["params"]
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_IESH, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
+    cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nelectrons = 3, 1, wl["nstates"], wl["nelectrons"]
+    params = np.array([P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"]])
+    masses = np.array([wl["mass"]])
+    eps = np.ascontiguousarray(wl["eps"])
+    V = np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 6, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta = wl["beta"]
+    cfg.ntraj_max = ntraj
+    cfg.init_kind = L.INIT_FERMI_DIRAC
+    cfg.save_stride = save_stride
+    cfg.max_hops = max_hops
+    cfg.exact_hop_probability = exact
+    cfg.traj_offset = traj_offset
+    return L.Engine(cfg, [params, masses, eps, V])
