@@ -1,4 +1,5 @@
-"""GB300 ensemble trajectory engine for NQCDynamics.jl's FSSH / RPSH hot path.
+"""GB300 ensemble trajectory engine for NQCDynamics.jl's hot path (FSSH, RPSH,
+IESH and MDEF ensembles).
 
 The compute runs in libnqcd_gb300.so (CUDA, sm_103a) behind the C ABI of
 include/nqcd_gpu.h; this package is the host-side mirror of the reference's
@@ -6,6 +7,19 @@ ensemble interface (see api.py) plus the ctypes binding (_lib.py).
 """
 from . import _lib
 from .api import (
+    AdiabaticIESH,
+    AdsorbateMetal3D,
+    AndersonHolstein,
+    DiabaticMDEF,
+    DisplacedHarmonic,
+    FermiDiracState,
+    GaussianBroadening,
+    OutputImpurityPopulation,
+    OutputKineticEnergy,
+    OutputPosition,
+    OutputPotentialEnergy,
+    ShenviGaussLegendre,
+    TrapezoidalRule,
     Adiabatic,
     Atoms,
     Diabatic,

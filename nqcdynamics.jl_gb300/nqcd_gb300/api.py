@@ -5,6 +5,11 @@ Names, argument meanings and error behaviour follow the reference:
   Atoms, TullyModelOne/Two/Three, SpinBoson + OhmicSpectralDensity   (NQCModels / NQCBase)
   Simulation[FSSH](atoms, model; rescaling)       src/simulations.jl:12-44, fssh.jl:206-213
   RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)   simulations.jl:46-73, rpsh.jl:5-7
+  Simulation[DiabaticMDEF](atoms, model; friction_method, temperature)   mdef.jl:79-100
+  Simulation[AdiabaticIESH](atoms, model; rescaling, estimate_probability)   iesh.jl:72-87
+  AndersonHolstein(impurity, bath; coupling, fermi_level, nelectrons),
+  TrapezoidalRule, ShenviGaussLegendre, GaussianBroadening      (NQCModels, NQCCalculators)
+  FermiDiracState(fermi_level, temperature; statetype)          (NQCDistributions)
   PureState(state, Adiabatic()/Diabatic()), DynamicalDistribution,
   PositionHarmonicWigner / VelocityHarmonicWigner           (NQCDistributions)
   OutputStateResolvedScattering1D, OutputSurfaceHops, OutputFinal,
@@ -125,6 +130,96 @@ class SpinBoson(Model):
         return (self.ϵ, self.Δ)
 
 
+# --- metal surfaces (AndersonHolstein) ---------------------------------------
+
+
+@dataclass
+class TrapezoidalRule:
+    """M evenly spaced bath levels on [bandmin, bandmax], weights de
+    (docs/src/NQCModels/systembathmodels.md:204-214)."""
+
+    M: int
+    bandmin: float
+    bandmax: float
+
+    def discretise(self):
+        from . import workload as WL
+
+        return WL.trapezoidal_rule(self.M, self.bandmin, self.bandmax)
+
+
+@dataclass
+class ShenviGaussLegendre:
+    """Gauss-Legendre halves below and above the Fermi level
+    (docs/src/NQCModels/systembathmodels.md:241-256)."""
+
+    M: int
+    bandmin: float
+    bandmax: float
+
+    def discretise(self, fermi_level=0.0):
+        from . import workload as WL
+
+        return WL.shenvi_gauss_legendre(self.M, self.bandmin, self.bandmax, fermi_level)
+
+
+@dataclass
+class DisplacedHarmonic:
+    """One-dimensional impurity: U0 = k x^2 / 2, U1 = k (x - g)^2 / 2 + delta
+    (the adsorbate of the MDEF benchmark configuration)."""
+
+    k: float
+    g: float
+    delta: float
+    ndofs = 1
+
+
+@dataclass
+class AdsorbateMetal3D:
+    """One atom in three dimensions above the metal:
+    U0 = kxy (x^2 + y^2)/2 + A exp(-a z), h = U1 - U0 = delta - B exp(-b z)
+    (the adsorbate of the IESH benchmark configuration)."""
+
+    kxy: float
+    A: float
+    a: float
+    delta: float
+    B: float
+    b: float
+    ndofs = 3
+
+
+class AndersonHolstein(Model):
+    """AndersonHolstein(impurity, bath; coupling, fermi_level, nelectrons):
+    impurity state coupled to bath levels e_k with V_k = coupling sqrt(w_k);
+    nstates = M + 1 (NQCModels AndersonHolstein, iesh.md:73)."""
+
+    def __init__(self, impurity, bath, coupling: float = 0.02, fermi_level: float = 0.0, nelectrons: int | None = None):
+        self.impurity = impurity
+        self.bath = bath
+        self.fermi_level = float(fermi_level)
+        eps, w = bath.discretise(self.fermi_level) if isinstance(bath, ShenviGaussLegendre) else bath.discretise()
+        self.eps = np.ascontiguousarray(eps, dtype=np.float64)
+        self.V = np.ascontiguousarray(coupling * np.sqrt(w), dtype=np.float64)
+        self.nstates = len(self.eps) + 1
+        self.nelectrons = self.nstates // 2 if nelectrons is None else int(nelectrons)
+        self.ndofs = impurity.ndofs
+        if isinstance(impurity, DisplacedHarmonic):
+            self.kind = L.MODEL_NEWNS_ANDERSON
+        elif isinstance(impurity, AdsorbateMetal3D):
+            self.kind = L.MODEL_NEWNS_ANDERSON_3D
+        else:
+            raise NotImplementedError("impurity model not on the GPU path")
+
+
+@dataclass
+class GaussianBroadening:
+    """Friction from the Gaussian-broadened golden rule, width sigma
+    (docs/src/NQCModels/frictionmodels.md:91-96)."""
+
+    σ: float
+
+
 # ---------------------------------------------------------------------------
 # Methods and simulations
 # ---------------------------------------------------------------------------
@@ -133,6 +228,22 @@ class SpinBoson(Model):
 @dataclass
 class FSSH:
     rescaling: str = "standard"
+
+    def __post_init__(self):
+        if self.rescaling not in L.RESCALE:
+            raise ValueError(f"rescaling {self.rescaling!r} not recognised (standard, vinversion, off)")
+
+
+class DiabaticMDEF:
+    """Electronic friction Langevin dynamics on a diabatic model (mdef.jl)."""
+
+
+@dataclass
+class AdiabaticIESH:
+    """Independent-electron surface hopping (iesh.jl:72-87)."""
+
+    rescaling: str = "standard"
+    estimate_probability: bool = True
 
     def __post_init__(self):
         if self.rescaling not in L.RESCALE:
@@ -150,13 +261,33 @@ class _MethodIndexed(type):
 class Simulation(metaclass=_MethodIndexed):
     """Simulation[FSSH](atoms, model; rescaling=:standard)."""
 
-    def __init__(self, atoms: Atoms, model: Model, method=FSSH, rescaling: str = "standard", temperature=0.0):
-        if method is not FSSH:
-            raise NotImplementedError(f"method {method} is not on the GPU path")
+    def __init__(self, atoms: Atoms, model: Model, method=FSSH, rescaling: str = "standard", temperature=0.0,
+                 friction_method=None, estimate_probability: bool = True):
         self.atoms = atoms
         self.model = model
-        self.method = FSSH(rescaling)
         self.temperature = float(temperature)
+        if method is DiabaticMDEF:
+            if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON:
+                raise NotImplementedError("DiabaticMDEF runs on AndersonHolstein(DisplacedHarmonic(...), bath)")
+            if not isinstance(friction_method, GaussianBroadening):
+                raise ValueError("DiabaticMDEF needs friction_method=GaussianBroadening(sigma)")
+            if not temperature > 0:
+                raise ValueError("MDEF needs a positive temperature")
+            if len(atoms) != 1:
+                raise ValueError("one adsorbate atom with one degree of freedom")
+            self.method = DiabaticMDEF()
+            self.friction_method = friction_method
+            return
+        if method is AdiabaticIESH:
+            if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON_3D:
+                raise NotImplementedError("AdiabaticIESH runs on AndersonHolstein(AdsorbateMetal3D(...), bath)")
+            if len(atoms) != 1:
+                raise ValueError("one adsorbate atom with three degrees of freedom")
+            self.method = AdiabaticIESH(rescaling, estimate_probability)
+            return
+        if method is not FSSH:
+            raise NotImplementedError(f"method {method} is not on the GPU path")
+        self.method = FSSH(rescaling)
         if isinstance(model, SpinBoson):
             if len(atoms) != model.N:
                 raise ValueError("SpinBoson needs one atom per bath mode")
@@ -270,9 +401,27 @@ class DynamicalDistribution:
 
 
 @dataclass
+class FermiDiracState:
+    """FermiDiracState(fermi_level, temperature; statetype=Adiabatic()):
+    occupations sampled at the temperature (atomic units of energy)."""
+
+    fermi_level: float
+    temperature: float
+    statetype: Any = field(default_factory=Adiabatic)
+
+    def __post_init__(self):
+        if not isinstance(self.statetype, Adiabatic):
+            raise NotImplementedError("the GPU path samples adiabatic occupations")
+
+    @property
+    def β(self):
+        return 1.0 / self.temperature
+
+
+@dataclass
 class ProductDistribution:
     nuclear: DynamicalDistribution
-    electronic: PureState
+    electronic: Any
 
 
 # ---------------------------------------------------------------------------
@@ -312,6 +461,23 @@ class OutputTotalEnergy:
     pass
 
 
+class OutputKineticEnergy:
+    pass
+
+
+class OutputPotentialEnergy:
+    pass
+
+
+class OutputPosition:
+    pass
+
+
+class OutputImpurityPopulation:
+    """IESH: population of the impurity state, row 0 of
+    iesh_diabatic_population (iesh.jl:351-369), at each save point."""
+
+
 class MeanReduction:
     pass
 
@@ -348,6 +514,8 @@ class EnsembleGB300:
     gap_fp64: float = 1e-3
     max_hops: int = 16
     seed: int = 20261203
+    friction_surrogate: Any = None  # MDEF: (weights, meta) of a trained network, or None
+    judge_every: int = 0
 
 
 # ---------------------------------------------------------------------------
@@ -408,6 +576,8 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
         raise TypeError("ensemble_algorithm must be EnsembleGB300")
     if isinstance(sim, RingPolymerSimulation):
         raise NotImplementedError("ring-polymer ensembles run through run_ring_polymer_ensemble")
+    if isinstance(getattr(sim, "method", None), (DiabaticMDEF, AdiabaticIESH)):
+        return _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, dt, saveat, seed, rng)
     if not isinstance(distribution, ProductDistribution):
         raise TypeError("distribution must be DynamicalDistribution * PureState")
     outputs = output if isinstance(output, (tuple, list)) else (output,)
@@ -459,6 +629,113 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
                     result["OutputSurfaceHops"] = final["nhops"]
                 else:
                     raise NotImplementedError(f"output {name} is not available on the GPU path")
+        result["_stats"] = stats
+        return result
+    finally:
+        eng.close()
+
+
+def _metal_config(sim, ntraj, alg, save_stride):
+    model = sim.model
+    mdef = isinstance(sim.method, DiabaticMDEF)
+    cfg = L.nqcd_config()
+    cfg.method = L.METHOD_MDEF if mdef else L.METHOD_IESH
+    cfg.model = model.kind
+    cfg.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[alg.precision]
+    cfg.ndofs, cfg.natoms, cfg.nstates = model.ndofs, 1, model.nstates
+    imp = model.impurity
+    if mdef:
+        params = np.array([imp.k, imp.g, imp.delta, model.fermi_level, sim.friction_method.σ])
+        cfg.beta = 1.0 / sim.temperature
+        cfg.use_friction_surrogate = int(alg.friction_surrogate is not None)
+        cfg.judge_every = alg.judge_every
+    else:
+        params = np.array([imp.kxy, imp.A, imp.a, imp.delta, imp.B, imp.b])
+        cfg.rescaling = L.RESCALE[sim.method.rescaling]
+        cfg.exact_hop_probability = int(not sim.method.estimate_probability)
+        cfg.nelectrons = model.nelectrons
+        cfg.max_hops = alg.max_hops
+    masses = np.ascontiguousarray(sim.atoms.masses, dtype=np.float64)
+    cfg.nparams, cfg.params, cfg.masses = len(params), L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(model.eps), L.dptr(model.eps), L.dptr(model.V)
+    cfg.ntraj_max = ntraj
+    cfg.save_stride = save_stride
+    return cfg, [params, masses, model.eps, model.V]
+
+
+def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, dt, saveat, seed, rng):
+    """run_dynamics for Simulation[DiabaticMDEF] and Simulation[AdiabaticIESH]."""
+    mdef = isinstance(sim.method, DiabaticMDEF)
+    outputs = output if isinstance(output, (tuple, list)) else (output,)
+    reduction = reduction if reduction is not None else MeanReduction()
+    if not isinstance(reduction, MeanReduction):
+        raise NotImplementedError("the GPU path reduces on the device: MeanReduction")
+    if mdef:
+        nuclear = distribution
+        if isinstance(distribution, ProductDistribution):
+            raise TypeError("DiabaticMDEF takes a nuclear DynamicalDistribution")
+    else:
+        if not (isinstance(distribution, ProductDistribution) and isinstance(distribution.electronic, FermiDiracState)):
+            raise TypeError("AdiabaticIESH takes DynamicalDistribution * FermiDiracState")
+        if abs(distribution.electronic.fermi_level - sim.model.fermi_level) > 1e-12:
+            raise ValueError("Fermi level of model and distribution do not match")  # iesh.jl:104-113
+        nuclear = distribution.nuclear
+    t0, t1 = float(tspan[0]), float(tspan[1])
+    timeseries = [o for o in outputs if o in (OutputKineticEnergy, OutputPotentialEnergy, OutputPosition,
+                                              OutputImpurityPopulation)
+                  or isinstance(o, (OutputKineticEnergy, OutputPotentialEnergy, OutputPosition, OutputImpurityPopulation))]
+    save_stride = 0
+    if timeseries:
+        if saveat is None:
+            raise ValueError("time-series outputs need saveat")
+        stride = float(saveat) / dt
+        if abs(stride - round(stride)) > 1e-9 or round(stride) < 1:
+            raise ValueError("saveat must be a positive multiple of dt on the GPU path")
+        save_stride = int(round(stride))
+    ntraj = int(trajectories)
+    rng = rng if rng is not None else np.random.default_rng(alg.seed if seed is None else seed)
+    r0 = nuclear.sample("r", ntraj, rng)
+    v0 = nuclear.sample("v", ntraj, rng)
+    cfg, keep = _metal_config(sim, ntraj, alg, save_stride)
+    if not mdef:
+        cfg.beta = distribution.electronic.β
+        cfg.init_kind = L.INIT_FERMI_DIRAC
+    eng = L.Engine(cfg, keep)
+    try:
+        if mdef and alg.friction_surrogate is not None:
+            eng.mlp_set(*alg.friction_surrogate)
+        eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0))
+        nsteps = int(round((t1 - t0) / dt))
+        obs = np.zeros(((nsteps // save_stride + 1) if save_stride else 1) * 4)
+        out, stats = eng.run(t0, t1, dt, alg.seed if seed is None else seed, observables=obs)
+        ob = obs[: out.nsave * 4].reshape(out.nsave, 4)
+        result: dict[str, Any] = {}
+        if save_stride:
+            result["Time"] = t0 + dt * save_stride * np.arange(out.nsave)
+        final = None
+        for o in outputs:
+            name = _output_name(o)
+            if name == "OutputKineticEnergy":
+                result[name] = ob[:, 2] if mdef else ob[:, 1]
+            elif name == "OutputPosition":
+                result[name] = ob[:, 0]  # MDEF: x; IESH: height z
+            elif name == "OutputPotentialEnergy" and not mdef:
+                result[name] = ob[:, 3]
+            elif name == "OutputImpurityPopulation" and not mdef:
+                result[name] = ob[:, 2]
+            elif name in ("OutputFinal", "OutputTotalEnergy", "OutputSurfaceHops"):
+                if final is None:
+                    final = eng.get_final(1) if mdef else eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
+                if name == "OutputFinal":
+                    result[name] = final
+                elif name == "OutputTotalEnergy":
+                    result[name] = final["energy"].mean(axis=0)
+                elif not mdef:
+                    result[name] = final["nhops"].mean()
+                else:
+                    raise NotImplementedError("DiabaticMDEF has no surface hops")
+            else:
+                raise NotImplementedError(f"output {name} is not available on the GPU path for this method")
         result["_stats"] = stats
         return result
     finally:

@@ -96,6 +96,38 @@ def eigen_continuous(model, r, Zprev):
     return w, Z * sgn[:, None, :]
 
 
+def unoccupied(state, nstates):
+    """Ascending unoccupied states (set_unoccupied_states!, DynamicsUtils.jl:162-171)."""
+    occ = set(int(x) for x in state)
+    return [s for s in range(nstates) if s not in occ]
+
+
+def overlap(psi, state):
+    """S[j, i] = psi[state[j], i] (compute_overlap!, iesh.jl:309-316)."""
+    return psi[np.asarray(state), :]
+
+
+def akj(psi, state, det_s, new_state):
+    """det S conj(det S') (calculate_Akj, iesh.jl:301-306)."""
+    return det_s * np.conj(np.linalg.det(overlap(psi, new_state)))
+
+
+def rescale_velocity(v, d, mass, dE, rescaling):
+    """Momentum rescaling along d for a hop with potential-energy change dE
+    (rescale_velocity!, surface_hopping.jl:64-168): returns (v, accepted)."""
+    aa = np.sum(d * d / mass) / 2
+    bb = np.dot(d, v)
+    disc = bb * bb - 4 * aa * dE
+    if disc < 0:
+        if rescaling == 1:  # :vinversion
+            dn = d / np.linalg.norm(d)
+            v = v - 2 * np.dot(v, dn) * dn
+        return v, False
+    root = np.sqrt(disc)
+    gam = (bb + root) / (2 * aa) if bb < 0 else (bb - root) / (2 * aa)
+    return v - gam * d / mass, True
+
+
 def sample_fermi_dirac(energies, ne, beta, seed, traj_ids):
     """Metropolis occupations: Ne electrons in N states (DynamicsUtils.jl:407-421)."""
     n, N = energies.shape
@@ -220,19 +252,7 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
             accept = True
             if rescaling != 2:
                 d = gh[t] * z0[t, m] * z0[t, old] / (w[t, old] - w[t, m])  # d_alpha[m, old]
-                aa = np.sum(d * d / mass) / 2
-                bb = np.dot(d, v[t])
-                cc = w[t, m] - w[t, old]
-                disc = bb * bb - 4 * aa * cc
-                if disc < 0:
-                    accept = False
-                    if rescaling == 1:
-                        dn = d / np.linalg.norm(d)
-                        v[t] = v[t] - 2 * np.dot(v[t], dn) * dn
-                else:
-                    root = np.sqrt(disc)
-                    gam = (bb + root) / (2 * aa) if bb < 0 else (bb - root) / (2 * aa)
-                    v[t] = v[t] - gam * d / mass
+                v[t], accept = rescale_velocity(v[t], d, mass, w[t, m] - w[t, old], rescaling)
             if accept:
                 state[t, nn] = m
                 hops[t].append((step, int(old), int(m)))

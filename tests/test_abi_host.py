@@ -147,3 +147,48 @@ def test_unknown_rescaling_and_outputs_rejected():
         N.Simulation[N.FSSH](N.Atoms(2000.0), N.TullyModelOne(), rescaling="bogus")
     with pytest.raises(ValueError):
         N.OutputStateResolvedScattering1D(None, "sideways")
+
+
+def _iesh_sim(**kw):
+    m = N.AndersonHolstein(N.AdsorbateMetal3D(1e-3, 0.2, 1.2, 0.08, 0.3, 0.6), N.TrapezoidalRule(79, -0.5, 0.5),
+                           coupling=0.04)
+    return N.Simulation[N.AdiabaticIESH](N.Atoms(1837.0), m, **kw), m
+
+
+def test_metal_models_and_methods_map_to_the_abi():
+    sim, m = _iesh_sim(rescaling="vinversion", estimate_probability=False)
+    assert m.nstates == 80 and m.nelectrons == 40 and m.kind == L.MODEL_NEWNS_ANDERSON_3D
+    eps, w = workload.trapezoidal_rule(79, -0.5, 0.5)
+    np.testing.assert_allclose(m.eps, eps)
+    np.testing.assert_allclose(m.V, 0.04 * np.sqrt(w))
+    cfg, _ = api._metal_config(sim, 16, N.EnsembleGB300("fp32"), 0)
+    assert cfg.method == L.METHOD_IESH and cfg.nelectrons == 40 and cfg.rescaling == 1
+    assert cfg.exact_hop_probability == 1 and cfg.nbath == 79 and cfg.nstates == 80
+    md = N.AndersonHolstein(N.DisplacedHarmonic(0.0294, 1.0, -0.0147), N.ShenviGaussLegendre(200, -0.5, 0.5))
+    sim2 = N.Simulation[N.DiabaticMDEF](N.Atoms(1837.0), md, friction_method=N.GaussianBroadening(0.01),
+                                        temperature=1 / 1052.6)
+    cfg2, _ = api._metal_config(sim2, 16, N.EnsembleGB300("fp64"), 10)
+    assert cfg2.method == L.METHOD_MDEF and cfg2.nstates == 201 and cfg2.params[4] == 0.01
+    assert cfg2.beta == pytest.approx(1052.6) and cfg2.save_stride == 10
+
+
+def test_metal_simulation_arguments_are_checked():
+    md = N.AndersonHolstein(N.DisplacedHarmonic(0.03, 1.0, -0.015), N.ShenviGaussLegendre(40, -0.5, 0.5))
+    with pytest.raises(ValueError):  # friction method required
+        N.Simulation[N.DiabaticMDEF](N.Atoms(1837.0), md, temperature=0.001)
+    with pytest.raises(NotImplementedError):  # IESH needs the three-dimensional adsorbate
+        N.Simulation[N.AdiabaticIESH](N.Atoms(1837.0), md)
+    with pytest.raises(ValueError):
+        _iesh_sim(rescaling="bogus")
+    sim, m = _iesh_sim()
+    nuc = N.DynamicalDistribution(np.zeros(3), np.array([0.0, 0.0, 12.0]), (3, 1))
+    # iesh.jl:104-113: the distribution's Fermi level must be the model's
+    with pytest.raises(ValueError):
+        N.run_dynamics(sim, (0.0, 10.0), nuc * N.FermiDiracState(0.1, 1e-3), output=N.OutputFinal, trajectories=2,
+                       ensemble_algorithm=N.EnsembleGB300("fp32"))
+    with pytest.raises(TypeError):
+        N.run_dynamics(sim, (0.0, 10.0), nuc, output=N.OutputFinal, trajectories=2,
+                       ensemble_algorithm=N.EnsembleGB300("fp32"))
+    with pytest.raises(ValueError):  # time series need saveat
+        N.run_dynamics(sim, (0.0, 10.0), nuc * N.FermiDiracState(0.0, 1e-3), output=N.OutputKineticEnergy,
+                       trajectories=2, ensemble_algorithm=N.EnsembleGB300("fp32"))

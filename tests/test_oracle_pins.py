@@ -248,3 +248,111 @@ def test_mdef_oracle_friction_and_force_consistency():
     assert np.all(out["friction"] >= -1e-15)
     z = MO.normal(7, np.arange(20000), 3)
     assert abs(z.mean()) < 0.03 and abs(z.std() - 1) < 0.03
+
+
+# ---------------------------------------------------------------------------
+# IESH oracle pins: the known answers of the reference's test/Dynamics/iesh.jl
+# ---------------------------------------------------------------------------
+def _iesh():
+    import iesh_oracle as IO
+    return IO
+
+
+def test_iesh_unoccupied_known_answers():
+    # iesh.jl:71-78 (1-based there): occupied 1:15 -> 16:31, occupied 6:20 -> 1:5, 21:31
+    IO = _iesh()
+    assert IO.unoccupied(list(range(15)), 31) == list(range(15, 31))
+    assert IO.unoccupied(list(range(5, 20)), 31) == list(range(5)) + list(range(20, 31))
+
+
+def test_iesh_overlap_and_akj_known_answers():
+    # iesh.jl:87-110: overlap of the initial orbitals is the identity; with every
+    # electron in state 1 only the first column is ones; A_kj(state, state) = 1
+    IO = _iesh()
+    n, ne = 31, 15
+    psi = np.zeros((n, ne))
+    psi[np.arange(ne), np.arange(ne)] = 1.0
+    np.testing.assert_array_equal(IO.overlap(psi, list(range(ne))), np.eye(ne))
+    S = IO.overlap(psi, [0] * ne)
+    assert np.all(S[:, 0] == 1) and np.all(S[:, 1:] == 0)
+    assert IO.akj(psi, list(range(ne)), 1.0, list(range(ne))) == pytest.approx(1.0)
+
+
+def _narrow_band_model(IO, M=30):
+    # the band of iesh.jl:17-25: Gamma = 6.4e-3, W = 3 Gamma, TrapezoidalRule(M, -W, W)
+    G = 6.4e-3
+    W = 3 * G
+    eps = np.linspace(-W, W, M)
+    V = np.full(M, np.sqrt(G / (2 * np.pi)) * np.sqrt(2 * W / (M - 1)))
+    return IO.Metal3D(kxy=0.0, A=0.0, a=1.0, delta=0.0, B=0.0, b=1.0, eps=eps, V=V)
+
+
+def test_iesh_fermi_dirac_zero_temperature_fills_lowest_states():
+    # iesh.jl:39-44: at 0 K the sampled occupations are the lowest nelectrons states
+    IO = _iesh()
+    model = _narrow_band_model(IO)
+    n = 16
+    r = np.zeros((n, 3))
+    w, _ = IO.eigen_continuous(model, r, np.tile(np.eye(31), (n, 1, 1)))
+    st = IO.sample_fermi_dirac(w, 15, 1e12, 3, np.arange(n, dtype=np.uint64))
+    np.testing.assert_array_equal(st, np.tile(np.arange(15), (n, 1)))
+
+
+def test_iesh_fermi_dirac_statistics():
+    # iesh.jl:51-69: sample averages of the occupations match the Fermi function
+    # (isapprox on vectors: norm of the difference within 0.2 of the norm)
+    IO = _iesh()
+    model = _narrow_band_model(IO)
+    n, ne, beta = 2000, 15, 1 / 9.5e-4
+    r = np.zeros((n, 3))
+    w, _ = IO.eigen_continuous(model, r, np.tile(np.eye(31), (n, 1, 1)))
+    st = IO.sample_fermi_dirac(w, ne, beta, 7, np.arange(n, dtype=np.uint64))
+    avg = np.zeros(31)
+    for row in st:
+        avg[row] += 1
+    avg /= n
+    lam = w[0]
+    lo, hi = lam[0], lam[-1]
+    for _ in range(200):  # Fermi level with sum f = ne (bisection)
+        mu = 0.5 * (lo + hi)
+        if np.sum(1 / (1 + np.exp(beta * (lam - mu)))) > ne:
+            hi = mu
+        else:
+            lo = mu
+    occ = 1 / (1 + np.exp(beta * (lam - mu)))
+    assert np.linalg.norm(avg - occ) <= 0.2 * np.linalg.norm(occ)
+
+
+def test_iesh_hop_rescaling_conserves_energy():
+    # iesh.jl:122-152: after a successful hop dKE = -dE (rtol 1e-3)
+    IO = _iesh()
+    rng = np.random.default_rng(4)
+    mass = np.array([2000.0, 2000.0, 2000.0])
+    for _ in range(20):
+        v = rng.normal(0, 0.01, 3)
+        d = rng.normal(0, 1.0, 3)
+        dE = rng.uniform(-0.01, 0.01)
+        v2, ok = IO.rescale_velocity(v, d, mass, dE, 0)
+        ke = lambda u: 0.5 * np.sum(mass * u * u)
+        if ok:
+            assert ke(v2) - ke(v) == pytest.approx(-dE, rel=1e-3, abs=1e-12)
+        else:  # frustrated: velocity unchanged (:standard)
+            np.testing.assert_array_equal(v2, v)
+
+
+def test_iesh_dynamics_conserves_energy():
+    # Verlet + exact propagator + rescaled hops: total energy (KE + U0 + occupied
+    # eigenvalues) drifts only by the step error and the cached force after hops
+    IO = _iesh()
+    from nqcd_gb300 import workload as WL
+
+    wl = WL.newns_anderson_iesh(4, nstates=20, nelectrons=10, z0=3.0)
+    P = wl["params"]
+    model = IO.Metal3D(kxy=P["kxy"], A=P["A"], a=P["a"], delta=P["delta"], B=P["B"], b=P["b"], eps=wl["eps"],
+                       V=wl["V"])
+    res = IO.run_iesh(model, mass=wl["mass"], ne=10, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"], dt=wl["dt"],
+                      nsteps=300, seed=3)
+    assert np.all(np.abs(res["energy"][:, 1] - res["energy"][:, 0]) < 5e-4)
+    for t in range(4):  # orbitals stay orthonormal
+        g = res["psi"][t].conj().T @ res["psi"][t]
+        assert np.abs(g - np.eye(10)).max() < 1e-10
