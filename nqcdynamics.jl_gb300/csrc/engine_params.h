@@ -25,6 +25,12 @@ struct FsshParams {
     int64_t ntraj;
     int64_t traj_offset;
     double t0, t1, dt;
+    // step schedule of [t0, t1] (the reference integrator's: steps of dt, a
+    // shorter last step, times snapped to t1), precomputed on the host for the
+    // fast kernels, which keep no FP64 clock
+    int32_t nsteps_total;
+    float h_first, h_mid, h_last;  // step lengths: first, interior, last
+    float sa1, sb1;                // first step's interpolation weights (the buffer starts at t = 0)
     uint64_t seed;
     int32_t save_stride;
     int32_t nsave;
@@ -55,7 +61,11 @@ cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s);
 inline int fssh2_lanes_per_traj(int model, int precision) {
     return (model == 10 /* MODEL_SPINBOSON */ && precision != 0 /* FP64 */) ? 4 : 1;
 }
-cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* out,
+// out[k] = sum over rows p of partial[p][k], deterministic: rows are summed in
+// fixed chunks in parallel (tmp: [reduce_chunks(nparts, width)][width]) and the
+// chunk sums in ascending order.
+int64_t reduce_chunks(int64_t nparts, int64_t width);
+cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* tmp, double* out,
                                    cudaStream_t s);
 
 }  // namespace nqcd

@@ -124,6 +124,56 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>&
     }
 }
 
+// Fast-path electronic step on the host-computed schedule: interpolation
+// weights (sa, sb) = (sa1, sb1) on the first step (the buffer starts at
+// t = 0) and (0, 1) afterwards, which is what the FP64 clock gives; below the
+// gap threshold the FP64 sub-integrator runs on the same relative times.
+__device__ __forceinline__ void electronics2_sched(const FsshParams& p, const EBuf<float>& buf, bool first, float h,
+                                                   float gap, Sig2<float>& sg) {
+    const float dtsub = (float)(p.dt / 5.0);
+    if (gap < p.gap_fp64) {
+        const double hd = h;
+        const double tn = first ? p.t0 + hd : hd, t = first ? p.t0 : 0.0;
+        EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, 0.0, buf.E0n, buf.E1n, buf.Dn, tn};
+        Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
+        Interp64 fn(b64);
+        electronic_macro_step2<double>(fn, t, hd, p.dt / 5.0, s64);
+        sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
+    } else {
+        InterpS32 fn(buf, first ? p.sa1 : 0.f, first ? p.sb1 : 1.f);
+        electronic_macro_step2_fast(fn, h, dtsub, sg);
+    }
+}
+
+// FP32 form of diabatic_pop2 and of the warp sum of the population products
+// (fast paths): no FP64 arithmetic in the step loop.
+__device__ __forceinline__ void diabatic_pop2_f(const Sig2<float>& sg, int s, const float Z[4], float pop[2]) {
+    const float sp00 = s == 0 ? 1.f : 0.f, sp11 = s == 1 ? 1.f : 0.f, sp01 = sg.x;
+    const float M00 = Z[0] * sp00 + Z[2] * sp01, M01 = Z[0] * sp01 + Z[2] * sp11;
+    const float M10 = Z[1] * sp00 + Z[3] * sp01, M11 = Z[1] * sp01 + Z[3] * sp11;
+    pop[0] = M00 * Z[0] + M01 * Z[2];
+    pop[1] = M10 * Z[1] + M11 * Z[3];
+}
+
+__device__ __forceinline__ void warp_save_popcorr_f(const FsshParams& p, int isave, bool active, const float pop0[2],
+                                                    const float pop[2]) {
+    float c[4];
+    c[0] = active ? pop0[0] * pop[0] : 0.f;
+    c[1] = active ? pop0[0] * pop[1] : 0.f;
+    c[2] = active ? pop0[1] * pop[0] : 0.f;
+    c[3] = active ? pop0[1] * pop[1] : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) c[q] += __shfl_xor_sync(0xffffffffu, c[q], off);
+    if ((threadIdx.x & 31) == 0 && isave < p.nsave) {
+        int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        double* dst = p.popcorr_partial + (warp * p.nsave + isave) * 4;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst[q] = (double)c[q];
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ void write_sigma(const FsshParams& p, int64_t i, const Sig2<R>& sg) {
     const int64_t N = p.ntraj;
@@ -197,8 +247,13 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
     EBuf<R> buf = {R(0), R(0), R(0), 0.0, R(0), R(0), R(0), 0.0};
     int nh = 0, nf = 0, step = 0;
     double t = p.t0;
-    while (t < p.t1) {
-        double h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
+    // plain path: the reference's FP64 clock; fast path: the host schedule
+    while (IsFast<R>::value ? step < p.nsteps_total : t < p.t1) {
+        double h;
+        if constexpr (IsFast<R>::value)
+            h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
+        else
+            h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
         double half = h / 2.0;
         double vtmp = v + half * k;
         x = x + h * vtmp;
@@ -208,13 +263,17 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         buf.E0c = buf.E0n;
         buf.E1c = buf.E1n;
         buf.Dc = buf.Dn;
-        buf.tc = buf.tn;
         buf.E0n = w[0];
         buf.E1n = w[1];
         buf.Dn = R(0) + nac * (R)v;
-        buf.tn = t + h;
-        electronics2<R>(p, buf, t, h, w[1] - w[0], sg);
-        t = snap_time(t + h, p.t1);
+        if constexpr (IsFast<R>::value) {
+            electronics2_sched(p, buf, step == 0, (float)h, w[1] - w[0], sg);
+        } else {
+            buf.tc = buf.tn;
+            buf.tn = t + h;
+            electronics2<R>(p, buf, t, h, w[1] - w[0], sg);
+            t = snap_time(t + h, p.t1);
+        }
         step += 1;
 
         // hop test
@@ -255,9 +314,15 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
             }
         }
         if (p.save_stride > 0 && step % p.save_stride == 0) {
-            double pop[2];
-            diabatic_pop2<R>(sg, state, Z, pop);
-            warp_save_popcorr(p, isave++, active, pop0, pop);
+            if constexpr (IsFast<R>::value) {
+                float pf[2], p0f[2] = {(float)pop0[0], (float)pop0[1]};
+                diabatic_pop2_f(sg, state, Z, pf);
+                warp_save_popcorr_f(p, isave++, active, p0f, pf);
+            } else {
+                double pop[2];
+                diabatic_pop2<R>(sg, state, Z, pop);
+                warp_save_popcorr(p, isave++, active, pop0, pop);
+            }
         }
     }
 

@@ -125,21 +125,22 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
     double e0 = 0.5 * (double)ke + (double)w[state];
     float Mk = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];  // M_ss of the cached force
 
-    double pop0[2] = {0.0, 0.0};
+    float pop0[2] = {0.f, 0.f};
     int isave = 0;
     const bool lead = lane_g == 0;
     if (p.save_stride > 0) {
-        diabatic_pop2<float>(sg, state, Z, pop0);
-        warp_save_popcorr(p, isave++, active && lead, pop0, pop0);
+        diabatic_pop2_f(sg, state, Z, pop0);
+        warp_save_popcorr_f(p, isave++, active && lead, pop0, pop0);
     }
 
     EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
     int nh = 0, nf = 0, step = 0;
-    double t = p.t0;
     float cv = 0.f;
-    while (t < p.t1) {
-        const double hd = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
-        const float h = (float)hd, half = 0.5f * h;
+    const float dtf = (float)p.dt;
+    // the host's step schedule replaces the reference's FP64 clock (no FP64 in the loop)
+    while (step < p.nsteps_total) {
+        const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
+        const float half = 0.5f * h;
         // B (cached force) and A
         s0 = 0.f;
         cr = 0.f;
@@ -178,20 +179,17 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
         buf.E0c = buf.E0n;
         buf.E1c = buf.E1n;
         buf.Dc = buf.Dn;
-        buf.tc = buf.tn;
         buf.E0n = w[0] - vmean;
         buf.E1n = w[1] - vmean;
         buf.Dn = cv * dscale;
-        buf.tn = t + hd;
-        electronics2<float>(p, buf, t, hd, gap, sg);
-        t = snap_time(t + hd, p.t1);
+        electronics2_sched(p, buf, step == 0, h, gap, sg);
         step += 1;
 
         // hop test (identical in all G lanes of the group)
         const int s = state;
         float re = sg.x / (s == 0 ? sg.p : sg.q);
         float nsm = (s == 0 ? 1.0f : -1.0f) * cv * dscale;
-        float prob = clamp01<float>(2.0f * re * nsm * (float)p.dt);
+        float prob = clamp01<float>(2.0f * re * nsm * dtf);
         float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
         if (prob > u) {
             const int ns = 1 - s;
@@ -232,9 +230,9 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
             }
         }
         if (p.save_stride > 0 && step % p.save_stride == 0) {
-            double pop[2];
-            diabatic_pop2<float>(sg, state, Z, pop);
-            warp_save_popcorr(p, isave++, active && lead, pop0, pop);
+            float pop[2];
+            diabatic_pop2_f(sg, state, Z, pop);
+            warp_save_popcorr_f(p, isave++, active && lead, pop0, pop);
         }
     }
 

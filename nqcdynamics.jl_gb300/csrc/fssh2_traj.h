@@ -176,6 +176,8 @@ struct InterpS32 {
         sa = den != 0.0 ? (float)((t - b.tc) / den) : 0.f;
         sb = den != 0.0 ? (float)(h / den) : 0.f;
     }
+    NQCD_HD InterpS32(const EBuf<float>& b, float sa_, float sb_) : E0c(b.E0c), E1c(b.E1c), Dc(b.Dc),
+        dE0(b.E0n - b.E0c), dE1(b.E1n - b.E1c), dD(b.Dn - b.Dc), sa(sa_), sb(sb_) {}
     NQCD_HD Sig2<float> f(float sigma, const Sig2<float>& u) const {
         float s = sa + sb * sigma;
         float D = Dc + dD * s;

@@ -76,6 +76,18 @@ __global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
         p[i] = v;
 }
 
+// tmp[c][k] = sum of partial[p][k] over the rows p of chunk c, ascending p.
+__global__ void reduce_chunks_kernel(const double* __restrict__ partial, int64_t nparts, int64_t width,
+                                     int64_t rows_per_chunk, double* __restrict__ tmp) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= width) return;
+    const int64_t p0 = (int64_t)blockIdx.y * rows_per_chunk;
+    const int64_t p1 = p0 + rows_per_chunk < nparts ? p0 + rows_per_chunk : nparts;
+    double acc = 0.0;
+    for (int64_t q = p0; q < p1; ++q) acc += partial[q * width + k];
+    tmp[(int64_t)blockIdx.y * width + k] = acc;
+}
+
 // out[k] = sum_p partial[p][k] in ascending p (deterministic).
 __global__ void reduce_partials_kernel(const double* __restrict__ partial, int64_t nparts, int64_t width,
                                        double* __restrict__ out) {
@@ -166,6 +178,8 @@ struct nqcd_handle {
     double* d_energy = nullptr;
     double* d_partial = nullptr;
     int64_t partial_cap = 0;
+    double* d_redtmp = nullptr;  // chunk sums of the partial reduction
+    int64_t redtmp_cap = 0;
     double* d_popcorr = nullptr;
     unsigned long long* d_counts = nullptr;  // [0..3] scatter, [4..7] stats
     double* d_stage = nullptr;               // staging for layout gathers
@@ -228,7 +242,7 @@ void free_all(nqcd_handle* h) {
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
                     h->d_rpU, h->d_rpcay, h->d_rpUf, h->d_rpcayf, h->d_nbeads, h->d_class_traj,
                     h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2,
-                    h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im};
+                    h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im, h->d_redtmp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mlp_free(h->mlp);
@@ -722,6 +736,26 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.t0 = t0;
     p.t1 = t1;
     p.dt = dt;
+    {
+        // the reference integrator's step schedule, for the fast kernels (the
+        // plain kernels run the same FP64 clock themselves)
+        double tt = t0, hf = 0.0, hl = 0.0;
+        int64_t n = 0;
+        while (tt < t1 && n < nsteps + 1) {
+            const double hh = (t1 - tt) < dt ? (t1 - tt) : dt;
+            if (n == 0) hf = hh;
+            hl = hh;
+            tt = snap_time(tt + hh, t1);
+            ++n;
+        }
+        p.nsteps_total = (int32_t)n;
+        p.h_first = (float)hf;
+        p.h_mid = (float)dt;
+        p.h_last = (float)hl;
+        const double den = t0 + hf;  // the interpolation buffer starts at t = 0
+        p.sa1 = den != 0.0 ? (float)(t0 / den) : 0.f;
+        p.sb1 = den != 0.0 ? (float)(hf / den) : 0.f;
+    }
     p.seed = seed;
     p.save_stride = stride;
     p.nsave = nsave;
@@ -906,7 +940,17 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     NQCD_CUDA(h, cudaEventRecord(h->evk1, s));
     ++launches;
     if (nsave > 0) {
-        NQCD_CUDA(h, launch_reduce_partials(h->d_partial, nwarps, (int64_t)nsave * 4, h->d_popcorr, s));
+        const int64_t need = reduce_chunks(nwarps, (int64_t)nsave * 4) * nsave * 4;
+        if (need > h->redtmp_cap) {
+            NQCD_CUDA(h, cudaStreamSynchronize(s));
+            if (h->d_redtmp) cudaFree(h->d_redtmp);
+            h->d_redtmp = nullptr;
+            h->redtmp_cap = 0;
+            NQCD_CUDA(h, dalloc(&h->d_redtmp, need));
+            h->redtmp_cap = need;
+        }
+        NQCD_CUDA(h, launch_reduce_partials(h->d_partial, nwarps, (int64_t)nsave * 4, h->d_redtmp, h->d_popcorr, s));
+        ++launches;
         ++launches;
     }
     stats_kernel<<<(unsigned)((N + 255) / 256 < 1024 ? (N + 255) / 256 : 1024), 256, 0, s>>>(
@@ -1255,8 +1299,23 @@ int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
 }  // extern "C"
 
 namespace nqcd {
-cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* out, cudaStream_t s) {
-    reduce_partials_kernel<<<(unsigned)((width + 127) / 128), 128, 0, s>>>(partial, nparts, width, out);
+int64_t reduce_chunks(int64_t nparts, int64_t width) {
+    const int64_t colblocks = (width + 127) / 128;
+    int64_t chunks = 2048 / (colblocks > 0 ? colblocks : 1);  // about 2048 blocks in the first pass
+    if (chunks < 1) chunks = 1;
+    if (chunks > 65535) chunks = 65535;
+    return chunks < nparts ? chunks : (nparts > 0 ? nparts : 1);
+}
+
+cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* tmp, double* out,
+                                   cudaStream_t s) {
+    const int64_t chunks = reduce_chunks(nparts, width);
+    const int64_t rows = (nparts + chunks - 1) / chunks;
+    dim3 grid((unsigned)((width + 127) / 128), (unsigned)chunks);
+    reduce_chunks_kernel<<<grid, 128, 0, s>>>(partial, nparts, width, rows, tmp);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    reduce_partials_kernel<<<(unsigned)((width + 127) / 128), 128, 0, s>>>(tmp, chunks, width, out);
     return cudaGetLastError();
 }
 }  // namespace nqcd
