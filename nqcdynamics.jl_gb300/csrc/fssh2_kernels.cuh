@@ -128,8 +128,9 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>&
 // weights (sa, sb) = (sa1, sb1) on the first step (the buffer starts at
 // t = 0) and (0, 1) afterwards, which is what the FP64 clock gives; below the
 // gap threshold the FP64 sub-integrator runs on the same relative times.
-__device__ __forceinline__ void electronics2_sched(const FsshParams& p, const EBuf<float>& buf, bool first, float h,
-                                                   float gap, Sig2<float>& sg) {
+template <typename P>  // FsshParams or RpshParams
+__device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>& buf, bool first, float h, float gap,
+                                                   Sig2<float>& sg) {
     const float dtsub = (float)(p.dt / 5.0);
     if (gap < p.gap_fp64) {
         const double hd = h;

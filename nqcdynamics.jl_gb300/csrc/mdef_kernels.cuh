@@ -134,9 +134,9 @@ __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib,
             sh.z2[wib][i] = z2;
         }
     }
-    double sF = (double)accF;
-    for (int off = 16; off > 0; off >>= 1) sF += __shfl_xor_sync(0xffffffffu, sF, off);
-    force = p.k * x + (double)dh * sF;
+    // warp sum in the working precision (no FP64 shuffle-adds on the fast path)
+    for (int off = 16; off > 0; off >>= 1) accF += __shfl_xor_sync(0xffffffffu, accF, off);
+    force = p.k * x + (double)dh * (double)accF;
     friction = 0.0;
     if (!want_friction) return;
     __syncwarp();
@@ -161,9 +161,8 @@ __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib,
         }
         acc += zn * inner * df;
     }
-    double sacc = (double)acc;
-    for (int off = 16; off > 0; off >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, off);
-    friction = -3.14159265358979323846 * (double)dh * (double)dh * (double)norm * sacc;
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    friction = -3.14159265358979323846 * (double)dh * (double)dh * (double)norm * (double)acc;
     __syncwarp();
 }
 
@@ -201,6 +200,15 @@ __device__ __forceinline__ double noise_normal(uint64_t seed, uint64_t traj, uin
     return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
 }
 
+// Fast path: the same Box-Muller transform of the same Philox block with
+// 24-bit uniforms in FP32.
+__device__ __forceinline__ float noise_normal_f(uint64_t seed, uint64_t traj, uint32_t step) {
+    u32x4 b = rng_block(seed, traj, step, RNG_NOISE);
+    const float u1 = 1.f - (float)(b.x >> 8) * 0x1.0p-24f;
+    const float u2 = (float)(b.z >> 8) * 0x1.0p-24f;
+    return sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams p) {
     __shared__ MdefShared<R> sh;
@@ -223,6 +231,7 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
     }
     double x = p.x[i], v = p.v[i];
     const double m = p.mass, T = 1.0 / p.beta, dt = p.dt, half = 0.5;
+    const float inv_m_f = (float)(1.0 / m), dt_f = (float)dt, sig_f = (float)sqrt(T / m);
     double F, fr;
     mdef_electronic<R>(p, sh, wib, lam, x, p.friction_out != nullptr, F, fr);
     if (p.force_out || p.friction_out) {  // single-evaluation mode (force/friction tables, training data)
@@ -278,12 +287,22 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
             mdef_electronic<R>(p, sh, wib, lam, x, true, Fm, lamv);
             ++n_exact;
         }
-        double gam = lamv / m;  // friction / (sqrt m sqrt m)
-        if (gam < 0.0) gam = 0.0;
-        double c1 = exp(-gam * dt);
-        double c2 = sqrt(1.0 - c1 * c1);
-        double xi = noise_normal(p.seed, gid, (uint32_t)step);
-        v = c1 * v + c2 * (sqrt(T / m) * xi);  // O
+        if constexpr (std::is_same<R, float>::value) {
+            // O step in FP32: c2 = sqrt(1 - c1^2) as sqrt(-expm1(-2 gamma dt)), accurate for small gamma dt
+            float gdt = (float)lamv * inv_m_f * dt_f;
+            if (gdt < 0.f) gdt = 0.f;
+            const float c1 = expf(-gdt);
+            const float c2 = sqrtf(-expm1f(-2.f * gdt));
+            const float xi = noise_normal_f(p.seed, gid, (uint32_t)step);
+            v = (double)c1 * v + (double)(c2 * sig_f * xi);
+        } else {
+            double gam = lamv / m;  // friction / (sqrt m sqrt m)
+            if (gam < 0.0) gam = 0.0;
+            double c1 = exp(-gam * dt);
+            double c2 = sqrt(1.0 - c1 * c1);
+            double xi = noise_normal(p.seed, gid, (uint32_t)step);
+            v = c1 * v + c2 * (sqrt(T / m) * xi);  // O
+        }
         x = x + (half * dt) * v;                // A
         double Fn, dummy;
         mdef_electronic<R>(p, sh, wib, lam, x, false, Fn, dummy);

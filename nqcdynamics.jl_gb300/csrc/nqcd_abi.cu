@@ -839,6 +839,12 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         rq.t0 = t0;
         rq.t1 = t1;
         rq.dt = dt;
+        rq.nsteps_total = p.nsteps_total;
+        rq.h_first = p.h_first;
+        rq.h_mid = p.h_mid;
+        rq.h_last = p.h_last;
+        rq.sa1 = p.sa1;
+        rq.sb1 = p.sb1;
         rq.seed = seed;
         rq.terminate_x = h->cfg.terminate_x;
         rq.max_hops = h->cfg.max_hops;

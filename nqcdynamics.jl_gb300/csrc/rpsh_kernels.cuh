@@ -28,6 +28,7 @@
 
 #include <cuda_runtime.h>
 
+#include "fssh2_kernels.cuh"
 #include "fssh2_traj.h"
 
 namespace nqcd {
@@ -47,6 +48,10 @@ struct RpshParams {
     int64_t ntraj;
     int64_t traj_offset;
     double t0, t1, dt;
+    // step schedule for the fast path (see FsshParams)
+    int32_t nsteps_total;
+    float h_first, h_mid, h_last;
+    float sa1, sb1;
     uint64_t seed;
     double terminate_x;
     int32_t max_hops;
@@ -400,10 +405,12 @@ __device__ __noinline__ void rpsh_traj_fast(const RpshParams& p, int cls, int64_
 
     EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
     int nh = 0, nf = 0, step = 0;
-    double t = p.t0;
-    while (t < p.t1) {
-        double hd = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
-        float h = (float)hd, half = 0.5f * h;
+    const float dtf = (float)p.dt;
+    // the host's step schedule replaces the reference's FP64 clock
+    while (step < p.nsteps_total) {
+        const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
+        const double hd = h;
+        const float half = 0.5f * h;
         // B kick: centroid part in FP64, deviations in FP32
         float kbar = 0.f;
 #pragma unroll
@@ -456,28 +463,16 @@ __device__ __noinline__ void rpsh_traj_fast(const RpshParams& p, int cls, int64_
         buf.E0c = buf.E0n;
         buf.E1c = buf.E1n;
         buf.Dc = buf.Dn;
-        buf.tc = buf.tn;
         buf.E0n = w[0];
         buf.E1n = w[1];
         buf.Dn = nac * (float)vc;
-        buf.tn = t + hd;
-        if (gap < p.gap_fp64) {
-            EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, buf.tc, buf.E0n, buf.E1n, buf.Dn, buf.tn};
-            Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
-            Interp64 fn(b64);
-            electronic_macro_step2<double>(fn, t, hd, p.dt / 5.0, s64);
-            sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
-        } else {
-            InterpS32 fn(buf, t, hd);
-            electronic_macro_step2_fast(fn, h, (float)(p.dt / 5.0), sg);
-        }
-        t = snap_time(t + hd, p.t1);
+        electronics2_sched(p, buf, step == 0, h, gap, sg);
         step += 1;
 
         const int s = state;
         float re = sg.x / (s == 0 ? sg.p : sg.q);
         float nsm = s == 0 ? nac : -nac;
-        float prob = clamp01<float>(2.0f * (float)vc * re * nsm * (float)p.dt);
+        float prob = clamp01<float>(2.0f * (float)vc * re * nsm * dtf);
         float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
         if (prob > u) {
             const int ns = 1 - s;
