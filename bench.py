@@ -313,7 +313,10 @@ def main():
              "fp32_kahan": "fssh2_sb_fast_kernel<AccKahan,25>"}[chosen]
     roofline = {"bound": "fp32-core" if chosen != "fp64" else "fp64-core", "achieved": achieved,
                 "peak": fp32_peak if chosen != "fp64" else fp64_peak, "unit": "TFLOP/s",
-                "traffic": None,
+                # DRAM bytes per launch from the ncu capture in profiles/ (20 000 trajectories,
+                # scaled by the number of trajectories; the kernel keeps its state on chip)
+                "traffic": 2.0e8 * ntraj / 100_000 if chosen == "fp32_kahan" else None,
+                "traffic_source": "profiles/fssh2_sb_fast_kahan_spinboson100_ncu.md (ncu dram__bytes, scaled)",
                 "peak_source": "measured FMA throughput (project microbenchmark); MEASURED_PEAKS has no CUDA-core entry",
                 "flops_per_traj_step": WL.ref_flops_per_traj_step(nmodes), "kernel": kname,
                 "kernel_ms": ker_ms, "hbm_peak_gbs": 6751.1,

@@ -31,6 +31,7 @@ struct FsshParams {
     int32_t nsteps_total;
     float h_first, h_mid, h_last;  // step lengths: first, interior, last
     float sa1, sb1;                // first step's interpolation weights (the buffer starts at t = 0)
+    float dtsub;                   // Tsit5 sub-step dt/5 (FP32)
     uint64_t seed;
     int32_t save_stride;
     int32_t nsave;

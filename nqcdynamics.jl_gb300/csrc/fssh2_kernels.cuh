@@ -131,7 +131,7 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>&
 template <typename P>  // FsshParams or RpshParams
 __device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>& buf, bool first, float h, float gap,
                                                    Sig2<float>& sg) {
-    const float dtsub = (float)(p.dt / 5.0);
+    const float dtsub = p.dtsub;
     if (gap < p.gap_fp64) {
         const double hd = h;
         const double tn = first ? p.t0 + hd : hd, t = first ? p.t0 : 0.0;
@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
     EBuf<R> buf = {R(0), R(0), R(0), 0.0, R(0), R(0), R(0), 0.0};
     int nh = 0, nf = 0, step = 0;
     double t = p.t0;
+    const R dtR = (R)p.dt;
     // plain path: the reference's FP64 clock; fast path: the host schedule
     while (IsFast<R>::value ? step < p.nsteps_total : t < p.t1) {
         double h;
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         R inv = R(1) / (s == 0 ? sg.p : sg.q);
         R re = sg.x * inv;
         R nsm = s == 0 ? nac : -nac;
-        R prob = clamp01<R>(R(0) + R(2) * (R)v * re * nsm * (R)p.dt);
+        R prob = clamp01<R>(R(0) + R(2) * (R)v * re * nsm * dtR);
         double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
         if ((double)prob > u) {
             const int ns = 1 - s;

@@ -755,6 +755,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         const double den = t0 + hf;  // the interpolation buffer starts at t = 0
         p.sa1 = den != 0.0 ? (float)(t0 / den) : 0.f;
         p.sb1 = den != 0.0 ? (float)(hf / den) : 0.f;
+        p.dtsub = (float)(dt / 5.0);
     }
     p.seed = seed;
     p.save_stride = stride;
@@ -845,6 +846,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         rq.h_last = p.h_last;
         rq.sa1 = p.sa1;
         rq.sb1 = p.sb1;
+        rq.dtsub = p.dtsub;
         rq.seed = seed;
         rq.terminate_x = h->cfg.terminate_x;
         rq.max_hops = h->cfg.max_hops;

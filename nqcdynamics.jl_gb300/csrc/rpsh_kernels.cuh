@@ -52,6 +52,7 @@ struct RpshParams {
     int32_t nsteps_total;
     float h_first, h_mid, h_last;
     float sa1, sb1;
+    float dtsub;
     uint64_t seed;
     double terminate_x;
     int32_t max_hops;
