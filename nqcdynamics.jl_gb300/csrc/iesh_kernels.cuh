@@ -248,6 +248,23 @@ __device__ inline double iesh_block_sum(double x, double* red) {
     return red[64];
 }
 
+// FP32 form of iesh_block_sum (the fast path keeps its per-step sums off the FP64 pipe).
+__device__ inline float iesh_block_sum_f(float x, double* red_) {
+    float* red = (float*)red_;
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) red[w] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float s = l < nw ? red[l] : 0.f;
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (l == 0) red[64] = s;
+    }
+    __syncthreads();
+    return red[64];
+}
+
 __device__ inline void iesh_block_minmax(double& lo, double& hi, double* red) {
     for (int off = 16; off > 0; off >>= 1) {
         lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, off));
@@ -289,9 +306,10 @@ __device__ inline Cx<R> cx_div(Cx<R> a, Cx<R> b) {
 }
 
 // (re, im) * 2^e with |re| + |im| kept in [0.5, 1): products of many pivots
-// without overflow or underflow.
-__device__ inline void scaled_mul(double& re, double& im, int& e, double br, double bi, int be) {
-    const double nr = re * br - im * bi, ni = re * bi + im * br;
+// without overflow or underflow, in the working precision.
+template <typename T>
+__device__ inline void scaled_mul(T& re, T& im, int& e, T br, T bi, int be) {
+    const T nr = re * br - im * bi, ni = re * bi + im * br;
     int ex;
     frexp(fabs(nr) + fabs(ni), &ex);
     re = ldexp(nr, -ex);
@@ -354,7 +372,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     int* piv = (int*)(smem + L.o_piv);
     double* red = (double*)(smem + L.o_red);
     // misc: [0] K [1] sin(c dt) [2] cos(c dt), then the full-evaluation flag [3] v_z [4] h [5] dh/dz
-    //       [6] v . grad h [7] singular S [8] c [9] 1/hw [10] w/hw [11] J_0
+    //       [6] v . grad h [8] c [9] 1/hw [10] w/hw [11] J_0
     double* misc = (double*)(smem + L.o_misc);
 
     const int N = L.N, Ne = L.Ne, Nu = L.Nu, Np = L.Np, Nep = L.Nep, M = p.nbath;
@@ -732,95 +750,131 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         }
 
         // ---- hop test (iesh.jl:231-335, 390-411) ----
-        Cx<R>* Sm = phiB;              // S^T, [Nep][Nep]
+        // S^T stored by columns: column c of S^T is row occ[c] of psi, Qc[c * Nep + r] = S^T[r][c]
+        Cx<R>* Qc = phiB;
         Cx<R>* Rh = phiB + Nep * Nep;  // right-hand sides psi[unocc, :]^T, [Nep][Nu]
         for (int q = tid; q < Ne * Ne; q += nthr) {
-            const int c = q / Ne, j = q - c * Ne;
-            Sm[c * Nep + j] = phiA[occ[j] * Nep + c];
+            const int c = q / Ne, r = q - c * Ne;
+            Qc[c * Nep + r] = phiA[occ[c] * Nep + r];
         }
         __syncthreads();
         double det_r = 0.0, det_i = 0.0;
         int det_e = 0;
-        // LU with partial pivoting of S^T: warp 0 picks the pivot, swaps and
-        // scales the pivot column; all warps share the trailing update (rows
-        // by warp, columns by lane); two barriers per column.
+        // LU with partial pivoting of S^T, column c owned by warp c % nwarp.  The
+        // owner of a column picks its pivot, swaps and scales it right after its
+        // own updates; after one barrier each warp applies the row swap to all
+        // its columns (the factored L columns too, as getrf) and the rank-1
+        // update to its columns right of the pivot.  piv[col] = -1 marks a zero
+        // pivot (each entry is written once, so a late warp reads its own).
         bool singular = false;
         const int nwarp = nthr >> 5;
         for (int col = 0; col < Ne; ++col) {
-            if (warp == 0) {
-                R best = R(-1);
-                int bi = col;
+            if (warp == col % nwarp) {
+                Cx<R>* qc = Qc + col * Nep;
+                // pivot: largest |re| + |im| (first on ties) via a max-reduction of
+                // the magnitude's bit pattern (non-negative floats order as integers)
+                unsigned key = 0u;
+                int bi = Ne;
                 for (int rr = col + lane; rr < Ne; rr += 32) {
-                    const Cx<R> x = Sm[rr * Nep + col];
-                    const R mg = fabs(x.re) + fabs(x.im);
-                    if (mg > best) {
-                        best = mg;
+                    const Cx<R> x = qc[rr];
+                    const unsigned kk = __float_as_uint((float)(fabs(x.re) + fabs(x.im)));
+                    if (kk > key || bi == Ne) {
+                        key = kk;
                         bi = rr;
                     }
                 }
-                for (int off = 16; off > 0; off >>= 1) {
-                    const R ob = __shfl_xor_sync(0xffffffffu, best, off);
-                    const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-                    if (ob > best || (ob == best && oi < bi)) {
-                        best = ob;
-                        bi = oi;
+                const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+                const int cand = (key == kmax && bi < Ne) ? bi : Ne;
+                bi = __reduce_min_sync(0xffffffffu, (unsigned)cand);
+                const bool ok = kmax > 0u;
+                if (ok) {
+                    if (lane == 0 && bi != col) {
+                        const Cx<R> t = qc[col];
+                        qc[col] = qc[bi];
+                        qc[bi] = t;
+                    }
+                    __syncwarp();
+                    const Cx<R> pv = qc[col];
+                    const R inv = R(1) / (pv.re * pv.re + pv.im * pv.im);  // x / pv = x conj(pv) / |pv|^2
+                    for (int rr = col + 1 + lane; rr < Ne; rr += 32) {
+                        const Cx<R> x = qc[rr];
+                        qc[rr] = {(x.re * pv.re + x.im * pv.im) * inv, (x.im * pv.re - x.re * pv.im) * inv};
                     }
                 }
-                if (best > R(0)) {
-                    if (bi != col)
-                        for (int q = lane; q < Ne; q += 32) {
-                            const Cx<R> t = Sm[col * Nep + q];
-                            Sm[col * Nep + q] = Sm[bi * Nep + q];
-                            Sm[bi * Nep + q] = t;
-                        }
-                    __syncwarp();
-                    const Cx<R> pv = Sm[col * Nep + col];
-                    for (int rr = col + 1 + lane; rr < Ne; rr += 32) Sm[rr * Nep + col] = cx_div<R>(Sm[rr * Nep + col], pv);
-                }
-                if (lane == 0) {
-                    piv[col] = bi;
-                    misc[7] = best > R(0) ? 0.0 : 1.0;
-                }
+                if (lane == 0) piv[col] = ok ? bi : -1;
             }
             __syncthreads();
-            if (misc[7] != 0.0) {
+            const int pr = piv[col];
+            if (pr < 0) {
                 singular = true;
                 break;
             }
-            for (int rr = col + 1 + warp; rr < Ne; rr += nwarp) {
-                const Cx<R> l = Sm[rr * Nep + col];
-                for (int cc = col + 1 + lane; cc < Ne; cc += 32) {
-                    const Cx<R> u = Sm[col * Nep + cc];
-                    Cx<R>& t = Sm[rr * Nep + cc];
-                    t.re -= l.re * u.re - l.im * u.im;
-                    t.im -= l.re * u.im + l.im * u.re;
+            // this warp's columns: w, w + nwarp, ...; swap rows col and pr in all of them
+            if (pr != col)
+                for (int cc = warp + nwarp * lane; cc < Ne; cc += 32 * nwarp) {
+                    if (cc == col) continue;
+                    Cx<R>* qcc = Qc + cc * Nep;
+                    const Cx<R> t = qcc[col];
+                    qcc[col] = qcc[pr];
+                    qcc[pr] = t;
+                }
+            __syncwarp();
+            const Cx<R>* lcol = Qc + col * Nep;
+            const int r0 = col + 1 + lane, r1 = r0 + 32;
+            const Cx<R> l0 = r0 < Ne ? lcol[r0] : Cx<R>{R(0), R(0)};
+            const Cx<R> l1 = r1 < Ne ? lcol[r1] : Cx<R>{R(0), R(0)};
+            const int cc0 = col + 1 + ((warp - (col + 1)) % nwarp + nwarp) % nwarp;
+#pragma unroll 2
+            for (int cc = cc0; cc < Ne; cc += nwarp) {
+                Cx<R>* qcc = Qc + cc * Nep;
+                const Cx<R> u = qcc[col];
+                if (r0 < Ne) {
+                    Cx<R> t = qcc[r0];
+                    t.re -= l0.re * u.re - l0.im * u.im;
+                    t.im -= l0.re * u.im + l0.im * u.re;
+                    qcc[r0] = t;
+                }
+                if (r1 < Ne) {
+                    Cx<R> t = qcc[r1];
+                    t.re -= l1.re * u.re - l1.im * u.im;
+                    t.im -= l1.re * u.im + l1.im * u.re;
+                    qcc[r1] = t;
                 }
             }
-            __syncthreads();
+            for (int rr = col + 65 + lane; rr < Ne; rr += 32)  // systems beyond 64 + 1 electrons
+                for (int cc = cc0; cc < Ne; cc += nwarp) {
+                    Cx<R>* qcc = Qc + cc * Nep;
+                    const Cx<R> l = lcol[rr], u = qcc[col];
+                    Cx<R> t = qcc[rr];
+                    t.re -= l.re * u.re - l.im * u.im;
+                    t.im -= l.re * u.im + l.im * u.re;
+                    qcc[rr] = t;
+                }
         }
+        __syncthreads();
         R sabs = R(0);
         if (warp == 0) {
-            if (!singular) {  // det S on lane 0
-                double dr = 1.0, di = 0.0;
+            if (!singular) {  // det S on lane 0, as a scaled product in the working precision
+                R dr = R(1), di = R(0);
                 int de = 0, swaps = 0;
                 for (int q = lane; q < Ne; q += 32) {
-                    const Cx<R> d = Sm[q * Nep + q];
-                    scaled_mul(dr, di, de, (double)d.re, (double)d.im, 0);
+                    const Cx<R> d = Qc[q * Nep + q];
+                    scaled_mul<R>(dr, di, de, d.re, d.im, 0);
                     if (piv[q] != q) ++swaps;
                 }
                 for (int off = 16; off > 0; off >>= 1) {
-                    const double orr = __shfl_xor_sync(0xffffffffu, dr, off);
-                    const double oii = __shfl_xor_sync(0xffffffffu, di, off);
+                    const R orr = __shfl_xor_sync(0xffffffffu, dr, off);
+                    const R oii = __shfl_xor_sync(0xffffffffu, di, off);
                     const int oe = __shfl_xor_sync(0xffffffffu, de, off);
-                    scaled_mul(dr, di, de, orr, oii, oe);
+                    scaled_mul<R>(dr, di, de, orr, oii, oe);
                     swaps += __shfl_xor_sync(0xffffffffu, swaps, off);
                 }
                 if (swaps & 1) {
                     dr = -dr;
                     di = -di;
                 }
-                det_r = dr;
-                det_i = di;
+                det_r = (double)dr;
+                det_i = (double)di;
                 det_e = de;
             }
         } else {
@@ -830,7 +884,11 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                 sabs += fabs(At[occ[n] * Np + unocc[mm]]);
             }
         }
-        const double sumabs = fabs(w) * iesh_block_sum((double)sabs, red);
+        double sumabs;
+        if constexpr (std::is_same<R, float>::value)
+            sumabs = fabs(w) * (double)iesh_block_sum_f(sabs, red);
+        else
+            sumabs = fabs(w) * iesh_block_sum((double)sabs, red);
         const double u = std::is_same<R, double>::value
                              ? rng_uniform(p.seed, gid, (uint32_t)step, RNG_HOP)
                              : (double)rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP);
@@ -865,7 +923,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                 for (int rr = 1; rr < Ne; ++rr) {
                     Cx<R> y = Rh[rr * Nu + mm];
                     for (int q = 0; q < rr; ++q) {
-                        const Cx<R> l = Sm[rr * Nep + q], x = Rh[q * Nu + mm];
+                        const Cx<R> l = Qc[q * Nep + rr], x = Rh[q * Nu + mm];
                         y.re -= l.re * x.re - l.im * x.im;
                         y.im -= l.re * x.im + l.im * x.re;
                     }
@@ -874,11 +932,11 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                 for (int rr = Ne - 1; rr >= 0; --rr) {
                     Cx<R> y = Rh[rr * Nu + mm];
                     for (int q = rr + 1; q < Ne; ++q) {
-                        const Cx<R> a = Sm[rr * Nep + q], x = Rh[q * Nu + mm];
+                        const Cx<R> a = Qc[q * Nep + rr], x = Rh[q * Nu + mm];
                         y.re -= a.re * x.re - a.im * x.im;
                         y.im -= a.re * x.im + a.im * x.re;
                     }
-                    Rh[rr * Nu + mm] = cx_div<R>(y, Sm[rr * Nep + rr]);
+                    Rh[rr * Nu + mm] = cx_div<R>(y, Qc[rr * Nep + rr]);
                 }
                 // p_mn = 2 dt Re(Y_nm) (v.d)_mn, (v.d)_mn = -w A[m][state n]
                 const int m = unocc[mm];
