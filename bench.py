@@ -428,7 +428,7 @@ def secondary(args, dist):
                    "traj_steps_per_step": f["traj_steps"], "bead_steps_per_step": f["bead_steps"]}
             nbar = f["bead_steps"] / max(1, f["traj_steps"])
             ref_flops = 6600 + 100 * nbar + 8 * nbar * nbar + 6 * nbar
-            kname = "rpsh_persistent_kernel<float>"
+            kname = "rpsh_group_kernel<float>"
         elif wk == "mdef":
             n = args.ntraj if args.ntraj != 100_000 else 50_000
             nsteps = args.nsteps or 2000

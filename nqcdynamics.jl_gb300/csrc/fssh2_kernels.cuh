@@ -146,6 +146,35 @@ __device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>
     }
 }
 
+// Position / velocity accumulators of the fast paths:
+//   AccF64   FP64 accumulator (one FP64 add per update),
+//   AccKahan FP32 value + FP32 compensation (Kahan summation, four FP32 ops
+//            per update), used where the FP64 pipe (1/73 of the FP32 rate on
+//            this GPU, measured) would bound the step.
+struct AccF64 {
+    double x;
+    __device__ __forceinline__ void load(double d) { x = d; }
+    __device__ __forceinline__ double get() const { return x; }
+    __device__ __forceinline__ float f() const { return (float)x; }
+    __device__ __forceinline__ void add(float inc) { x += (double)inc; }
+};
+
+struct AccKahan {
+    float s, c;  // value ~ s - c
+    __device__ __forceinline__ void load(double d) {
+        s = (float)d;
+        c = -(float)(d - (double)s);
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+    __device__ __forceinline__ float f() const { return s; }
+    __device__ __forceinline__ void add(float inc) {
+        float y = __fsub_rn(inc, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+
 // FP32 form of diabatic_pop2 and of the warp sum of the population products
 // (fast paths): no FP64 arithmetic in the step loop.
 __device__ __forceinline__ void diabatic_pop2_f(const Sig2<float>& sg, int s, const float Z[4], float pop[2]) {

@@ -25,29 +25,7 @@
 
 namespace nqcd {
 
-struct AccF64 {
-    double x;
-    __device__ __forceinline__ void load(double d) { x = d; }
-    __device__ __forceinline__ double get() const { return x; }
-    __device__ __forceinline__ float f() const { return (float)x; }
-    __device__ __forceinline__ void add(float inc) { x += (double)inc; }
-};
-
-struct AccKahan {
-    float s, c;  // value ~ s - c
-    __device__ __forceinline__ void load(double d) {
-        s = (float)d;
-        c = -(float)(d - (double)s);
-    }
-    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
-    __device__ __forceinline__ float f() const { return s; }
-    __device__ __forceinline__ void add(float inc) {
-        float y = __fsub_rn(inc, c);
-        float t = __fadd_rn(s, y);
-        c = __fsub_rn(__fsub_rn(t, s), y);
-        s = t;
-    }
-};
+// AccF64 and AccKahan are defined in fssh2_kernels.cuh.
 
 template <int G>
 __device__ __forceinline__ float group_sum(float x) {

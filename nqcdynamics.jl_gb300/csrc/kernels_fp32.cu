@@ -19,32 +19,37 @@ cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s) {
     return launch_fssh2<float>(p, s);
 }
 
-// The per-thread stack limit must cover the kernel's spilled bead arrays.
-static cudaError_t ensure_rpsh_stack_fp32() {
-    cudaFuncAttributes a;
-    cudaError_t e = cudaFuncGetAttributes(&a, rpsh_persistent_kernel<float>);
-    if (e != cudaSuccess) return e;
-    size_t cur = 0;
-    e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
-    if (e != cudaSuccess) return e;
-    size_t need = a.localSizeBytes;
-    if (cur < need) e = cudaDeviceSetLimit(cudaLimitStackSize, need);
-    return e;
-}
-
-int rpsh_grid_fp32() {
+// Fast ring-polymer kernels, one per bead count (see rpsh_group_kernel).
+template <int Q, int GL>
+static int rpsh_group_grid_t() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, rpsh_persistent_kernel<float>, kRpshBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, rpsh_group_kernel<Q, GL>, kRpshBlock, 0);
     return sms * (per > 0 ? per : 1);
 }
 
-cudaError_t launch_rpsh_fp32(const RpshParams& p, int blocks, cudaStream_t s) {
-    cudaError_t e = ensure_rpsh_stack_fp32();
-    if (e != cudaSuccess) return e;
-    return launch_rpsh<float>(p, blocks, s);
+#define NQCD_RP_SHAPES(X) X(1, 1) X(1, 2) X(1, 4) X(5, 1) X(2, 4) X(5, 2) X(4, 4) X(8, 4)
+
+int rpsh_group_grid(int beads) {
+#define X(Q, GL) \
+    if (beads == Q * GL) return rpsh_group_grid_t<Q, GL>();
+    NQCD_RP_SHAPES(X)
+#undef X
+    return 0;
 }
+
+cudaError_t launch_rpsh_group(int beads, const RpshParams& p, int blocks, cudaStream_t s) {
+#define X(Q, GL)                                                    \
+    if (beads == Q * GL) {                                          \
+        rpsh_group_kernel<Q, GL><<<blocks, kRpshBlock, 0, s>>>(p); \
+        return cudaGetLastError();                                  \
+    }
+    NQCD_RP_SHAPES(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+#undef NQCD_RP_SHAPES
 
 cudaError_t launch_mdef_fp32(const MdefParams& p, cudaStream_t s) { return launch_mdef<float>(p, s); }
 

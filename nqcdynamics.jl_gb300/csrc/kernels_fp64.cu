@@ -35,7 +35,7 @@ int rpsh_grid_fp64() {
 cudaError_t launch_rpsh_fp64(const RpshParams& p, int blocks, cudaStream_t s) {
     cudaError_t e = ensure_rpsh_stack_fp64();
     if (e != cudaSuccess) return e;
-    return launch_rpsh<double>(p, blocks, s);
+    return launch_rpsh_plain<double>(p, blocks, s);
 }
 
 cudaError_t launch_mdef_fp64(const MdefParams& p, cudaStream_t s) { return launch_mdef<double>(p, s); }

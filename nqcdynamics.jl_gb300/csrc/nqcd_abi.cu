@@ -10,6 +10,7 @@
 #include <chrono>
 #include <new>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/nqcd_gpu.h"
@@ -25,9 +26,9 @@ using namespace nqcd;
 
 namespace nqcd {
 int rpsh_grid_fp64();
-int rpsh_grid_fp32();
+int rpsh_group_grid(int beads);
 cudaError_t launch_rpsh_fp64(const RpshParams& p, int blocks, cudaStream_t s);
-cudaError_t launch_rpsh_fp32(const RpshParams& p, int blocks, cudaStream_t s);
+cudaError_t launch_rpsh_group(int beads, const RpshParams& p, int blocks, cudaStream_t s);
 cudaError_t launch_mdef_fp64(const MdefParams& p, cudaStream_t s);
 cudaError_t launch_mdef_fp32(const MdefParams& p, cudaStream_t s);
 cudaError_t launch_iesh_fp64(const IeshParams& p, cudaStream_t s);
@@ -158,6 +159,9 @@ struct nqcd_handle {
     std::string err;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+    // fast ring polymers: one stream per bead-count kernel, forked from and joined to `stream`
+    cudaStream_t rp_streams[kNumRpCounts] = {nullptr};
+    cudaEvent_t rp_fork = nullptr, rp_join[kNumRpCounts] = {nullptr};
     int64_t cap = 0;
     int64_t ntraj = 0;
     int64_t ndof = 0;  // per trajectory (ndofs * natoms)
@@ -187,7 +191,7 @@ struct nqcd_handle {
     // ring polymers: normal-mode tables per instantiated bead count, bead-count classes
     int64_t rp_U_off[kNumRpCounts] = {0};
     double *d_rpU = nullptr, *d_rpcay = nullptr;
-    float *d_rpUf = nullptr, *d_rpcayf = nullptr;
+    float* d_rpcirc = nullptr;  // fast path: circulant free-step coefficients, [count][32][4]
     int32_t *d_nbeads = nullptr, *d_class_traj = nullptr, *d_block_class = nullptr;
     unsigned long long* d_queue = nullptr;
     double* d_rpscratch = nullptr;  // plain path bead arrays, grown on demand
@@ -198,6 +202,7 @@ struct nqcd_handle {
     int class_model[kRpshMaxClasses] = {0};
     int64_t class_begin[kRpshMaxClasses + 1] = {0};
     std::vector<int32_t> traj_beads, traj_models;  // host copies (ring polymers)
+    std::vector<float> traj_speed;                 // |initial centroid velocity| (host initial conditions only)
     // MDEF: bath levels and squared couplings; friction surrogate
     double *d_eps = nullptr, *d_V2 = nullptr;
     MlpState mlp;
@@ -240,7 +245,7 @@ void free_all(nqcd_handle* h) {
     void* ptrs[] = {h->d_mass, h->d_bath_c, h->d_bath_w2, h->d_r0, h->d_v0, h->d_r, h->d_v, h->d_sig0,
                     h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
-                    h->d_rpU, h->d_rpcay, h->d_rpUf, h->d_rpcayf, h->d_nbeads, h->d_class_traj,
+                    h->d_rpU, h->d_rpcay, h->d_rpcirc, h->d_nbeads, h->d_class_traj,
                     h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2,
                     h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im, h->d_redtmp};
     for (void* p : ptrs)
@@ -250,6 +255,11 @@ void free_all(nqcd_handle* h) {
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->evk0) cudaEventDestroy(h->evk0);
     if (h->evk1) cudaEventDestroy(h->evk1);
+    for (int c = 0; c < kNumRpCounts; ++c) {
+        if (h->rp_streams[c]) cudaStreamDestroy(h->rp_streams[c]);
+        if (h->rp_join[c]) cudaEventDestroy(h->rp_join[c]);
+    }
+    if (h->rp_fork) cudaEventDestroy(h->rp_fork);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -452,6 +462,13 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     NQCD_CREATE(cudaEventCreate(&h->ev1));
     NQCD_CREATE(cudaEventCreate(&h->evk0));
     NQCD_CREATE(cudaEventCreate(&h->evk1));
+    if (rp) {
+        NQCD_CREATE(cudaEventCreateWithFlags(&h->rp_fork, cudaEventDisableTiming));
+        for (int c = 0; c < kNumRpCounts; ++c) {
+            NQCD_CREATE(cudaStreamCreateWithFlags(&h->rp_streams[c], cudaStreamNonBlocking));
+            NQCD_CREATE(cudaEventCreateWithFlags(&h->rp_join[c], cudaEventDisableTiming));
+        }
+    }
 
     std::vector<double> mass(ndof), bc(ndof, 0.0), bw2(ndof, 0.0);
     for (int64_t I = 0; I < ndof; ++I) mass[I] = rp ? cfg->masses[0] : cfg->masses[I / cfg->ndofs];
@@ -511,15 +528,11 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
             off += (int64_t)kRpCounts[c] * kRpCounts[c];
         }
         std::vector<double> U(off);
-        std::vector<float> Uf(off);
         for (int c = 0; c < kNumRpCounts; ++c) nm_transform_matrix(kRpCounts[c], U.data() + h->rp_U_off[c]);
-        for (int64_t q = 0; q < off; ++q) Uf[q] = (float)U[q];
         NQCD_CREATE(dalloc(&h->d_rpU, off));
-        NQCD_CREATE(dalloc(&h->d_rpUf, off));
         NQCD_CREATE(cudaMemcpy(h->d_rpU, U.data(), off * sizeof(double), cudaMemcpyHostToDevice));
-        NQCD_CREATE(cudaMemcpy(h->d_rpUf, Uf.data(), off * sizeof(float), cudaMemcpyHostToDevice));
         NQCD_CREATE(dalloc(&h->d_rpcay, 4 * 32 * kNumRpCounts));
-        NQCD_CREATE(dalloc(&h->d_rpcayf, 4 * 32 * kNumRpCounts));
+        NQCD_CREATE(dalloc(&h->d_rpcirc, 4 * 32 * kNumRpCounts));
         NQCD_CREATE(dalloc(&h->d_nbeads, cap));
         NQCD_CREATE(dalloc(&h->d_class_traj, cap));
         NQCD_CREATE(dalloc(&h->d_queue, kRpshMaxClasses));
@@ -560,6 +573,15 @@ static int build_rp_classes(nqcd_handle* h, int64_t* h2d) {
     }
     std::vector<int32_t> order(ntraj);
     for (int64_t t = 0; t < ntraj; ++t) order[fillpos[key_of[t]]++] = (int32_t)t;
+    if ((int64_t)h->traj_speed.size() == ntraj) {
+        // slowest first within each class: the slow trajectories run longest,
+        // and starting them first keeps them off the end of the launch
+        // (results do not depend on the order)
+        const float* sp = h->traj_speed.data();
+        for (int k = 0; k < h->nclass; ++k)
+            std::stable_sort(order.begin() + h->class_begin[k], order.begin() + h->class_begin[k + 1],
+                             [sp](int32_t a, int32_t b) { return sp[a] < sp[b]; });
+    }
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_class_traj, order.data(), ntraj * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
     *h2d += ntraj * (int64_t)sizeof(int32_t);
@@ -568,10 +590,12 @@ static int build_rp_classes(nqcd_handle* h, int64_t* h2d) {
 
 // Per-trajectory bead counts (host array nbeads, NULL = nbeads_max for all);
 // every trajectory starts on the handle's model.
-static int set_bead_classes(nqcd_handle* h, int64_t ntraj, const int32_t* nbeads, int64_t* h2d) {
+static int set_bead_classes(nqcd_handle* h, int64_t ntraj, const int32_t* nbeads, const double* v0_host,
+                            int64_t* h2d) {
     if (h->cfg.method != NQCD_METHOD_RPSH) return NQCD_OK;
     h->traj_beads.assign(ntraj, h->cfg.nbeads_max);
     h->traj_models.assign(ntraj, h->cfg.model);
+    h->traj_speed.clear();
     for (int64_t t = 0; t < ntraj; ++t) {
         int b = nbeads ? nbeads[t] : h->cfg.nbeads_max;
         bool known = false;
@@ -580,6 +604,15 @@ static int set_bead_classes(nqcd_handle* h, int64_t ntraj, const int32_t* nbeads
             return fail(h, NQCD_ERR_UNSUPPORTED,
                         "nqcd_set_initial: bead counts must be one of 1, 2, 4, 5, 8, 10, 16, 32 and <= nbeads_max");
         h->traj_beads[t] = b;
+    }
+    if (v0_host) {
+        h->traj_speed.resize(ntraj);
+        const int64_t nd = h->ndof;
+        for (int64_t t = 0; t < ntraj; ++t) {
+            double sv = 0.0;
+            for (int j = 0; j < h->traj_beads[t]; ++j) sv += v0_host[t * nd + j];
+            h->traj_speed[t] = (float)fabs(sv / h->traj_beads[t]);
+        }
     }
     return build_rp_classes(h, h2d);
 }
@@ -647,7 +680,7 @@ int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const doub
     NQCD_CUDA(h, transpose(h->d_stage, h->d_v0, ntraj, h->ndof, h->stream));
     NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
     h2d += 2 * n * (int64_t)sizeof(double);
-    rc = set_bead_classes(h, ntraj, nbeads, &h2d);
+    rc = set_bead_classes(h, ntraj, nbeads, v0, &h2d);
     if (rc) return rc;
     return set_initial_common(h, ntraj, sig_re, sig_im, state0, &h2d);
 }
@@ -664,7 +697,7 @@ int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0, c
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_v0, d_v0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
     int64_t h2d = 0;
-    int rc = set_bead_classes(h, ntraj, nbeads, &h2d);
+    int rc = set_bead_classes(h, ntraj, nbeads, nullptr, &h2d);
     if (rc) return rc;
     return set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
 }
@@ -779,7 +812,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         // Cayley propagators for this dt, one slot of 32 modes per instantiated bead count
         const bool plain = h->cfg.precision == NQCD_PREC_FP64;
         std::vector<double> cay(4 * 32 * kNumRpCounts, 0.0);
-        std::vector<float> cayf(cay.size(), 0.0f);
+        std::vector<float> circ(cay.size(), 0.0f);
         RpshParams rq;
         memset(&rq, 0, sizeof(rq));
         for (int k = 0; k < h->nclass; ++k) {
@@ -787,13 +820,17 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
             cayley_matrices(n, h->cfg.beta, dt, cay.data() + 4 * 32 * slot);
             rq.class_beads[k] = n;
             rq.U[k] = h->d_rpU + h->rp_U_off[slot];
-            rq.Uf[k] = h->d_rpUf + h->rp_U_off[slot];
             rq.cay[k] = h->d_rpcay + 4 * 32 * slot;
-            rq.cayf[k] = h->d_rpcayf + 4 * 32 * slot;
+            rq.circf[k] = reinterpret_cast<const float4*>(h->d_rpcirc + 4 * 32 * slot);
+            if (!plain && !circulant_free_step(n, h->cfg.beta, dt, circ.data() + 4 * 32 * slot))
+                return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_run: ring-polymer free step is not circulant");
         }
-        for (size_t q = 0; q < cay.size(); ++q) cayf[q] = (float)cay[q];
         // persistent grid; blocks start on classes in proportion to their estimated work
-        int grid = plain ? rpsh_grid_fp64() : rpsh_grid_fp32();
+        int grid = plain ? rpsh_grid_fp64() : 0;
+        for (int k = 0; k < h->nclass && !plain; ++k) {
+            const int gk = rpsh_group_grid(h->class_beads[k]);
+            grid = gk > grid ? gk : grid;
+        }
         if (grid > kMaxRpGrid) grid = kMaxRpGrid;
         if (grid < 1) grid = 1;
         std::vector<double> cost(h->nclass);
@@ -804,7 +841,12 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
             total += cost[k];
         }
         std::vector<int32_t> bc(grid, 0);
-        {
+        if (!plain) {
+            // each bead-count kernel serves only its own classes: block b starts
+            // at class b mod nclass and takes the next one of its bead count,
+            // which spreads a kernel's blocks evenly over its classes
+            for (int q = 0; q < grid; ++q) bc[q] = q % h->nclass;
+        } else {
             int pos = 0;
             for (int k = 0; k < h->nclass; ++k) {
                 int nb = (int)(grid * cost[k] / (total > 0 ? total : 1.0));
@@ -814,10 +856,10 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
             for (; pos < grid; ++pos) bc[pos] = h->nclass - 1;
         }
         NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpcay, cay.data(), cay.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-        NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpcayf, cayf.data(), cayf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpcirc, circ.data(), circ.size() * sizeof(float), cudaMemcpyHostToDevice, s));
         NQCD_CUDA(h, cudaMemcpyAsync(h->d_block_class, bc.data(), grid * sizeof(int32_t), cudaMemcpyHostToDevice, s));
         NQCD_CUDA(h, cudaMemsetAsync(h->d_queue, 0, kRpshMaxClasses * sizeof(unsigned long long), s));
-        h2d += (int64_t)(cay.size() * sizeof(double) + cayf.size() * sizeof(float) + grid * sizeof(int32_t));
+        h2d += (int64_t)(cay.size() * sizeof(double) + circ.size() * sizeof(float) + grid * sizeof(int32_t));
         for (int k = 0; k < h->nclass; ++k) {
             // the handle's model uses its parameters; the other Tully models their published defaults
             static const double kTullyDefaults[3][8] = {{0.01, 1.6, 0.005, 1.0, 0, 0, 0, 0},
@@ -881,7 +923,28 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
             rq.scratch_stride = threads;
         }
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
-        e = plain ? launch_rpsh_fp64(rq, grid, s) : launch_rpsh_fp32(rq, grid, s);
+        if (plain) {
+            e = launch_rpsh_fp64(rq, grid, s);
+        } else {
+            // one persistent kernel per bead count present, each with the grid
+            // that fills the GPU, concurrently on forked streams and largest
+            // bead count first: a kernel's blocks retire as its queues drain
+            // and the next kernel's blocks take their place
+            NQCD_CUDA(h, cudaEventRecord(h->rp_fork, s));
+            int k = 0;
+            for (int c = kNumRpCounts - 1; c >= 0 && e == cudaSuccess; --c) {
+                bool present = false;
+                for (int q = 0; q < h->nclass; ++q) present |= h->class_beads[q] == kRpCounts[c];
+                if (!present) continue;
+                NQCD_CUDA(h, cudaStreamWaitEvent(h->rp_streams[k], h->rp_fork, 0));
+                e = launch_rpsh_group(kRpCounts[c], rq, rpsh_group_grid(kRpCounts[c]), h->rp_streams[k]);
+                if (e != cudaSuccess) break;
+                NQCD_CUDA(h, cudaEventRecord(h->rp_join[k], h->rp_streams[k]));
+                NQCD_CUDA(h, cudaStreamWaitEvent(s, h->rp_join[k], 0));
+                ++k;
+                if (k > 1) ++launches;  // the common path below counts one
+            }
+        }
     } else if (iesh) {
         IeshParams q;
         memset(&q, 0, sizeof(q));

@@ -10,20 +10,21 @@
 //
 // Uneven ensembles: trajectories carry their own bead count (one of the
 // instantiated counts 1, 2, 4, 5, 8, 10, 16, 32).  The host sorts them
-// into bead-count classes; one persistent launch serves all classes.  Each
-// thread takes a trajectory from its class's atomic queue, integrates it
+// into bead-count classes; one persistent launch serves all classes.  A
+// worker takes a trajectory from its class's atomic queue, integrates it
 // until the termination test or the end time, then refills its slot with the
 // next trajectory; when its class is drained it moves on to the other
-// classes, so threads never idle while work is left.  The queues are plain
+// classes, so workers never idle while work is left.  The queues are plain
 // atomic counters: there is no spin-wait anywhere.
 //
-//   R = double: plain path, every operation in the CPU oracle's order
-//               (translation unit built with -fmad=false): bit-identical.
-//   R = float : fast path.  Bead coordinates are split into the centroid
-//               (FP64) and deviations from it (FP32); the normal-mode
-//               transform, Cayley step, bead forces and the electronics run
-//               in FP32.  Since the rescaling shifts every bead by the same
-//               amount, hops change only the FP64 centroid velocity.
+//   plain path (rpsh_persistent_kernel): one thread per trajectory, FP64,
+//               every operation in the CPU oracle's order (translation unit
+//               built with -fmad=false): bit-identical.
+//   fast path (rpsh_group_kernel): one lane per bead.  Bead coordinates are
+//               split into the centroid (FP64) and deviations from it (FP32);
+//               the free ring-polymer step, bead forces and the electronics
+//               run in FP32.  Since the rescaling shifts every bead by the
+//               same amount, hops change only the FP64 centroid velocity.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -62,8 +63,7 @@ struct RpshParams {
     const int32_t* class_traj;              // trajectory indices grouped by class
     const double* U[kRpshMaxClasses];       // per class: n*n column-major U[j + n*k]
     const double* cay[kRpshMaxClasses];     // per class: [n][4]
-    const float* Uf[kRpshMaxClasses];       // FP32 copies for the fast path
-    const float* cayf[kRpshMaxClasses];
+    const float4* circf[kRpshMaxClasses];   // fast path: per class [B] circulant free-step coefficients
     unsigned long long* queue;              // [nclass] next index within each class
     int32_t first_class_of_block_stride;    // blocks per class assignment stride (see host)
     const int32_t* block_class;             // [gridDim.x] preferred class of each block
@@ -143,11 +143,11 @@ __device__ __forceinline__ R rp_bead_accel(int model, const R* mp, R x, int s, R
     tully_potential<R>(model, mp, x, V);
     eigen2_phase<R>(V, I2, w, Z);
     tully_derivative<R>(model, mp, x, D);
-    R z0 = Z[2 * s], z1 = Z[2 * s + 1];
+    R z0 = s == 0 ? Z[0] : Z[2], z1 = s == 0 ? Z[1] : Z[3];  // selects keep Z in registers
     R T0 = D[0] * z0 + D[1] * z1;
     R T1 = D[1] * z0 + D[2] * z1;
     R a = z0 * T0 + z1 * T1;
-    if (ws) *ws = w[s];
+    if (ws) *ws = s == 0 ? w[0] : w[1];
     return -a / mass;
 }
 
@@ -338,192 +338,331 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
 // ---------------------------------------------------------------------------
 // fast trajectory: FP64 centroid, FP32 internal modes and electronics
 // ---------------------------------------------------------------------------
-template <int B>
-__device__ __noinline__ void rpsh_traj_fast(const RpshParams& p, int cls, int64_t i) {
-    const int64_t N = p.ntraj;
-    const int64_t gid = p.traj_offset + i;
+// ---------------------------------------------------------------------------
+// fast path: a group of GL lanes per trajectory, Q beads per lane
+// ---------------------------------------------------------------------------
+// A warp serves one bead-count class at a time, split into 32/GL groups of GL
+// lanes; lane j of a group holds beads jQ .. jQ+Q-1 (B = GL Q exactly:
+// B = 1, 2, 4, 8, 16, 32 -> GL = 1, 2, 4, 4, 4, 4; B = 5, 10 -> GL = 1, 2).
+// The per-trajectory state (centroid position and velocity, electronic
+// density matrix, active state, hop test) is computed redundantly by the GL
+// lanes of the group and is bitwise the same on all of them: group sums are
+// per-lane sums followed by xor butterflies, and at every level a lane and its
+// partner add the same two operands.  Four lanes per trajectory keep the
+// redundant electronics (five Tsit5 sub-steps per nuclear step) shared by
+// eight trajectories per warp, while the bead work is split four ways.  The
+// centroid is accumulated in Kahan-compensated FP32 (AccKahan): FP64
+// arithmetic in the step (1/73 of the FP32 rate) would bound it.
+//
+// The free ring-polymer step acts on the bead deviations through the
+// bead-space propagator M = sum_{k >= 1} u_k cay_k u_k^T (normal modes u_k,
+// Cayley blocks cay_k; the centroid mode is left out exactly as in the
+// normal-mode form, bcb_electronics.jl:67-71).  The cyclic ring's normal
+// modes are Fourier modes whose degenerate pairs share one frequency, so M
+// is circulant: M[b][m] = c[(b - m) mod B], four coefficient vectors
+// (x<-x, x<-v, v<-x, v<-v) per class, computed on the host in FP64.  Lane j
+// forms out[jQ + q] = sum_d c[d] in[jQ + q - d] by offsets d = d1 Q + d0:
+// the inputs of one d1 are the bead blocks of lanes j - d1 and j - d1 - 1,
+// so a step costs each lane GL block shuffles and 4 B Q multiply-adds.
+//
+// A group whose trajectory ends (termination test or end of the schedule)
+// writes it out and takes the class queue's next trajectory before the next
+// step; the warp moves to another class once every group found the queue
+// empty.
+
+struct RpLanes {
+    int j, base;    // lane within the group, first lane of the group
+    unsigned mask;  // the group's lanes
+};
+
+template <int GL, typename T>
+__device__ __forceinline__ T rp_group_sum(const RpLanes& g, T x) {
+#pragma unroll
+    for (int off = GL >> 1; off > 0; off >>= 1) x += __shfl_xor_sync(g.mask, x, off);
+    return x;
+}
+
+// State of the trajectory a group is integrating.
+template <int Q>
+struct RpTraj {
+    int64_t i;
+    AccKahan xc, vc;          // centroid
+    float dx[Q], dv[Q], k[Q]; // this lane's beads: deviations from the centroid, accelerations
+    float Zc[4], w[2], nac;
+    Sig2<float> sg;
+    EBuf<float> buf;
+    int state, nh, nf, step;
+    double e0;
+};
+
+// Ring-polymer energy of the group's trajectory on state s (the plain path's
+// rp_energy, summed over the group's beads).
+template <int Q, int GL>
+__device__ __forceinline__ double rp_group_energy(const RpshParams& p, const RpLanes& g, int model, const float* mp,
+                                                  double xc, double vc, const float (&dx)[Q], const float (&dv)[Q],
+                                                  int s) {
+    constexpr int B = Q * GL;
     const double mass = p.mass;
-    const float massf = (float)mass;
-    const float* __restrict__ U = p.Uf[cls];
-    const float* __restrict__ cay = p.cayf[cls];
+    const float next = GL == 1 ? dx[0] : __shfl_sync(g.mask, dx[0], g.base + ((g.j + 1) & (GL - 1)));
+    double spring = 0.0, ke = 0.0, pe = 0.0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const double d = (double)dx[q] - (double)(q + 1 < Q ? dx[q + 1] : next);
+        if (B > 1) spring += mass * d * d;
+        const double vj = vc + (double)dv[q];
+        ke += mass * vj * vj;
+        float ws;
+        rp_bead_accel<float>(model, mp, (float)(xc + (double)dx[q]), s, (float)mass, &ws);
+        pe += ws;
+    }
+    spring = rp_group_sum<GL>(g, spring);
+    ke = rp_group_sum<GL>(g, ke);
+    pe = rp_group_sum<GL>(g, pe);
+    const double wn = B / p.beta;
+    return spring * (wn * wn) / 2.0 + ke / 2.0 + pe;
+}
+
+template <int Q>
+__device__ __forceinline__ void rp_update_centroid(int model, const float* mp, RpTraj<Q>& t) {
+    float V[3], D[3], Zn[4], A[3];
+    tully_potential<float>(model, mp, t.xc.f(), V);
+    eigen2_phase<float>(V, t.Zc, t.w, Zn);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) t.Zc[q] = Zn[q];
+    tully_derivative<float>(model, mp, t.xc.f(), D);
+    adiabatic_derivative2<float>(D, t.Zc, A);
+    t.nac = A[1] / (t.w[1] - t.w[0]);
+}
+
+template <int Q, int GL>
+__device__ __forceinline__ void rp_group_begin(const RpshParams& p, const RpLanes& g, int model, const float* mp,
+                                               int64_t i, RpTraj<Q>& t) {
+    constexpr int B = Q * GL;
+    const int64_t N = p.ntraj;
+    t.i = i;
+    double r[Q], v[Q], sr = 0.0, sv = 0.0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        r[q] = p.r[(int64_t)(g.j * Q + q) * N + i];
+        v[q] = p.v[(int64_t)(g.j * Q + q) * N + i];
+        sr += r[q];
+        sv += v[q];
+    }
+    const double xc = rp_group_sum<GL>(g, sr) / B, vc = rp_group_sum<GL>(g, sv) / B;
+    t.xc.load(xc);
+    t.vc.load(vc);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        t.dx[q] = (float)(r[q] - xc);
+        t.dv[q] = (float)(v[q] - vc);
+    }
+    t.Zc[0] = 1.f;
+    t.Zc[1] = 0.f;
+    t.Zc[2] = 0.f;
+    t.Zc[3] = 1.f;
+    rp_update_centroid(model, mp, t);
+    rp_init_sigma<float>(p, i, t.sg, t.state);
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+        t.k[q] = rp_bead_accel<float>(model, mp, (float)(xc + (double)t.dx[q]), t.state, (float)p.mass, nullptr);
+    t.e0 = p.energy ? rp_group_energy<Q, GL>(p, g, model, mp, xc, vc, t.dx, t.dv, t.state) : 0.0;
+    t.buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
+    t.nh = t.nf = t.step = 0;
+}
+
+template <int Q, int GL>
+__device__ __forceinline__ void rp_group_finish(const RpshParams& p, const RpLanes& g, int model, const float* mp,
+                                                const RpTraj<Q>& t) {
+    const int64_t N = p.ntraj;
+    const double xc = t.xc.get(), vc = t.vc.get();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        p.r[(int64_t)(g.j * Q + q) * N + t.i] = xc + (double)t.dx[q];
+        p.v[(int64_t)(g.j * Q + q) * N + t.i] = vc + (double)t.dv[q];
+    }
+    const double x0 = __shfl_sync(g.mask, xc + (double)t.dx[0], g.base);
+    const double e1 = p.energy ? rp_group_energy<Q, GL>(p, g, model, mp, xc, vc, t.dx, t.dv, t.state) : 0.0;
+    if (g.j == 0) rp_write_final<float>(p, t.i, t.sg, t.state, t.nh, t.nf, t.step, t.e0, e1, x0);
+}
+
+// Free ring-polymer step of the deviations: (dx, dv) <- M (dx, dv), M circulant.
+template <int Q, int GL>
+__device__ __forceinline__ void rp_free_step(const RpLanes& g, const float4* __restrict__ circ, float (&dx)[Q],
+                                             float (&dv)[Q]) {
+    float nx[Q], nv[Q], ax[Q], av[Q], bx[Q], bv[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        nx[q] = nv[q] = 0.f;
+        ax[q] = dx[q];
+        av[q] = dv[q];
+    }
+#pragma unroll
+    for (int d1 = 0; d1 < GL; ++d1) {
+        // bead block of lane j - d1 - 1 (the wrap-around part of this d1's window)
+        const int src = g.base + ((g.j - d1 - 1) & (GL - 1));
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            bx[q] = GL == 1 ? dx[q] : __shfl_sync(g.mask, dx[q], src);
+            bv[q] = GL == 1 ? dv[q] : __shfl_sync(g.mask, dv[q], src);
+        }
+#pragma unroll
+        for (int d0 = 0; d0 < Q; ++d0) {
+            const float4 c = __ldg(circ + d1 * Q + d0);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const float xs = q >= d0 ? ax[q - d0] : bx[Q + q - d0];
+                const float vs = q >= d0 ? av[q - d0] : bv[Q + q - d0];
+                nx[q] = fmaf(c.x, xs, fmaf(c.y, vs, nx[q]));
+                nv[q] = fmaf(c.z, xs, fmaf(c.w, vs, nv[q]));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            ax[q] = bx[q];
+            av[q] = bv[q];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        dx[q] = nx[q];
+        dv[q] = nv[q];
+    }
+}
+
+// One step of the group's trajectory; returns true when it has ended.
+template <int Q, int GL>
+__device__ __forceinline__ bool rp_group_step(const RpshParams& p, const RpLanes& g, int model, const float* mp,
+                                              const float4* __restrict__ circ, RpTraj<Q>& t) {
+    constexpr float invB = 1.0f / (Q * GL);
+    const float massf = (float)p.mass;
+    const int step = t.step;
+    const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
+    const float half = 0.5f * h;
+    // B kick: centroid and deviations
+    float ks = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) ks += t.k[q];
+    float kbar = rp_group_sum<GL>(g, ks) * invB;
+    AccKahan vct = t.vc;
+    vct.add(half * kbar);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) t.dv[q] += half * (t.k[q] - kbar);
+    // free ring polymer: centroid drifts, deviations through the circulant propagator
+    t.xc.add(h * vct.f());
+    rp_free_step<Q, GL>(g, circ, t.dx, t.dv);
+    // bead forces, B kick
+    const float xcf = t.xc.f();
+    ks = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        t.k[q] = rp_bead_accel<float>(model, mp, xcf + t.dx[q], t.state, massf, nullptr);
+        ks += t.k[q];
+    }
+    kbar = rp_group_sum<GL>(g, ks) * invB;
+    t.vc = vct;
+    t.vc.add(half * kbar);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) t.dv[q] += half * (t.k[q] - kbar);
+    rp_update_centroid(model, mp, t);
+    const float gap = t.w[1] - t.w[0];
+    t.buf.E0c = t.buf.E0n;
+    t.buf.E1c = t.buf.E1n;
+    t.buf.Dc = t.buf.Dn;
+    t.buf.E0n = t.w[0];
+    t.buf.E1n = t.w[1];
+    t.buf.Dn = t.nac * t.vc.f();
+    electronics2_sched(p, t.buf, step == 0, h, gap, t.sg);
+    t.step = step + 1;
+
+    const int s = t.state;
+    const float re = t.sg.x / (s == 0 ? t.sg.p : t.sg.q);
+    const float nsm = s == 0 ? t.nac : -t.nac;
+    const float prob = clamp01<float>(2.0f * t.vc.f() * re * nsm * (float)p.dt);
+    const float u = rng_uniform_f(p.seed, (uint64_t)(p.traj_offset + t.i), (uint32_t)t.step, RNG_HOP);
+    if (prob > u) {
+        const int ns = 1 - s;
+        bool accept = true;
+        if (p.rescaling != RESCALE_OFF) {
+            const double d = ns < s ? (double)t.nac : -(double)t.nac;
+            const double aa = d * d / p.mass / 2.0;
+            const double vc = t.vc.get();
+            const double bb = d * vc;
+            const double cc = ns == 0 ? (double)t.w[0] - (double)t.w[1] : (double)t.w[1] - (double)t.w[0];
+            const double disc = bb * bb - 4.0 * aa * cc;
+            if (disc < 0.0) {
+                accept = false;
+                if (p.rescaling == RESCALE_VINVERSION) {  // only the centroid moves along d (1 DoF)
+                    t.vc.s = -t.vc.s;
+                    t.vc.c = -t.vc.c;
+                }
+            } else {
+                const double root = sqrt(disc);
+                const double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
+                t.vc.load(vc - gamma * d / p.mass);
+            }
+        }
+        if (accept) {
+            if (g.j == 0) rp_log_hop(p, t.i, t.nh, t.step, s, ns);
+            t.nh += 1;
+            t.state = ns;
+        } else {
+            t.nf += 1;
+        }
+    }
+    return t.step >= p.nsteps_total || (p.terminate_x > 0.0 && fabsf(t.xc.f()) > (float)p.terminate_x);
+}
+
+// All trajectories of class cls, groups of GL lanes refilled from its queue.
+template <int Q, int GL>
+__device__ __forceinline__ void rp_serve_class(const RpshParams& p, int cls) {
+    const int lane = threadIdx.x & 31;
+    RpLanes g;
+    g.j = lane & (GL - 1);
+    g.base = lane & ~(GL - 1);
+    g.mask = GL == 32 ? 0xffffffffu : ((1u << GL) - 1u) << g.base;
+    const int model = p.class_model[cls];
     float mp[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) mp[q] = (float)p.class_mp[cls][q];
-    const int model = p.class_model[cls];
-    // centroid (FP64) and deviations (FP32)
-    double xc = 0.0, vc = 0.0;
-    float dx[B], dv[B], k[B], qm[B], pm[B];
-    {
-        double rr[B], vv[B];
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            rr[j] = p.r[(int64_t)j * N + i];
-            vv[j] = p.v[(int64_t)j * N + i];
-            xc += rr[j];
-            vc += vv[j];
-        }
-        xc /= B;
-        vc /= B;
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            dx[j] = (float)(rr[j] - xc);
-            dv[j] = (float)(vv[j] - vc);
-        }
-    }
-    float Zc[4] = {1.f, 0.f, 0.f, 1.f}, w[2], A[3], nac;
-    auto update_centroid = [&](double x) {
-        float V[3], D[3], Zn[4];
-        tully_potential<float>(model, mp, (float)x, V);
-        eigen2_phase<float>(V, Zc, w, Zn);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) Zc[q] = Zn[q];
-        tully_derivative<float>(model, mp, (float)x, D);
-        adiabatic_derivative2<float>(D, Zc, A);
-        nac = A[1] / (w[1] - w[0]);
-    };
-    auto rp_energy = [&](int s) {
-        double wn = B / p.beta;
-        double spring = 0.0, ke = 0.0, pe = 0.0;
-        for (int j = 0; j < B; ++j) {
-            int jn = (j + 1) % B;
-            double d = (double)dx[j] - (double)dx[jn];
-            if (B > 1) spring += mass * d * d;
-            double vj = vc + (double)dv[j];
-            ke += mass * vj * vj;
-            float ws;
-            rp_bead_accel<float>(model, mp, (float)(xc + (double)dx[j]), s, massf, &ws);
-            pe += ws;
-        }
-        return spring * (wn * wn) / 2.0 + ke / 2.0 + pe;
-    };
-    update_centroid(xc);
-    Sig2<float> sg;
-    int state;
-    rp_init_sigma<float>(p, i, sg, state);
-#pragma unroll
-    for (int j = 0; j < B; ++j) k[j] = rp_bead_accel<float>(model, mp, (float)(xc + (double)dx[j]), state, massf, nullptr);
-    const double e0 = p.energy ? rp_energy(state) : 0.0;
-
-    EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
-    int nh = 0, nf = 0, step = 0;
-    const float dtf = (float)p.dt;
-    // the host's step schedule replaces the reference's FP64 clock
-    while (step < p.nsteps_total) {
-        const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
-        const double hd = h;
-        const float half = 0.5f * h;
-        // B kick: centroid part in FP64, deviations in FP32
-        float kbar = 0.f;
-#pragma unroll
-        for (int j = 0; j < B; ++j) kbar += k[j];
-        kbar *= 1.0f / B;
-        double vct = vc + (double)(half * kbar);
-#pragma unroll
-        for (int j = 0; j < B; ++j) dv[j] += half * (k[j] - kbar);
-        // free ring polymer: centroid mode is a free particle, internal modes rotate (Cayley)
-        xc = xc + hd * vct;
-#pragma unroll
-        for (int kk = 1; kk < B; ++kk) {
-            float a = 0.f, b = 0.f;
-#pragma unroll
-            for (int j = 0; j < B; ++j) {
-                float u = U[j + B * kk];
-                a += u * dx[j];
-                b += u * dv[j];
-            }
-            const float* c = cay + 4 * kk;
-            qm[kk] = c[0] * a + c[1] * b;
-            pm[kk] = c[2] * a + c[3] * b;
-        }
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            float a = 0.f, b = 0.f;
-#pragma unroll
-            for (int kk = 1; kk < B; ++kk) {
-                float u = U[j + B * kk];
-                a += u * qm[kk];
-                b += u * pm[kk];
-            }
-            dx[j] = a;
-            dv[j] = b;
-        }
-        // bead forces, B kick
-        kbar = 0.f;
-        const float xcf = (float)xc;
-#pragma unroll
-        for (int j = 0; j < B; ++j) {
-            k[j] = rp_bead_accel<float>(model, mp, xcf + dx[j], state, massf, nullptr);
-            kbar += k[j];
-        }
-        kbar *= 1.0f / B;
-        vc = vct + (double)(half * kbar);
-#pragma unroll
-        for (int j = 0; j < B; ++j) dv[j] += half * (k[j] - kbar);
-        update_centroid(xc);
-        const float gap = w[1] - w[0];
-        buf.E0c = buf.E0n;
-        buf.E1c = buf.E1n;
-        buf.Dc = buf.Dn;
-        buf.E0n = w[0];
-        buf.E1n = w[1];
-        buf.Dn = nac * (float)vc;
-        electronics2_sched(p, buf, step == 0, h, gap, sg);
-        step += 1;
-
-        const int s = state;
-        float re = sg.x / (s == 0 ? sg.p : sg.q);
-        float nsm = s == 0 ? nac : -nac;
-        float prob = clamp01<float>(2.0f * (float)vc * re * nsm * dtf);
-        float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
-        if (prob > u) {
-            const int ns = 1 - s;
-            bool accept = true;
-            if (p.rescaling != RESCALE_OFF) {
-                double d = ns < s ? (double)nac : -(double)nac;
-                double aa = d * d / mass / 2.0;
-                double bb = d * vc;
-                double cc = (double)w[ns] - (double)w[s];
-                double disc = bb * bb - 4.0 * aa * cc;
-                if (disc < 0.0) {
-                    accept = false;
-                    if (p.rescaling == RESCALE_VINVERSION) vc = -vc;  // only the centroid moves along d (1 DoF)
-                } else {
-                    double root = sqrt(disc);
-                    double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
-                    vc = vc - gamma * d / mass;
-                }
-            }
-            if (accept) {
-                rp_log_hop(p, i, nh, step, s, ns);
-                nh += 1;
-                state = ns;
+    const float4* circ = p.circf[cls];
+    const int64_t begin = p.class_begin[cls], count = p.class_begin[cls + 1] - begin;
+    RpTraj<Q> t;
+    bool has = false, drained = count <= 0;
+    while (true) {
+        if (!has && !drained) {  // uniform within the group
+            unsigned long long idx = 0ull;
+            if (g.j == 0) idx = atomicAdd(p.queue + cls, 1ull);
+            idx = __shfl_sync(g.mask, idx, g.base);
+            if ((int64_t)idx < count) {
+                rp_group_begin<Q, GL>(p, g, model, mp, p.class_traj[begin + (int64_t)idx], t);
+                has = true;
             } else {
-                nf += 1;
+                drained = true;
             }
         }
-        if (p.terminate_x > 0.0 && fabs(xc) > p.terminate_x) break;
+        if (__all_sync(0xffffffffu, drained)) break;
+        if (has && rp_group_step<Q, GL>(p, g, model, mp, circ, t)) {
+            rp_group_finish<Q, GL>(p, g, model, mp, t);
+            has = false;
+        }
     }
-    double x0 = 0.0;
-#pragma unroll
-    for (int j = 0; j < B; ++j) {
-        double xj = xc + (double)dx[j];
-        if (j == 0) x0 = xj;
-        p.r[(int64_t)j * N + i] = xj;
-        p.v[(int64_t)j * N + i] = vc + (double)dv[j];
-    }
-    const double e1 = p.energy ? rp_energy(state) : 0.0;
-    rp_write_final<float>(p, i, sg, state, nh, nf, step, e0, e1, x0);
 }
 
-template <typename R, int B>
-__device__ __forceinline__ void rpsh_traj(const RpshParams& p, int cls, int64_t i) {
-    if constexpr (std::is_same<R, double>::value)
-        rpsh_traj_plain<B>(p, cls, i);
-    else
-        rpsh_traj_fast<B>(p, cls, i);
+// Persistent fast kernel of one bead count B = Q GL: warps over the classes
+// with B beads (the Tully models), groups over their trajectories.  The
+// shapes are separate kernels because one kernel holding all of them needs
+// the register budget of the largest everywhere; the host launches them
+// concurrently on forked streams (instantiated in the FP32 translation unit).
+template <int Q, int GL>
+__global__ void __launch_bounds__(kRpshBlock) rpsh_group_kernel(const RpshParams p) {
+    int cls = p.block_class[blockIdx.x];
+    for (int visited = 0; visited < p.nclass; ++visited, cls = (cls + 1) % p.nclass)
+        if (p.class_beads[cls] == Q * GL) rp_serve_class<Q, GL>(p, cls);
 }
 
-// Persistent launch: refill-on-finish work queues per bead-count class.
+// Plain path persistent launch: refill-on-finish work queues per bead-count
+// class, one thread per trajectory (R = double, instantiated in the FP64
+// translation unit only).
 template <typename R>
 __global__ void __launch_bounds__(kRpshBlock) rpsh_persistent_kernel(const RpshParams p) {
     int cls = p.block_class[blockIdx.x];
@@ -537,23 +676,34 @@ __global__ void __launch_bounds__(kRpshBlock) rpsh_persistent_kernel(const RpshP
         }
         const int64_t i = p.class_traj[begin + idx];
         switch (p.class_beads[cls]) {
-            case 1: rpsh_traj<R, 1>(p, cls, i); break;
-            case 2: rpsh_traj<R, 2>(p, cls, i); break;
-            case 4: rpsh_traj<R, 4>(p, cls, i); break;
-            case 5: rpsh_traj<R, 5>(p, cls, i); break;
-            case 8: rpsh_traj<R, 8>(p, cls, i); break;
-            case 10: rpsh_traj<R, 10>(p, cls, i); break;
-            case 16: rpsh_traj<R, 16>(p, cls, i); break;
-            case 32: rpsh_traj<R, 32>(p, cls, i); break;
+            case 1: rpsh_traj_plain<1>(p, cls, i); break;
+            case 2: rpsh_traj_plain<2>(p, cls, i); break;
+            case 4: rpsh_traj_plain<4>(p, cls, i); break;
+            case 5: rpsh_traj_plain<5>(p, cls, i); break;
+            case 8: rpsh_traj_plain<8>(p, cls, i); break;
+            case 10: rpsh_traj_plain<10>(p, cls, i); break;
+            case 16: rpsh_traj_plain<16>(p, cls, i); break;
+            case 32: rpsh_traj_plain<32>(p, cls, i); break;
             default: break;  // the host admits only the instantiated bead counts
         }
     }
 }
 
 template <typename R>
-cudaError_t launch_rpsh(const RpshParams& p, int blocks, cudaStream_t s) {
+cudaError_t launch_rpsh_plain(const RpshParams& p, int blocks, cudaStream_t s) {
     rpsh_persistent_kernel<R><<<blocks, kRpshBlock, 0, s>>>(p);
     return cudaGetLastError();
+}
+
+// Lane-group shape (beads per lane Q, lanes per trajectory GL) of a bead count.
+inline void rpsh_group_shape(int beads, int& Q, int& GL) {
+    switch (beads) {
+        case 1: Q = 1, GL = 1; break;
+        case 2: Q = 1, GL = 2; break;
+        case 5: Q = 5, GL = 1; break;
+        case 10: Q = 5, GL = 2; break;
+        default: Q = beads / 4, GL = 4; break;  // 4, 8, 16, 32
+    }
 }
 
 }  // namespace nqcd

@@ -127,3 +127,40 @@ def test_rpsh_fast_observables():
     # termination time agrees to a few steps for trajectories with the same hop history
     same = (a["nhops"] == b["nhops"]) & (a["state"] == b["state"])
     assert np.mean(np.abs(a["nsteps"][same] - b["nsteps"][same]) <= 2) > 0.95
+
+
+@pytest.mark.parametrize("model,rescaling", [(2, 0), (3, 1)])
+def test_rpsh_fast_every_bead_count(model, rescaling):
+    """The lane-group fast kernel with bead counts that fill a group (1, 2, 4,
+    8, 16, 32) and that leave padding lanes (5, 10): same hop histories as the
+    plain path for almost all trajectories, and for those the final centroid
+    and ring-polymer energy agree to FP32 accuracy; ring-polymer energy is
+    conserved along hop-free trajectories."""
+    ntraj = 3000
+    r0, v0, nb = rp_inputs(ntraj, 21, counts=(1, 2, 4, 5, 8, 10, 16, 32))
+    res = {}
+    for prec in (L.PREC_FP64, L.PREC_FP32):
+        eng = make_rp_engine(model, ntraj, precision=prec, rescaling=rescaling)
+        try:
+            res[prec] = run_rp(eng, r0, v0, nb, 6000.0, 5)
+        finally:
+            eng.close()
+    a, b = res[L.PREC_FP64], res[L.PREC_FP32]
+    same = (a["nhops"] == b["nhops"]) & (a["state"] == b["state"]) & (a["nfrustrated"] == b["nfrustrated"])
+    assert np.mean(same) > 0.95
+    for bc in (1, 2, 5, 10, 32):
+        assert np.mean(same[nb == bc]) > 0.9, bc
+    sel = same & (np.abs(a["nsteps"] - b["nsteps"]) <= 2)
+    assert np.mean(sel) > 0.93
+    xa = np.array([a["r"][t, : nb[t]].mean() for t in range(ntraj)])
+    xb = np.array([b["r"][t, : nb[t]].mean() for t in range(ntraj)])
+    assert np.max(np.abs(xa[sel] - xb[sel])) < 0.05
+    # initial energies: same initial condition, FP32 bead forces and energies
+    np.testing.assert_allclose(b["energy"][:, 0], a["energy"][:, 0], rtol=2e-4, atol=1e-6)
+    quiet = sel & (a["nhops"] == 0) & (a["nfrustrated"] == 0)
+    drift_a = np.abs(a["energy"][quiet, 1] - a["energy"][quiet, 0])
+    drift_b = np.abs(b["energy"][quiet, 1] - b["energy"][quiet, 0])
+    assert np.median(drift_b) <= 10 * np.median(drift_a) + 1e-6
+    # per-trajectory outputs are written once, at the trajectory's own index
+    assert np.all(b["nsteps"] > 0)
+    assert np.all(np.isfinite(b["r"][:, 0]))
