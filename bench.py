@@ -400,7 +400,7 @@ def secondary(args, dist):
                    "plain": sc["fp64"].tolist(), "fast": sc["fp32"].tolist()}
             cfg = {"workload": "fssh_tully1_x-10_p10_traj10k_dt1_t3000", "ntraj_per_gpu": n, "nsteps": 3000}
             ref_flops = WL.ref_flops_per_traj_step(1)
-            kname = "fssh2_tully_kernel<float>"
+            kname = "fssh2_tully_fast_kernel<float>"
         elif wk == "rpsh":
             n = args.ntraj if args.ntraj != 100_000 else 200_000
             nsub = min(n, 20_000)

@@ -372,6 +372,137 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
     if (p.scatter) atomicAdd(p.scatter + (x > 0.0 ? 2 : 0) + state, 1ull);
 }
 
+// Fast one-dimensional Tully kernel: the steps of fssh2_tully_kernel<float>
+// with no FP64 arithmetic in the step loop.  Position and velocity are
+// Kahan-compensated FP32 accumulators (AccKahan), the force, step lengths and
+// hop test are FP32; FP64 remains in the set-up, the rare momentum rescaling
+// and the FP64 electronics below the gap threshold.  With one trajectory per
+// thread and few trajectories per SM this kernel is bound by the latency of
+// one step, to which every FP64 operation (1/73 of the FP32 rate) adds.
+// (R = float; a template so that only the FP32 translation unit emits it.)
+template <typename R>
+__global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const FsshParams p) {
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i0 < p.ntraj;
+    const int64_t i = active ? i0 : p.ntraj - 1;
+    const int64_t gid = p.traj_offset + i;
+
+    float mp[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) mp[q] = (float)p.mp[q];
+    const double mass = p.mass[0];
+    const float inv_mass = (float)(1.0 / mass);
+    AccKahan x, v;
+    x.load(p.r[i]);
+    v.load(p.v[i]);
+
+    float Z[4] = {1.f, 0.f, 0.f, 1.f};
+    float w[2], A[3], nac;
+    auto update_cache = [&](float xx) {
+        float V[3], D[3], Zn[4];
+        tully_potential<float>(p.model, mp, xx, V);
+        eigen2_phase<float>(V, Z, w, Zn);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Z[q] = Zn[q];
+        tully_derivative<float>(p.model, mp, xx, D);
+        adiabatic_derivative2<float>(D, Z, A);
+        nac = A[1] / (w[1] - w[0]);
+    };
+    auto accel = [&](int s) -> float { return -(s == 0 ? A[0] : A[2]) * inv_mass; };
+
+    update_cache(x.f());
+    Sig2<float> sg;
+    int state;
+    init_electronics2<float>(p, i, gid, Z, sg, state);
+    float k = accel(state);
+    const double v0 = v.get();
+    const double e0 = (0.0 + mass * (v0 * v0)) / 2.0 + (double)(state == 0 ? w[0] : w[1]);
+    float pop0[2] = {0.f, 0.f};
+    int isave = 0;
+    if (p.save_stride > 0) {
+        diabatic_pop2_f(sg, state, Z, pop0);
+        warp_save_popcorr_f(p, isave++, active, pop0, pop0);
+    }
+
+    EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
+    int nh = 0, nf = 0, step = 0;
+    const float dtf = (float)p.dt;
+    while (step < p.nsteps_total) {
+        const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
+        const float half = 0.5f * h;
+        v.add(half * k);
+        x.add(h * v.f());
+        update_cache(x.f());
+        k = accel(state);
+        v.add(half * k);
+        buf.E0c = buf.E0n;
+        buf.E1c = buf.E1n;
+        buf.Dc = buf.Dn;
+        buf.E0n = w[0];
+        buf.E1n = w[1];
+        buf.Dn = nac * v.f();
+        electronics2_sched(p, buf, step == 0, h, w[1] - w[0], sg);
+        step += 1;
+
+        // hop test
+        const int s = state;
+        const float re = sg.x / (s == 0 ? sg.p : sg.q);
+        const float nsm = s == 0 ? nac : -nac;
+        const float prob = clamp01<float>(2.0f * v.f() * re * nsm * dtf);
+        const float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
+        if (prob > u) {
+            const int ns = 1 - s;
+            bool accept = true;
+            if (p.rescaling != RESCALE_OFF) {
+                const double vd = v.get();
+                const double d = (double)(ns < s ? nac : -nac);
+                const double aa = (0.0 + d * d / mass) / 2.0;
+                const double bb = 0.0 + d * vd;
+                const double cc = ns == 0 ? (double)w[0] - (double)w[1] : (double)w[1] - (double)w[0];
+                const double disc = bb * bb - 4.0 * aa * cc;
+                if (disc < 0.0) {
+                    accept = false;
+                    if (p.rescaling == RESCALE_VINVERSION) {  // one degree of freedom: v -> -v
+                        v.s = -v.s;
+                        v.c = -v.c;
+                    }
+                } else {
+                    const double root = sqrt(disc);
+                    const double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
+                    v.load(vd - gamma * d / mass);
+                }
+            }
+            if (accept) {
+                log_hop(p, active, i, nh, step, s, ns);
+                nh += 1;
+                state = ns;
+            } else {
+                nf += 1;
+            }
+        }
+        if (p.save_stride > 0 && step % p.save_stride == 0) {
+            float pf[2];
+            diabatic_pop2_f(sg, state, Z, pf);
+            warp_save_popcorr_f(p, isave++, active, pop0, pf);
+        }
+    }
+
+    if (!active) return;
+    const double xf = x.get(), vf = v.get();
+    p.r[i] = xf;
+    p.v[i] = vf;
+    write_sigma<float>(p, i, sg);
+    p.state[i] = state;
+    if (p.nhops) p.nhops[i] = nh;
+    if (p.nfrustrated) p.nfrustrated[i] = nf;
+    if (p.nsteps) p.nsteps[i] = step;
+    if (p.energy) {
+        p.energy[i] = e0;
+        p.energy[p.ntraj + i] = (0.0 + mass * (vf * vf)) / 2.0 + (double)(state == 0 ? w[0] : w[1]);
+    }
+    if (p.scatter) atomicAdd(p.scatter + (xf > 0.0 ? 2 : 0) + state, 1ull);
+}
+
 // ---------------------------------------------------------------------------
 // Spin-boson (N bath modes, unit or given masses)
 // ---------------------------------------------------------------------------
@@ -631,6 +762,8 @@ cudaError_t launch_fssh2(const FsshParams& p, cudaStream_t s) {
     int64_t blocks = (p.ntraj + kFsshBlock - 1) / kFsshBlock;
     if (p.model == MODEL_SPINBOSON)
         fssh2_spinboson_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
+    else if constexpr (IsFast<R>::value)
+        fssh2_tully_fast_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
     else
         fssh2_tully_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
     return cudaGetLastError();

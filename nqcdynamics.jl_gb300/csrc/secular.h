@@ -17,10 +17,13 @@
 
 namespace nqcd {
 
+// Reciprocal of a secular-sum denominator.  FP32 (fast paths): the hardware
+// approximate reciprocal (about 1 ulp); its error is of the order of the
+// rounding already allowed for by the stopping test below.
 template <typename R>
 __device__ __forceinline__ R secular_rcp(R d) {
     if constexpr (std::is_same<R, float>::value)
-        return __frcp_rn(d);
+        return __fdividef(1.0f, d);
     else
         return 1.0 / d;
 }
@@ -46,6 +49,21 @@ __device__ __forceinline__ void secular_root(const R* __restrict__ eps, const R*
         o = b;
         dlo = R(0);
         dhi = Lbound;
+    } else if (std::is_same<R, float>::value && lam_io > a && lam_io < b) {
+        // fast path with a warm start inside the interval: measure from the
+        // pole nearer to it over the whole interval (the root moves little
+        // between evaluations), which saves the midpoint evaluation
+        if (lam_io - a < b - lam_io) {
+            jo = i - 1;
+            o = a;
+            dlo = R(0);
+            dhi = b - a;
+        } else {
+            jo = i;
+            o = b;
+            dlo = a - b;
+            dhi = R(0);
+        }
     } else {
         // which half: sign of f at the midpoint decides the nearer pole
         R mid = a + R(0.5) * (b - a);
