@@ -14,6 +14,8 @@
 // closed-form values) in the test suite.
 #pragma once
 
+#include <type_traits>
+
 #include "nqcd_math.h"
 
 namespace nqcd {
@@ -116,9 +118,19 @@ NQCD_HD void eigen2_phase(const T H[3], const T Zprev[4], T w[2], T Z[4]) {
             v1x = b;
             v1y = rad - h;
         }
-        T n = sqrt(v1x * v1x + v1y * v1y);
-        v1x = v1x / n;
-        v1y = v1y / n;
+#if defined(__CUDA_ARCH__)
+        if constexpr (std::is_same<T, float>::value) {
+            // fast paths: normalise with the hardware reciprocal square root
+            const float rn = rsqrtf(v1x * v1x + v1y * v1y);
+            v1x = v1x * rn;
+            v1y = v1y * rn;
+        } else
+#endif
+        {
+            T n = sqrt(v1x * v1x + v1y * v1y);
+            v1x = v1x / n;
+            v1y = v1y / n;
+        }
     }
     // column 0 = (-v1y, v1x), column 1 = (v1x, v1y)
     T z00 = -v1y, z10 = v1x, z01 = v1x, z11 = v1y;

@@ -151,6 +151,19 @@ __device__ __forceinline__ R rp_bead_accel(int model, const R* mp, R x, int s, R
     return -a / mass;
 }
 
+// Fast-path form: the same force with the reciprocal mass precomputed.
+__device__ __forceinline__ float rp_bead_accel_f(int model, const float* mp, float x, int s, float inv_mass) {
+    float V[3], D[3], w[2], Z[4];
+    const float I2[4] = {1.f, 0.f, 0.f, 1.f};
+    tully_potential<float>(model, mp, x, V);
+    eigen2_phase<float>(V, I2, w, Z);
+    tully_derivative<float>(model, mp, x, D);
+    const float z0 = s == 0 ? Z[0] : Z[2], z1 = s == 0 ? Z[1] : Z[3];
+    const float T0 = D[0] * z0 + D[1] * z1;
+    const float T1 = D[1] * z0 + D[2] * z1;
+    return -(z0 * T0 + z1 * T1) * inv_mass;
+}
+
 // ---------------------------------------------------------------------------
 // plain FP64 trajectory (oracle order)
 // ---------------------------------------------------------------------------
@@ -464,7 +477,7 @@ __device__ __forceinline__ void rp_group_begin(const RpshParams& p, const RpLane
     rp_init_sigma<float>(p, i, t.sg, t.state);
 #pragma unroll
     for (int q = 0; q < Q; ++q)
-        t.k[q] = rp_bead_accel<float>(model, mp, (float)(xc + (double)t.dx[q]), t.state, (float)p.mass, nullptr);
+        t.k[q] = rp_bead_accel_f(model, mp, (float)(xc + (double)t.dx[q]), t.state, (float)(1.0 / p.mass));
     t.e0 = p.energy ? rp_group_energy<Q, GL>(p, g, model, mp, xc, vc, t.dx, t.dv, t.state) : 0.0;
     t.buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
     t.nh = t.nf = t.step = 0;
@@ -534,7 +547,7 @@ template <int Q, int GL>
 __device__ __forceinline__ bool rp_group_step(const RpshParams& p, const RpLanes& g, int model, const float* mp,
                                               const float4* __restrict__ circ, RpTraj<Q>& t) {
     constexpr float invB = 1.0f / (Q * GL);
-    const float massf = (float)p.mass;
+    const float inv_mass = (float)(1.0 / p.mass);
     const int step = t.step;
     const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
     const float half = 0.5f * h;
@@ -555,7 +568,7 @@ __device__ __forceinline__ bool rp_group_step(const RpshParams& p, const RpLanes
     ks = 0.f;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        t.k[q] = rp_bead_accel<float>(model, mp, xcf + t.dx[q], t.state, massf, nullptr);
+        t.k[q] = rp_bead_accel_f(model, mp, xcf + t.dx[q], t.state, inv_mass);
         ks += t.k[q];
     }
     kbar = rp_group_sum<GL>(g, ks) * invB;
