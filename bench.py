@@ -500,7 +500,8 @@ def secondary(args, dist):
     line = {
         "metric": METRIC, "workload": wk, "value": fast["value"], "unit": UNIT, "n_gpus": dist.world, "steps": steps,
         "warmup": warm, "ms_per_step": fast["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32+fp64acc", "data": "synthetic", "chosen_path": "fp32", "config": cfg,
+        "vs_baseline": None, "dtype": {"tully1": "fp32+kahan-acc", "rpsh": "fp32+kahan-acc"}.get(wk, "fp32+fp64acc"),
+        "data": "synthetic", "chosen_path": "fp32", "config": cfg,
         "plain_fp64": {"value": plain["value"], "unit": UNIT, "speedup_chosen_vs_plain": fast["value"] / plain["value"]},
         "observable_error": obs,
         "reference_equivalent": {"flops_per_traj_step": ref_flops,

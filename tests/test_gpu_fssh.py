@@ -131,13 +131,16 @@ def test_spinboson_fp64_bitwise():
     np.testing.assert_allclose(eng["popcorr"] / ntraj * ntraj, orc["popcorr"], rtol=1e-12, atol=1e-14)
 
 
-def test_tully_fp32_observables():
-    # fast path: scattering probabilities within 3 sigma of the FP64 result
+@pytest.mark.parametrize("model,rescaling,p0", [(1, 0, 10.0), (2, 1, 12.0), (3, 2, 15.0), (2, 0, 25.0)])
+def test_tully_fp32_observables(model, rescaling, p0):
+    # fast path (FP32 step loop with Kahan-compensated position and velocity):
+    # scattering probabilities within 3 sigma of the FP64 result, every
+    # rescaling mode (standard, velocity inversion, none)
     ntraj, m = 8192, 2000.0
     r0 = np.full((ntraj, 1), -10.0)
-    v0 = np.full((ntraj, 1), 10.0 / m)
-    cfg64, k64 = make_cfg(1, TULLY[1], 1, m, ntraj)
-    cfg32, k32 = make_cfg(1, TULLY[1], 1, m, ntraj, precision=L.PREC_FP32)
+    v0 = np.full((ntraj, 1), p0 / m)
+    cfg64, k64 = make_cfg(model, TULLY[model], 1, m, ntraj, rescaling=rescaling)
+    cfg32, k32 = make_cfg(model, TULLY[model], 1, m, ntraj, precision=L.PREC_FP32, rescaling=rescaling)
     a = run_engine(cfg64, k64, r0, v0, 0.0, 3000.0, 1.0, 42, 1)
     b = run_engine(cfg32, k32, r0, v0, 0.0, 3000.0, 1.0, 42, 1)
     p = a["scatter"]
