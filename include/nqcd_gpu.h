@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 101
+#define NQCD_ABI_VERSION 102
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -43,7 +43,16 @@ enum nqcd_status {
     NQCD_ERR_STATE = -7        /* call out of order (e.g. run before set_initial) */
 };
 
-enum nqcd_method { NQCD_METHOD_FSSH = 1, NQCD_METHOD_RPSH = 2, NQCD_METHOD_IESH = 3, NQCD_METHOD_MDEF = 4 };
+enum nqcd_method {
+    NQCD_METHOD_FSSH = 1,
+    NQCD_METHOD_RPSH = 2,
+    NQCD_METHOD_IESH = 3,
+    NQCD_METHOD_MDEF = 4,
+    NQCD_METHOD_EHRENFEST = 5 /* Simulation{Ehrenfest} (EhrenfestMethods/ehrenfest.jl): the FSSH integrator
+                                (BABwithTsit5) with the mean-field force -sum_nm (Z^T dH Z)_nm Re sigma_nm of
+                                the step's initial density matrix and no hopping; two-state models.
+                                Scattering outputs are the populations diag(Re sigma) summed by side. */
+};
 
 enum nqcd_model {
     NQCD_MODEL_TULLY1 = 1,    /* params: A, B, C, D */

@@ -18,6 +18,7 @@ struct FsshParams {
     double sum_c2_over_m;     // sum_j c_j^2 / m_j (spin-boson fast path)
     // method
     int32_t rescaling;
+    int32_t ehrenfest;        // 1: Ehrenfest (mean-field force from sigma, no hopping), 0: FSSH
     int32_t init_kind;
     int32_t init_state;
     float gap_fp64;           // fast path: FP64 electronics below this adiabatic gap

@@ -49,9 +49,13 @@ __device__ __forceinline__ void warp_save_popcorr(const FsshParams& p, int isave
 
 // diag(U sigma' U^T), sigma' = Re(sigma) with diagonal replaced by the
 // occupied state (fssh.jl:300-310).
+// Ehrenfest (ehrenfest.jl:79-89): the density matrix itself on the diagonal.
 template <typename R>
-__device__ __forceinline__ void diabatic_pop2(const Sig2<R>& sg, int s, const R Z[4], double pop[2]) {
-    double sp00 = s == 0 ? 1.0 : 0.0, sp11 = s == 1 ? 1.0 : 0.0, sp01 = (double)sg.x;
+__device__ __forceinline__ void diabatic_pop2(const Sig2<R>& sg, int s, const R Z[4], double pop[2],
+                                              bool ehrenfest = false) {
+    double sp00 = ehrenfest ? (double)sg.p : (s == 0 ? 1.0 : 0.0);
+    double sp11 = ehrenfest ? (double)sg.q : (s == 1 ? 1.0 : 0.0);
+    double sp01 = (double)sg.x;
     double U00 = Z[0], U10 = Z[1], U01 = Z[2], U11 = Z[3];
     double M00 = U00 * sp00 + U01 * sp01;
     double M01 = U00 * sp01 + U01 * sp11;
@@ -59,6 +63,20 @@ __device__ __forceinline__ void diabatic_pop2(const Sig2<R>& sg, int s, const R 
     double M11 = U10 * sp01 + U11 * sp11;
     pop[0] = M00 * U00 + M01 * U01;
     pop[1] = M10 * U10 + M11 * U11;
+}
+
+// Ehrenfest force weight (ehrenfest.jl:50-69): sum_m sum_n A_nm Re sigma_nm
+// for a symmetric 2x2 A = (A00, A01, A11), in the reference's loop order
+// (m outer, n inner); Re sigma_10 = Re sigma_01 = x.
+template <typename R>
+__device__ __forceinline__ R ehrenfest_weight(R A00, R A01, R A11, const Sig2<R>& sg) {
+    return ((A00 * sg.p + A01 * sg.x) + A01 * sg.x) + A11 * sg.q;
+}
+
+// Ehrenfest potential energy (ehrenfest.jl:92-101): sum_i Re sigma_ii E_i.
+template <typename R>
+__device__ __forceinline__ double ehrenfest_potential(const Sig2<R>& sg, const R w[2]) {
+    return (double)sg.p * (double)w[0] + (double)sg.q * (double)w[1];
 }
 
 // Initial electronic variables: adiabatic pure state, or a diabatic pure
@@ -177,8 +195,10 @@ struct AccKahan {
 
 // FP32 form of diabatic_pop2 and of the warp sum of the population products
 // (fast paths): no FP64 arithmetic in the step loop.
-__device__ __forceinline__ void diabatic_pop2_f(const Sig2<float>& sg, int s, const float Z[4], float pop[2]) {
-    const float sp00 = s == 0 ? 1.f : 0.f, sp11 = s == 1 ? 1.f : 0.f, sp01 = sg.x;
+__device__ __forceinline__ void diabatic_pop2_f(const Sig2<float>& sg, int s, const float Z[4], float pop[2],
+                                                bool ehrenfest = false) {
+    const float sp00 = ehrenfest ? sg.p : (s == 0 ? 1.f : 0.f), sp11 = ehrenfest ? sg.q : (s == 1 ? 1.f : 0.f);
+    const float sp01 = sg.x;
     const float M00 = Z[0] * sp00 + Z[2] * sp01, M01 = Z[0] * sp01 + Z[2] * sp11;
     const float M10 = Z[1] * sp00 + Z[3] * sp01, M11 = Z[1] * sp01 + Z[3] * sp11;
     pop[0] = M00 * Z[0] + M01 * Z[2];
@@ -255,22 +275,25 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         adiabatic_derivative2<R>(D, Z, A);
         nac = A[1] / (w[1] - w[0]);
     };
-    auto accel = [&](int s) -> double {
-        R a = s == 0 ? A[0] : A[2];
-        return (double)(-a / (R)mass);
-    };
-
-    update_cache(x);
     Sig2<R> sg;
     int state;
+    const bool ehr = p.ehrenfest != 0;
+    // FSSH: force of the occupied state; Ehrenfest: of the current density matrix
+    auto accel = [&](int s) -> double {
+        R a = ehr ? ehrenfest_weight<R>(A[0], A[1], A[2], sg) : (s == 0 ? A[0] : A[2]);
+        return (double)(-a / (R)mass);
+    };
+    auto pot = [&]() { return ehr ? ehrenfest_potential<R>(sg, w) : (double)w[state]; };
+
+    update_cache(x);
     init_electronics2<R>(p, i, gid, Z, sg, state);
     double k = accel(state);
 
-    double e0 = (0.0 + mass * (v * v)) / 2.0 + (double)w[state];
+    double e0 = (0.0 + mass * (v * v)) / 2.0 + pot();
     double pop0[2] = {0.0, 0.0};
     int isave = 0;
     if (p.save_stride > 0) {
-        diabatic_pop2<R>(sg, state, Z, pop0);
+        diabatic_pop2<R>(sg, state, Z, pop0, ehr);
         warp_save_popcorr(p, isave++, active, pop0, pop0);
     }
 
@@ -314,7 +337,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         R nsm = s == 0 ? nac : -nac;
         R prob = clamp01<R>(R(0) + R(2) * (R)v * re * nsm * dtR);
         double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
-        if ((double)prob > u) {
+        if (!ehr && (double)prob > u) {  // Ehrenfest: no hopping
             const int ns = 1 - s;
             bool accept = true;
             if (p.rescaling != RESCALE_OFF) {
@@ -347,11 +370,11 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         if (p.save_stride > 0 && step % p.save_stride == 0) {
             if constexpr (IsFast<R>::value) {
                 float pf[2], p0f[2] = {(float)pop0[0], (float)pop0[1]};
-                diabatic_pop2_f(sg, state, Z, pf);
+                diabatic_pop2_f(sg, state, Z, pf, ehr);
                 warp_save_popcorr_f(p, isave++, active, p0f, pf);
             } else {
                 double pop[2];
-                diabatic_pop2<R>(sg, state, Z, pop);
+                diabatic_pop2<R>(sg, state, Z, pop, ehr);
                 warp_save_popcorr(p, isave++, active, pop0, pop);
             }
         }
@@ -367,7 +390,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
     if (p.nsteps) p.nsteps[i] = step;
     if (p.energy) {
         p.energy[i] = e0;
-        p.energy[p.ntraj + i] = (0.0 + mass * (v * v)) / 2.0 + (double)w[state];
+        p.energy[p.ntraj + i] = (0.0 + mass * (v * v)) / 2.0 + pot();
     }
     if (p.scatter) atomicAdd(p.scatter + (x > 0.0 ? 2 : 0) + state, 1ull);
 }
@@ -408,19 +431,24 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
         adiabatic_derivative2<float>(D, Z, A);
         nac = A[1] / (w[1] - w[0]);
     };
-    auto accel = [&](int s) -> float { return -(s == 0 ? A[0] : A[2]) * inv_mass; };
-
-    update_cache(x.f());
     Sig2<float> sg;
     int state;
+    const bool ehr = p.ehrenfest != 0;
+    // FSSH: force of the occupied state; Ehrenfest: of the current density matrix
+    auto accel = [&](int s) -> float {
+        return -(ehr ? ehrenfest_weight<float>(A[0], A[1], A[2], sg) : (s == 0 ? A[0] : A[2])) * inv_mass;
+    };
+    auto pot = [&]() { return ehr ? ehrenfest_potential<float>(sg, w) : (double)(state == 0 ? w[0] : w[1]); };
+
+    update_cache(x.f());
     init_electronics2<float>(p, i, gid, Z, sg, state);
     float k = accel(state);
     const double v0 = v.get();
-    const double e0 = (0.0 + mass * (v0 * v0)) / 2.0 + (double)(state == 0 ? w[0] : w[1]);
+    const double e0 = (0.0 + mass * (v0 * v0)) / 2.0 + pot();
     float pop0[2] = {0.f, 0.f};
     int isave = 0;
     if (p.save_stride > 0) {
-        diabatic_pop2_f(sg, state, Z, pop0);
+        diabatic_pop2_f(sg, state, Z, pop0, ehr);
         warp_save_popcorr_f(p, isave++, active, pop0, pop0);
     }
 
@@ -450,7 +478,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
         const float nsm = s == 0 ? nac : -nac;
         const float prob = clamp01<float>(2.0f * v.f() * re * nsm * dtf);
         const float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
-        if (prob > u) {
+        if (!ehr && prob > u) {  // Ehrenfest: no hopping
             const int ns = 1 - s;
             bool accept = true;
             if (p.rescaling != RESCALE_OFF) {
@@ -482,7 +510,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
         }
         if (p.save_stride > 0 && step % p.save_stride == 0) {
             float pf[2];
-            diabatic_pop2_f(sg, state, Z, pf);
+            diabatic_pop2_f(sg, state, Z, pf, ehr);
             warp_save_popcorr_f(p, isave++, active, pop0, pf);
         }
     }
@@ -498,7 +526,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
     if (p.nsteps) p.nsteps[i] = step;
     if (p.energy) {
         p.energy[i] = e0;
-        p.energy[p.ntraj + i] = (0.0 + mass * (vf * vf)) / 2.0 + (double)(state == 0 ? w[0] : w[1]);
+        p.energy[p.ntraj + i] = (0.0 + mass * (vf * vf)) / 2.0 + pot();
     }
     if (p.scatter) atomicAdd(p.scatter + (xf > 0.0 ? 2 : 0) + state, 1ull);
 }
@@ -551,6 +579,16 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         R z0 = Zk[2 * s], z1 = Zk[2 * s + 1];
         return z0 * (d00 * z0) + z1 * (d11 * z1);
     };
+    // Ehrenfest: sum_nm (Z^T dH_I Z)_nm Re sigma_nm, elements in oracle order
+    auto adi_ehr = [&](const R Zk[4], const Sig2<R>& sgk, double rI, int I) -> R {
+        R d0 = (R)(w2j[I] * rI);
+        R d00 = d0 + (R)cj[I], d11 = d0 - (R)cj[I];
+        R A00 = Zk[0] * (d00 * Zk[0]) + Zk[1] * (d11 * Zk[1]);
+        R A11 = Zk[2] * (d00 * Zk[2]) + Zk[3] * (d11 * Zk[3]);
+        R A01 = Zk[0] * (d00 * Zk[2]) + Zk[1] * (d11 * Zk[3]);
+        return ehrenfest_weight<R>(A00, A01, A11, sgk);
+    };
+    const bool ehr = p.ehrenfest != 0;
 
     double s0 = 0.0, cr = 0.0, ke = 0.0;
     for (int I = 0; I < nd; ++I) {
@@ -564,14 +602,15 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
     Sig2<R> sg;
     int state;
     init_electronics2<R>(p, i, gid, Z, sg, state);
-    double e0 = ke / 2.0 + (double)w[state];
+    double e0 = ke / 2.0 + (ehr ? ehrenfest_potential<R>(sg, w) : (double)w[state]);
     R Zk[4] = {Z[0], Z[1], Z[2], Z[3]};  // eigenvectors the cached force was computed with
     int sk = state;                      // state the cached force was computed for
+    Sig2<R> sgk = sg;                    // Ehrenfest: density matrix the cached force was computed with
 
     double pop0[2] = {0.0, 0.0};
     int isave = 0;
     if (p.save_stride > 0) {
-        diabatic_pop2<R>(sg, state, Z, pop0);
+        diabatic_pop2<R>(sg, state, Z, pop0, ehr);
         warp_save_popcorr(p, isave++, active, pop0, pop0);
     }
 
@@ -587,7 +626,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         for (int I = 0; I < nd; ++I) {
             double rI = r[(int64_t)I * N];
             double vI = v[(int64_t)I * N];
-            double kI = (double)(-adi_ss(Zk, sk, rI, I) / (R)mj[I]);
+            double kI = (double)(-(ehr ? adi_ehr(Zk, sgk, rI, I) : adi_ss(Zk, sk, rI, I)) / (R)mj[I]);
             double vt = vI + half * kI;
             double rn = rI + h * vt;
             if (active) {
@@ -610,9 +649,10 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
                 double vt = v[(int64_t)I * N];
                 double d0 = w2j[I] * rI;
                 double d00 = d0 + cj[I], d11 = d0 - cj[I];
-                double ass = state == 0 ? Z[0] * (d00 * Z[0]) + Z[1] * (d11 * Z[1])
-                                        : Z[2] * (d00 * Z[2]) + Z[3] * (d11 * Z[3]);
+                double a00 = Z[0] * (d00 * Z[0]) + Z[1] * (d11 * Z[1]);
+                double a11 = Z[2] * (d00 * Z[2]) + Z[3] * (d11 * Z[3]);
                 double a01 = Z[0] * (d00 * Z[2]) + Z[1] * (d11 * Z[3]);
+                double ass = ehr ? ehrenfest_weight<double>(a00, a01, a11, sg) : (state == 0 ? a00 : a11);
                 double kI = -ass / mj[I];
                 double vn = vt + half * kI;
                 double nI = a01 / (w[1] - w[0]);
@@ -624,7 +664,8 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
             }
             Dn = 0.0 + acc;
         } else {
-            const float Mss = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];
+            const float M00 = Z[0] * Z[0] - Z[1] * Z[1], M11 = Z[2] * Z[2] - Z[3] * Z[3];
+            const float Mss = ehr ? ehrenfest_weight<float>(M00, (float)M01, M11, sg) : (state == 0 ? M00 : M11);
             for (int I = 0; I < nd; ++I) {
                 double rI = r[(int64_t)I * N];
                 double vt = v[(int64_t)I * N];
@@ -640,6 +681,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         Zk[2] = Z[2];
         Zk[3] = Z[3];
         sk = state;
+        sgk = sg;
         buf.E0c = buf.E0n;
         buf.E1c = buf.E1n;
         buf.Dc = buf.Dn;
@@ -670,7 +712,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
             prob = clamp01<float>(2.0f * re * nsm * (float)p.dt);
         }
         double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
-        if ((double)prob > u) {
+        if (!ehr && (double)prob > u) {  // Ehrenfest: no hopping
             const int ns = 1 - s;
             const double sgn = ns < s ? 1.0 : -1.0;  // d(new, old) = sgn * d01
             bool accept = true;
@@ -733,7 +775,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         }
         if (p.save_stride > 0 && step % p.save_stride == 0) {
             double pop[2];
-            diabatic_pop2<R>(sg, state, Z, pop);
+            diabatic_pop2<R>(sg, state, Z, pop, ehr);
             warp_save_popcorr(p, isave++, active, pop0, pop);
         }
     }
@@ -751,7 +793,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
             ke1 = ke1 + mj[I] * (vI * vI);
         }
         p.energy[i] = e0;
-        p.energy[N + i] = ke1 / 2.0 + (double)w[state];
+        p.energy[N + i] = ke1 / 2.0 + (ehr ? ehrenfest_potential<R>(sg, w) : (double)w[state]);
     }
     if (p.scatter) atomicAdd(p.scatter + (r[0] > 0.0 ? 2 : 0) + state, 1ull);
 }

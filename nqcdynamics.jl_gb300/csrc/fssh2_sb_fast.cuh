@@ -37,7 +37,10 @@ __device__ __forceinline__ float group_sum(float x) {
 constexpr int kSbFastBlock = 128;
 constexpr int kSbGroup = 4;
 
-template <typename Acc, int NPL>
+// Ehr = true: Ehrenfest (mean-field force from the density matrix, no
+// hopping); a template parameter so that the surface-hopping instantiation
+// keeps its register allocation.
+template <typename Acc, int NPL, bool Ehr>
 __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshParams p) {
     constexpr int G = kSbGroup;
     extern __shared__ float4 bath[];  // (c, w2, 1/m, c^2/m) per mode
@@ -100,14 +103,22 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
     Sig2<float> sg;
     int state;
     init_electronics2<float>(p, i, gid, Z, sg, state);
-    double e0 = 0.5 * (double)ke + (double)w[state];
-    float Mk = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];  // M_ss of the cached force
+    constexpr bool ehr = Ehr;
+    // weight of the coupling force c_I in the cached force: M_ss (FSSH) or
+    // sum_nm M_nm Re sigma_nm (Ehrenfest), M = Z^T sigma_z Z
+    auto force_weight = [&]() {
+        const float M00 = Z[0] * Z[0] - Z[1] * Z[1], M11 = Z[2] * Z[2] - Z[3] * Z[3];
+        return ehr ? ehrenfest_weight<float>(M00, Z[0] * Z[2] - Z[1] * Z[3], M11, sg) : (state == 0 ? M00 : M11);
+    };
+    auto pot = [&]() { return ehr ? ehrenfest_potential<float>(sg, w) : (double)w[state]; };
+    double e0 = 0.5 * (double)ke + pot();
+    float Mk = force_weight();
 
     float pop0[2] = {0.f, 0.f};
     int isave = 0;
     const bool lead = lane_g == 0;
     if (p.save_stride > 0) {
-        diabatic_pop2_f(sg, state, Z, pop0);
+        diabatic_pop2_f(sg, state, Z, pop0, ehr);
         warp_save_popcorr_f(p, isave++, active && lead, pop0, pop0);
     }
 
@@ -141,7 +152,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
         set_eigen(s0, cr);
         const float gap = w[1] - w[0];
         const float M01 = Z[0] * Z[2] - Z[1] * Z[3];
-        Mk = state == 0 ? Z[0] * Z[0] - Z[1] * Z[1] : Z[2] * Z[2] - Z[3] * Z[3];
+        Mk = force_weight();
         // B with the new force; c.v
         cv = 0.f;
 #pragma unroll
@@ -169,7 +180,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
         float nsm = (s == 0 ? 1.0f : -1.0f) * cv * dscale;
         float prob = clamp01<float>(2.0f * re * nsm * dtf);
         float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
-        if (prob > u) {
+        if (!ehr && prob > u) {  // Ehrenfest: no hopping
             const int ns = 1 - s;
             const float sgn = ns < s ? 1.0f : -1.0f;  // d(new, old) = sgn * c_I * dscale
             bool accept = true;
@@ -209,7 +220,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
         }
         if (p.save_stride > 0 && step % p.save_stride == 0) {
             float pop[2];
-            diabatic_pop2_f(sg, state, Z, pop);
+            diabatic_pop2_f(sg, state, Z, pop, ehr);
             warp_save_popcorr_f(p, isave++, active && lead, pop0, pop);
         }
     }
@@ -239,7 +250,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
     if (p.nsteps) p.nsteps[i] = step;
     if (p.energy) {
         p.energy[i] = e0;
-        p.energy[N + i] = 0.5 * (double)ke + (double)w[state];
+        p.energy[N + i] = 0.5 * (double)ke + pot();
     }
     if (p.scatter) atomicAdd(p.scatter + (p.r[i] > 0.0 ? 2 : 0) + state, 1ull);
 }
@@ -249,7 +260,10 @@ cudaError_t launch_sb_fast_npl(const FsshParams& p, cudaStream_t s) {
     int64_t threads = p.ntraj * kSbGroup;
     int64_t blocks = (threads + kSbFastBlock - 1) / kSbFastBlock;
     size_t shmem = sizeof(float4) * kSbGroup * NPL;
-    fssh2_sb_fast_kernel<Acc, NPL><<<(unsigned)blocks, kSbFastBlock, shmem, s>>>(p);
+    if (p.ehrenfest)
+        fssh2_sb_fast_kernel<Acc, NPL, true><<<(unsigned)blocks, kSbFastBlock, shmem, s>>>(p);
+    else
+        fssh2_sb_fast_kernel<Acc, NPL, false><<<(unsigned)blocks, kSbFastBlock, shmem, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -99,6 +99,22 @@ __global__ void reduce_partials_kernel(const double* __restrict__ partial, int64
     out[k] = acc;
 }
 
+// Ehrenfest state-resolved scattering (OutputStateResolvedScattering1D with
+// the adiabatic populations diag(Re sigma), ehrenfest.jl:74-77): per
+// trajectory (reflected p, reflected q, transmitted p, transmitted q), summed
+// afterwards by the fixed-order partial reduction.
+__global__ void ehrenfest_scatter_kernel(const double* __restrict__ r, const double* __restrict__ sigma, int64_t n,
+                                         double* __restrict__ part) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const bool tr = r[i] > 0.0;
+        const double p0 = sigma[i], p1 = sigma[6 * n + i];
+        part[4 * i + 0] = tr ? 0.0 : p0;
+        part[4 * i + 1] = tr ? 0.0 : p1;
+        part[4 * i + 2] = tr ? p0 : 0.0;
+        part[4 * i + 3] = tr ? p1 : 0.0;
+    }
+}
+
 // Run statistics: steps, hops, frustrated hops, non-finite trajectories.
 __global__ void stats_kernel(const int32_t* nsteps, const int32_t* nhops, const int32_t* nfrust,
                              const double* r, const double* v, int64_t ndof, int64_t ntraj,
@@ -326,7 +342,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     if (!cfg || !out) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: null argument");
     *out = nullptr;
     if (cfg->method != NQCD_METHOD_FSSH && cfg->method != NQCD_METHOD_RPSH && cfg->method != NQCD_METHOD_MDEF &&
-        cfg->method != NQCD_METHOD_IESH)
+        cfg->method != NQCD_METHOD_IESH && cfg->method != NQCD_METHOD_EHRENFEST)
         return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: method not supported by this build");
     const bool rp = cfg->method == NQCD_METHOD_RPSH;
     const bool mdef = cfg->method == NQCD_METHOD_MDEF;
@@ -621,7 +637,8 @@ static int set_initial_common(nqcd_handle* h, int64_t ntraj, const double* sig_r
                               const int32_t* state0, int64_t* h2d) {
     const int64_t N = ntraj;
     // MDEF carries no electronic state: only FSSH and RPSH read sigma and state0
-    const bool two_state = h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH;
+    const bool two_state = h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH ||
+                           h->cfg.method == NQCD_METHOD_EHRENFEST;
     if (h->cfg.method == NQCD_METHOD_IESH && h->cfg.init_kind == NQCD_INIT_GIVEN) {
         // occupations (nelectrons, ntraj) column-major -> device [electron][trajectory]
         if (!state0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: IESH with NQCD_INIT_GIVEN needs the occupations in state0");
@@ -737,6 +754,19 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     }
     cudaStream_t s = h->stream;
     int launches = 0;
+    if (h->cfg.method == NQCD_METHOD_EHRENFEST && out && out->scattering) {
+        // population-sum buffers of the Ehrenfest scattering output
+        int rc = ensure_stage(h, 4 * N + 4);
+        if (rc) return rc;
+        const int64_t need = reduce_chunks(N, 4) * 4;
+        if (need > h->redtmp_cap) {
+            if (h->d_redtmp) cudaFree(h->d_redtmp);
+            h->d_redtmp = nullptr;
+            h->redtmp_cap = 0;
+            NQCD_CUDA(h, dalloc(&h->d_redtmp, need));
+            h->redtmp_cap = need;
+        }
+    }
     NQCD_CUDA(h, cudaEventRecord(h->ev0, s));
     const int64_t nd = h->ndof;
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_r, h->d_r0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -761,6 +791,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.bath_w2 = h->d_bath_w2;
     p.sum_c2_over_m = h->sum_c2_over_m;
     p.rescaling = h->cfg.rescaling;
+    p.ehrenfest = h->cfg.method == NQCD_METHOD_EHRENFEST ? 1 : 0;
     p.init_kind = h->cfg.init_kind;
     p.init_state = h->cfg.init_state;
     p.gap_fp64 = (float)h->cfg.gap_fp64;
@@ -805,7 +836,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.hop_log = h->d_hoplog;
     p.energy = h->d_energy;
     p.popcorr_partial = h->d_partial;
-    p.scatter = h->d_counts;
+    p.scatter = p.ehrenfest ? nullptr : h->d_counts;  // Ehrenfest: population sums after the run
     cudaError_t e = cudaSuccess;
     int64_t h2d = 0;
     if (h->cfg.method == NQCD_METHOD_RPSH) {
@@ -1028,6 +1059,17 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         h->d_nsteps, h->d_nhops, h->d_nfrust, h->d_r, h->d_v, nd, N, h->d_counts + 4);
     NQCD_CUDA(h, cudaGetLastError());
     ++launches;
+    // Ehrenfest scattering: population sums in a fixed order (buffers sized before the run)
+    const bool ehr_scatter = h->cfg.method == NQCD_METHOD_EHRENFEST && out && out->scattering;
+    double esc[4] = {0.0, 0.0, 0.0, 0.0};
+    if (ehr_scatter) {
+        ehrenfest_scatter_kernel<<<(unsigned)((N + 255) / 256 < 1024 ? (N + 255) / 256 : 1024), 256, 0, s>>>(
+            h->d_r, h->d_sig, N, h->d_stage);
+        NQCD_CUDA(h, cudaGetLastError());
+        NQCD_CUDA(h, launch_reduce_partials(h->d_stage, N, 4, h->d_redtmp, h->d_stage + 4 * N, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(esc, h->d_stage + 4 * N, sizeof(esc), cudaMemcpyDeviceToHost, s));
+        launches += 3;
+    }
     NQCD_CUDA(h, cudaEventRecord(h->ev1, s));
 
     unsigned long long counts[16];
@@ -1047,7 +1089,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     if (out) {
         out->nsave = nsave;
         if (out->scattering)
-            for (int q = 0; q < 4; ++q) out->scattering[q] = (double)counts[q] / (double)N;
+            for (int q = 0; q < 4; ++q)
+                out->scattering[q] = (ehr_scatter ? esc[q] : (double)counts[q]) / (double)N;
         double* dst = (mdef || iesh) ? out->observables : out->population_correlation;
         if (dst && nsave > 0)
             for (int k = 0; k < nsave * 4; ++k) dst[k] = pc[k] / (double)N;

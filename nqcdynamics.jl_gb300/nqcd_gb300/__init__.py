@@ -24,6 +24,7 @@ from .api import (
     Atoms,
     Diabatic,
     DynamicalDistribution,
+    Ehrenfest,
     EnsembleGB300,
     EnsembleSerial,
     EnsembleThreads,

@@ -4,6 +4,7 @@ Names, argument meanings and error behaviour follow the reference:
 
   Atoms, TullyModelOne/Two/Three, SpinBoson + OhmicSpectralDensity   (NQCModels / NQCBase)
   Simulation[FSSH](atoms, model; rescaling)       src/simulations.jl:12-44, fssh.jl:206-213
+  Simulation[Ehrenfest](atoms, model)             EhrenfestMethods/ehrenfest.jl:41-43
   RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)   simulations.jl:46-73, rpsh.jl:5-7
   Simulation[DiabaticMDEF](atoms, model; friction_method, temperature)   mdef.jl:79-100
   Simulation[AdiabaticIESH](atoms, model; rescaling, estimate_probability)   iesh.jl:72-87
@@ -234,6 +235,11 @@ class FSSH:
             raise ValueError(f"rescaling {self.rescaling!r} not recognised (standard, vinversion, off)")
 
 
+class Ehrenfest:
+    """Mean-field (Ehrenfest) dynamics on a two-state model (ehrenfest.jl):
+    the FSSH integrator with the force of the density matrix and no hops."""
+
+
 class DiabaticMDEF:
     """Electronic friction Langevin dynamics on a diabatic model (mdef.jl)."""
 
@@ -285,9 +291,12 @@ class Simulation(metaclass=_MethodIndexed):
                 raise ValueError("one adsorbate atom with three degrees of freedom")
             self.method = AdiabaticIESH(rescaling, estimate_probability)
             return
-        if method is not FSSH:
+        if method is Ehrenfest:
+            self.method = Ehrenfest()
+        elif method is FSSH:
+            self.method = FSSH(rescaling)
+        else:
             raise NotImplementedError(f"method {method} is not on the GPU path")
-        self.method = FSSH(rescaling)
         if isinstance(model, SpinBoson):
             if len(atoms) != model.N:
                 raise ValueError("SpinBoson needs one atom per bath mode")
@@ -530,10 +539,11 @@ def _output_name(o):
 def build_config(sim, electronic: PureState, ntraj: int, alg: EnsembleGB300, save_stride: int):
     model = sim.model
     cfg = L.nqcd_config()
-    cfg.method = L.METHOD_FSSH
+    ehrenfest = isinstance(sim.method, Ehrenfest)
+    cfg.method = L.METHOD_EHRENFEST if ehrenfest else L.METHOD_FSSH
     cfg.model = model.kind
     cfg.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32, "fp32_kahan": L.PREC_FP32_KAHAN}[alg.precision]
-    cfg.rescaling = L.RESCALE[sim.method.rescaling]
+    cfg.rescaling = 0 if ehrenfest else L.RESCALE[sim.method.rescaling]
     cfg.ndofs = model.ndofs
     cfg.natoms = len(sim.atoms)
     cfg.nstates = model.nstates

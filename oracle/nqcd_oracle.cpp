@@ -148,6 +148,28 @@ void acceleration(const Cache& c, int ndof, const double* mass, int s, double* k
     for (int I = 0; I < ndof; ++I) k[I] = -adi_elem(c, I, s, s) / mass[I];
 }
 
+// Ehrenfest acceleration (ehrenfest.jl:50-69): a_I = -sum_m sum_n
+// (Z^T dH_I Z)_nm Re sigma_nm / m_I, the sum in the reference's loop order
+// (m outer, n inner); the models here have no separate state-independent
+// derivative (the spin-boson bath term is on the diagonal of dH_I).
+void acceleration_ehrenfest(const Cache& c, int ndof, const double* mass, const cx sig[NS][NS], double* k) {
+    for (int I = 0; I < ndof; ++I) {
+        double acc = adi_elem(c, I, 0, 0) * sig[0][0].re;
+        for (int q = 1; q < NS * NS; ++q) {
+            const int mm = q / NS, n = q % NS;
+            acc = acc + adi_elem(c, I, n, mm) * sig[n][mm].re;
+        }
+        k[I] = -acc / mass[I];
+    }
+}
+
+// Ehrenfest potential energy (ehrenfest.jl:92-101): sum_i Re sigma_ii E_i.
+double ehrenfest_potential(const Cache& c, const cx sig[NS][NS]) {
+    double pe = sig[0][0].re * c.w[0];
+    for (int i = 1; i < NS; ++i) pe = pe + sig[i][i].re * c.w[i];
+    return pe;
+}
+
 // ---------------------------------------------------------------------------
 // Electronic density-matrix ODE (electronic_dynamics.jl:106-221)
 // ---------------------------------------------------------------------------
@@ -297,13 +319,17 @@ bool rescale_velocity(const oracle_fssh_args& a, Traj& tr, const double* mass, i
     return true;
 }
 
-// diabatic population of FSSH (fssh.jl:300-310): diag(U sigma' U^T)
-void diabatic_population(const Traj& tr, double pop[NS]) {
+// diabatic population of FSSH (fssh.jl:300-310): diag(U sigma' U^T) with the
+// occupied state on the diagonal of sigma'; Ehrenfest (ehrenfest.jl:79-89):
+// sigma' = Re sigma.
+void diabatic_population(const Traj& tr, double pop[NS], bool ehrenfest = false) {
     double sp[NS][NS];
     for (int i = 0; i < NS; ++i)
         for (int j = 0; j < NS; ++j) sp[i][j] = tr.sig[i][j].re;
-    for (int i = 0; i < NS; ++i) sp[i][i] = 0.0;
-    sp[tr.state][tr.state] = 1.0;
+    if (!ehrenfest) {
+        for (int i = 0; i < NS; ++i) sp[i][i] = 0.0;
+        sp[tr.state][tr.state] = 1.0;
+    }
     double U[NS][NS] = {{tr.cache.Z[0], tr.cache.Z[2]}, {tr.cache.Z[1], tr.cache.Z[3]}};
     double M[NS][NS];
     for (int i = 0; i < NS; ++i)
@@ -391,16 +417,20 @@ void run_one_fssh(const oracle_fssh_args& a, const Model& m, int64_t it, oracle_
     // DensityMatrixODEProblem parameters start zeroed at t = 0 (electronic_dynamics.jl:209-218)
     memset(&tr.buf, 0, sizeof(tr.buf));
 
-    // initialize!: update_cache!(r); k = a(r, state)   (bab_electronics.jl:48-59)
+    // initialize!: update_cache!(r); k = a(r, state) or a(r, sigma)   (bab_electronics.jl:48-59)
+    const bool ehr = a.method == 1;
     update_cache(m, tr.r.data(), ndof, tr.cache);
     init_electronics(a, gid, tr);
-    acceleration(tr.cache, ndof, a.mass, tr.state, tr.k.data());
+    if (ehr)
+        acceleration_ehrenfest(tr.cache, ndof, a.mass, tr.sig, tr.k.data());
+    else
+        acceleration(tr.cache, ndof, a.mass, tr.state, tr.k.data());
 
-    double e0 = kinetic_energy(tr.v, a.mass) + tr.cache.w[tr.state];
+    double e0 = kinetic_energy(tr.v, a.mass) + (ehr ? ehrenfest_potential(tr.cache, tr.sig) : tr.cache.w[tr.state]);
     int nsave = 0;
     double pop0[NS];
     if (a.save_stride > 0) {
-        diabatic_population(tr, pop0);
+        diabatic_population(tr, pop0, ehr);
         for (int i = 0; i < NS; ++i)
             for (int j = 0; j < NS; ++j) part.popcorr[0 * 4 + 2 * i + j] += pop0[i] * pop0[j];
         nsave = 1;
@@ -417,13 +447,27 @@ void run_one_fssh(const oracle_fssh_args& a, const Model& m, int64_t it, oracle_
         for (int I = 0; I < ndof; ++I) tr.vtmp[I] = tr.v[I] + half * tr.k[I];
         for (int I = 0; I < ndof; ++I) tr.r[I] = tr.r[I] + h * tr.vtmp[I];
         update_cache(m, tr.r.data(), ndof, tr.cache);
-        acceleration(tr.cache, ndof, a.mass, tr.state, tr.k.data());
+        // Ehrenfest: the force of the density matrix the step starts with (sigma_prev)
+        if (ehr)
+            acceleration_ehrenfest(tr.cache, ndof, a.mass, tr.sig, tr.k.data());
+        else
+            acceleration(tr.cache, ndof, a.mass, tr.state, tr.k.data());
         for (int I = 0; I < ndof; ++I) tr.v[I] = tr.vtmp[I] + half * tr.k[I];
         update_parameters(tr.buf, tr.cache, ndof, tr.v.data(), t + h);
         electronic_macro_step(tr.buf, t, h, dtsub, tr.sig);
         t = nqcd::snap_time(t + h, a.t1);
         step += 1;
 
+        if (ehr) {  // no hopping callback
+            if (a.save_stride > 0 && step % a.save_stride == 0) {
+                double pop[NS];
+                diabatic_population(tr, pop, true);
+                for (int i = 0; i < NS; ++i)
+                    for (int j = 0; j < NS; ++j) part.popcorr[nsave * 4 + 2 * i + j] += pop0[i] * pop[j];
+                nsave += 1;
+            }
+            continue;
+        }
         // HoppingCallback (surface_hopping.jl:2-16, fssh.jl:254-289)
         double prob[NS] = {0.0, 0.0};
         const int s = tr.state;
@@ -475,13 +519,17 @@ void run_one_fssh(const oracle_fssh_args& a, const Model& m, int64_t it, oracle_
     if (o->nsteps) o->nsteps[it] = step;
     if (o->energy) {
         o->energy[2 * it] = e0;
-        o->energy[2 * it + 1] = kinetic_energy(tr.v, a.mass) + tr.cache.w[tr.state];
+        o->energy[2 * it + 1] =
+            kinetic_energy(tr.v, a.mass) + (ehr ? ehrenfest_potential(tr.cache, tr.sig) : tr.cache.w[tr.state]);
     }
-    // OutputStateResolvedScattering1D, adiabatic populations (DynamicsOutputs.jl:313-338)
-    if (tr.r[0] > 0.0)
-        part.scatter[2 + tr.state] += 1.0;
-    else
-        part.scatter[tr.state] += 1.0;
+    // OutputStateResolvedScattering1D, adiabatic populations (DynamicsOutputs.jl:313-338):
+    // the occupied state (FSSH) or diag(Re sigma) (Ehrenfest, ehrenfest.jl:74-77)
+    const int side = tr.r[0] > 0.0 ? 2 : 0;
+    if (ehr) {
+        for (int i = 0; i < NS; ++i) part.scatter[side + i] += tr.sig[i][i].re;
+    } else {
+        part.scatter[side + tr.state] += 1.0;
+    }
 }
 
 

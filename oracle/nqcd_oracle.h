@@ -33,6 +33,7 @@ typedef struct {
     int32_t nbeads;         // ring polymer: beads per trajectory (RPSH entry only)
     double beta;            // ring polymer: inverse temperature
     double terminate_x;     // ring polymer: stop when |x_centroid| > terminate_x (0 = off)
+    int32_t method;         // 0 FSSH, 1 Ehrenfest (oracle_fssh_run only)
 } oracle_fssh_args;
 
 typedef struct {

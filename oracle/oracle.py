@@ -42,6 +42,7 @@ class oracle_fssh_args(C.Structure):
         ("nbeads", C.c_int32),
         ("beta", C.c_double),
         ("terminate_x", C.c_double),
+        ("method", C.c_int32),
     ]
 
 
@@ -138,10 +139,12 @@ def cayley(n: int, beta: float, dt: float) -> np.ndarray:
 
 def run_fssh(*, model, params, ndof, mass, r0, v0, t0, t1, dt, seed, rescaling=0, init_kind=1, init_state=0,
              sigma0=None, state0=None, bath_c=None, bath_w2=None, save_stride=0, max_hops=16,
-             nthreads=None, traj_offset=0):
-    """Run the oracle FSSH ensemble; returns a dict of final per-trajectory data."""
+             nthreads=None, traj_offset=0, ehrenfest=False):
+    """Run the oracle FSSH (or, with ehrenfest=True, Ehrenfest) ensemble;
+    returns a dict of final per-trajectory data."""
     ntraj = r0.shape[0]
     a = oracle_fssh_args()
+    a.method = 1 if ehrenfest else 0
     a.model = model
     for q, x in enumerate(params):
         a.params[q] = x

@@ -356,3 +356,74 @@ def test_iesh_dynamics_conserves_energy():
     for t in range(4):  # orbitals stay orthonormal
         g = res["psi"][t].conj().T @ res["psi"][t]
         assert np.abs(g - np.eye(10)).max() < 1e-10
+
+
+def _tully_vd(kind, x):
+    import ctypes as C
+
+    V, D, pp = np.zeros(3), np.zeros(3), np.zeros(8)
+    pp[: len(TULLY[kind])] = TULLY[kind]
+    dp = C.POINTER(C.c_double)
+    O.lib().oracle_tully(kind, pp.ctypes.data_as(dp), C.c_double(x), V.ctypes.data_as(dp), D.ctypes.data_as(dp))
+    return np.array([[V[0], V[1]], [V[1], V[2]]]), np.array([[D[0], D[1]], [D[1], D[2]]])
+
+
+def _ehrenfest_dop853(kind, m, x0, v0, t1):
+    """Independent high-accuracy Ehrenfest integration (the reference's test
+    compares its integrator with Feagin12 the same way), in the diabatic basis:
+    dc/dt = -i H(x) c, m dv/dt = -c^H dH/dx c, starting in the lower
+    adiabatic state; returns x, v and the final adiabatic populations."""
+    from scipy.integrate import solve_ivp
+
+    c0 = np.linalg.eigh(_tully_vd(kind, x0)[0])[1][:, 0].astype(complex)
+
+    def rhs(t, y):
+        H, dH = _tully_vd(kind, y[0])
+        c = y[2:4] + 1j * y[4:6]
+        dc = -1j * (H @ c)
+        return [y[1], -np.real(np.conj(c) @ dH @ c) / m, dc[0].real, dc[1].real, dc[0].imag, dc[1].imag]
+
+    y0 = [x0, v0, c0[0].real, c0[1].real, c0[0].imag, c0[1].imag]
+    y = solve_ivp(rhs, (0.0, t1), y0, method="DOP853", rtol=1e-12, atol=1e-13).y[:, -1]
+    c = y[2:4] + 1j * y[4:6]
+    Z = np.linalg.eigh(_tully_vd(kind, y[0])[0])[1]
+    return y[0], y[1], np.abs(Z.T @ c) ** 2
+
+
+def test_ehrenfest_reference_algorithm_comparison():
+    """test/Dynamics/ehrenfest.jl:40-66: Tully model 2, mass 2000, p = 100
+    from x = -10, t in [0, 50], dt = 2e-3 -- total energy conserved, and
+    position, velocity and populations equal to an independent high-accuracy
+    integration (the reference's tolerances: 1e-3 and 1e-1; met here to
+    1e-6)."""
+    pytest.importorskip("scipy")
+    m, x0, v0 = 2000.0, -10.0, 100.0 / 2000.0
+    res = O.run_fssh(model=2, params=TULLY[2], ndof=1, mass=m, r0=np.array([[x0]]), v0=np.array([[v0]]), t0=0.0,
+                     t1=50.0, dt=2e-3, seed=1, ehrenfest=True, nthreads=1)
+    assert res["sigma"][0, 0, 0].real == pytest.approx(np.abs(res["sigma"][0, 0, 0]))
+    e0, e1 = res["energy"][0]
+    assert abs(e1 - e0) < 1e-6
+    xe, ve, pe = _ehrenfest_dop853(2, m, x0, v0, 50.0)
+    assert res["r"][0, 0] == pytest.approx(xe, rel=1e-6)
+    assert res["v"][0, 0] == pytest.approx(ve, rel=1e-6)
+    assert res["sigma"][0, 0, 0].real == pytest.approx(pe[0], abs=1e-6)
+    assert res["nhops"][0] == 0
+
+
+@pytest.mark.parametrize("kind,p0,x0,t1", [(1, 20.0, -8.0, 1600.0), (2, 30.0, -8.0, 1100.0)])
+def test_ehrenfest_through_the_coupling_region(kind, p0, x0, t1):
+    """Ehrenfest (BAB + Tsit5 electronics, force from the step's initial
+    density matrix, ehrenfest.jl:50-69) through the avoided crossing at
+    dt = 0.1: second-order agreement with the high-accuracy integration."""
+    pytest.importorskip("scipy")
+    m = 2000.0
+    res = O.run_fssh(model=kind, params=TULLY[kind], ndof=1, mass=m, r0=np.array([[x0]]), v0=np.array([[p0 / m]]),
+                     t0=0.0, t1=t1, dt=0.1, seed=1, ehrenfest=True, nthreads=1)
+    xe, ve, pe = _ehrenfest_dop853(kind, m, x0, p0 / m, t1)
+    assert res["r"][0, 0] == pytest.approx(xe, rel=1e-4)
+    assert res["v"][0, 0] == pytest.approx(ve, rel=1e-4)
+    sig = res["sigma"][0]
+    assert sig[0, 0].real == pytest.approx(pe[0], abs=1e-4)
+    assert sig[1, 1].real == pytest.approx(pe[1], abs=1e-4)
+    assert 0.2 < pe[1] < 0.8  # a genuine population transfer
+    assert abs(res["energy"][0, 1] - res["energy"][0, 0]) < 1e-4 * res["energy"][0, 0]
