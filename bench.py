@@ -19,9 +19,10 @@ configuration's shapes (nqcd_gb300/workload.py).
 the host cores (the reference itself is Julia and cannot run here).
 
 --workload tully1|rpsh|mdef|iesh measures the other benchmark configurations
-(C1, C3, C4, C5; nqcd_gb300/configs.py) the same way: the chosen fast path on
-the full ensemble, the plain FP64 path, and the observable error between the
-two on a common subset.  These are records for the design notes; the default
+(C1, C3, C4, C5; nqcd_gb300/configs.py), and --workload ehrenfest the
+Ehrenfest method on the headline's spin-boson ensemble, the same way: the
+chosen fast path on the full ensemble, the plain FP64 path, and the
+observable error between the two on a common subset.  These are records for the design notes; the default
 run is the headline configuration.
 Multi-GPU (torchrun): each rank runs an independent replica shard of
 trajectories (global trajectory ids offset by rank); no collective on the
@@ -62,7 +63,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="spinboson", choices=["spinboson", "tully1", "rpsh", "mdef", "iesh"])
+    ap.add_argument("--workload", default="spinboson",
+                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest"])
     ap.add_argument("--nsteps", type=int, default=0, help="secondary workloads: nuclear steps of the fast path")
     return ap.parse_args()
 
@@ -164,9 +166,9 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # engine helpers
 # ---------------------------------------------------------------------------
-def make_engine(L, prec, w, c, ntraj, nmodes, save_stride, traj_offset):
+def make_engine(L, prec, w, c, ntraj, nmodes, save_stride, traj_offset, method=None):
     cfg = L.nqcd_config()
-    cfg.method, cfg.model, cfg.precision = L.METHOD_FSSH, L.MODEL_SPINBOSON, prec
+    cfg.method, cfg.model, cfg.precision = method or L.METHOD_FSSH, L.MODEL_SPINBOSON, prec
     cfg.rescaling = 0
     cfg.ndofs, cfg.natoms, cfg.nstates = 1, nmodes, 2
     params = np.array([0.0, 1.0])
@@ -468,6 +470,32 @@ def secondary(args, dist):
                    "surrogate_friction_evals": st.surrogate_friction_evals, "exact_friction_evals": st.exact_friction_evals}
             ref_flops = 9 * 201**3 + 10 * 201**2
             kname = "mdef_kernel<float>"
+        elif wk == "ehrenfest":
+            # Ehrenfest on the headline's spin-boson ensemble (100 modes, 100 000
+            # trajectories, dt = 0.05, t in [0, 20], population correlation every 0.1)
+            n, nmodes = args.ntraj, args.nmodes
+            w, c, r0, v0 = WL.spin_boson_inputs(n, nmodes, traj_offset=rank_off * n)
+            stride = int(round(0.1 / args.dt))
+            nsteps = int(round(args.t1 / args.dt))
+            obsv = {}
+            # both paths on the whole ensemble (one thread per trajectory fills the GPU only there)
+            for name, prec, nt in (("fp64", L.PREC_FP64, n), ("fp32", L.PREC_FP32_KAHAN, n)):
+                eng = make_engine(L, prec, w, c, nt, nmodes, stride, rank_off * n, method=L.METHOD_EHRENFEST)
+                eng.set_initial(np.ascontiguousarray(r0[:nt]), np.ascontiguousarray(v0[:nt]))
+                pc = np.zeros((nsteps // stride + 1) * 4)
+                plain = name == "fp64"
+                res[name] = _timed(eng, lambda: eng.run(0.0, args.t1, args.dt, seed, popcorr=pc),
+                                   1 if plain else warm, 1 if plain else steps, dist)
+                obsv[name] = pc.reshape(-1, 4).copy()
+                eng.close()
+            da = obsv["fp64"][:, 0] - obsv["fp64"][:, 1]
+            db = obsv["fp32"][:, 0] - obsv["fp32"][:, 1]
+            obs = {"quantity": "max_t |<P1-P2>(t)| fast - plain FP64 (population-difference correlation)",
+                   "value": float(np.max(np.abs(db - da))), "tolerance": 0.01}
+            cfg = {"workload": "ehrenfest_spinboson_ohmic100_traj100k_dt0.05_t20", "ntraj_per_gpu": n,
+                   "modes": nmodes, "nsteps": nsteps}
+            ref_flops = WL.ref_flops_per_traj_step(nmodes)
+            kname = "fssh2_sb_fast_kernel<AccKahan,25,Ehrenfest>"
         else:  # iesh
             n = args.ntraj if args.ntraj != 100_000 else 20_000
             nsteps = args.nsteps or 500
@@ -500,7 +528,8 @@ def secondary(args, dist):
     line = {
         "metric": METRIC, "workload": wk, "value": fast["value"], "unit": UNIT, "n_gpus": dist.world, "steps": steps,
         "warmup": warm, "ms_per_step": fast["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"tully1": "fp32+kahan-acc", "rpsh": "fp32+kahan-acc"}.get(wk, "fp32+fp64acc"),
+        "vs_baseline": None,
+        "dtype": {"tully1": "fp32+kahan-acc", "rpsh": "fp32+kahan-acc", "ehrenfest": "fp32+kahan-acc"}.get(wk, "fp32+fp64acc"),
         "data": "synthetic", "chosen_path": "fp32", "config": cfg,
         "plain_fp64": {"value": plain["value"], "unit": UNIT, "speedup_chosen_vs_plain": fast["value"] / plain["value"]},
         "observable_error": obs,
