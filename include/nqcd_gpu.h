@@ -168,6 +168,34 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out);
 int nqcd_set_initial(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, const double* sig_re,
                      const double* sig_im, const int32_t* state0, const int32_t* nbeads);
 
+/* Per-degree-of-freedom distribution of a DynamicalDistribution component
+ * (NQCDistributions; src/Ensembles/selections.jl:24-101): a fixed value, a
+ * normal distribution (PositionHarmonicWigner / VelocityHarmonicWigner are
+ * normal with the harmonic Wigner widths) or a uniform distribution. */
+enum nqcd_sampler_kind { NQCD_SAMPLE_FIXED = 0, NQCD_SAMPLE_NORMAL = 1, NQCD_SAMPLE_UNIFORM = 2 };
+
+typedef struct nqcd_sampler {
+    int32_t kind;     /* nqcd_sampler_kind */
+    int32_t reserved;
+    double a, b;      /* FIXED: value a; NORMAL: mean a, standard deviation b >= 0; UNIFORM: [a, b) */
+} nqcd_sampler;
+
+/* Initial positions and velocities sampled on the device for `ntraj`
+ * trajectories (no host sampling or host-to-device copy of the ensemble):
+ * position[d], velocity[d] for d < ndofs*natoms in the (ndofs, natoms)
+ * column-major order of nqcd_set_initial.  Trajectory t (global index
+ * traj_offset + t) draws from the Philox4x32-10 block with counter
+ * (index low, index high, d, 5) for its position and (..., d, 6) for its
+ * velocity and key = seed: with U(h, l) = ((h << 32 | l) >> 11) * 2^-53,
+ *   NORMAL:  a + b * sqrt(-2 ln(1 - U(w0, w1))) * cos(2 pi U(w2, w3)),
+ *   UNIFORM: a + (b - a) * U(w0, w1),
+ * so a sharded ensemble equals the single-process one.  The electronic
+ * initial state follows cfg->init_kind as in nqcd_set_initial
+ * (NQCD_INIT_GIVEN is rejected: it needs host data).  Not for ring polymers.
+ * NQCD_ERR_ARG on a bad sampler (unknown kind, negative width, b < a). */
+int nqcd_sample_initial(nqcd_handle* h, int64_t ntraj, const nqcd_sampler* position, const nqcd_sampler* velocity,
+                        uint64_t seed);
+
 /* Same as nqcd_set_initial with r0/v0 already on the device in the engine's
  * structure-of-arrays layout [dof][trajectory] (dof = ndofs*natoms[*nbeads]). */
 int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0_soa, const double* d_v0_soa,

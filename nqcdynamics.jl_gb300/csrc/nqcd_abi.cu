@@ -115,6 +115,33 @@ __global__ void ehrenfest_scatter_kernel(const double* __restrict__ r, const dou
     }
 }
 
+// Device-side initial conditions (nqcd_sample_initial): entry q of the
+// [2][ndof][n] grid is (position|velocity, degree of freedom d, trajectory t),
+// drawn from its own Philox block; written to the SoA initial-condition arrays.
+// Uniform draws use explicitly rounded operations so that they equal the
+// documented formula bit for bit.
+__global__ void sample_initial_kernel(const nqcd_sampler* __restrict__ tab, int ndof, int64_t n, int64_t offset,
+                                      uint64_t seed, double* __restrict__ r0, double* __restrict__ v0) {
+    const int64_t total = 2 * (int64_t)ndof * n;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = q % n, rest = q / n;
+        const int d = (int)(rest % ndof), which = (int)(rest / ndof);
+        const nqcd_sampler sp = tab[which * ndof + d];
+        double x = sp.a;
+        if (sp.kind != NQCD_SAMPLE_FIXED) {
+            const u32x4 w = rng_block(seed, (uint64_t)(offset + t), (uint32_t)d, which ? RNG_INIT_VELOCITY : RNG_INIT_POSITION);
+            const double u = u01_from_words(w.x, w.y);
+            if (sp.kind == NQCD_SAMPLE_UNIFORM) {
+                x = __dadd_rn(sp.a, __dmul_rn(__dsub_rn(sp.b, sp.a), u));
+            } else {
+                const double g = sqrt(-2.0 * log(1.0 - u)) * cos(6.283185307179586 * u01_from_words(w.z, w.w));
+                x = __dadd_rn(sp.a, __dmul_rn(sp.b, g));
+            }
+        }
+        (which ? v0 : r0)[(int64_t)d * n + t] = x;
+    }
+}
+
 // Run statistics: steps, hops, frustrated hops, non-finite trajectories.
 __global__ void stats_kernel(const int32_t* nsteps, const int32_t* nhops, const int32_t* nfrust,
                              const double* r, const double* v, int64_t ndof, int64_t ntraj,
@@ -716,6 +743,39 @@ int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0, c
     int64_t h2d = 0;
     int rc = set_bead_classes(h, ntraj, nbeads, nullptr, &h2d);
     if (rc) return rc;
+    return set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
+}
+
+int nqcd_sample_initial(nqcd_handle* h, int64_t ntraj, const nqcd_sampler* position, const nqcd_sampler* velocity,
+                        uint64_t seed) {
+    if (!h) return NQCD_ERR_ARG;
+    if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: ntraj outside 1..ntraj_max");
+    if (!position || !velocity) return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: position and velocity samplers are required");
+    if (h->cfg.method == NQCD_METHOD_RPSH)
+        return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_sample_initial: ring-polymer beads take nqcd_set_initial");
+    if (h->cfg.method != NQCD_METHOD_MDEF && h->cfg.init_kind == NQCD_INIT_GIVEN)
+        return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: NQCD_INIT_GIVEN needs nqcd_set_initial");
+    const int nd = (int)h->ndof;
+    std::vector<nqcd_sampler> tab(2 * (size_t)nd);
+    for (int d = 0; d < 2 * nd; ++d) {
+        const nqcd_sampler sp = d < nd ? position[d] : velocity[d - nd];
+        const bool ok = (sp.kind == NQCD_SAMPLE_FIXED && isfinite(sp.a)) ||
+                        (sp.kind == NQCD_SAMPLE_NORMAL && isfinite(sp.a) && isfinite(sp.b) && sp.b >= 0.0) ||
+                        (sp.kind == NQCD_SAMPLE_UNIFORM && isfinite(sp.a) && isfinite(sp.b) && sp.b >= sp.a);
+        if (!ok) return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: bad sampler (kind, finite parameters, width >= 0, b >= a)");
+        tab[d] = sp;
+    }
+    const int64_t bytes = (int64_t)(tab.size() * sizeof(nqcd_sampler));
+    int rc = ensure_stage(h, (bytes + 7) / 8);
+    if (rc) return rc;
+    NQCD_CUDA(h, cudaMemcpyAsync(h->d_stage, tab.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+    const int64_t total = 2 * (int64_t)nd * ntraj;
+    const int64_t blocks = (total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096;
+    sample_initial_kernel<<<(unsigned)blocks, 256, 0, h->stream>>>(reinterpret_cast<const nqcd_sampler*>(h->d_stage), nd,
+                                                                     ntraj, h->cfg.traj_offset, seed, h->d_r0, h->d_v0);
+    NQCD_CUDA(h, cudaGetLastError());
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    int64_t h2d = bytes;
     return set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
 }
 

@@ -72,6 +72,8 @@ enum RngStream : uint32_t {
     RNG_INIT_STATE = 2, // uniform for sampling the initial adiabatic state (fssh.jl:222)
     RNG_NOISE = 3,      // Gaussian Wiener increments for MDEF (mdef_baoab.jl:164)
     RNG_INIT_FD = 4,    // Fermi-Dirac occupation sampling (DynamicsUtils.jl:194-208)
+    RNG_INIT_POSITION = 5, // device-side initial positions (selections.jl:24-101); counter z = degree of freedom
+    RNG_INIT_VELOCITY = 6, // device-side initial velocities
 };
 
 // 53-bit uniform in [0, 1) from the two high words of one Philox block.

@@ -30,6 +30,8 @@ from .api import (
     EnsembleThreads,
     FSSH,
     MeanReduction,
+    Normal,
+    Uniform,
     OhmicSpectralDensity,
     OutputFinal,
     OutputStateResolvedScattering1D,

@@ -99,10 +99,28 @@ class nqcd_stats(C.Structure):
     ]
 
 
+class nqcd_sampler(C.Structure):
+    """One degree of freedom of a DynamicalDistribution component (nqcd_gpu.h)."""
+
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("a", C.c_double), ("b", C.c_double)]
+
+
+SAMPLE_FIXED, SAMPLE_NORMAL, SAMPLE_UNIFORM = 0, 1, 2
+
+
+def samplers(specs):
+    """ctypes array of nqcd_sampler from (kind, a, b) triples."""
+    arr = (nqcd_sampler * len(specs))()
+    for q, (kind, a, b) in enumerate(specs):
+        arr[q].kind, arr[q].a, arr[q].b = int(kind), float(a), float(b)
+    return arr
+
+
 EXPORTED = [
     "nqcd_version",
     "nqcd_create",
     "nqcd_set_initial",
+    "nqcd_sample_initial",
     "nqcd_set_initial_device",
     "nqcd_run",
     "nqcd_get_final",
@@ -150,6 +168,8 @@ def load(path: Path | str | None = None) -> C.CDLL:
     lib.nqcd_create.argtypes = [C.POINTER(nqcd_config), C.POINTER(C.c_void_p)]
     lib.nqcd_set_initial.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP, DP, IP, IP]
     lib.nqcd_set_initial_device.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, IP]
+    lib.nqcd_sample_initial.argtypes = [C.c_void_p, C.c_int64, C.POINTER(nqcd_sampler), C.POINTER(nqcd_sampler),
+                                        C.c_uint64]
     lib.nqcd_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_uint64,
                              C.POINTER(nqcd_outputs), C.POINTER(nqcd_stats)]
     lib.nqcd_get_final.argtypes = [C.c_void_p, DP, DP, DP, DP, IP, IP, IP, IP, DP]
@@ -209,6 +229,12 @@ class Engine:
         ntraj = r0.shape[0]
         self._check(self.lib.nqcd_set_initial(self.h, ntraj, dptr(r0), dptr(v0), dptr(sig_re), dptr(sig_im),
                                               iptr(state0), iptr(nbeads)))
+        self.ntraj = ntraj
+
+    def sample_initial(self, ntraj: int, position, velocity, seed: int):
+        """Initial conditions sampled on the device; position/velocity are
+        sequences of (kind, a, b) per degree of freedom."""
+        self._check(self.lib.nqcd_sample_initial(self.h, ntraj, samplers(position), samplers(velocity), seed))
         self.ntraj = ntraj
 
     def set_initial_device(self, ntraj: int, d_r0: int, d_v0: int):

@@ -12,7 +12,7 @@ Names, argument meanings and error behaviour follow the reference:
   TrapezoidalRule, ShenviGaussLegendre, GaussianBroadening      (NQCModels, NQCCalculators)
   FermiDiracState(fermi_level, temperature; statetype)          (NQCDistributions)
   PureState(state, Adiabatic()/Diabatic()), DynamicalDistribution,
-  PositionHarmonicWigner / VelocityHarmonicWigner           (NQCDistributions)
+  PositionHarmonicWigner / VelocityHarmonicWigner, Normal, Uniform  (NQCDistributions, Distributions)
   OutputStateResolvedScattering1D, OutputSurfaceHops, OutputFinal,
   OutputTotalEnergy                                         src/DynamicsOutputs.jl
   PopulationCorrelationFunction(sim, Diabatic())            src/TimeCorrelationFunctions.jl:61-88
@@ -367,6 +367,9 @@ class PositionHarmonicWigner:
     def sigma(self):
         return math.sqrt(1.0 / (2.0 * self.m * self.ω * math.tanh(self.β * self.ω / 2.0)))
 
+    def sampler(self):
+        return (L.SAMPLE_NORMAL, 0.0, self.sigma())
+
 
 @dataclass
 class VelocityHarmonicWigner:
@@ -376,6 +379,34 @@ class VelocityHarmonicWigner:
 
     def sigma(self):
         return math.sqrt(self.ω / (2.0 * self.m * math.tanh(self.β * self.ω / 2.0)))
+
+    def sampler(self):
+        return (L.SAMPLE_NORMAL, 0.0, self.sigma())
+
+
+@dataclass
+class Normal:
+    """Distributions.Normal(mean, std) for one degree of freedom."""
+
+    mean: float = 0.0
+    std: float = 1.0
+
+    def sigma(self):
+        return self.std
+
+    def sampler(self):
+        return (L.SAMPLE_NORMAL, self.mean, self.std)
+
+
+@dataclass
+class Uniform:
+    """Distributions.Uniform(a, b) for one degree of freedom."""
+
+    a: float = 0.0
+    b: float = 1.0
+
+    def sampler(self):
+        return (L.SAMPLE_UNIFORM, self.a, self.b)
 
 
 class DynamicalDistribution:
@@ -391,14 +422,39 @@ class DynamicalDistribution:
     def __mul__(self, other):
         return ProductDistribution(self, other)
 
+    def samplers(self, which):
+        """Per-dof (kind, a, b) triples for device-side sampling
+        (nqcd_sample_initial), or ValueError if the specification holds
+        explicit per-trajectory samples."""
+        spec = self.velocity if which == "v" else self.position
+        n = int(np.prod(self.size))
+        if hasattr(spec, "sampler"):
+            return [spec.sampler()] * n
+        flat = list(np.asarray(spec, dtype=object).reshape(-1, order="F"))
+        if len(flat) == 1 and not hasattr(flat[0], "sampler"):
+            return [(L.SAMPLE_FIXED, float(flat[0]), 0.0)] * n
+        if len(flat) == n:
+            return [s.sampler() if hasattr(s, "sampler") else (L.SAMPLE_FIXED, float(s), 0.0) for s in flat]
+        raise ValueError("explicit per-trajectory samples cannot be drawn on the device")
+
     def sample(self, which, ntraj, rng):
         spec = self.velocity if which == "v" else self.position
         n = int(np.prod(self.size))
+        if hasattr(spec, "sampler"):
+            spec = [spec] * n
         if isinstance(spec, (list, tuple)) or (isinstance(spec, np.ndarray) and spec.dtype == object):
             flat = list(np.asarray(spec, dtype=object).reshape(-1, order="F"))
-            if len(flat) == n and all(hasattr(s, "sigma") for s in flat):
-                sig = np.array([s.sigma() for s in flat])
-                return rng.standard_normal((ntraj, n)) * sig
+            if len(flat) == n and any(hasattr(s, "sampler") for s in flat):
+                out = np.empty((ntraj, n))
+                for d, s in enumerate(flat):
+                    kind, a, b = s.sampler() if hasattr(s, "sampler") else (L.SAMPLE_FIXED, float(s), 0.0)
+                    if kind == L.SAMPLE_FIXED:
+                        out[:, d] = a
+                    elif kind == L.SAMPLE_UNIFORM:
+                        out[:, d] = a + (b - a) * rng.random(ntraj)
+                    else:
+                        out[:, d] = a + b * rng.standard_normal(ntraj)
+                return out
         arr = np.asarray(spec, dtype=np.float64)
         if arr.size == 1:
             return np.full((ntraj, n), float(arr))
@@ -525,6 +581,7 @@ class EnsembleGB300:
     seed: int = 20261203
     friction_surrogate: Any = None  # MDEF: (weights, meta) of a trained network, or None
     judge_every: int = 0
+    device_sampling: bool = False   # draw the nuclear initial conditions on the GPU (nqcd_sample_initial)
 
 
 # ---------------------------------------------------------------------------
@@ -605,13 +662,20 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
                 raise ValueError("saveat must be a positive multiple of dt on the GPU path")
             save_stride = int(round(stride))
     ntraj = int(trajectories)
-    rng = rng if rng is not None else np.random.default_rng(alg.seed if seed is None else seed)
-    r0 = distribution.nuclear.sample("r", ntraj, rng)
-    v0 = distribution.nuclear.sample("v", ntraj, rng)
+    seed_ = alg.seed if seed is None else seed
+    if alg.device_sampling:
+        pos, vel = distribution.nuclear.samplers("r"), distribution.nuclear.samplers("v")
+    else:
+        rng = rng if rng is not None else np.random.default_rng(seed_)
+        r0 = distribution.nuclear.sample("r", ntraj, rng)
+        v0 = distribution.nuclear.sample("v", ntraj, rng)
     cfg, keep = build_config(sim, distribution.electronic, ntraj, alg, save_stride)
     eng = L.Engine(cfg, keep)
     try:
-        eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0))
+        if alg.device_sampling:
+            eng.sample_initial(ntraj, pos, vel, seed_)
+        else:
+            eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0))
         sc = np.zeros(4)
         pc = None
         if save_stride:

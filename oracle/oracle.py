@@ -263,3 +263,38 @@ def run_rpsh(*, model, params, mass, r0, v0, nbeads, beta, t0, t1, dt, seed, res
             sig_c[:, i, j] = sig[:, 2 * (2 * i + j)] + 1j * sig[:, 2 * (2 * i + j) + 1]
     return dict(r=r, v=v, sigma=sig_c, state=state, hop_log=hop_log, nhops=nh, nfrustrated=nf, nsteps=ns, energy=en,
                 scatter=sc / ntraj)
+
+
+# ---------------------------------------------------------------------------
+# Device-side initial-condition sampling (nqcd_sample_initial), restated.
+# ---------------------------------------------------------------------------
+RNG_INIT_POSITION, RNG_INIT_VELOCITY = 5, 6
+
+
+def sample_initial(position, velocity, ntraj, seed, traj_offset=0):
+    """The engine's sampler (include/nqcd_gpu.h, nqcd_sample_initial) in
+    numpy: per trajectory and degree of freedom one Philox4x32-10 block with
+    counter (index low, index high, dof, 5 | 6) and key = seed; FIXED a,
+    UNIFORM a + (b - a) U(w0, w1), NORMAL a + b sqrt(-2 ln(1 - U(w0, w1)))
+    cos(2 pi U(w2, w3)).  Returns r0, v0 of shape (ntraj, ndof)."""
+    from mdef_oracle import philox
+
+    traj = np.arange(ntraj, dtype=np.uint64) + np.uint64(traj_offset)
+    out = []
+    for specs, stream in ((position, RNG_INIT_POSITION), (velocity, RNG_INIT_VELOCITY)):
+        x = np.empty((ntraj, len(specs)))
+        for d, (kind, a, b) in enumerate(specs):
+            if kind == 0:
+                x[:, d] = a
+                continue
+            w = philox((traj & np.uint64(0xFFFFFFFF)).astype(np.uint32), (traj >> np.uint64(32)).astype(np.uint32),
+                       np.full(ntraj, d, np.uint32), np.full(ntraj, stream, np.uint32), seed & 0xFFFFFFFF,
+                       (seed >> 32) & 0xFFFFFFFF)
+            u = (((w[0].astype(np.uint64) << np.uint64(32)) | w[1].astype(np.uint64)) >> np.uint64(11)) * 2.0**-53
+            if kind == 2:
+                x[:, d] = a + (b - a) * u
+            else:
+                u2 = (((w[2].astype(np.uint64) << np.uint64(32)) | w[3].astype(np.uint64)) >> np.uint64(11)) * 2.0**-53
+                x[:, d] = a + b * (np.sqrt(-2.0 * np.log(1.0 - u)) * np.cos(6.283185307179586 * u2))
+        out.append(x)
+    return out[0], out[1]
