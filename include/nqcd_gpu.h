@@ -48,10 +48,15 @@ enum nqcd_method {
     NQCD_METHOD_RPSH = 2,
     NQCD_METHOD_IESH = 3,
     NQCD_METHOD_MDEF = 4,
-    NQCD_METHOD_EHRENFEST = 5 /* Simulation{Ehrenfest} (EhrenfestMethods/ehrenfest.jl): the FSSH integrator
+    NQCD_METHOD_EHRENFEST = 5, /* Simulation{Ehrenfest} (EhrenfestMethods/ehrenfest.jl): the FSSH integrator
                                 (BABwithTsit5) with the mean-field force -sum_nm (Z^T dH Z)_nm Re sigma_nm of
                                 the step's initial density matrix and no hopping; two-state models.
                                 Scattering outputs are the populations diag(Re sigma) summed by side. */
+    NQCD_METHOD_EHRENFEST_NA = 6 /* Simulation{EhrenfestNA} (EhrenfestMethods/ehrenfest_na.jl) on
+                                NQCD_MODEL_NEWNS_ANDERSON_3D: the IESH integrator and Fermi-Dirac initial
+                                orbitals with the mean-field force of the orbitals before each propagation,
+                                -dh/dq sum_e |sum_n z0_n psi_ne|^2, and no hopping (configured like IESH;
+                                observables[2] is sum_e |sum_n z0_n psi_ne|^2, [3] U0 + sum l_i |psi_ie|^2). */
 };
 
 enum nqcd_model {

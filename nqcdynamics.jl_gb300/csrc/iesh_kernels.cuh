@@ -81,6 +81,7 @@ struct IeshParams {
     int32_t rescaling;
     int32_t init_kind;
     int32_t exact_probability;      // 1: every step evaluates all probabilities (estimate_probability = false)
+    int32_t ehrenfest_na;           // 1: Simulation{EhrenfestNA} (mean-field force of the orbitals, no hops)
     int32_t save_stride, nsave, max_hops;
     int64_t ntraj, traj_offset;
     double dt;
@@ -419,10 +420,33 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         }
         __syncthreads();
     };
+    // EhrenfestNA (ehrenfest_na.jl): the force and energy come from the orbitals
+    // instead of the occupations.  With A = dh z0 z0^T the force weight
+    // sum_e sum_nm A_nm Re(psi_ne conj(psi_me)) is dh times the impurity
+    // population sum_e |sum_a z0_a psi_ae|^2 (ehrenfest_na.jl:74-90); the band
+    // energy is sum_e sum_i l_i |psi_ie|^2 (ehrenfest_na.jl:106-117).  Block-wide.
+    const bool ena = p.ehrenfest_na != 0;
+    double ena_imp = 0.0, ena_band = 0.0;
+    auto orbital_sums = [&]() {
+        double ci = 0.0, cb = 0.0;
+        for (int e = tid; e < Ne; e += nthr) {
+            R ar = R(0), ai = R(0), b = R(0);
+            for (int a = 0; a < N; ++a) {
+                const Cx<R> c = phiA[a * Nep + e];
+                ar += z0[a] * c.re;
+                ai += z0[a] * c.im;
+                b += lam[a] * (c.re * c.re + c.im * c.im);
+            }
+            ci += (double)ar * (double)ar + (double)ai * (double)ai;
+            cb += (double)b;
+        }
+        ena_imp = iesh_block_sum(ci, red);
+        ena_band = iesh_block_sum(cb, red);
+    };
     auto accel = [&](double dh) {  // warp 0
         R acc = R(0);
         for (int jj = lane; jj < Ne; jj += 32) acc += z2[occ[jj]];
-        const double occsum = (double)warp_sum<R>(acc);
+        const double occsum = ena ? ena_imp : (double)warp_sum<R>(acc);
         const double eaz = iesh_wall<R>(p, r[2]);
         k[0] = -(p.kxy * r[0]) * inv_mass;
         k[1] = -(p.kxy * r[1]) * inv_mass;
@@ -431,7 +455,8 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     auto potential = [&]() {  // warp 0: U0 + sum of occupied eigenvalues (iesh.jl:380-388)
         R acc = R(0);
         for (int jj = lane; jj < Ne; jj += 32) acc += lam[occ[jj]];
-        return 0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) + p.A * iesh_wall<R>(p, r[2]) + (double)warp_sum<R>(acc);
+        const double band = ena ? ena_band : (double)warp_sum<R>(acc);
+        return 0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) + p.A * iesh_wall<R>(p, r[2]) + band;
     };
     auto kinetic = [&]() { return 0.5 * mass * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
     auto rebuild_unocc = [&]() {  // ascending, as set_unoccupied_states! (DynamicsUtils.jl:162-171)
@@ -543,6 +568,10 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     }
     __syncthreads();
     for (int jj = tid; jj < Ne; jj += nthr) phiA[occ[jj] * Nep + jj] = {R(1), R(0)};
+    if (ena) {
+        __syncthreads();
+        orbital_sums();
+    }
     double e0 = 0.0;
     if (warp == 0) {
         accel(dhz);
@@ -571,7 +600,11 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             }
             contrib = (double)ar * (double)ar + (double)ai * (double)ai - (double)sq + (double)z2[occ[tid]];
         }
-        const double nimp = iesh_block_sum(contrib, red);
+        double nimp = iesh_block_sum(contrib, red);
+        if (ena) {  // impurity population of the orbitals themselves
+            orbital_sums();
+            nimp = ena_imp;
+        }
         if (warp == 0) {
             const double pe = potential();
             if (lane == 0 && isave < p.nsave) {
@@ -605,6 +638,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         }
         __syncthreads();
         roots();
+        if (ena) orbital_sums();  // orbitals before this step's propagation, roots at the new position
         if (warp == 0) {
             accel(dhz);
 #pragma unroll
@@ -749,6 +783,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             __syncthreads();
         }
 
+        if (!ena) {  // EhrenfestNA: no hopping
         // ---- hop test (iesh.jl:231-335, 390-411) ----
         // S^T stored by columns: column c of S^T is row occ[c] of psi, Qc[c * Nep + r] = S^T[r][c]
         Cx<R>* Qc = phiB;
@@ -996,10 +1031,12 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             __syncthreads();
             if (warp == 0) v[2] = misc[3];  // hop counts live in thread 0, which writes them out
         }
+        }  // !ena
         if (p.save_stride > 0 && p.obs_partial && step % p.save_stride == 0) save(isave++);
     }
 
     double e1 = 0.0;
+    if (ena && p.energy) orbital_sums();
     if (warp == 0 && p.energy) {
         const double pe = potential();
         e1 = kinetic() + pe;

@@ -369,11 +369,13 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     if (!cfg || !out) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: null argument");
     *out = nullptr;
     if (cfg->method != NQCD_METHOD_FSSH && cfg->method != NQCD_METHOD_RPSH && cfg->method != NQCD_METHOD_MDEF &&
-        cfg->method != NQCD_METHOD_IESH && cfg->method != NQCD_METHOD_EHRENFEST)
+        cfg->method != NQCD_METHOD_IESH && cfg->method != NQCD_METHOD_EHRENFEST &&
+        cfg->method != NQCD_METHOD_EHRENFEST_NA)
         return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: method not supported by this build");
     const bool rp = cfg->method == NQCD_METHOD_RPSH;
     const bool mdef = cfg->method == NQCD_METHOD_MDEF;
-    const bool iesh = cfg->method == NQCD_METHOD_IESH;
+    // EhrenfestNA runs in the IESH kernel (same model, integrator and initial orbitals)
+    const bool iesh = cfg->method == NQCD_METHOD_IESH || cfg->method == NQCD_METHOD_EHRENFEST_NA;
     const int model = cfg->model;
     if (iesh) {
         if (model != NQCD_MODEL_NEWNS_ANDERSON_3D)
@@ -666,7 +668,8 @@ static int set_initial_common(nqcd_handle* h, int64_t ntraj, const double* sig_r
     // MDEF carries no electronic state: only FSSH and RPSH read sigma and state0
     const bool two_state = h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_RPSH ||
                            h->cfg.method == NQCD_METHOD_EHRENFEST;
-    if (h->cfg.method == NQCD_METHOD_IESH && h->cfg.init_kind == NQCD_INIT_GIVEN) {
+    if ((h->cfg.method == NQCD_METHOD_IESH || h->cfg.method == NQCD_METHOD_EHRENFEST_NA) &&
+        h->cfg.init_kind == NQCD_INIT_GIVEN) {
         // occupations (nelectrons, ntraj) column-major -> device [electron][trajectory]
         if (!state0) return fail(h, NQCD_ERR_ARG, "nqcd_set_initial: IESH with NQCD_INIT_GIVEN needs the occupations in state0");
         const int ne = h->nelec, ns = h->nstates;
@@ -787,7 +790,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     auto wall0 = std::chrono::steady_clock::now();
     const int64_t N = h->ntraj;
     const bool mdef = h->cfg.method == NQCD_METHOD_MDEF;
-    const bool iesh = h->cfg.method == NQCD_METHOD_IESH;
+    const bool iesh = h->cfg.method == NQCD_METHOD_IESH || h->cfg.method == NQCD_METHOD_EHRENFEST_NA;
     // FSSH and RPSH step like the reference's integrator (a last partial step
     // up to t1); MDEF and IESH take whole steps of dt only
     const double span = (t1 - t0) / dt;
@@ -1056,6 +1059,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.rescaling = h->cfg.rescaling;
         q.init_kind = h->cfg.init_kind;
         q.exact_probability = h->cfg.exact_hop_probability ? 1 : 0;
+        q.ehrenfest_na = h->cfg.method == NQCD_METHOD_EHRENFEST_NA ? 1 : 0;
         q.save_stride = stride;
         q.nsave = nsave;
         q.max_hops = h->cfg.max_hops;
@@ -1194,7 +1198,7 @@ int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double*
         NQCD_CUDA(h, cudaMemcpyAsync(pairs[q], h->d_stage, nd * N * sizeof(double), cudaMemcpyDeviceToHost, s));
         NQCD_CUDA(h, cudaStreamSynchronize(s));
     }
-    if (h->cfg.method == NQCD_METHOD_IESH) {
+    if (h->cfg.method == NQCD_METHOD_IESH || h->cfg.method == NQCD_METHOD_EHRENFEST_NA) {
         const int64_t ne = h->nelec, ns = h->nstates;
         if (sig_re) NQCD_CUDA(h, cudaMemcpyAsync(sig_re, h->d_psi_re, ne * ns * N * sizeof(double), cudaMemcpyDeviceToHost, s));
         if (sig_im) NQCD_CUDA(h, cudaMemcpyAsync(sig_im, h->d_psi_im, ne * ns * N * sizeof(double), cudaMemcpyDeviceToHost, s));

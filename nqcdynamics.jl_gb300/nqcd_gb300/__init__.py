@@ -24,6 +24,7 @@ from .api import (
     Atoms,
     Diabatic,
     DynamicalDistribution,
+    EhrenfestNA,
     Ehrenfest,
     EnsembleGB300,
     EnsembleSerial,

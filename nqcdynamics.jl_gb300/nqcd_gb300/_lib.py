@@ -23,7 +23,7 @@ ERRORS = {
     -7: "NQCD_ERR_STATE",
 }
 
-METHOD_FSSH, METHOD_RPSH, METHOD_IESH, METHOD_MDEF, METHOD_EHRENFEST = 1, 2, 3, 4, 5
+METHOD_FSSH, METHOD_RPSH, METHOD_IESH, METHOD_MDEF, METHOD_EHRENFEST, METHOD_EHRENFEST_NA = 1, 2, 3, 4, 5, 6
 MODEL_TULLY1, MODEL_TULLY2, MODEL_TULLY3, MODEL_SPINBOSON, MODEL_NEWNS_ANDERSON = 1, 2, 3, 10, 20
 MODEL_NEWNS_ANDERSON_3D = 21
 MLP_NPARAMS = 4353

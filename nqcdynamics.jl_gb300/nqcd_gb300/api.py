@@ -8,6 +8,7 @@ Names, argument meanings and error behaviour follow the reference:
   RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)   simulations.jl:46-73, rpsh.jl:5-7
   Simulation[DiabaticMDEF](atoms, model; friction_method, temperature)   mdef.jl:79-100
   Simulation[AdiabaticIESH](atoms, model; rescaling, estimate_probability)   iesh.jl:72-87
+  Simulation[EhrenfestNA](atoms, model)           EhrenfestMethods/ehrenfest_na.jl:30-32
   AndersonHolstein(impurity, bath; coupling, fermi_level, nelectrons),
   TrapezoidalRule, ShenviGaussLegendre, GaussianBroadening      (NQCModels, NQCCalculators)
   FermiDiracState(fermi_level, temperature; statetype)          (NQCDistributions)
@@ -244,6 +245,11 @@ class DiabaticMDEF:
     """Electronic friction Langevin dynamics on a diabatic model (mdef.jl)."""
 
 
+class EhrenfestNA:
+    """Mean-field dynamics of independent electrons in a metal
+    (ehrenfest_na.jl): the IESH integrator with the force of the orbitals."""
+
+
 @dataclass
 class AdiabaticIESH:
     """Independent-electron surface hopping (iesh.jl:72-87)."""
@@ -284,12 +290,12 @@ class Simulation(metaclass=_MethodIndexed):
             self.method = DiabaticMDEF()
             self.friction_method = friction_method
             return
-        if method is AdiabaticIESH:
+        if method is AdiabaticIESH or method is EhrenfestNA:
             if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON_3D:
-                raise NotImplementedError("AdiabaticIESH runs on AndersonHolstein(AdsorbateMetal3D(...), bath)")
+                raise NotImplementedError(f"{method.__name__} runs on AndersonHolstein(AdsorbateMetal3D(...), bath)")
             if len(atoms) != 1:
                 raise ValueError("one adsorbate atom with three degrees of freedom")
-            self.method = AdiabaticIESH(rescaling, estimate_probability)
+            self.method = AdiabaticIESH(rescaling, estimate_probability) if method is AdiabaticIESH else EhrenfestNA()
             return
         if method is Ehrenfest:
             self.method = Ehrenfest()
@@ -643,7 +649,7 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
         raise TypeError("ensemble_algorithm must be EnsembleGB300")
     if isinstance(sim, RingPolymerSimulation):
         raise NotImplementedError("ring-polymer ensembles run through run_ring_polymer_ensemble")
-    if isinstance(getattr(sim, "method", None), (DiabaticMDEF, AdiabaticIESH)):
+    if isinstance(getattr(sim, "method", None), (DiabaticMDEF, AdiabaticIESH, EhrenfestNA)):
         return _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, dt, saveat, seed, rng)
     if not isinstance(distribution, ProductDistribution):
         raise TypeError("distribution must be DynamicalDistribution * PureState")
@@ -713,7 +719,8 @@ def _metal_config(sim, ntraj, alg, save_stride):
     model = sim.model
     mdef = isinstance(sim.method, DiabaticMDEF)
     cfg = L.nqcd_config()
-    cfg.method = L.METHOD_MDEF if mdef else L.METHOD_IESH
+    ena = isinstance(sim.method, EhrenfestNA)
+    cfg.method = L.METHOD_MDEF if mdef else (L.METHOD_EHRENFEST_NA if ena else L.METHOD_IESH)
     cfg.model = model.kind
     cfg.precision = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[alg.precision]
     cfg.ndofs, cfg.natoms, cfg.nstates = model.ndofs, 1, model.nstates
@@ -725,8 +732,8 @@ def _metal_config(sim, ntraj, alg, save_stride):
         cfg.judge_every = alg.judge_every
     else:
         params = np.array([imp.kxy, imp.A, imp.a, imp.delta, imp.B, imp.b])
-        cfg.rescaling = L.RESCALE[sim.method.rescaling]
-        cfg.exact_hop_probability = int(not sim.method.estimate_probability)
+        cfg.rescaling = 0 if ena else L.RESCALE[sim.method.rescaling]
+        cfg.exact_hop_probability = 0 if ena else int(not sim.method.estimate_probability)
         cfg.nelectrons = model.nelectrons
         cfg.max_hops = alg.max_hops
     masses = np.ascontiguousarray(sim.atoms.masses, dtype=np.float64)

@@ -153,6 +153,17 @@ def total_energy(model, r, v, w, state, mass):
     return 0.5 * mass * np.sum(v * v, axis=1) + model.U0(r) + np.take_along_axis(w, state, axis=1).sum(1)
 
 
+def total_energy_ehrenfest_na(model, r, v, w, psi, mass):
+    """KE + U0 + sum_e sum_i E_i |psi_ie|^2 (ehrenfest_na.jl:106-117)."""
+    return 0.5 * mass * np.sum(v * v, axis=1) + model.U0(r) + np.einsum("ti,tie->t", w, np.abs(psi) ** 2)
+
+
+def impurity_population_ehrenfest_na(psi, Z):
+    """Impurity population of the orbitals: sum_e |sum_a z0_a psi_ae|^2."""
+    amp = np.einsum("ta,tae->te", Z[:, 0, :], psi)
+    return (np.abs(amp) ** 2).sum(1)
+
+
 def impurity_population(psi, Z, state):
     """Row 0 of iesh_diabatic_population (iesh.jl:351-369) per trajectory."""
     z0 = Z[:, 0, :]
@@ -162,9 +173,14 @@ def impurity_population(psi, Z, state):
 
 
 def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, max_hops=16,
-             estimate=True, initial_state=None):
+             estimate=True, initial_state=None, ehrenfest_na=False):
     """estimate: the reference's estimate_probability screen (iesh.jl:251-254).
-    initial_state: given occupations (ntraj, ne) instead of Fermi-Dirac sampling."""
+    initial_state: given occupations (ntraj, ne) instead of Fermi-Dirac sampling.
+    ehrenfest_na: Simulation{EhrenfestNA} instead (ehrenfest_na.jl): the same
+    integrator and initial orbitals (verlet_with_electronics.jl:51-65), the
+    force of the orbitals before propagation, -sum_e sum_nm A_nm
+    Re(psi_ne conj(psi_me)) = -dh |sum_n z0_n psi_ne|^2 summed over e
+    (ehrenfest_na.jl:74-90; A = dh z0 z0^T for this model), and no hops."""
     n = r0.shape[0]
     N = model.nstates
     traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
@@ -180,20 +196,28 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
     hops = [[] for _ in range(n)]
     nfr = np.zeros(n, np.int32)
 
-    def accel(w, Z, r, state):
+    def accel(w, Z, r, state, psi):
         gh = model.grad_h(r)
         z0 = Z[:, 0, :]
-        occ = np.take_along_axis(z0, state, axis=1) ** 2
-        return -(model.grad_U0(r) + gh * occ.sum(1)[:, None]) / mass
+        if ehrenfest_na:
+            occsum = (np.abs(np.einsum("ta,tae->te", z0, psi)) ** 2).sum(1)
+        else:
+            occsum = (np.take_along_axis(z0, state, axis=1) ** 2).sum(1)
+        return -(model.grad_U0(r) + gh * occsum[:, None]) / mass
 
-    k = accel(w, Z, r, state)
-    e0 = total_energy(model, r, v, w, state, mass)
+    def energy(w, psi):
+        if ehrenfest_na:
+            return total_energy_ehrenfest_na(model, r, v, w, psi, mass)
+        return total_energy(model, r, v, w, state, mass)
+
+    k = accel(w, Z, r, state, psi)
+    e0 = energy(w, psi)
     nfull = 0
     for step in range(1, nsteps + 1):
         vt = v + (dt / 2) * k
         r = r + dt * vt
         w, Z = eigen_continuous(model, r, Z)
-        k = accel(w, Z, r, state)
+        k = accel(w, Z, r, state, psi)
         v = vt + (dt / 2) * k
         gh = model.grad_h(r)
         z0 = Z[:, 0, :]
@@ -210,6 +234,8 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
         mu, U = np.linalg.eigh(Heff)
         P = np.einsum("tij,tj,tkj->tik", U, np.exp(-1j * mu * dt), U.conj())
         psi = P @ psi
+        if ehrenfest_na:
+            continue
         # hopping
         wh = uniform(seed, traj, step, RNG_HOP)
         rnd = u53(wh[0], wh[1])
@@ -258,6 +284,7 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
                 hops[t].append((step, int(old), int(m)))
             else:
                 nfr[t] += 1
-    e1 = total_energy(model, r, v, w, state, mass)
+    e1 = energy(w, psi)
+    nimp = impurity_population_ehrenfest_na(psi, Z) if ehrenfest_na else impurity_population(psi, Z, state)
     return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, Z=Z, w=w, initial_state=states,
-                energy=np.stack([e0, e1], axis=1), nimp=impurity_population(psi, Z, state), nfull=nfull)
+                energy=np.stack([e0, e1], axis=1), nimp=nimp, nfull=nfull)

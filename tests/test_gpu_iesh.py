@@ -23,10 +23,10 @@ pytestmark = pytest.mark.gpu
 
 
 def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_DIRAC, max_hops=32, save_stride=0,
-              exact=0):
+              exact=0, method=L.METHOD_IESH):
     P = wl["params"]
     cfg = L.nqcd_config()
-    cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_IESH, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
+    cfg.method, cfg.model, cfg.precision, cfg.rescaling = method, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
     cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nelectrons = 3, 1, wl["nstates"], wl["nelectrons"]
     params = np.array([P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"]])
     masses = np.array([wl["mass"]])

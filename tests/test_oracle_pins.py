@@ -427,3 +427,65 @@ def test_ehrenfest_through_the_coupling_region(kind, p0, x0, t1):
     assert sig[1, 1].real == pytest.approx(pe[1], abs=1e-4)
     assert 0.2 < pe[1] < 0.8  # a genuine population transfer
     assert abs(res["energy"][0, 1] - res["energy"][0, 0]) < 1e-4 * res["energy"][0, 0]
+
+
+def _metal_dop853_ehrenfest(model, mass, r0, v0, psi0, Z0, t1):
+    """Exact Ehrenfest dynamics of the independent electrons in the diabatic
+    basis (no eigenvectors, no couplings): d phi/dt = -i H phi,
+    m dv/dt = -grad U0 - grad h sum_e |phi_0e|^2."""
+    from scipy.integrate import solve_ivp
+
+    N, ne = psi0.shape
+    phi0 = Z0 @ psi0
+
+    def rhs(t, y):
+        r = y[0:3][None]
+        phi = (y[6:6 + N * ne] + 1j * y[6 + N * ne:]).reshape(N, ne)
+        imp = np.sum(np.abs(phi[0]) ** 2)
+        dphi = -1j * (model.hamiltonian(r)[0] @ phi)
+        return np.concatenate([y[3:6], -(model.grad_U0(r)[0] + model.grad_h(r)[0] * imp) / mass, dphi.real.ravel(),
+                               dphi.imag.ravel()])
+
+    y0 = np.concatenate([r0, v0, phi0.real.ravel(), phi0.imag.ravel()])
+    y = solve_ivp(rhs, (0.0, t1), y0, method="DOP853", rtol=1e-10, atol=1e-12).y[:, -1]
+    phi = (y[6:6 + N * ne] + 1j * y[6 + N * ne:]).reshape(N, ne)
+    return y[0:3], y[3:6], np.sum(np.abs(phi[0]) ** 2)
+
+
+def test_ehrenfest_na_fixed_step_against_high_accuracy():
+    """test/Dynamics/ehrenfest_na.jl:22-49 restated on the three-dimensional
+    metal model: the fixed-step integrator (VerletwithElectronics with the
+    force of the pre-propagation orbitals) agrees with a high-accuracy
+    integration of the same equations (the reference: Vern9 at 1e-15,
+    rtol 1e-3 on positions and velocities), and its energy error is of first
+    order in dt (the force lags the orbitals by one propagation)."""
+    pytest.importorskip("scipy")
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "nqcdynamics.jl_gb300"))
+    import iesh_oracle as IO
+    from nqcd_gb300 import workload as WL
+
+    wl = WL.newns_anderson_iesh(2, nstates=20, nelectrons=10, z0=3.5)
+    P = wl["params"]
+    model = IO.Metal3D(kxy=P["kxy"], A=P["A"], a=P["a"], delta=P["delta"], B=P["B"], b=P["b"], eps=wl["eps"],
+                       V=wl["V"])
+    t1 = 400 * wl["dt"]
+    runs = {}
+    for q in (2, 4):
+        runs[q] = IO.run_iesh(model, mass=wl["mass"], ne=10, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"],
+                              dt=wl["dt"] / q, nsteps=400 * q, seed=5, ehrenfest_na=True)
+    res = runs[4]
+    assert all(len(h) == 0 for h in res["hops"])
+    for t in range(2):
+        psi0 = np.zeros((20, 10))
+        psi0[res["initial_state"][t], np.arange(10)] = 1.0
+        Z0 = np.linalg.eigh(model.hamiltonian(wl["r0"][t:t + 1]))[1][0]
+        r, v, imp = _metal_dop853_ehrenfest(model, wl["mass"], wl["r0"][t], wl["v0"][t], psi0, Z0, t1)
+        np.testing.assert_allclose(res["r"][t], r, rtol=1e-3)
+        np.testing.assert_allclose(res["v"][t], v, rtol=1e-3, atol=1e-6)
+        assert abs(res["nimp"][t] - imp) < 5e-3
+    d2 = np.abs(runs[2]["energy"][:, 1] - runs[2]["energy"][:, 0])
+    d4 = np.abs(runs[4]["energy"][:, 1] - runs[4]["energy"][:, 0])
+    assert np.all((d2 / d4 > 1.6) & (d2 / d4 < 2.5))
