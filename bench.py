@@ -19,8 +19,9 @@ configuration's shapes (nqcd_gb300/workload.py).
 the host cores (the reference itself is Julia and cannot run here).
 
 --workload tully1|rpsh|mdef|iesh measures the other benchmark configurations
-(C1, C3, C4, C5; nqcd_gb300/configs.py), and --workload ehrenfest the
-Ehrenfest method on the headline's spin-boson ensemble, the same way: the
+(C1, C3, C4, C5; nqcd_gb300/configs.py), --workload ehrenfest the Ehrenfest
+method on the headline's spin-boson ensemble and --workload ehrenfest_na
+EhrenfestNA on the C5 ensemble, the same way: the
 chosen fast path on the full ensemble, the plain FP64 path, and the
 observable error between the two on a common subset.  These are records for the design notes; the default
 run is the headline configuration.
@@ -64,7 +65,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="spinboson",
-                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest"])
+                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest", "ehrenfest_na"])
     ap.add_argument("--nsteps", type=int, default=0, help="secondary workloads: nuclear steps of the fast path")
     return ap.parse_args()
 
@@ -496,14 +497,15 @@ def secondary(args, dist):
                    "modes": nmodes, "nsteps": nsteps}
             ref_flops = WL.ref_flops_per_traj_step(nmodes)
             kname = "fssh2_sb_fast_kernel<AccKahan,25,Ehrenfest>"
-        else:  # iesh
+        else:  # iesh, ehrenfest_na (the same model, integrator and kernel)
             n = args.ntraj if args.ntraj != 100_000 else 20_000
             nsteps = args.nsteps or 500
             nsub, stride = 608, 100
             wl = WL.newns_anderson_iesh(n, traj_offset=rank_off * n)
             obsv = {}
             for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
-                eng = C.iesh_newns_anderson(L, wl, nt, prec, save_stride=stride, traj_offset=rank_off * n)
+                eng = C.iesh_newns_anderson(L, wl, nt, prec, save_stride=stride, traj_offset=rank_off * n,
+                                            method=L.METHOD_EHRENFEST_NA if wk == "ehrenfest_na" else L.METHOD_IESH)
                 eng.set_initial(np.ascontiguousarray(wl["r0"][:nt]), np.ascontiguousarray(wl["v0"][:nt]))
                 ob = np.zeros((nsteps // stride + 1) * 4)
                 sub = name != "fp32"
@@ -518,7 +520,7 @@ def secondary(args, dist):
                    "impurity_population_abs_error": float(np.max(np.abs(b[:, 2] - a[:, 2]))), "tolerance": 0.01}
             st = res["fp32"]["st"]
             terms = st.propagator_terms / max(1, st.traj_steps)
-            cfg = {"workload": "iesh_newns_anderson_80states_40e_3dof_traj20k_dt0.1fs", "ntraj_per_gpu": n,
+            cfg = {"workload": ("ehrenfest_na" if wk == "ehrenfest_na" else "iesh") + "_newns_anderson_80states_40e_3dof_traj20k_dt0.1fs", "ntraj_per_gpu": n,
                    "nsteps": nsteps, "chebyshev_terms_per_step": terms,
                    "full_hop_evaluations_per_step": st.hop_evaluations / max(1, st.traj_steps)}
             ref_flops = 3.5e7

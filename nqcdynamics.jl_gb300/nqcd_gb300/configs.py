@@ -88,12 +88,15 @@ def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0,
     return L.Engine(cfg, [params, masses, eps, V])
 
 
-def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max_hops=0, exact=0, traj_offset=0):
+def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max_hops=0, exact=0, traj_offset=0,
+                        method=None):
     """C5: IESH on the three-dimensional Newns-Anderson adsorbate, Fermi-Dirac
-    initial occupations."""
+    initial occupations (method=L.METHOD_EHRENFEST_NA: EhrenfestNA on the same
+    system)."""
     P = wl["params"]
     cfg = L.nqcd_config()
-    cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_IESH, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
+    cfg.method, cfg.model, cfg.precision, cfg.rescaling = (method or L.METHOD_IESH), L.MODEL_NEWNS_ANDERSON_3D, \
+        precision, rescaling
     cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nelectrons = 3, 1, wl["nstates"], wl["nelectrons"]
     params = np.array([P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"]])
     masses = np.array([wl["mass"]])
