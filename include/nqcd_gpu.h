@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 102
+#define NQCD_ABI_VERSION 103
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -119,6 +119,9 @@ typedef struct nqcd_config {
     int32_t nelectrons;   /* IESH: electrons (occupied one-electron states) */
     int32_t exact_hop_probability; /* IESH: 1 = no estimate screen (estimate_probability = false) */
     int32_t reserved[2];
+    double decoherence_C; /* IESH: energy-based decoherence correction (DecoherenceCorrectionEDC(C),
+                             decoherence_corrections.jl:21-39, applied after every step as the callback
+                             of iesh.jl:424-441); 0 = none (the reference's default), 0.1 = EDC() */
 } nqcd_config;
 
 typedef struct nqcd_outputs {

@@ -82,6 +82,7 @@ struct IeshParams {
     int32_t init_kind;
     int32_t exact_probability;      // 1: every step evaluates all probabilities (estimate_probability = false)
     int32_t ehrenfest_na;           // 1: Simulation{EhrenfestNA} (mean-field force of the orbitals, no hops)
+    double edc_C;                   // > 0: energy-based decoherence correction after every step
     int32_t save_stride, nsave, max_hops;
     int64_t ntraj, traj_offset;
     double dt;
@@ -1032,6 +1033,37 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             if (warp == 0) v[2] = misc[3];  // hop counts live in thread 0, which writes them out
         }
         }  // !ena
+        if (p.edc_C > 0.0) {
+            // DecoherenceCorrectionEDC (decoherence_corrections.jl:21-39, callback
+            // iesh.jl:424-441), after the hop: in the column of electron e with
+            // occupied state s, psi_j *= exp(-dt / tau_j), tau_j = (1 + C / Ekin) /
+            // |E_j - E_s| for j != s, then psi_s rescaled to restore the norm
+            if (tid == 0) misc[7] = kinetic();
+            __syncthreads();
+            const double ekin = misc[7];
+            for (int e = tid; e < Ne; e += nthr) {
+                const int s = occ[e];
+                R unocc_norm = R(0);
+                for (int j = 0; j < N; ++j) {
+                    if (j == s) continue;
+                    const R tau = (R)((1.0 + p.edc_C / ekin) / fabs((double)lam[j] - (double)lam[s]));
+                    R f;
+                    if constexpr (std::is_same<R, float>::value)
+                        f = __expf(-(R)dt / tau);
+                    else
+                        f = nqcd_exp(-dt / tau);
+                    Cx<R> c = phiA[j * Nep + e];
+                    c.re *= f;
+                    c.im *= f;
+                    phiA[j * Nep + e] = c;
+                    unocc_norm += c.re * c.re + c.im * c.im;
+                }
+                const Cx<R> cm = phiA[s * Nep + e];
+                const R g = sqrt((R(1) - unocc_norm) / (cm.re * cm.re + cm.im * cm.im));
+                phiA[s * Nep + e] = {cm.re * g, cm.im * g};
+            }
+            __syncthreads();
+        }
         if (p.save_stride > 0 && p.obs_partial && step % p.save_stride == 0) save(isave++);
     }
 

@@ -431,6 +431,10 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: unknown model");
         if (cfg->nstates != 2) return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: only two-state models");
     }
+    if (!(cfg->decoherence_C >= 0.0 && cfg->decoherence_C < 1e300))
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: decoherence_C must be finite and >= 0");
+    if (cfg->decoherence_C != 0.0 && cfg->method != NQCD_METHOD_IESH)
+        return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: the decoherence correction applies to IESH");
     if (cfg->precision != NQCD_PREC_FP64 && cfg->precision != NQCD_PREC_FP32 && cfg->precision != NQCD_PREC_FP32_KAHAN)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown precision");
     if (cfg->rescaling < 0 || cfg->rescaling > 2) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: unknown rescaling");
@@ -1060,6 +1064,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.init_kind = h->cfg.init_kind;
         q.exact_probability = h->cfg.exact_hop_probability ? 1 : 0;
         q.ehrenfest_na = h->cfg.method == NQCD_METHOD_EHRENFEST_NA ? 1 : 0;
+        q.edc_C = h->cfg.decoherence_C;
         q.save_stride = stride;
         q.nsave = nsave;
         q.max_hops = h->cfg.max_hops;

@@ -23,6 +23,7 @@ from .api import (
     Adiabatic,
     Atoms,
     Diabatic,
+    DecoherenceCorrectionEDC,
     DynamicalDistribution,
     EhrenfestNA,
     Ehrenfest,

@@ -65,6 +65,7 @@ class nqcd_config(C.Structure):
         ("nelectrons", C.c_int32),
         ("exact_hop_probability", C.c_int32),
         ("reserved", C.c_int32 * 2),
+        ("decoherence_C", C.c_double),
     ]
 
 

@@ -251,11 +251,19 @@ class EhrenfestNA:
 
 
 @dataclass
+class DecoherenceCorrectionEDC:
+    """Energy-based decoherence correction (decoherence_corrections.jl:8-13)."""
+
+    C: float = 0.1
+
+
+@dataclass
 class AdiabaticIESH:
     """Independent-electron surface hopping (iesh.jl:72-87)."""
 
     rescaling: str = "standard"
     estimate_probability: bool = True
+    decoherence: Any = None  # None (DecoherenceCorrectionNone) or DecoherenceCorrectionEDC
 
     def __post_init__(self):
         if self.rescaling not in L.RESCALE:
@@ -274,7 +282,7 @@ class Simulation(metaclass=_MethodIndexed):
     """Simulation[FSSH](atoms, model; rescaling=:standard)."""
 
     def __init__(self, atoms: Atoms, model: Model, method=FSSH, rescaling: str = "standard", temperature=0.0,
-                 friction_method=None, estimate_probability: bool = True):
+                 friction_method=None, estimate_probability: bool = True, decoherence=None):
         self.atoms = atoms
         self.model = model
         self.temperature = float(temperature)
@@ -295,7 +303,10 @@ class Simulation(metaclass=_MethodIndexed):
                 raise NotImplementedError(f"{method.__name__} runs on AndersonHolstein(AdsorbateMetal3D(...), bath)")
             if len(atoms) != 1:
                 raise ValueError("one adsorbate atom with three degrees of freedom")
-            self.method = AdiabaticIESH(rescaling, estimate_probability) if method is AdiabaticIESH else EhrenfestNA()
+            if decoherence is not None and not isinstance(decoherence, DecoherenceCorrectionEDC):
+                raise NotImplementedError("decoherence: DecoherenceCorrectionEDC or None")
+            self.method = AdiabaticIESH(rescaling, estimate_probability, decoherence) if method is AdiabaticIESH \
+                else EhrenfestNA()
             return
         if method is Ehrenfest:
             self.method = Ehrenfest()
@@ -734,6 +745,8 @@ def _metal_config(sim, ntraj, alg, save_stride):
         params = np.array([imp.kxy, imp.A, imp.a, imp.delta, imp.B, imp.b])
         cfg.rescaling = 0 if ena else L.RESCALE[sim.method.rescaling]
         cfg.exact_hop_probability = 0 if ena else int(not sim.method.estimate_probability)
+        if not ena and sim.method.decoherence is not None:
+            cfg.decoherence_C = sim.method.decoherence.C
         cfg.nelectrons = model.nelectrons
         cfg.max_hops = alg.max_hops
     masses = np.ascontiguousarray(sim.atoms.masses, dtype=np.float64)

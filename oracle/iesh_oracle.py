@@ -172,15 +172,30 @@ def impurity_population(psi, Z, state):
     return (np.abs(amp) ** 2 - sq).sum(1) + (np.take_along_axis(z0, state, axis=1) ** 2).sum(1)
 
 
+def apply_decoherence_edc(psi, C, occupied, dt, E, ekin):
+    """apply_decoherence_correction! (decoherence_corrections.jl:21-39): Eq. 17
+    of Granucci and Persico, J. Chem. Phys. 126, 134114 (2007), in place."""
+    norm = 0.0
+    for i in range(len(psi)):
+        if i != occupied:
+            tau = (1.0 + C / ekin) / abs(E[i] - E[occupied])
+            psi[i] = psi[i] * np.exp(-dt / tau)
+            norm += abs(psi[i]) ** 2
+    cm = psi[occupied]
+    psi[occupied] = cm * np.sqrt((1.0 - norm) / abs(cm) ** 2)
+
+
 def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, max_hops=16,
-             estimate=True, initial_state=None, ehrenfest_na=False):
+             estimate=True, initial_state=None, ehrenfest_na=False, decoherence_C=0.0):
     """estimate: the reference's estimate_probability screen (iesh.jl:251-254).
     initial_state: given occupations (ntraj, ne) instead of Fermi-Dirac sampling.
     ehrenfest_na: Simulation{EhrenfestNA} instead (ehrenfest_na.jl): the same
     integrator and initial orbitals (verlet_with_electronics.jl:51-65), the
     force of the orbitals before propagation, -sum_e sum_nm A_nm
     Re(psi_ne conj(psi_me)) = -dh |sum_n z0_n psi_ne|^2 summed over e
-    (ehrenfest_na.jl:74-90; A = dh z0 z0^T for this model), and no hops."""
+    (ehrenfest_na.jl:74-90; A = dh z0 z0^T for this model), and no hops.
+    decoherence_C > 0: DecoherenceCorrectionEDC(C) applied to every electron's
+    column after each step's hop (iesh.jl:424-441)."""
     n = r0.shape[0]
     N = model.nstates
     traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
@@ -284,6 +299,11 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
                 hops[t].append((step, int(old), int(m)))
             else:
                 nfr[t] += 1
+        if decoherence_C > 0.0:
+            for t in range(n):
+                ekin = 0.5 * mass * np.sum(v[t] * v[t])
+                for e in range(ne):
+                    apply_decoherence_edc(psi[t, :, e], decoherence_C, int(state[t, e]), dt, w[t], ekin)
     e1 = energy(w, psi)
     nimp = impurity_population_ehrenfest_na(psi, Z) if ehrenfest_na else impurity_population(psi, Z, state)
     return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, Z=Z, w=w, initial_state=states,

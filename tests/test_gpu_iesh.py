@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 
 def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_DIRAC, max_hops=32, save_stride=0,
-              exact=0, method=L.METHOD_IESH):
+              exact=0, method=L.METHOD_IESH, decoherence=0.0):
     P = wl["params"]
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision, cfg.rescaling = method, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
@@ -40,6 +40,7 @@ def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_D
     cfg.max_hops = max_hops
     cfg.save_stride = save_stride
     cfg.exact_hop_probability = exact
+    cfg.decoherence_C = decoherence
     return L.Engine(cfg, [params, masses, eps, V])
 
 
@@ -143,3 +144,19 @@ def test_iesh_fast_path_observables():
     se = fa["nhops"].std() / np.sqrt(n)
     assert abs(fb["nhops"].mean() - fa["nhops"].mean()) <= 3 * se + 0.01
     assert np.mean(fa["nhops"] == fb["nhops"]) > 0.9
+
+
+def test_iesh_decoherence_edc_fp64_matches_oracle():
+    """IESH with DecoherenceCorrectionEDC(0.1) (decoherence_corrections.jl:21-39,
+    applied after every step, iesh.jl:424-441): hop sequences identical to the
+    oracle's, r, v and orbitals to 1e-8, and the correction changes the run."""
+    n, nsteps = 16, 600
+    wl = WL.newns_anderson_iesh(n, nstates=20, nelectrons=10, z0=3.0)
+    fin = run_engine(wl, n, nsteps, 11, decoherence=0.1)
+    o = IO.run_iesh(oracle_model(wl), mass=wl["mass"], ne=10, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"],
+                    dt=wl["dt"], nsteps=nsteps, seed=11, decoherence_C=0.1)
+    compare_with_oracle(fin, o, n)
+    plain = run_engine(wl, n, nsteps, 11)
+    assert np.max(np.abs(plain["psi"] - fin["psi"])) > 1e-3
+    norms = np.linalg.norm(fin["psi"], axis=1)
+    np.testing.assert_allclose(norms, 1.0, atol=1e-10)

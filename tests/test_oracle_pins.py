@@ -489,3 +489,28 @@ def test_ehrenfest_na_fixed_step_against_high_accuracy():
     d2 = np.abs(runs[2]["energy"][:, 1] - runs[2]["energy"][:, 0])
     d4 = np.abs(runs[4]["energy"][:, 1] - runs[4]["energy"][:, 0])
     assert np.all((d2 / d4 > 1.6) & (d2 / d4 < 2.5))
+
+
+def test_decoherence_edc_reference_properties():
+    """test/Dynamics/test_decoherence_corrections.jl: after one correction the
+    unoccupied populations shrink, the occupied one grows, the norm stays 1;
+    and each unoccupied coefficient is scaled by exp(-dt |E_j - E_s| / (1 + C/Ekin))
+    (decoherence_corrections.jl:21-39, C = 0.1 by default)."""
+    import iesh_oracle as IO
+
+    rng = np.random.default_rng(3)
+    psi = rng.random(4) + 1j * rng.random(4)
+    psi /= np.linalg.norm(psi)
+    orig = psi.copy()
+    occupied, dt, E, ekin = 1, 0.1, np.array([0.1, 0.2, 0.3, 0.4]), 0.25
+    IO.apply_decoherence_edc(psi, 0.1, occupied, dt, E, ekin)
+    for i in range(4):
+        if i != occupied:
+            assert abs(psi[i]) ** 2 < abs(orig[i]) ** 2
+            assert psi[i] == pytest.approx(orig[i] * np.exp(-dt * abs(E[i] - E[occupied]) / (1 + 0.1 / ekin)),
+                                           rel=1e-14)
+        else:
+            assert abs(psi[i]) ** 2 > abs(orig[i]) ** 2
+            assert np.angle(psi[i]) == pytest.approx(np.angle(orig[i]))
+    assert np.linalg.norm(orig) == pytest.approx(1.0)
+    assert np.linalg.norm(psi) == pytest.approx(1.0)
