@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 103
+#define NQCD_ABI_VERSION 104
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -152,6 +152,8 @@ typedef struct nqcd_stats {
     int64_t unconverged_roots;        /* MDEF, IESH: secular roots that hit the iteration cap */
     int64_t hop_evaluations;          /* IESH: steps whose hop probabilities were evaluated in full */
     int64_t propagator_terms;         /* IESH: Chebyshev terms summed over trajectory steps */
+    int64_t electronics_fp64_steps;   /* FSSH, Ehrenfest, RPSH fast paths: steps whose electronics ran in
+                                         FP64 because the adiabatic gap was below gap_fp64 */
 } nqcd_stats;
 
 typedef struct nqcd_handle nqcd_handle;
@@ -271,6 +273,14 @@ int nqcd_mlp_loss_grad(nqcd_handle* h, int64_t n, const double* x, const double*
 /* Accepted hops of the last run, [ntraj][max_hops][3] = (step, from, to), -1 padded
  * (DynamicsOutputs.OutputSurfaceHops, src/DynamicsOutputs.jl:235-243). */
 int nqcd_get_hop_log(nqcd_handle* h, int32_t* log);
+
+/* Per-trajectory status of the last nqcd_run (host arrays of ntraj, NULL to
+ * skip): nonfinite[t] = 1 where a final position or velocity is not finite
+ * (the trajectories counted in nqcd_stats.flagged), fp64_steps[t] = steps of
+ * a fast path whose electronics ran in FP64 because the adiabatic gap was
+ * below gap_fp64 (0 on the plain path and for MDEF/IESH).  Frustrated-hop
+ * counts come from nqcd_get_final. */
+int nqcd_get_status(nqcd_handle* h, int32_t* nonfinite, int32_t* fp64_steps);
 
 /* Message of the last failed call on this handle (or of the last failed
  * nqcd_create in this thread when h is NULL). */

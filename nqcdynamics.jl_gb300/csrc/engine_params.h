@@ -51,6 +51,7 @@ struct FsshParams {
     double* energy;           // [2][ntraj]
     double* popcorr_partial;  // [nwarps][nsave][4]
     unsigned long long* scatter;  // [4]
+    int32_t* fp64_steps;      // [ntraj] fast paths: steps whose electronics ran in FP64 (gap below gap_fp64)
 };
 
 // Host launchers (one translation unit per precision).

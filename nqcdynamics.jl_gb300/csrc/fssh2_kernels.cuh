@@ -148,9 +148,10 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>&
 // gap threshold the FP64 sub-integrator runs on the same relative times.
 template <typename P>  // FsshParams or RpshParams
 __device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>& buf, bool first, float h, float gap,
-                                                   Sig2<float>& sg) {
+                                                   Sig2<float>& sg, int& nfp64) {
     const float dtsub = p.dtsub;
     if (gap < p.gap_fp64) {
+        ++nfp64;  // steps integrated with the FP64 electronics (per-trajectory status)
         const double hd = h;
         const double tn = first ? p.t0 + hd : hd, t = first ? p.t0 : 0.0;
         EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, 0.0, buf.E0n, buf.E1n, buf.Dn, tn};
@@ -321,7 +322,8 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         buf.E1n = w[1];
         buf.Dn = R(0) + nac * (R)v;
         if constexpr (IsFast<R>::value) {
-            electronics2_sched(p, buf, step == 0, (float)h, w[1] - w[0], sg);
+            int nfp64_unused = 0;
+            electronics2_sched(p, buf, step == 0, (float)h, w[1] - w[0], sg, nfp64_unused);
         } else {
             buf.tc = buf.tn;
             buf.tn = t + h;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
     }
 
     EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
-    int nh = 0, nf = 0, step = 0;
+    int nh = 0, nf = 0, step = 0, nfp64 = 0;
     const float dtf = (float)p.dt;
     while (step < p.nsteps_total) {
         const float h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
@@ -469,7 +471,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
         buf.E0n = w[0];
         buf.E1n = w[1];
         buf.Dn = nac * v.f();
-        electronics2_sched(p, buf, step == 0, h, w[1] - w[0], sg);
+        electronics2_sched(p, buf, step == 0, h, w[1] - w[0], sg, nfp64);
         step += 1;
 
         // hop test
@@ -519,6 +521,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
     const double xf = x.get(), vf = v.get();
     p.r[i] = xf;
     p.v[i] = vf;
+    if (p.fp64_steps) p.fp64_steps[i] = nfp64;
     write_sigma<float>(p, i, sg);
     p.state[i] = state;
     if (p.nhops) p.nhops[i] = nh;

@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
     }
 
     EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
-    int nh = 0, nf = 0, step = 0;
+    int nh = 0, nf = 0, step = 0, nfp64 = 0;
     float cv = 0.f;
     const float dtf = (float)p.dt;
     // the host's step schedule replaces the reference's FP64 clock (no FP64 in the loop)
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
         buf.E0n = w[0] - vmean;
         buf.E1n = w[1] - vmean;
         buf.Dn = cv * dscale;
-        electronics2_sched(p, buf, step == 0, h, gap, sg);
+        electronics2_sched(p, buf, step == 0, h, gap, sg, nfp64);
         step += 1;
 
         // hop test (identical in all G lanes of the group)
@@ -243,6 +243,7 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
         }
     }
     if (!lead) return;
+    if (p.fp64_steps) p.fp64_steps[i] = nfp64;
     write_sigma<float>(p, i, sg);
     p.state[i] = state;
     if (p.nhops) p.nhops[i] = nh;

@@ -145,9 +145,10 @@ __global__ void sample_initial_kernel(const nqcd_sampler* __restrict__ tab, int 
 // Run statistics: steps, hops, frustrated hops, non-finite trajectories.
 __global__ void stats_kernel(const int32_t* nsteps, const int32_t* nhops, const int32_t* nfrust,
                              const double* r, const double* v, int64_t ndof, int64_t ntraj,
-                             unsigned long long* out) {
-    unsigned long long a = 0, b = 0, c = 0, d = 0;
+                             unsigned long long* out, const int32_t* fp64_steps, unsigned long long* out_fp64) {
+    unsigned long long a = 0, b = 0, c = 0, d = 0, e = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ntraj; i += (int64_t)gridDim.x * blockDim.x) {
+        if (fp64_steps) e += (unsigned long long)fp64_steps[i];
         a += (unsigned long long)nsteps[i];
         b += (unsigned long long)nhops[i];
         c += (unsigned long long)nfrust[i];
@@ -160,12 +161,23 @@ __global__ void stats_kernel(const int32_t* nsteps, const int32_t* nhops, const 
         b += __shfl_xor_sync(0xffffffffu, b, off);
         c += __shfl_xor_sync(0xffffffffu, c, off);
         d += __shfl_xor_sync(0xffffffffu, d, off);
+        e += __shfl_xor_sync(0xffffffffu, e, off);
     }
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(out + 0, a);
         atomicAdd(out + 1, b);
         atomicAdd(out + 2, c);
         atomicAdd(out + 3, d);
+        if (fp64_steps) atomicAdd(out_fp64, e);
+    }
+}
+
+// Per-trajectory status: 1 where a final position or velocity is not finite.
+__global__ void nonfinite_kernel(const double* r, const double* v, int64_t ndof, int64_t ntraj, int32_t* flag) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ntraj; i += (int64_t)gridDim.x * blockDim.x) {
+        bool bad = false;
+        for (int64_t I = 0; I < ndof; ++I) bad |= !isfinite(r[I * ntraj + i]) || !isfinite(v[I * ntraj + i]);
+        flag[i] = bad ? 1 : 0;
     }
 }
 
@@ -237,6 +249,7 @@ struct nqcd_handle {
     float* d_rpcirc = nullptr;  // fast path: circulant free-step coefficients, [count][32][4]
     int32_t *d_nbeads = nullptr, *d_class_traj = nullptr, *d_block_class = nullptr;
     unsigned long long* d_queue = nullptr;
+    int32_t* d_fp64steps = nullptr;  // two-state methods: per trajectory, steps with FP64 electronics
     double* d_rpscratch = nullptr;  // plain path bead arrays, grown on demand
     int64_t rpscratch_cap = 0;
     int nclass = 0;
@@ -290,7 +303,7 @@ void free_all(nqcd_handle* h) {
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
                     h->d_rpU, h->d_rpcay, h->d_rpcirc, h->d_nbeads, h->d_class_traj,
                     h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2,
-                    h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im, h->d_redtmp};
+                    h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im, h->d_redtmp, h->d_fp64steps};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mlp_free(h->mlp);
@@ -547,6 +560,10 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     NQCD_CREATE(dalloc(&h->d_nhops, cap));
     NQCD_CREATE(dalloc(&h->d_nfrust, cap));
     NQCD_CREATE(dalloc(&h->d_nsteps, cap));
+    if (!mdef && !iesh) {  // FSSH, Ehrenfest, RPSH: per-trajectory FP64-electronics step counts
+        NQCD_CREATE(dalloc(&h->d_fp64steps, cap));
+        NQCD_CREATE(cudaMemset(h->d_fp64steps, 0, cap * sizeof(int32_t)));
+    }
     if (cfg->max_hops > 0) NQCD_CREATE(dalloc(&h->d_hoplog, (int64_t)cfg->max_hops * 3 * cap));
     NQCD_CREATE(dalloc(&h->d_energy, 2 * cap));
     NQCD_CREATE(dalloc(&h->d_counts, 16));
@@ -786,6 +803,29 @@ int nqcd_sample_initial(nqcd_handle* h, int64_t ntraj, const nqcd_sampler* posit
     return set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
 }
 
+int nqcd_get_status(nqcd_handle* h, int32_t* nonfinite, int32_t* fp64_steps) {
+    if (!h) return NQCD_ERR_ARG;
+    if (!h->has_run) return fail(h, NQCD_ERR_STATE, "nqcd_get_status: call nqcd_run first");
+    const int64_t N = h->ntraj;
+    if (nonfinite) {
+        int rc = ensure_stage(h, (N + 1) / 2);
+        if (rc) return rc;
+        int32_t* flag = reinterpret_cast<int32_t*>(h->d_stage);
+        nonfinite_kernel<<<(unsigned)((N + 255) / 256 < 1024 ? (N + 255) / 256 : 1024), 256, 0, h->stream>>>(
+            h->d_r, h->d_v, h->ndof, N, flag);
+        NQCD_CUDA(h, cudaGetLastError());
+        NQCD_CUDA(h, cudaMemcpyAsync(nonfinite, flag, N * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (fp64_steps) {
+        if (h->d_fp64steps)
+            NQCD_CUDA(h, cudaMemcpyAsync(fp64_steps, h->d_fp64steps, N * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+        else
+            memset(fp64_steps, 0, N * sizeof(int32_t));
+    }
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    return NQCD_OK;
+}
+
 int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out, nqcd_stats* stats) {
     if (!h) return NQCD_ERR_ARG;
     if (!h->initial_set) return fail(h, NQCD_ERR_STATE, "nqcd_run: call nqcd_set_initial first");
@@ -841,6 +881,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_sig, h->d_sig0, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_state, h->d_state0, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 16 * sizeof(unsigned long long), s));
+    if (h->d_fp64steps) NQCD_CUDA(h, cudaMemsetAsync(h->d_fp64steps, 0, N * sizeof(int32_t), s));
     if (h->d_hoplog) {
         int64_t nl = (int64_t)h->cfg.max_hops * 3 * N;
         fill_i32_kernel<<<(unsigned)((nl + 255) / 256 < 4096 ? (nl + 255) / 256 : 4096), 256, 0, s>>>(h->d_hoplog, nl, -1);
@@ -904,6 +945,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.energy = h->d_energy;
     p.popcorr_partial = h->d_partial;
     p.scatter = p.ehrenfest ? nullptr : h->d_counts;  // Ehrenfest: population sums after the run
+    p.fp64_steps = h->d_fp64steps;
     cudaError_t e = cudaSuccess;
     int64_t h2d = 0;
     if (h->cfg.method == NQCD_METHOD_RPSH) {
@@ -1005,6 +1047,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         rq.hop_log = h->d_hoplog;
         rq.energy = h->d_energy;
         rq.scatter = h->d_counts;
+        rq.fp64_steps = h->d_fp64steps;
         if (plain) {
             int maxb = 1;
             for (int k = 0; k < h->nclass; ++k) maxb = h->class_beads[k] > maxb ? h->class_beads[k] : maxb;
@@ -1125,7 +1168,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         ++launches;
     }
     stats_kernel<<<(unsigned)((N + 255) / 256 < 1024 ? (N + 255) / 256 : 1024), 256, 0, s>>>(
-        h->d_nsteps, h->d_nhops, h->d_nfrust, h->d_r, h->d_v, nd, N, h->d_counts + 4);
+        h->d_nsteps, h->d_nhops, h->d_nfrust, h->d_r, h->d_v, nd, N, h->d_counts + 4, h->d_fp64steps,
+        h->d_counts + 12);
     NQCD_CUDA(h, cudaGetLastError());
     ++launches;
     // Ehrenfest scattering: population sums in a fixed order (buffers sized before the run)
@@ -1176,6 +1220,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         stats->hops = (int64_t)counts[5];
         stats->frustrated = (int64_t)counts[6];
         stats->flagged = (int64_t)counts[7];
+        stats->electronics_fp64_steps = h->d_fp64steps ? (int64_t)counts[12] : 0;
         stats->device_ms = ms;
         stats->kernel_ms = kms;
         stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();

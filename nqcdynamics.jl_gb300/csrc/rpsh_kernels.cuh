@@ -78,6 +78,7 @@ struct RpshParams {
     int32_t* hop_log;  // [max_hops][3][ntraj]
     double* energy;    // [2][ntraj]
     unsigned long long* scatter;  // [4]
+    int32_t* fp64_steps;          // [ntraj] fast path: steps with FP64 electronics (gap below gap_fp64)
     // plain path: bead-array scratch, [6 * bead count][scratch_stride] doubles
     double* scratch;
     int64_t scratch_stride;  // threads in the launch
@@ -404,7 +405,7 @@ struct RpTraj {
     float Zc[4], w[2], nac;
     Sig2<float> sg;
     EBuf<float> buf;
-    int state, nh, nf, step;
+    int state, nh, nf, step, nfp64;
     double e0;
 };
 
@@ -480,7 +481,7 @@ __device__ __forceinline__ void rp_group_begin(const RpshParams& p, const RpLane
         t.k[q] = rp_bead_accel_f(model, mp, (float)(xc + (double)t.dx[q]), t.state, (float)(1.0 / p.mass));
     t.e0 = p.energy ? rp_group_energy<Q, GL>(p, g, model, mp, xc, vc, t.dx, t.dv, t.state) : 0.0;
     t.buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
-    t.nh = t.nf = t.step = 0;
+    t.nh = t.nf = t.step = t.nfp64 = 0;
 }
 
 template <int Q, int GL>
@@ -495,7 +496,10 @@ __device__ __forceinline__ void rp_group_finish(const RpshParams& p, const RpLan
     }
     const double x0 = __shfl_sync(g.mask, xc + (double)t.dx[0], g.base);
     const double e1 = p.energy ? rp_group_energy<Q, GL>(p, g, model, mp, xc, vc, t.dx, t.dv, t.state) : 0.0;
-    if (g.j == 0) rp_write_final<float>(p, t.i, t.sg, t.state, t.nh, t.nf, t.step, t.e0, e1, x0);
+    if (g.j == 0) {
+        rp_write_final<float>(p, t.i, t.sg, t.state, t.nh, t.nf, t.step, t.e0, e1, x0);
+        if (p.fp64_steps) p.fp64_steps[t.i] = t.nfp64;
+    }
 }
 
 // Free ring-polymer step of the deviations: (dx, dv) <- M (dx, dv), M circulant.
@@ -584,7 +588,7 @@ __device__ __forceinline__ bool rp_group_step(const RpshParams& p, const RpLanes
     t.buf.E0n = t.w[0];
     t.buf.E1n = t.w[1];
     t.buf.Dn = t.nac * t.vc.f();
-    electronics2_sched(p, t.buf, step == 0, h, gap, t.sg);
+    electronics2_sched(p, t.buf, step == 0, h, gap, t.sg, t.nfp64);
     t.step = step + 1;
 
     const int s = t.state;

@@ -22,6 +22,7 @@ ERRORS = {
     -6: "NQCD_ERR_UNSUPPORTED",
     -7: "NQCD_ERR_STATE",
 }
+globals().update({name: code for code, name in ERRORS.items()})  # NQCD_ERR_ARG = -1, ...
 
 METHOD_FSSH, METHOD_RPSH, METHOD_IESH, METHOD_MDEF, METHOD_EHRENFEST, METHOD_EHRENFEST_NA = 1, 2, 3, 4, 5, 6
 MODEL_TULLY1, MODEL_TULLY2, MODEL_TULLY3, MODEL_SPINBOSON, MODEL_NEWNS_ANDERSON = 1, 2, 3, 10, 20
@@ -97,6 +98,7 @@ class nqcd_stats(C.Structure):
         ("unconverged_roots", C.c_int64),
         ("hop_evaluations", C.c_int64),
         ("propagator_terms", C.c_int64),
+        ("electronics_fp64_steps", C.c_int64),
     ]
 
 
@@ -126,6 +128,7 @@ EXPORTED = [
     "nqcd_run",
     "nqcd_get_final",
     "nqcd_get_hop_log",
+    "nqcd_get_status",
     "nqcd_set_trajectory_models",
     "nqcd_mdef_evaluate",
     "nqcd_train_friction_mlp",
@@ -175,6 +178,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
                              C.POINTER(nqcd_outputs), C.POINTER(nqcd_stats)]
     lib.nqcd_get_final.argtypes = [C.c_void_p, DP, DP, DP, DP, IP, IP, IP, IP, DP]
     lib.nqcd_get_hop_log.argtypes = [C.c_void_p, IP]
+    lib.nqcd_get_status.argtypes = [C.c_void_p, IP, IP]
     lib.nqcd_set_trajectory_models.argtypes = [C.c_void_p, IP]
     lib.nqcd_mdef_evaluate.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP]
     lib.nqcd_train_friction_mlp.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32, C.c_int32,
@@ -237,6 +241,14 @@ class Engine:
         sequences of (kind, a, b) per degree of freedom."""
         self._check(self.lib.nqcd_sample_initial(self.h, ntraj, samplers(position), samplers(velocity), seed))
         self.ntraj = ntraj
+
+    def get_status(self):
+        """Per-trajectory status of the last run: non-finite flags and FP64
+        electronics step counts."""
+        nonfinite = np.empty(self.ntraj, np.int32)
+        fp64 = np.empty(self.ntraj, np.int32)
+        self._check(self.lib.nqcd_get_status(self.h, iptr(nonfinite), iptr(fp64)))
+        return dict(nonfinite=nonfinite, fp64_steps=fp64)
 
     def set_initial_device(self, ntraj: int, d_r0: int, d_v0: int):
         self._check(self.lib.nqcd_set_initial_device(self.h, ntraj, C.c_void_p(d_r0), C.c_void_p(d_v0), None))

@@ -5,6 +5,8 @@ states and hop sequences (the oracle and the kernels evaluate the same
 operations in the same order).  Fast FP32 path: ensemble observables
 within the stated tolerance of the FP64 oracle.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -195,3 +197,50 @@ def test_engine_errors():
     bad.method = 99
     with pytest.raises(L.EngineError):
         L.Engine(bad)
+
+
+def test_per_trajectory_status():
+    """nqcd_get_status: non-finite final states flagged per trajectory, and
+    the steps each fast-path trajectory integrated with the FP64 electronics
+    (every step when gap_fp64 exceeds any gap; none for the NaN trajectory,
+    whose gap compares false), summed into nqcd_stats."""
+    ntraj, m, nsteps = 512, 2000.0, 200
+    r0 = np.full((ntraj, 1), -10.0)
+    v0 = np.full((ntraj, 1), 15.0 / m)
+    r0[7, 0] = np.nan
+    cfg, keep = make_cfg(1, TULLY[1], 1, m, ntraj, precision=L.PREC_FP32)
+    cfg.gap_fp64 = 1e9
+    eng = L.Engine(cfg, keep)
+    try:
+        eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0))
+        # the run completes and reports the non-finite trajectory as NQCD_ERR_NAN
+        out, st = L.nqcd_outputs(), L.nqcd_stats()
+        rc = eng.lib.nqcd_run(eng.h, 0.0, float(nsteps), 1.0, 3, ctypes.byref(out), ctypes.byref(st))
+        assert rc == L.NQCD_ERR_NAN
+        status = eng.get_status()
+    finally:
+        eng.close()
+    expect_nf = np.zeros(ntraj, np.int32)
+    expect_nf[7] = 1
+    np.testing.assert_array_equal(status["nonfinite"], expect_nf)
+    assert st.flagged == 1
+    expect_fb = np.full(ntraj, nsteps, np.int32)
+    expect_fb[7] = 0
+    np.testing.assert_array_equal(status["fp64_steps"], expect_fb)
+    assert st.electronics_fp64_steps == expect_fb.sum()
+    # spin-boson fast kernel (4 lanes per trajectory), and the plain path (no fallback)
+    nm, n2 = 100, 256
+    w, c, rs, vs = spin_boson_case(n2, nm, seed=2)
+    for prec, fb in ((L.PREC_FP32_KAHAN, 40), (L.PREC_FP64, 0)):
+        cfg, keep = make_cfg(L.MODEL_SPINBOSON, (0.0, 1.0), nm, 1.0, n2, precision=prec, init_kind=2, bath=(c, w))
+        cfg.gap_fp64 = 1e9
+        eng = L.Engine(cfg, keep)
+        try:
+            eng.set_initial(np.ascontiguousarray(rs), np.ascontiguousarray(vs))
+            _, st = eng.run(0.0, 2.0, 0.05, 3)
+            status = eng.get_status()
+        finally:
+            eng.close()
+        np.testing.assert_array_equal(status["fp64_steps"], fb)
+        np.testing.assert_array_equal(status["nonfinite"], 0)
+        assert st.electronics_fp64_steps == fb * n2

@@ -29,7 +29,7 @@ def rp_inputs(ntraj, seed, counts=(4, 5, 8, 10, 16, 32)):
     return r0, v0, nb
 
 
-def make_rp_engine(model, ntraj, precision=L.PREC_FP64, rescaling=0, terminate_x=10.0, max_hops=16):
+def make_rp_engine(model, ntraj, precision=L.PREC_FP64, rescaling=0, terminate_x=10.0, max_hops=16, gap_fp64=1e-3):
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision, cfg.rescaling = L.METHOD_RPSH, model, precision, rescaling
     cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nbeads_max = 1, 1, 2, BMAX
@@ -41,7 +41,7 @@ def make_rp_engine(model, ntraj, precision=L.PREC_FP64, rescaling=0, terminate_x
     cfg.init_kind, cfg.init_state = L.INIT_ADIABATIC_PURE, 0
     cfg.max_hops = max_hops
     cfg.terminate_x = terminate_x
-    cfg.gap_fp64 = 1e-3
+    cfg.gap_fp64 = gap_fp64
     return L.Engine(cfg, [p, m])
 
 
@@ -192,3 +192,18 @@ def test_rpsh_fast_independent_of_queue_order():
         np.testing.assert_array_equal(a[key], b[key], err_msg=key)
         np.testing.assert_array_equal(a[key], c[key], err_msg=key)
     assert a["nhops"].sum() > 0
+
+
+def test_rpsh_fast_status_counts_fp64_steps():
+    # every step of every trajectory in FP64 electronics: the count equals the trajectory's own step count
+    ntraj = 600
+    r0, v0, nb = rp_inputs(ntraj, 41, counts=(4, 8, 16, 32, 5, 10))
+    eng = make_rp_engine(1, ntraj, precision=L.PREC_FP32, gap_fp64=1e9)
+    try:
+        fin = run_rp(eng, r0, v0, nb, 4000.0, 9)
+        status = eng.get_status()
+    finally:
+        eng.close()
+    np.testing.assert_array_equal(status["fp64_steps"], fin["nsteps"])
+    assert fin["stats"].electronics_fp64_steps == int(fin["nsteps"].sum())
+    np.testing.assert_array_equal(status["nonfinite"], 0)
