@@ -22,9 +22,6 @@ namespace nqcd {
 
 constexpr int kFsshBlock = 128;
 
-template <typename R>
-struct IsFast : std::integral_constant<bool, std::is_same<R, float>::value> {};
-
 // Per-warp partial sums of the diabatic population correlation at one save
 // point (TimeCorrelationFunctions.jl:61-88); reduced over warps afterwards in
 // a fixed order, so the ensemble mean is deterministic.
@@ -119,27 +116,13 @@ __device__ __forceinline__ void init_electronics2(const FsshParams& p, int64_t i
     state = (S[0][0] < tt) ? 1 : 0;
 }
 
-// One electronic macro step: plain path in FP64; fast path in FP32 unless
-// the adiabatic gap is below gap_fp64.
-template <typename R>
-__device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<R>& buf, double t, double h,
-                                             R gap, Sig2<R>& sg) {
+// One electronic macro step of the plain path (FP64, the reference's
+// fixed sub-steps of dt/5 on the FP64 clock).
+__device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<double>& buf, double t, double h,
+                                             Sig2<double>& sg) {
     const double dtsub = p.dt / 5.0;
-    if constexpr (!IsFast<R>::value) {
-        Interp64 fn(buf);
-        electronic_macro_step2<double>(fn, t, h, dtsub, sg);
-    } else {
-        if (gap < p.gap_fp64) {
-            EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, buf.tc, buf.E0n, buf.E1n, buf.Dn, buf.tn};
-            Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
-            Interp64 fn(b64);
-            electronic_macro_step2<double>(fn, t, h, dtsub, s64);
-            sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
-        } else {
-            InterpS32 fn(buf, t, h);
-            electronic_macro_step2_fast(fn, (float)h, (float)dtsub, sg);
-        }
-    }
+    Interp64 fn(buf);
+    electronic_macro_step2<double>(fn, t, h, dtsub, sg);
 }
 
 // Fast-path electronic step on the host-computed schedule: interpolation
@@ -302,13 +285,9 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
     int nh = 0, nf = 0, step = 0;
     double t = p.t0;
     const R dtR = (R)p.dt;
-    // plain path: the reference's FP64 clock; fast path: the host schedule
-    while (IsFast<R>::value ? step < p.nsteps_total : t < p.t1) {
-        double h;
-        if constexpr (IsFast<R>::value)
-            h = step == 0 ? p.h_first : (step + 1 == p.nsteps_total ? p.h_last : p.h_mid);
-        else
-            h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
+    // the reference's FP64 clock
+    while (t < p.t1) {
+        double h = (p.t1 - t) < p.dt ? (p.t1 - t) : p.dt;
         double half = h / 2.0;
         double vtmp = v + half * k;
         x = x + h * vtmp;
@@ -321,13 +300,10 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         buf.E0n = w[0];
         buf.E1n = w[1];
         buf.Dn = R(0) + nac * (R)v;
-        if constexpr (IsFast<R>::value) {
-            int nfp64_unused = 0;
-            electronics2_sched(p, buf, step == 0, (float)h, w[1] - w[0], sg, nfp64_unused);
-        } else {
+        {
             buf.tc = buf.tn;
             buf.tn = t + h;
-            electronics2<R>(p, buf, t, h, w[1] - w[0], sg);
+            electronics2(p, buf, t, h, sg);
             t = snap_time(t + h, p.t1);
         }
         step += 1;
@@ -370,15 +346,9 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
             }
         }
         if (p.save_stride > 0 && step % p.save_stride == 0) {
-            if constexpr (IsFast<R>::value) {
-                float pf[2], p0f[2] = {(float)pop0[0], (float)pop0[1]};
-                diabatic_pop2_f(sg, state, Z, pf, ehr);
-                warp_save_popcorr_f(p, isave++, active, p0f, pf);
-            } else {
-                double pop[2];
-                diabatic_pop2<R>(sg, state, Z, pop, ehr);
-                warp_save_popcorr(p, isave++, active, pop0, pop);
-            }
+            double pop[2];
+            diabatic_pop2<R>(sg, state, Z, pop, ehr);
+            warp_save_popcorr(p, isave++, active, pop0, pop);
         }
     }
 
@@ -560,17 +530,10 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
     // Hamiltonian from the sums s0 = sum w2 r^2 and cr = c.r
     auto set_eigen = [&](double s0, double cr) {
         R V[3], Zn[4];
-        if constexpr (!IsFast<R>::value) {
-            double V0 = 0.5 * s0;
-            V[0] = (V0 + cr) + eps;
-            V[1] = Delta;
-            V[2] = (V0 - cr) - eps;
-        } else {
-            R V0 = (R)(0.5 * s0);
-            V[0] = (V0 + (R)cr) + eps;
-            V[1] = Delta;
-            V[2] = (V0 - (R)cr) - eps;
-        }
+        double V0 = 0.5 * s0;
+        V[0] = (V0 + cr) + eps;
+        V[1] = Delta;
+        V[2] = (V0 - cr) - eps;
         eigen2_phase<R>(V, Z, w, Zn);
 #pragma unroll
         for (int q = 0; q < 4; ++q) Z[q] = Zn[q];
@@ -640,12 +603,9 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
             cr = cr + cj[I] * rn;
         }
         set_eigen(s0, cr);
-        const R gap = w[1] - w[0];
         // B with the new force; couplings
         R Dn;
-        double cv = 0.0;
-        R M01 = Z[0] * Z[2] - Z[1] * Z[3];
-        if constexpr (!IsFast<R>::value) {
+        {
             double acc = 0.0;
             for (int I = 0; I < nd; ++I) {
                 double rI = r[(int64_t)I * N];
@@ -666,18 +626,6 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
                 acc = acc + nI * vn;
             }
             Dn = 0.0 + acc;
-        } else {
-            const float M00 = Z[0] * Z[0] - Z[1] * Z[1], M11 = Z[2] * Z[2] - Z[3] * Z[3];
-            const float Mss = ehr ? ehrenfest_weight<float>(M00, (float)M01, M11, sg) : (state == 0 ? M00 : M11);
-            for (int I = 0; I < nd; ++I) {
-                double rI = r[(int64_t)I * N];
-                double vt = v[(int64_t)I * N];
-                float kI = -((float)(w2j[I] * rI) + (float)cj[I] * Mss) / (float)mj[I];
-                double vn = vt + half * (double)kI;
-                if (active) v[(int64_t)I * N] = vn;
-                cv = cv + cj[I] * vn;
-            }
-            Dn = (float)cv * (M01 / gap);
         }
         Zk[0] = Z[0];
         Zk[1] = Z[1];
@@ -693,7 +641,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         buf.E1n = w[1];
         buf.Dn = Dn;
         buf.tn = t + h;
-        electronics2<R>(p, buf, t, h, gap, sg);
+        electronics2(p, buf, t, h, sg);
         t = snap_time(t + h, p.t1);
         step += 1;
 
@@ -702,7 +650,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         R inv = R(1) / (s == 0 ? sg.p : sg.q);
         R re = sg.x * inv;
         R prob;
-        if constexpr (!IsFast<R>::value) {
+        {
             double acc = 0.0;
             for (int I = 0; I < nd; ++I) {
                 double nI = nacs[(int64_t)I * N];
@@ -710,9 +658,6 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
                 acc = acc + 2.0 * v[(int64_t)I * N] * re * nsm * p.dt;
             }
             prob = clamp01<double>(acc);
-        } else {
-            float nsm = (s == 0 ? 1.0f : -1.0f) * (float)cv * (M01 / gap);
-            prob = clamp01<float>(2.0f * re * nsm * (float)p.dt);
         }
         double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
         if (!ehr && (double)prob > u) {  // Ehrenfest: no hopping
@@ -721,16 +666,10 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
             bool accept = true;
             if (p.rescaling != RESCALE_OFF) {
                 double aa = 0.0, bb = 0.0;
-                double dscale = (double)M01 / (double)gap;  // fast path: d_I = sgn * c_I * M01 / gap
-                if constexpr (!IsFast<R>::value) {
-                    for (int I = 0; I < nd; ++I) {
-                        double d = sgn * nacs[(int64_t)I * N];
-                        aa = aa + d * d / mj[I];
-                        bb = bb + d * v[(int64_t)I * N];
-                    }
-                } else {
-                    aa = dscale * dscale * p.sum_c2_over_m;
-                    bb = sgn * dscale * cv;
+                for (int I = 0; I < nd; ++I) {
+                    double d = sgn * nacs[(int64_t)I * N];
+                    aa = aa + d * d / mj[I];
+                    bb = bb + d * v[(int64_t)I * N];
                 }
                 aa = aa / 2.0;
                 double cc = (double)w[ns] - (double)w[s];
@@ -740,29 +679,26 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
                     if (p.rescaling == RESCALE_VINVERSION) {
                         double nrm = 0.0;
                         for (int I = 0; I < nd; ++I) {
-                            double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                            double d = sgn * nacs[(int64_t)I * N];
                             nrm = nrm + d * d;
                         }
                         nrm = sqrt(nrm);
                         double g = 0.0;
                         for (int I = 0; I < nd; ++I) {
-                            double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                            double d = sgn * nacs[(int64_t)I * N];
                             g = g + v[(int64_t)I * N] * (d / nrm);
                         }
                         for (int I = 0; I < nd; ++I) {
-                            double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                            double d = sgn * nacs[(int64_t)I * N];
                             double vn = v[(int64_t)I * N] - 2.0 * g * (d / nrm);
                             if (active) v[(int64_t)I * N] = vn;
-                        }
-                        if constexpr (IsFast<R>::value) {
-                            cv = 0.0;  // c.v is not reused after the hop test
                         }
                     }
                 } else {
                     double root = sqrt(disc);
                     double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
                     for (int I = 0; I < nd; ++I) {
-                        double d = IsFast<R>::value ? sgn * cj[I] * dscale : sgn * nacs[(int64_t)I * N];
+                        double d = sgn * nacs[(int64_t)I * N];
                         double vn = v[(int64_t)I * N] - gamma * d / mj[I];
                         if (active) v[(int64_t)I * N] = vn;
                     }
@@ -801,16 +737,24 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
     if (p.scatter) atomicAdd(p.scatter + (r[0] > 0.0 ? 2 : 0) + state, 1ull);
 }
 
+// Plain path (R = double): one thread per trajectory, both model families.
 template <typename R>
 cudaError_t launch_fssh2(const FsshParams& p, cudaStream_t s) {
+    static_assert(std::is_same<R, double>::value, "the fast paths have their own kernels");
     if (p.ntraj <= 0) return cudaSuccess;
     int64_t blocks = (p.ntraj + kFsshBlock - 1) / kFsshBlock;
     if (p.model == MODEL_SPINBOSON)
         fssh2_spinboson_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
-    else if constexpr (IsFast<R>::value)
-        fssh2_tully_fast_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
     else
         fssh2_tully_kernel<R><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// Fast one-dimensional Tully path.
+inline cudaError_t launch_tully_fast(const FsshParams& p, cudaStream_t s) {
+    if (p.ntraj <= 0) return cudaSuccess;
+    int64_t blocks = (p.ntraj + kFsshBlock - 1) / kFsshBlock;
+    fssh2_tully_fast_kernel<float><<<(unsigned)blocks, kFsshBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -11,12 +11,12 @@ namespace nqcd {
 
 cudaError_t launch_fssh2_fp32(const FsshParams& p, cudaStream_t s) {
     if (p.model == MODEL_SPINBOSON) return launch_sb_fast<AccF64>(p, s);
-    return launch_fssh2<float>(p, s);
+    return launch_tully_fast(p, s);
 }
 
 cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s) {
     if (p.model == MODEL_SPINBOSON) return launch_sb_fast<AccKahan>(p, s);
-    return launch_fssh2<float>(p, s);
+    return launch_tully_fast(p, s);
 }
 
 // Fast ring-polymer kernels, one per bead count (see rpsh_group_kernel).
