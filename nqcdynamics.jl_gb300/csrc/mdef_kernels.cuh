@@ -77,6 +77,10 @@ struct MdefParams {
     unsigned long long* counters;  // [0] exact friction evaluations, [1] surrogate evaluations, [2] non-converged roots
     double* friction_out;   // optional: exact friction at x (single evaluation mode), [ntraj]
     double* force_out;      // optional: force at x, [ntraj]
+    // ring polymers (RingPolymerSimulation{DiabaticMDEF}, rpmdef_kernel): x, v are [bead][ntraj]
+    int32_t nbeads;         // 0 or 1: classical nuclei (mdef_kernel)
+    const double* rp_U;     // [nbeads * nbeads] normal-mode matrix, column-major U[j + n k]
+    const double* rp_half;  // [nbeads][4] half-step Cayley matrices (c11, c12, c21, c22)
 };
 
 template <typename R>
@@ -193,8 +197,8 @@ __device__ inline float mlp_friction(const MlpWeights& w, float x) {
 }
 
 // Standard normal of (trajectory, step): Box-Muller on one Philox block.
-__device__ __forceinline__ double noise_normal(uint64_t seed, uint64_t traj, uint32_t step) {
-    u32x4 b = rng_block(seed, traj, step, RNG_NOISE);
+__device__ __forceinline__ double noise_normal(uint64_t seed, uint64_t traj, uint32_t step, uint32_t dof = 0) {
+    u32x4 b = rng_block(seed, traj, step, RNG_NOISE + 16u * dof);
     double u1 = 1.0 - u01_from_words(b.x, b.y);
     double u2 = u01_from_words(b.z, b.w);
     return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
@@ -202,8 +206,8 @@ __device__ __forceinline__ double noise_normal(uint64_t seed, uint64_t traj, uin
 
 // Fast path: the same Box-Muller transform of the same Philox block with
 // 24-bit uniforms in FP32.
-__device__ __forceinline__ float noise_normal_f(uint64_t seed, uint64_t traj, uint32_t step) {
-    u32x4 b = rng_block(seed, traj, step, RNG_NOISE);
+__device__ __forceinline__ float noise_normal_f(uint64_t seed, uint64_t traj, uint32_t step, uint32_t dof = 0) {
+    u32x4 b = rng_block(seed, traj, step, RNG_NOISE + 16u * dof);
     const float u1 = 1.f - (float)(b.x >> 8) * 0x1.0p-24f;
     const float u2 = (float)(b.z >> 8) * 0x1.0p-24f;
     return sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
@@ -324,8 +328,134 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Ring-polymer MDEF (RingPolymerSimulation{DiabaticMDEF}, rpmdef.jl) with the
+// BCOCB integrator (bcocb.jl:79-105): per step B (each bead's Fermi-weighted
+// force, rpmdef.jl:30-55), half Cayley step of the free ring polymer in
+// normal modes, O in bead space with each bead's own broadened friction and
+// noise at the ring-polymer temperature n T (steps.jl:71-107), half Cayley
+// step, B.  One CTA per trajectory: its kMdefWarps warps take the beads in
+// turn (bead j on warp j mod kMdefWarps; a warp's secular roots start from its
+// previous bead's, which lies close by), and warp 0 does the ring-polymer
+// algebra on the bead arrays in shared memory.  The per-bead noise is the
+// Philox normal of (trajectory, step, dof = bead).
+// ---------------------------------------------------------------------------
+constexpr int kRpMdefMaxBeads = 32;
+
+template <typename R>
+__global__ void __launch_bounds__(32 * kMdefWarps) rpmdef_kernel(const MdefParams p) {
+    __shared__ MdefShared<R> sh;
+    __shared__ double bx[kRpMdefMaxBeads], bv[kRpMdefMaxBeads], bk[kRpMdefMaxBeads];
+    __shared__ double qx[kRpMdefMaxBeads], qv[kRpMdefMaxBeads];
+    for (int k = threadIdx.x; k < p.nbath; k += blockDim.x) {
+        sh.eps[k] = (R)p.eps[k];
+        sh.V2[k] = (R)p.V2[k];
+    }
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t i = blockIdx.x;
+    const uint64_t gid = (uint64_t)(p.traj_offset + i);
+    const int64_t N = p.ntraj;
+    const int B = p.nbeads, M = p.nbath;
+    const double m = p.mass, dt = p.dt, half = 0.5;
+    const double sig_rp = sqrt((double)B / p.beta / m);  // sqrt(T_rp / m), T_rp = n T
+    for (int j = threadIdx.x; j < B; j += blockDim.x) {
+        bx[j] = p.x[(int64_t)j * N + i];
+        bv[j] = p.v[(int64_t)j * N + i];
+    }
+    R lam[kMdefRootsPerLane];
+#pragma unroll
+    for (int q = 0; q < kMdefRootsPerLane; ++q) {
+        int idx = lane + 32 * q;
+        lam[q] = R(0);
+        if (idx <= M) lam[q] = idx == 0 ? (R)p.eps[0] - R(1e-3) : (R)p.eps[idx - 1] + R(1e-9);
+    }
+    __syncthreads();
+    // forces of all beads (warp w: beads w, w + kMdefWarps, ...)
+    auto forces = [&]() {
+        for (int j = wib; j < B; j += kMdefWarps) {
+            double F, fr;
+            mdef_electronic<R>(p, sh, wib, lam, bx[j], false, F, fr);
+            if (lane == 0) bk[j] = -F / m;
+        }
+        __syncthreads();
+    };
+    // half Cayley step of the free ring polymer: to normal modes, rotate, back (warp 0)
+    auto free_half = [&]() {
+        if (wib == 0) {
+            if (lane < B) {
+                double a = 0.0, b = 0.0;
+                for (int j = 0; j < B; ++j) {
+                    const double u = p.rp_U[j + B * lane];
+                    a = a + u * bx[j];
+                    b = b + u * bv[j];
+                }
+                const double* c = p.rp_half + 4 * lane;
+                qx[lane] = c[0] * a + c[1] * b;
+                qv[lane] = c[2] * a + c[3] * b;
+            }
+            __syncwarp();
+            if (lane < B) {
+                double a = 0.0, b = 0.0;
+                for (int k = 0; k < B; ++k) {
+                    const double u = p.rp_U[lane + B * k];
+                    a = a + u * qx[k];
+                    b = b + u * qv[k];
+                }
+                bx[lane] = a;
+                bv[lane] = b;
+            }
+        }
+        __syncthreads();
+    };
+    forces();
+    unsigned long long n_exact = 0;
+    for (int step = 1; step <= p.nsteps; ++step) {
+        if (threadIdx.x < B) bv[threadIdx.x] = bv[threadIdx.x] + (half * dt) * bk[threadIdx.x];  // B
+        __syncthreads();
+        free_half();  // C
+        for (int j = wib; j < B; j += kMdefWarps) {  // O
+            double F, lamv;
+            mdef_electronic<R>(p, sh, wib, lam, bx[j], true, F, lamv);
+            ++n_exact;
+            if (lane == 0) {
+                if constexpr (std::is_same<R, float>::value) {
+                    float gdt = (float)lamv / (float)m * (float)dt;
+                    if (gdt < 0.f) gdt = 0.f;
+                    const float c1 = expf(-gdt), c2 = sqrtf(-expm1f(-2.f * gdt));
+                    const float xi = noise_normal_f(p.seed, gid, (uint32_t)step, (uint32_t)j);
+                    bv[j] = (double)c1 * bv[j] + (double)(c2 * (float)sig_rp * xi);
+                } else {
+                    double gam = lamv / m;
+                    if (gam < 0.0) gam = 0.0;
+                    const double c1 = exp(-gam * dt), c2 = sqrt(1.0 - c1 * c1);
+                    bv[j] = c1 * bv[j] + c2 * (sig_rp * noise_normal(p.seed, gid, (uint32_t)step, (uint32_t)j));
+                }
+            }
+        }
+        __syncthreads();
+        free_half();  // C
+        forces();     // B (new forces)
+        if (threadIdx.x < B) bv[threadIdx.x] = bv[threadIdx.x] + (half * dt) * bk[threadIdx.x];
+        __syncthreads();
+    }
+    for (int j = threadIdx.x; j < B; j += blockDim.x) {
+        p.x[(int64_t)j * N + i] = bx[j];
+        p.v[(int64_t)j * N + i] = bv[j];
+    }
+    if (p.counters && lane == 0) atomicAdd(p.counters + 0, n_exact);
+}
+
+template <typename R>
+cudaError_t launch_rpmdef(const MdefParams& p, cudaStream_t s) {
+    if (p.ntraj <= 0) return cudaSuccess;
+    if (p.nbath > kMdefMaxBath || p.nbath < 1 || p.nbeads < 1 || p.nbeads > kRpMdefMaxBeads) return cudaErrorInvalidValue;
+    rpmdef_kernel<R><<<(unsigned)p.ntraj, 32 * kMdefWarps, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
 template <typename R>
 cudaError_t launch_mdef(const MdefParams& p, cudaStream_t s) {
+    if (p.nbeads > 1) return launch_rpmdef<R>(p, s);
     if (p.ntraj <= 0) return cudaSuccess;
     if (p.nbath > kMdefMaxBath || p.nbath < 1) return cudaErrorInvalidValue;
     int64_t blocks = (p.ntraj + kMdefWarps - 1) / kMdefWarps;

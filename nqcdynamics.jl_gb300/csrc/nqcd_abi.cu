@@ -250,6 +250,7 @@ struct nqcd_handle {
     int32_t *d_nbeads = nullptr, *d_class_traj = nullptr, *d_block_class = nullptr;
     unsigned long long* d_queue = nullptr;
     int32_t* d_fp64steps = nullptr;  // two-state methods: per trajectory, steps with FP64 electronics
+    double* d_rpmdef = nullptr;      // ring-polymer MDEF: normal-mode matrix [n*n] and half Cayley steps [n][4]
     double* d_rpscratch = nullptr;  // plain path bead arrays, grown on demand
     int64_t rpscratch_cap = 0;
     int nclass = 0;
@@ -302,7 +303,7 @@ void free_all(nqcd_handle* h) {
                     h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
                     h->d_rpU, h->d_rpcay, h->d_rpcirc, h->d_nbeads, h->d_class_traj,
-                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2,
+                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2, h->d_rpmdef,
                     h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im, h->d_redtmp, h->d_fp64steps};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -435,6 +436,13 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
         if (cfg->nparams < 5 || !cfg->params || !(cfg->params[4] > 0.0))
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: Newns-Anderson needs k, g, delta, mu, sigma > 0");
         if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: MDEF needs beta > 0");
+        if (cfg->nbeads_max > 1) {  // RingPolymerSimulation{DiabaticMDEF}
+            if (cfg->nbeads_max > kRpMdefMaxBeads)
+                return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ring-polymer MDEF takes 2..32 beads");
+            if (cfg->save_stride != 0 || cfg->use_friction_surrogate)
+                return fail(nullptr, NQCD_ERR_UNSUPPORTED,
+                            "nqcd_create: ring-polymer MDEF reports final states only and uses the exact friction");
+        }
         if (!cfg->masses || !(cfg->masses[0] > 0.0) || cfg->ntraj_max <= 0 || cfg->save_stride < 0)
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: mass, ntraj_max and save_stride are required");
     }
@@ -469,7 +477,8 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring-polymer runs report final-state outputs only");
         if (!(cfg->terminate_x >= 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: terminate_x must be >= 0");
     }
-    const int64_t ndof = rp ? (int64_t)cfg->nbeads_max : (int64_t)cfg->ndofs * cfg->natoms;
+    const bool rp_mdef = mdef && cfg->nbeads_max > 1;
+    const int64_t ndof = (rp || rp_mdef) ? (int64_t)cfg->nbeads_max : (int64_t)cfg->ndofs * cfg->natoms;
     int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? 5 : (iesh ? 6 : 4))));
     if (cfg->nparams < need_params || !cfg->params)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: too few model parameters");
@@ -560,6 +569,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     NQCD_CREATE(dalloc(&h->d_nhops, cap));
     NQCD_CREATE(dalloc(&h->d_nfrust, cap));
     NQCD_CREATE(dalloc(&h->d_nsteps, cap));
+    if (rp_mdef) NQCD_CREATE(dalloc(&h->d_rpmdef, cfg->nbeads_max * cfg->nbeads_max + 4 * cfg->nbeads_max));
     if (!mdef && !iesh) {  // FSSH, Ehrenfest, RPSH: per-trajectory FP64-electronics step counts
         NQCD_CREATE(dalloc(&h->d_fp64steps, cap));
         NQCD_CREATE(cudaMemset(h->d_fp64steps, 0, cap * sizeof(int32_t)));
@@ -1142,6 +1152,30 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         NQCD_CUDA(h, cudaMemsetAsync(h->d_nhops, 0, N * sizeof(int32_t), s));
         NQCD_CUDA(h, cudaMemsetAsync(h->d_nfrust, 0, N * sizeof(int32_t), s));
         if (nsave > 0) NQCD_CUDA(h, cudaMemsetAsync(h->d_partial, 0, nwarps * nsave * 4 * sizeof(double), s));
+        if (h->cfg.nbeads_max > 1) {
+            // ring polymer: normal modes and half-step Cayley matrices (cayley_propagator(half=true),
+            // ring_polymer.jl:71-82: the square root of the full step, (C + I) / sqrt(tr C + 2) as det C = 1)
+            const int nb = h->cfg.nbeads_max;
+            std::vector<double> tab((size_t)nb * nb + 4 * (size_t)nb);
+            nm_transform_matrix(nb, tab.data());
+            double* hc = tab.data() + (size_t)nb * nb;
+            cayley_matrices(nb, h->cfg.beta, dt, hc);
+            for (int k = 0; k < nb; ++k) {
+                double* c = hc + 4 * k;
+                const double sc = 1.0 / sqrt(c[0] + c[3] + 2.0);
+                c[0] = (c[0] + 1.0) * sc;
+                c[1] = c[1] * sc;
+                c[2] = c[2] * sc;
+                c[3] = (c[3] + 1.0) * sc;
+            }
+            NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpmdef, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+            NQCD_CUDA(h, cudaMemsetAsync(h->d_energy, 0, 2 * N * sizeof(double), s));
+            mp.nbeads = nb;
+            mp.rp_U = h->d_rpmdef;
+            mp.rp_half = h->d_rpmdef + (size_t)nb * nb;
+            mp.energy = nullptr;
+            mp.obs_partial = nullptr;
+        }
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         e = h->cfg.precision == NQCD_PREC_FP64 ? launch_mdef_fp64(mp, s) : launch_mdef_fp32(mp, s);
     } else {

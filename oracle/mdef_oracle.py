@@ -172,3 +172,56 @@ def energy(model, x, v, mass, beta):
     """Classical potential of DiabaticMDEF (mdef.jl:162-175) plus kinetic energy."""
     w, _ = np.linalg.eigh(model.hamiltonian(x))
     return 0.5 * mass * v * v + model.U0(x) + np.sum(w * fermi(w, model.mu, beta), axis=1)
+
+
+def cayley_half(n: int, beta: float, dt: float) -> np.ndarray:
+    """cayley_propagator(beads, dt; half=true) (ring_polymer.jl:71-82): the
+    principal square root of each mode's full-step Cayley matrix C; det C = 1,
+    so sqrt(C) = (C + I) / sqrt(tr C + 2).  Returns [n][2][2]."""
+    import oracle as O
+
+    C = O.cayley(n, beta, dt)
+    tr = C[:, 0, 0] + C[:, 1, 1]
+    return (C + np.eye(2)[None]) / np.sqrt(tr + 2.0)[:, None, None]
+
+
+def run_rpmdef(model: NewnsAnderson, *, mass, beta, sigma, x0, v0, dt, nsteps, seed, traj_offset=0):
+    """RingPolymerSimulation{DiabaticMDEF} with BCOCB (bcocb.jl:79-105):
+    B (bead forces, rpmdef.jl:30-55), half Cayley step of the free ring
+    polymer in normal modes, O in bead space with each bead's friction at the
+    ring-polymer temperature n T (steps.jl:71-107, noise per bead from the
+    Philox normal stream with dof = bead), half Cayley step, B.
+    x0, v0: (ntraj, nbeads).  Returns x, v (ntraj, nbeads)."""
+    import oracle as O
+
+    x = np.asarray(x0, np.float64).copy()
+    v = np.asarray(v0, np.float64).copy()
+    n, B = x.shape
+    traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
+    U = O.nm_transform(B)             # U[j, k]: bead j, mode k
+    ch = cayley_half(B, beta, dt)     # omega_n = n / beta (RingPolymerParameters at the physical temperature)
+    Trp = B / beta
+
+    def force(x):
+        return -electronic(model, x.ravel(), beta, sigma, want_friction=False)["F"].reshape(n, B) / mass
+
+    def free_half(x, v):
+        q, p = x @ U, v @ U           # to normal modes
+        q2 = ch[:, 0, 0] * q + ch[:, 0, 1] * p
+        p2 = ch[:, 1, 0] * q + ch[:, 1, 1] * p
+        return q2 @ U.T, p2 @ U.T     # back to beads
+
+    k = force(x)
+    for step in range(1, nsteps + 1):
+        v = v + (0.5 * dt) * k                                       # B
+        x, v = free_half(x, v)                                       # C
+        lam = electronic(model, x.ravel(), beta, sigma)["friction"].reshape(n, B)
+        gam = np.maximum(lam / mass, 0.0)
+        c1 = np.exp(-gam * dt)
+        c2 = np.sqrt(1.0 - c1 * c1)
+        xi = np.stack([normal(seed, traj, step, dof=j) for j in range(B)], axis=1)
+        v = c1 * v + c2 * (np.sqrt(Trp / mass) * xi)                 # O
+        x, v = free_half(x, v)                                       # C
+        k = force(x)
+        v = v + (0.5 * dt) * k                                       # B
+    return x, v

@@ -23,7 +23,7 @@ from nqcd_gb300 import workload as WL
 pytestmark = pytest.mark.gpu
 
 
-def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, judge_every=0):
+def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, judge_every=0, nbeads=0):
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON, precision
     cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 1 + len(wl["eps"])
@@ -38,6 +38,7 @@ def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, 
     cfg.save_stride = save_stride
     cfg.use_friction_surrogate = int(surrogate)
     cfg.judge_every = judge_every
+    cfg.nbeads_max = nbeads
     return L.Engine(cfg, [params, masses, eps, V])
 
 
@@ -170,3 +171,51 @@ def test_friction_surrogate_trains_and_serves():
     np.testing.assert_allclose(surr[:, 2], exact[:, 2], rtol=0.02)
     # gain: the surrogate removes the midpoint electronic-structure evaluation
     assert st_s.kernel_ms < 0.8 * st_e.kernel_ms, (st_s.kernel_ms, st_e.kernel_ms)
+
+
+def rp_initial(wl, n, B):
+    x0 = np.repeat(wl["x0"][:, None], B, axis=1) + 0.02 * np.sin(2 * np.pi * np.arange(B) / B)[None]
+    v0 = np.repeat(wl["v0"][:, None], B, axis=1)
+    return x0, v0
+
+
+@pytest.mark.parametrize("B", [4, 6])
+def test_rpmdef_fp64_matches_oracle(B):
+    """RingPolymerSimulation{DiabaticMDEF} with BCOCB (bcocb.jl:79-105): bead
+    positions and velocities equal the oracle's to 1e-8 (its per-bead dense
+    eigendecompositions against the kernel's secular roots)."""
+    n, nsteps = 8, 100
+    wl = WL.newns_anderson_mdef(n, M=40)
+    x0, v0 = rp_initial(wl, n, B)
+    eng = make_mdef(wl, n, nbeads=B)
+    try:
+        eng.set_initial(np.ascontiguousarray(x0), np.ascontiguousarray(v0))
+        _, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 17)
+        fin = eng.get_final(B)
+    finally:
+        eng.close()
+    assert st.unconverged_roots == 0
+    x, v = MO.run_rpmdef(oracle_model(wl), mass=wl["mass"], beta=wl["beta"], sigma=wl["sigma"], x0=x0, v0=v0,
+                         dt=wl["dt"], nsteps=nsteps, seed=17)
+    np.testing.assert_allclose(fin["r"], x, rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(fin["v"], v, rtol=1e-8, atol=1e-12)
+
+
+def test_rpmdef_fp32_matches_fp64():
+    n, nsteps, B = 256, 200, 8
+    wl = WL.newns_anderson_mdef(n, M=200)
+    x0, v0 = rp_initial(wl, n, B)
+    out = {}
+    for prec in (L.PREC_FP64, L.PREC_FP32):
+        eng = make_mdef(wl, n, precision=prec, nbeads=B)
+        try:
+            eng.set_initial(np.ascontiguousarray(x0), np.ascontiguousarray(v0))
+            eng.run(0.0, nsteps * wl["dt"], wl["dt"], 3)
+            out[prec] = eng.get_final(B)
+        finally:
+            eng.close()
+    a, b = out[L.PREC_FP64], out[L.PREC_FP32]
+    # same noise, FP32 electronic structure: centroids within 1e-3 of their spread
+    ca, cb = a["r"].mean(1), b["r"].mean(1)
+    assert np.max(np.abs(ca - cb)) < 1e-3 * (ca.std() + 1e-3)
+    np.testing.assert_allclose(b["v"].mean(1), a["v"].mean(1), atol=1e-3 * np.abs(a["v"]).max())

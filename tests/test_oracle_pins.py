@@ -514,3 +514,27 @@ def test_decoherence_edc_reference_properties():
             assert np.angle(psi[i]) == pytest.approx(np.angle(orig[i]))
     assert np.linalg.norm(orig) == pytest.approx(1.0)
     assert np.linalg.norm(psi) == pytest.approx(1.0)
+
+
+def test_rpmdef_oracle_reduces_to_baoab_for_one_bead():
+    """BCOCB with one bead is BAOAB (the half Cayley steps of a free particle
+    are half drifts), and the half step squares to the full Cayley step
+    (ring_polymer.jl:71-82, half=true)."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "nqcdynamics.jl_gb300"))
+    import mdef_oracle as MO
+    from nqcd_gb300 import workload as WL
+
+    for nb in (2, 4, 8):
+        ch = MO.cayley_half(nb, 1024.0, 1.0)
+        np.testing.assert_allclose(np.einsum("kij,kjl->kil", ch, ch), O.cayley(nb, 1024.0, 1.0), atol=1e-14)
+    wl = WL.newns_anderson_mdef(3, M=40)
+    model = MO.NewnsAnderson(k=wl["k"], g=wl["g"], delta=wl["delta"], V=1.0, eps=wl["eps"], weights=wl["V"] ** 2,
+                             mu=wl["mu"])
+    kw = dict(mass=wl["mass"], beta=wl["beta"], sigma=wl["sigma"], dt=wl["dt"], nsteps=50, seed=4)
+    x1, v1 = MO.run_rpmdef(model, x0=wl["x0"][:, None], v0=wl["v0"][:, None], **kw)
+    x2, v2 = MO.run_mdef(model, x0=wl["x0"], v0=wl["v0"], **kw)
+    np.testing.assert_array_equal(x1[:, 0], x2)
+    np.testing.assert_array_equal(v1[:, 0], v2)
