@@ -330,10 +330,26 @@ class Simulation(metaclass=_MethodIndexed):
 
 
 class RingPolymerSimulation(metaclass=_MethodIndexed):
-    """RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)."""
+    """RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature) and
+    RingPolymerSimulation[DiabaticMDEF](atoms, model, n_beads; friction_method,
+    temperature) (rpmdef.jl:5-27)."""
 
     def __init__(self, atoms: Atoms, model: Model, n_beads, method=FSSH, rescaling: str = "standard",
-                 temperature: float = 0.0):
+                 temperature: float = 0.0, friction_method=None):
+        if method is DiabaticMDEF:
+            if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON:
+                raise NotImplementedError("ring-polymer MDEF runs on AndersonHolstein(DisplacedHarmonic(...), bath)")
+            if not isinstance(friction_method, GaussianBroadening):
+                raise ValueError("DiabaticMDEF needs friction_method=GaussianBroadening(sigma)")
+            if not temperature > 0:
+                raise ValueError("ring polymers need a positive temperature")
+            if len(atoms) != 1 or not 2 <= int(n_beads) <= 32:
+                raise ValueError("one adsorbate degree of freedom and 2..32 beads")
+            self.atoms, self.model, self.method = atoms, model, DiabaticMDEF()
+            self.friction_method = friction_method
+            self.temperature = float(temperature)
+            self.n_beads = int(n_beads)
+            return
         if method is not FSSH:
             raise NotImplementedError(f"method {method} is not on the GPU path")
         if isinstance(model, SpinBoson) or len(atoms) != 1:
@@ -659,7 +675,9 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
     if not isinstance(alg, EnsembleGB300):
         raise TypeError("ensemble_algorithm must be EnsembleGB300")
     if isinstance(sim, RingPolymerSimulation):
-        raise NotImplementedError("ring-polymer ensembles run through run_ring_polymer_ensemble")
+        if isinstance(sim.method, DiabaticMDEF):
+            return _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, dt, saveat, seed, rng)
+        raise NotImplementedError("ring-polymer surface hopping runs through run_ring_polymer_ensemble")
     if isinstance(getattr(sim, "method", None), (DiabaticMDEF, AdiabaticIESH, EhrenfestNA)):
         return _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, dt, saveat, seed, rng)
     if not isinstance(distribution, ProductDistribution):
@@ -787,10 +805,15 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
             raise ValueError("saveat must be a positive multiple of dt on the GPU path")
         save_stride = int(round(stride))
     ntraj = int(trajectories)
+    rp = isinstance(sim, RingPolymerSimulation)
+    if rp and save_stride:
+        raise NotImplementedError("ring-polymer MDEF reports final states (OutputFinal) on the GPU path")
     rng = rng if rng is not None else np.random.default_rng(alg.seed if seed is None else seed)
     r0 = nuclear.sample("r", ntraj, rng)
     v0 = nuclear.sample("v", ntraj, rng)
     cfg, keep = _metal_config(sim, ntraj, alg, save_stride)
+    if rp:
+        cfg.nbeads_max = sim.n_beads
     if not mdef:
         cfg.beta = distribution.electronic.β
         cfg.init_kind = L.INIT_FERMI_DIRAC
@@ -819,7 +842,8 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
                 result[name] = ob[:, 2]
             elif name in ("OutputFinal", "OutputTotalEnergy", "OutputSurfaceHops"):
                 if final is None:
-                    final = eng.get_final(1) if mdef else eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
+                    final = eng.get_final(sim.n_beads if rp else 1) if mdef else \
+                        eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
                 if name == "OutputFinal":
                     result[name] = final
                 elif name == "OutputTotalEnergy":

@@ -17,6 +17,7 @@ import pytest
 
 import mdef_oracle as MO
 import mlp_oracle as MLP
+import nqcd_gb300 as N
 from nqcd_gb300 import _lib as L
 from nqcd_gb300 import workload as WL
 
@@ -219,3 +220,20 @@ def test_rpmdef_fp32_matches_fp64():
     ca, cb = a["r"].mean(1), b["r"].mean(1)
     assert np.max(np.abs(ca - cb)) < 1e-3 * (ca.std() + 1e-3)
     np.testing.assert_allclose(b["v"].mean(1), a["v"].mean(1), atol=1e-3 * np.abs(a["v"]).max())
+
+
+def test_rpmdef_run_dynamics_matches_engine():
+    n, nsteps, B = 16, 60, 4
+    wl = WL.newns_anderson_mdef(n, M=40)
+    model = N.AndersonHolstein(N.DisplacedHarmonic(wl["k"], wl["g"], wl["delta"]),
+                               N.ShenviGaussLegendre(40, -0.5, 0.5), coupling=0.02)
+    sim = N.RingPolymerSimulation[N.DiabaticMDEF](N.Atoms(wl["mass"]), model, B,
+                                                  friction_method=N.GaussianBroadening(wl["sigma"]),
+                                                  temperature=1.0 / wl["beta"])
+    x0, v0 = rp_initial(wl, n, B)
+    dist = N.DynamicalDistribution(v0.reshape(n, 1, 1, B), x0.reshape(n, 1, 1, B), (1, 1, B))
+    res = N.run_dynamics(sim, (0.0, nsteps * wl["dt"]), dist, output=N.OutputFinal, trajectories=n, dt=wl["dt"],
+                         ensemble_algorithm=N.EnsembleGB300("fp64"), seed=8)
+    x, v = MO.run_rpmdef(oracle_model(wl), mass=wl["mass"], beta=wl["beta"], sigma=wl["sigma"], x0=x0, v0=v0,
+                         dt=wl["dt"], nsteps=nsteps, seed=8)
+    np.testing.assert_allclose(res["OutputFinal"]["r"], x, rtol=1e-8, atol=1e-10)
