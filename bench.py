@@ -19,12 +19,13 @@ configuration's shapes (nqcd_gb300/workload.py).
 the host cores (the reference itself is Julia and cannot run here).
 
 --workload tully1|rpsh|mdef|iesh measures the other benchmark configurations
-(C1, C3, C4, C5; nqcd_gb300/configs.py), --workload ehrenfest the Ehrenfest
-method on the headline's spin-boson ensemble and --workload ehrenfest_na
-EhrenfestNA on the C5 ensemble, the same way: the
-chosen fast path on the full ensemble, the plain FP64 path, and the
-observable error between the two on a common subset.  These are records for the design notes; the default
-run is the headline configuration.
+(C1, C3, C4, C5; nqcd_gb300/configs.py), and --workload ehrenfest,
+ehrenfest_na and rpmdef the Ehrenfest method on the headline's spin-boson
+ensemble, EhrenfestNA on the C5 ensemble and ring-polymer MDEF on the C4
+system, the same way: the chosen fast path on the full ensemble, the plain
+FP64 path, and the observable error between the two on a common subset.
+These are records for the design notes; the default run is the headline
+configuration.
 Multi-GPU (torchrun): each rank runs an independent replica shard of
 trajectories (global trajectory ids offset by rank); no collective on the
 data path, only a barrier and a max over ranks of the timings.
@@ -65,7 +66,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="spinboson",
-                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest", "ehrenfest_na"])
+                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest", "ehrenfest_na", "rpmdef"])
     ap.add_argument("--nsteps", type=int, default=0, help="secondary workloads: nuclear steps of the fast path")
     return ap.parse_args()
 
@@ -471,6 +472,31 @@ def secondary(args, dist):
                    "surrogate_friction_evals": st.surrogate_friction_evals, "exact_friction_evals": st.exact_friction_evals}
             ref_flops = 9 * 201**3 + 10 * 201**2
             kname = "mdef_kernel<float>"
+        elif wk == "rpmdef":
+            # ring-polymer MDEF (BCOCB) on the C4 system: 8 beads, exact friction
+            n = args.ntraj if args.ntraj != 100_000 else 10_000
+            nsteps, B = args.nsteps or 200, 8
+            nsub = min(n, 512)
+            wl = WL.newns_anderson_mdef(n, M=200, traj_offset=rank_off * n)
+            x0 = np.repeat(wl["x0"][:, None], B, axis=1)
+            v0 = np.repeat(wl["v0"][:, None], B, axis=1)
+            fin = {}
+            for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
+                eng = C.mdef_newns_anderson(L, wl, nt, prec, traj_offset=rank_off * n, nbeads=B)
+                eng.set_initial(np.ascontiguousarray(x0[:nt]), np.ascontiguousarray(v0[:nt]))
+                sub = name != "fp32"
+                res[name] = _timed(eng, lambda: eng.run(0.0, nsteps * wl["dt"], wl["dt"], seed),
+                                   1 if sub else warm, 1 if sub else steps, dist)
+                fin[name] = eng.get_final(B)
+                eng.close()
+            ca, cb = fin["fp64"]["r"].mean(1), fin["fp32_sub"]["r"].mean(1)
+            obs = {"quantity": "max |centroid x| difference fast - plain FP64 on 512 trajectories, relative to the "
+                               "centroid spread", "value": float(np.max(np.abs(ca - cb)) / (ca.std() + 1e-12)),
+                   "tolerance": 0.01}
+            cfg = {"workload": "rpmdef_newns_anderson_M200_beads8_traj10k_dt0.1fs", "ntraj_per_gpu": n,
+                   "nsteps": nsteps, "beads": B}
+            ref_flops = B * (9 * 201**3 + 10 * 201**2)
+            kname = "rpmdef_kernel<float>"
         elif wk == "ehrenfest":
             # Ehrenfest on the headline's spin-boson ensemble (100 modes, 100 000
             # trajectories, dt = 0.05, t in [0, 20], population correlation every 0.1)

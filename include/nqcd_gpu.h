@@ -98,7 +98,9 @@ typedef struct nqcd_config {
     int32_t ndofs;        /* degrees of freedom per atom */
     int32_t natoms;       /* atoms */
     int32_t nstates;      /* electronic states (2 for the supported models) */
-    int32_t nbeads_max;   /* ring polymer: largest bead count (0 or 1 for classical nuclei) */
+    int32_t nbeads_max;   /* ring polymer: largest bead count (0 or 1 for classical nuclei); with
+                             NQCD_METHOD_MDEF, 2..32 selects ring-polymer MDEF (BCOCB, rpmdef.jl) with
+                             this many beads for every trajectory (final states only) */
     int32_t nparams;      /* entries of params */
     const double* params; /* model parameters, see nqcd_model */
     int32_t nbath;        /* spin-boson bath modes (== natoms * ndofs) */

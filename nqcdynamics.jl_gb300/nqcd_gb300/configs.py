@@ -68,8 +68,10 @@ def rpsh_inputs(ntraj, bmax=32, mass=2000.0, x0=-9.5, seed=WL.SEED, traj_offset=
     return r0, v0, nb, models
 
 
-def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0, save_stride=0, traj_offset=0):
-    """C4: MDEF (electronic-friction Langevin) on the Newns-Anderson model."""
+def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0, save_stride=0, traj_offset=0,
+                        nbeads=0):
+    """C4: MDEF (electronic-friction Langevin) on the Newns-Anderson model
+    (nbeads > 1: ring-polymer MDEF with that many beads)."""
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON, precision
     cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 1 + len(wl["eps"])
@@ -85,6 +87,7 @@ def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0,
     cfg.use_friction_surrogate = int(surrogate)
     cfg.judge_every = judge_every
     cfg.traj_offset = traj_offset
+    cfg.nbeads_max = nbeads
     return L.Engine(cfg, [params, masses, eps, V])
 
 
