@@ -313,8 +313,8 @@ def main():
     flops_launch = WL.ref_flops_per_traj_step(nmodes) * ntraj * nsteps
     achieved = flops_launch / (ker_ms * 1e-3) / 1e12
     hbm_bytes = 2 * 2 * ntraj * nmodes * 8  # r, v read + written once per run by an on-chip kernel
-    kname = {"fp64": "fssh2_spinboson_kernel<double>", "fp32": "fssh2_sb_fast_kernel<AccF64,25>",
-             "fp32_kahan": "fssh2_sb_fast_kernel<AccKahan,25>"}[chosen]
+    kname = {"fp64": "fssh2_spinboson_kernel<double>", "fp32": "fssh2_sb_fast_kernel<AccF64,25,false>",
+             "fp32_kahan": "fssh2_sb_fast_kernel<AccKahan,25,false>"}[chosen]
     roofline = {"bound": "fp32-core" if chosen != "fp64" else "fp64-core", "achieved": achieved,
                 "peak": fp32_peak if chosen != "fp64" else fp64_peak, "unit": "TFLOP/s",
                 # DRAM bytes per launch from the ncu capture in profiles/ (20 000 trajectories,
@@ -522,7 +522,7 @@ def secondary(args, dist):
             cfg = {"workload": "ehrenfest_spinboson_ohmic100_traj100k_dt0.05_t20", "ntraj_per_gpu": n,
                    "modes": nmodes, "nsteps": nsteps}
             ref_flops = WL.ref_flops_per_traj_step(nmodes)
-            kname = "fssh2_sb_fast_kernel<AccKahan,25,Ehrenfest>"
+            kname = "fssh2_sb_fast_kernel<AccKahan,25,true>"
         else:  # iesh, ehrenfest_na (the same model, integrator and kernel)
             n = args.ntraj if args.ntraj != 100_000 else 20_000
             nsteps = args.nsteps or 500
