@@ -20,9 +20,9 @@ the host cores (the reference itself is Julia and cannot run here).
 
 --workload tully1|rpsh|mdef|iesh measures the other benchmark configurations
 (C1, C3, C4, C5; nqcd_gb300/configs.py), and --workload ehrenfest,
-ehrenfest_na and rpmdef the Ehrenfest method on the headline's spin-boson
-ensemble, EhrenfestNA on the C5 ensemble and ring-polymer MDEF on the C4
-system, the same way: the chosen fast path on the full ensemble, the plain
+ehrenfest_na, rpmdef and rpiesh the Ehrenfest method on the headline's
+spin-boson ensemble, EhrenfestNA on the C5 ensemble, ring-polymer MDEF on the
+C4 system and ring-polymer IESH on the C5 system, the same way: the chosen fast path on the full ensemble, the plain
 FP64 path, and the observable error between the two on a common subset.
 These are records for the design notes; the default run is the headline
 configuration.
@@ -66,7 +66,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="spinboson",
-                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest", "ehrenfest_na", "rpmdef"])
+                    choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest", "ehrenfest_na", "rpmdef",
+                             "rpiesh"])
     ap.add_argument("--nsteps", type=int, default=0, help="secondary workloads: nuclear steps of the fast path")
     return ap.parse_args()
 
@@ -497,6 +498,38 @@ def secondary(args, dist):
                    "nsteps": nsteps, "beads": B}
             ref_flops = B * (9 * 201**3 + 10 * 201**2)
             kname = "rpmdef_kernel<float>"
+        elif wk == "rpiesh":
+            # ring-polymer IESH (BCBWavefunction) on the C5 system: 8 beads per trajectory
+            n = args.ntraj if args.ntraj != 100_000 else 10_000
+            nsteps, B = args.nsteps or 300, 8
+            nsub = min(n, 608)
+            wl = WL.newns_anderson_rpiesh(n, B, traj_offset=rank_off * n)
+            fin = {}
+            for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
+                eng = C.iesh_newns_anderson(L, wl, nt, prec, traj_offset=rank_off * n, nbeads=B)
+                eng.set_initial(np.ascontiguousarray(wl["r0"][:nt]), np.ascontiguousarray(wl["v0"][:nt]))
+                sub = name != "fp32"
+                res[name] = _timed(eng, lambda: eng.run(0.0, nsteps * wl["dt"], wl["dt"], seed),
+                                   1 if sub else warm, 1 if sub else steps, dist)
+                fin[name] = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+                eng.close()
+            za, zb = fin["fp64"]["r"][:, :, 2].mean(1), fin["fp32_sub"]["r"][:, :, 2].mean(1)
+            ea, eb = fin["fp64"]["energy"][:, 1], fin["fp32_sub"]["energy"][:, 1]
+            obs = {"quantity": "relative error of the ensemble means of the final centroid height and the final "
+                               "ring-polymer energy on 608 trajectories vs plain FP64",
+                   "value": float(max(abs(zb.mean() - za.mean()) / abs(za.mean()),
+                                      abs(eb.mean() - ea.mean()) / abs(ea.mean()))), "tolerance": 0.01}
+            st = res["fp32"]["st"]
+            cfg = {"workload": "rpiesh_newns_anderson_80states_40e_3dof_beads8_traj10k_dt0.1fs", "ntraj_per_gpu": n,
+                   "nsteps": nsteps, "beads": B,
+                   "chebyshev_terms_per_step": st.propagator_terms / max(1, st.traj_steps),
+                   "full_hop_evaluations_per_step": st.hop_evaluations / max(1, st.traj_steps)}
+            # reference per step: eigendecomposition (9 N^3) and three derivative transforms
+            # (3 x 4 N^3) for every bead and the centroid, then the centroid propagator, orbital
+            # update and overlap (2.45e7 at N = 80)
+            ref_flops = (B + 1) * 21 * 80**3 + 2.45e7
+            kname = "rpiesh_kernel<float>"
+            res["fp32"]["bead_steps_per_s"] = res["fp32"]["value"] * B
         elif wk == "ehrenfest":
             # Ehrenfest on the headline's spin-boson ensemble (100 modes, 100 000
             # trajectories, dt = 0.05, t in [0, 20], population correlation every 0.1)

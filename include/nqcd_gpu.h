@@ -100,7 +100,11 @@ typedef struct nqcd_config {
     int32_t nstates;      /* electronic states (2 for the supported models) */
     int32_t nbeads_max;   /* ring polymer: largest bead count (0 or 1 for classical nuclei); with
                              NQCD_METHOD_MDEF, 2..32 selects ring-polymer MDEF (BCOCB, rpmdef.jl) with
-                             this many beads for every trajectory (final states only) */
+                             this many beads for every trajectory (final states only); with
+                             NQCD_METHOD_IESH, 2..32 selects ring-polymer IESH (BCBWavefunction,
+                             rpiesh.jl; <= 64 electrons, final states and energies only, no decoherence
+                             correction, beta also the Fermi-Dirac inverse temperature): bead forces from
+                             each bead's eigenstates, orbitals and hops from the centroid's */
     int32_t nparams;      /* entries of params */
     const double* params; /* model parameters, see nqcd_model */
     int32_t nbath;        /* spin-boson bath modes (== natoms * ndofs) */
@@ -203,7 +207,8 @@ typedef struct nqcd_sampler {
  *   UNIFORM: a + (b - a) * U(w0, w1),
  * so a sharded ensemble equals the single-process one.  The electronic
  * initial state follows cfg->init_kind as in nqcd_set_initial
- * (NQCD_INIT_GIVEN is rejected: it needs host data).  Not for ring polymers.
+ * (NQCD_INIT_GIVEN is rejected: it needs host data).  Not for ring polymers
+ * (NQCD_ERR_UNSUPPORTED: their beads take nqcd_set_initial).
  * NQCD_ERR_ARG on a bad sampler (unknown kind, negative width, b < a). */
 int nqcd_sample_initial(nqcd_handle* h, int64_t ntraj, const nqcd_sampler* position, const nqcd_sampler* velocity,
                         uint64_t seed);

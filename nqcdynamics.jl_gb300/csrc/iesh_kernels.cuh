@@ -64,6 +64,8 @@ namespace nqcd {
 
 constexpr int kIeshBlock = 256;
 constexpr int kIeshMaxStates = 128;
+constexpr int kRpIeshMaxBeads = 32;      // ring polymer: beads (one per lane of warp 0)
+constexpr int kRpIeshMaxElectrons = 64;  // ring polymer: electrons (two per lane in the bead roots)
 constexpr int kIeshMaxTerms = 128;  // Chebyshev terms
 constexpr int kIeshInv = 192;       // table of 1/n for the Bessel power series
 constexpr int kIeshFdChunk = 256;   // Metropolis iterations whose random numbers are drawn together
@@ -83,14 +85,18 @@ struct IeshParams {
     int32_t exact_probability;      // 1: every step evaluates all probabilities (estimate_probability = false)
     int32_t ehrenfest_na;           // 1: Simulation{EhrenfestNA} (mean-field force of the orbitals, no hops)
     double edc_C;                   // > 0: energy-based decoherence correction after every step
+    int32_t nbeads;                 // > 1: RingPolymerSimulation{AdiabaticIESH} (rpiesh_kernel)
+    const double* rp_U;             // [nbeads * nbeads] normal-mode matrix, column-major U[j + n k]
+    const double* rp_cay;           // [nbeads][4] full-step Cayley matrices (c11, c12, c21, c22)
+    double omega_n;                 // ring-polymer frequency nbeads / beta (spring energy)
     int32_t save_stride, nsave, max_hops;
     int64_t ntraj, traj_offset;
     double dt;
     int32_t nsteps;
     uint64_t seed;
     double cheb_tol;                // truncation of the Chebyshev series
-    double* r;                      // [3][ntraj] in/out
-    double* v;                      // [3][ntraj] in/out
+    double* r;                      // [3 * nbeads][ntraj] in/out (dof d of bead j at row d + 3 j)
+    double* v;                      // [3 * nbeads][ntraj] in/out
     const int32_t* occ0;            // [nelec][ntraj] given initial occupations (IESH_INIT_GIVEN)
     int32_t* occ;                   // [nelec][ntraj] final occupations (electron order)
     double* psi_re;                 // [ntraj][nelec][nstates] final orbitals, or null
@@ -111,9 +117,9 @@ struct alignas(2 * sizeof(R)) Cx {
 
 // Dynamic shared memory layout of one CTA (identical on host and device).
 struct IeshLayout {
-    int N, Ne, Nu, Np, Nep;
+    int N, Ne, Nu, Np, Nep, B;
     size_t o_eps, o_V2, o_lam, o_z2, o_z0, o_w64, o_At, o_phiA, o_phiB, o_out, o_J, o_Jr, o_inv, o_fdu, o_fdi, o_occ,
-        o_unocc, o_piv, o_red, o_misc, bytes;
+        o_unocc, o_piv, o_red, o_misc, o_rph, o_rpq, bytes;
 };
 
 NQCD_HD size_t iesh_take(size_t& o, size_t bytes) {
@@ -122,9 +128,11 @@ NQCD_HD size_t iesh_take(size_t& o, size_t bytes) {
     return at;
 }
 
+// B > 1: ring polymer of B beads (per-bead levels and sums, normal-mode scratch).
 template <typename R>
-NQCD_HD IeshLayout iesh_layout(int N, int Ne) {
+NQCD_HD IeshLayout iesh_layout(int N, int Ne, int B = 1) {
     IeshLayout L;
+    L.B = B;
     L.N = N;
     L.Ne = Ne;
     L.Nu = N - Ne;
@@ -153,6 +161,9 @@ NQCD_HD IeshLayout iesh_layout(int N, int Ne) {
     L.o_piv = iesh_take(o, sizeof(int) * L.Nep);
     L.o_red = iesh_take(o, sizeof(double) * 72);
     L.o_misc = iesh_take(o, sizeof(double) * 32);
+    // ring polymer: [4][B] bead h, dh/dz, occupied z0^2 sum, occupied eigenvalue sum; [6][B] normal modes
+    L.o_rph = B > 1 ? iesh_take(o, sizeof(double) * 4 * B) : 0;
+    L.o_rpq = B > 1 ? iesh_take(o, sizeof(double) * 6 * B) : 0;
     L.bytes = o;
     return L;
 }
@@ -350,10 +361,23 @@ __device__ inline double iesh_wall(const IeshParams& p, double z) {  // exp(-a z
 // lane holds the same copy) and the serial FP64 work; it publishes h, dh/dz
 // and v . grad h through shared memory.  All threads share the root solve,
 // the coupling matrix, the propagator and the hop linear algebra.
-template <typename R>
-__global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(const IeshParams p) {
+//
+// RP = true: RingPolymerSimulation{AdiabaticIESH} (rpiesh.jl) with
+// BCBWavefunction (bcb_wavefunction.jl:37-69).  Lane j of warp 0 holds bead j;
+// the step is a half kick, the full Cayley step of the free ring polymer in
+// normal modes (ring_polymer.jl:71-82), the bead forces from each bead's own
+// eigenstates summed over the shared occupied set (rpiesh.jl:20-37) and a half
+// kick.  The orbitals are propagated with the centroid velocity of the step's
+// start and the centroid eigenvalues and couplings of its end (the calculator
+// cache holds the end positions when propagate_wavefunction! reads it,
+// bcb_wavefunction.jl:59-68 with SurfaceHoppingMethods.jl:81-103); hops use
+// the final centroid velocity, and their velocity change is the same in every
+// bead (rpsh.jl:30-50).  Fermi-Dirac occupations come from the centroid
+// eigenvalues (iesh.jl:99-128).
+template <typename R, bool RP>
+__device__ __forceinline__ void iesh_body(const IeshParams& p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec);
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, RP ? p.nbeads : 1);
     R* eps = (R*)(smem + L.o_eps);
     R* V2 = (R*)(smem + L.o_V2);
     R* lam = (R*)(smem + L.o_lam);
@@ -376,6 +400,12 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     // misc: [0] K [1] sin(c dt) [2] cos(c dt), then the full-evaluation flag [3] v_z [4] h [5] dh/dz
     //       [6] v . grad h [8] c [9] 1/hw [10] w/hw [11] J_0
     double* misc = (double*)(smem + L.o_misc);
+    // ring polymer: rph[b] h, rph[NB + b] dh/dz, rph[2 NB + b] sum of occupied z0^2, rph[3 NB + b] sum of
+    // occupied eigenvalues of bead b; rpq [6][NB] normal-mode scratch.  misc[12] v . grad h of the final
+    // centroid velocity (hops), [13] final centroid v_z, [14] centroid z
+    double* rph = (double*)(smem + L.o_rph);
+    double* rpq = (double*)(smem + L.o_rpq);
+    const int NB = RP ? p.nbeads : 1;
 
     const int N = L.N, Ne = L.Ne, Nu = L.Nu, Np = L.Np, Nep = L.Nep, M = p.nbath;
     const int tid = threadIdx.x, nthr = blockDim.x, warp = tid >> 5, lane = tid & 31;
@@ -400,11 +430,12 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     }
     for (int q = tid; q < kIeshInv; q += nthr) inv[q] = q ? 1.0 / q : 0.0;
 
-    double r[3], v[3], k[3];  // meaningful in warp 0
+    double r[3], v[3], k[3];  // meaningful in warp 0 (ring polymer: bead `lane`, lanes >= NB a copy of bead 0)
+    const int bead = RP && lane < NB ? lane : 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        r[d] = p.r[d * NT + ti];
-        v[d] = p.v[d * NT + ti];
+        r[d] = p.r[(int64_t)(d + 3 * bead) * NT + ti];
+        v[d] = p.v[(int64_t)(d + 3 * bead) * NT + ti];
         k[d] = 0.0;
     }
     const double Lpad = fabs(p.eps[0]) + fabs(p.eps[M - 1]) + 1.0 + p.sumV2;
@@ -420,6 +451,131 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             z0[tid] = sqrt(zz);
         }
         __syncthreads();
+    };
+    // ---- ring polymer ----
+    // mean over the beads of warp 0 (the same value in every lane)
+    auto bead_mean = [&](double x) {
+        double sm = lane < NB ? x : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, off);
+        return sm / (double)NB;
+    };
+    // warp 0: h and dh/dz of each bead into rph, the centroid's into hz, dhz and misc[4], misc[5]
+    auto publish_levels = [&](double& hz_, double& dhz_) {
+        if constexpr (RP) {
+            double hb, dhb;
+            iesh_level<R>(p, r[2], hb, dhb);
+            if (lane < NB) {
+                rph[lane] = hb;
+                rph[NB + lane] = dhb;
+            }
+            const double zc = bead_mean(r[2]);
+            iesh_level<R>(p, zc, hz_, dhz_);
+            if (lane == 0) misc[14] = zc;
+        } else {
+            iesh_level<R>(p, r[2], hz_, dhz_);
+        }
+        if (lane == 0) {
+            misc[4] = hz_;
+            misc[5] = dhz_;
+        }
+    };
+    // roots of the occupied states of every bead (warp w: beads w, w + 8, ...; lane: electrons lane,
+    // lane + 32), reduced per bead to the sums of z0^2 and of the eigenvalues; after a barrier that
+    // published rph[0, 2 NB) and the occupations
+    R wl[kRpIeshMaxBeads / (kIeshBlock / 32)][2];  // warm starts (any value is a valid start)
+    if constexpr (RP) {
+#pragma unroll
+        for (int i = 0; i < kRpIeshMaxBeads / (kIeshBlock / 32); ++i) wl[i][0] = wl[i][1] = R(0);
+    }
+    auto bead_roots = [&]() {
+        if constexpr (RP) {
+#pragma unroll 1
+            for (int i = 0; i < kRpIeshMaxBeads / (kIeshBlock / 32); ++i) {
+                const int b = warp + (kIeshBlock / 32) * i;
+                if (b >= NB) break;  // warp-uniform
+                const double hb = rph[b];
+                R sz = R(0), sl = R(0);
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const int e = lane + 32 * j;
+                    if (e < Ne) {
+                        R zz;
+                        secular_root<R>(eps, V2, M, occ[e], (R)hb, (R)(fabs(hb) + Lpad), wl[i][j], zz, nonconv);
+                        sz += zz;
+                        sl += wl[i][j];
+                    }
+                }
+                sz = warp_sum<R>(sz);
+                sl = warp_sum<R>(sl);
+                if (lane == 0) {
+                    rph[2 * NB + b] = (double)sz;
+                    rph[3 * NB + b] = (double)sl;
+                }
+            }
+            __syncthreads();
+        }
+    };
+    // warp 0: full Cayley step of the free ring polymer (cayley_propagator(half=false),
+    // bcb_wavefunction.jl:52-56): to normal modes, rotate each mode, back to beads; per Cartesian dof
+    auto free_step = [&](double* x, double* y) {
+        if (lane < NB)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                rpq[d * NB + lane] = x[d];
+                rpq[(3 + d) * NB + lane] = y[d];
+            }
+        __syncwarp();
+        double qx[3] = {0.0, 0.0, 0.0}, qy[3] = {0.0, 0.0, 0.0};
+        if (lane < NB) {
+            const double* c = p.rp_cay + 4 * lane;  // mode `lane`
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double a = 0.0, b = 0.0;
+                for (int j = 0; j < NB; ++j) {
+                    const double u = p.rp_U[j + NB * lane];
+                    a = a + u * rpq[d * NB + j];
+                    b = b + u * rpq[(3 + d) * NB + j];
+                }
+                qx[d] = c[0] * a + c[1] * b;
+                qy[d] = c[2] * a + c[3] * b;
+            }
+        }
+        __syncwarp();
+        if (lane < NB)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                rpq[d * NB + lane] = qx[d];
+                rpq[(3 + d) * NB + lane] = qy[d];
+            }
+        __syncwarp();
+        if (lane < NB)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double a = 0.0, b = 0.0;
+                for (int q = 0; q < NB; ++q) {
+                    const double u = p.rp_U[lane + NB * q];
+                    a = a + u * rpq[d * NB + q];
+                    b = b + u * rpq[(3 + d) * NB + q];
+                }
+                x[d] = a;
+                y[d] = b;
+            }
+        __syncwarp();
+    };
+    // warp 0: ring-polymer Hamiltonian (DynamicsUtils.jl:74-79): kinetic + sum over beads of U0 and the
+    // occupied eigenvalues (rpiesh.jl:39-52) + spring energy (ring_polymer.jl:85-107); after bead_roots
+    auto rp_energy = [&]() {
+        const int nb = lane + 1 < NB ? lane + 1 : 0;
+        double sp = 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double dx = r[d] - __shfl_sync(0xffffffffu, r[d], nb);
+            sp += dx * dx;
+        }
+        const double e = 0.5 * mass * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) + 0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) +
+                         p.A * iesh_wall<R>(p, r[2]) + rph[3 * NB + bead] + 0.5 * mass * p.omega_n * p.omega_n * sp;
+        return bead_mean(e) * (double)NB;
     };
     // EhrenfestNA (ehrenfest_na.jl): the force and energy come from the orbitals
     // instead of the occupations.  With A = dh z0 z0^T the force weight
@@ -445,6 +601,13 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         ena_band = iesh_block_sum(cb, red);
     };
     auto accel = [&](double dh) {  // warp 0
+        if constexpr (RP) {  // bead `lane`: its own level derivative and occupied z0^2 (after bead_roots)
+            const double eaz = iesh_wall<R>(p, r[2]);
+            k[0] = -(p.kxy * r[0]) * inv_mass;
+            k[1] = -(p.kxy * r[1]) * inv_mass;
+            k[2] = -(-p.A * p.a * eaz + rph[NB + bead] * rph[2 * NB + bead]) * inv_mass;
+            return;
+        }
         R acc = R(0);
         for (int jj = lane; jj < Ne; jj += 32) acc += z2[occ[jj]];
         const double occsum = ena ? ena_imp : (double)warp_sum<R>(acc);
@@ -471,15 +634,10 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     // ---- initial electronic structure and occupations ----
     lam_own = tid == 0 ? eps[0] - R(1e-3) : (tid <= M ? eps[tid - 1] + R(1e-9) : R(0));
     double hz = 0.0, dhz = 0.0;
-    if (warp == 0) {
-        iesh_level<R>(p, r[2], hz, dhz);
-        if (lane == 0) {
-            misc[4] = hz;
-            misc[5] = dhz;
-        }
-    }
+    if (warp == 0) publish_levels(hz, dhz);
     __syncthreads();
     roots();
+    const double z_fd = RP ? misc[14] : r[2];  // where the Fermi-Dirac eigenvalues are taken
     if (p.init_kind == IESH_INIT_FERMI_DIRAC) {
         // Metropolis over occupations with the Boltzmann ratio (DynamicsUtils.jl:194-208).
         // Acceptance exp(-beta (e_j - e_i)) > u is tested as w_j > u w_i with
@@ -493,7 +651,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             if constexpr (std::is_same<R, double>::value) {
                 l64 = lam[tid];
             } else {
-                const double h64 = p.delta - p.B * nqcd_exp(-p.b * r[2]);
+                const double h64 = p.delta - p.B * nqcd_exp(-p.b * z_fd);
                 double zz;
                 l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9;
                 secular_root<double>(p.eps, p.V2, M, tid, h64, fabs(h64) + Lpad, l64, zz, nonconv);
@@ -509,7 +667,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             if constexpr (std::is_same<R, double>::value) {
                 w64[tid] = lam[tid];
             } else {
-                const double h64 = p.delta - p.B * nqcd_exp(-p.b * r[2]);
+                const double h64 = p.delta - p.B * nqcd_exp(-p.b * z_fd);
                 double zz, l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9;
                 secular_root<double>(p.eps, p.V2, M, tid, h64, fabs(h64) + Lpad, l64, zz, nullptr);
                 w64[tid] = l64;
@@ -573,11 +731,16 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         __syncthreads();
         orbital_sums();
     }
+    bead_roots();
     double e0 = 0.0;
     if (warp == 0) {
         accel(dhz);
-        const double pe = potential();
-        e0 = kinetic() + pe;
+        if constexpr (RP) {
+            e0 = rp_energy();
+        } else {
+            const double pe = potential();
+            e0 = kinetic() + pe;
+        }
     }
     __syncthreads();
 
@@ -626,25 +789,38 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     for (int step = 1; step <= p.nsteps; ++step) {
         // ---- velocity Verlet (verlet_with_electronics.jl:55-63) ----
         double vt[3];
+        double vzc0 = 0.0;  // ring polymer: centroid v_z at the step's start
         if (warp == 0) {
 #pragma unroll
             for (int d = 0; d < 3; ++d) vt[d] = v[d] + half * k[d];
+            if constexpr (RP) {
+                vzc0 = bead_mean(v[2]);
+                free_step(r, vt);
+            } else {
 #pragma unroll
-            for (int d = 0; d < 3; ++d) r[d] = r[d] + dt * vt[d];
-            iesh_level<R>(p, r[2], hz, dhz);
-            if (lane == 0) {
-                misc[4] = hz;
-                misc[5] = dhz;
+                for (int d = 0; d < 3; ++d) r[d] = r[d] + dt * vt[d];
             }
+            publish_levels(hz, dhz);
         }
         __syncthreads();
         roots();
+        bead_roots();
         if (ena) orbital_sums();  // orbitals before this step's propagation, roots at the new position
         if (warp == 0) {
             accel(dhz);
 #pragma unroll
             for (int d = 0; d < 3; ++d) v[d] = vt[d] + half * k[d];
-            if (lane == 0) misc[6] = v[2] * dhz;  // v . grad h: the couplings are d_alpha = dh/dalpha A
+            // v . grad h: the couplings are d_alpha = dh/dalpha A
+            if constexpr (RP) {
+                const double vzc = bead_mean(v[2]);
+                if (lane == 0) {
+                    misc[6] = vzc0 * dhz;
+                    misc[12] = vzc * dhz;
+                    misc[13] = vzc;
+                }
+            } else {
+                if (lane == 0) misc[6] = v[2] * dhz;
+            }
         }
         // ---- propagator (wavefunction_dynamics.jl:15-58) ----
         for (int q = tid; q < N * N; q += nthr) {
@@ -653,6 +829,7 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         }
         __syncthreads();
         const double w = misc[6];
+        const double wh = RP ? misc[12] : w;  // hops: v . grad h with the final (centroid) velocity
         double elo = 1e300, ehi = -1e300;
         if (tid < N) {
             R sacc = R(0);
@@ -922,9 +1099,9 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
         }
         double sumabs;
         if constexpr (std::is_same<R, float>::value)
-            sumabs = fabs(w) * (double)iesh_block_sum_f(sabs, red);
+            sumabs = fabs(wh) * (double)iesh_block_sum_f(sabs, red);
         else
-            sumabs = fabs(w) * iesh_block_sum((double)sabs, red);
+            sumabs = fabs(wh) * iesh_block_sum((double)sabs, red);
         const double u = std::is_same<R, double>::value
                              ? rng_uniform(p.seed, gid, (uint32_t)step, RNG_HOP)
                              : (double)rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP);
@@ -977,13 +1154,14 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                 // p_mn = 2 dt Re(Y_nm) (v.d)_mn, (v.d)_mn = -w A[m][state n]
                 const int m = unocc[mm];
                 for (int n = 0; n < Ne; ++n) {
-                    const double vdd = -w * (double)At[occ[n] * Np + m];
+                    const double vdd = -wh * (double)At[occ[n] * Np + m];
                     const double pr = clamp01<double>(2.0 * dt * (double)Rh[n * Nu + mm].re * vdd);
                     Rh[n * Nu + mm].re = (R)pr;
                 }
             }
             __syncthreads();
             if (tid == 0) {
+                double shift = 0.0;  // ring polymer: velocity change of every bead's z component
                 int sel_n = -1, sel_m = -1;
                 double cum = 0.0;
                 for (int n = 0; n < Ne && sel_n < 0; ++n)
@@ -1002,16 +1180,22 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                         // d[new, old] = dh A[new][old]; only its z component is nonzero
                         const double dz = dhz * (double)z0[nw] * (double)z0[old] / ((double)lam[old] - (double)lam[nw]);
                         const double aa = (dz * dz / mass) / 2.0;
-                        const double bb = dz * v[2];
+                        const double vz = RP ? misc[13] : v[2];  // hopping velocity: the centroid's
+                        const double bb = dz * vz;
                         const double cc = (double)lam[nw] - (double)lam[old];
                         const double disc = bb * bb - 4.0 * aa * cc;
                         if (disc < 0.0) {
                             accept = false;
-                            if (p.rescaling == RESCALE_VINVERSION) v[2] = -v[2];
+                            // invert the (centroid) velocity along d = dz e_z
+                            if (p.rescaling == RESCALE_VINVERSION) {
+                                if constexpr (RP) shift = -2.0 * vz;
+                                else v[2] = -v[2];
+                            }
                         } else {
                             const double root = sqrt(disc);
                             const double gam = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
-                            v[2] = v[2] - gam * dz / mass;
+                            if constexpr (RP) shift = -(gam * dz / mass);
+                            else v[2] = v[2] - gam * dz / mass;
                         }
                     }
                     if (accept) {
@@ -1027,10 +1211,13 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
                         ++nf;
                     }
                 }
-                misc[3] = v[2];
+                misc[3] = RP ? shift : v[2];
             }
             __syncthreads();
-            if (warp == 0) v[2] = misc[3];  // hop counts live in thread 0, which writes them out
+            if (warp == 0) {  // hop counts live in thread 0, which writes them out
+                if constexpr (RP) v[2] = v[2] + misc[3];
+                else v[2] = misc[3];
+            }
         }
         }  // !ena
         if (p.edc_C > 0.0) {
@@ -1070,8 +1257,12 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
     double e1 = 0.0;
     if (ena && p.energy) orbital_sums();
     if (warp == 0 && p.energy) {
-        const double pe = potential();
-        e1 = kinetic() + pe;
+        if constexpr (RP) {
+            e1 = rp_energy();  // bead sums of the last step's roots
+        } else {
+            const double pe = potential();
+            e1 = kinetic() + pe;
+        }
     }
     // final orbitals: (nstates, nelectrons) column-major per trajectory
     if (p.psi_re)
@@ -1082,12 +1273,13 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
             p.psi_im[(ti * Ne + c) * N + i] = (double)x.im;
         }
     for (int jj = tid; jj < Ne; jj += nthr) p.occ[(int64_t)jj * NT + ti] = occ[jj];
-    if (tid == 0) {
+    if (warp == 0 && lane < NB)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            p.r[d * NT + ti] = r[d];
-            p.v[d * NT + ti] = v[d];
+            p.r[(int64_t)(d + 3 * lane) * NT + ti] = r[d];
+            p.v[(int64_t)(d + 3 * lane) * NT + ti] = v[d];
         }
+    if (tid == 0) {
         if (p.nhops) p.nhops[ti] = nh;
         if (p.nfrustrated) p.nfrustrated[ti] = nf;
         if (p.nsteps_out) p.nsteps_out[ti] = p.nsteps;
@@ -1103,12 +1295,29 @@ __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(
 }
 
 template <typename R>
+__global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(const IeshParams p) {
+    iesh_body<R, false>(p);
+}
+
+// RingPolymerSimulation{AdiabaticIESH}: p.nbeads in 2..kRpIeshMaxBeads, p.nelec <= kRpIeshMaxElectrons
+template <typename R>
+__global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) rpiesh_kernel(const IeshParams p) {
+    iesh_body<R, true>(p);
+}
+
+template <typename R>
 cudaError_t launch_iesh(const IeshParams& p, cudaStream_t s) {
     if (p.ntraj <= 0) return cudaSuccess;
-    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec);
-    cudaError_t e = cudaFuncSetAttribute(iesh_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
+    const bool rp = p.nbeads > 1;
+    if (rp && (p.nbeads > kRpIeshMaxBeads || p.nelec > kRpIeshMaxElectrons)) return cudaErrorInvalidValue;
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, rp ? p.nbeads : 1);
+    cudaError_t e = cudaFuncSetAttribute(rp ? rpiesh_kernel<R> : iesh_kernel<R>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
     if (e != cudaSuccess) return e;
-    iesh_kernel<R><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
+    if (rp)
+        rpiesh_kernel<R><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
+    else
+        iesh_kernel<R><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -250,7 +250,8 @@ struct nqcd_handle {
     int32_t *d_nbeads = nullptr, *d_class_traj = nullptr, *d_block_class = nullptr;
     unsigned long long* d_queue = nullptr;
     int32_t* d_fp64steps = nullptr;  // two-state methods: per trajectory, steps with FP64 electronics
-    double* d_rpmdef = nullptr;      // ring-polymer MDEF: normal-mode matrix [n*n] and half Cayley steps [n][4]
+    double* d_rptab = nullptr;       // ring-polymer MDEF / IESH: normal-mode matrix [n*n] and Cayley steps [n][4]
+    int rp_beads = 1;                // ring-polymer MDEF / IESH: beads of every trajectory (1 otherwise)
     double* d_rpscratch = nullptr;  // plain path bead arrays, grown on demand
     int64_t rpscratch_cap = 0;
     int nclass = 0;
@@ -303,7 +304,7 @@ void free_all(nqcd_handle* h) {
                     h->d_sig, h->d_state0, h->d_state, h->d_scratch, h->d_nhops, h->d_nfrust, h->d_nsteps,
                     h->d_hoplog, h->d_energy, h->d_partial, h->d_popcorr, h->d_counts, h->d_stage,
                     h->d_rpU, h->d_rpcay, h->d_rpcirc, h->d_nbeads, h->d_class_traj,
-                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2, h->d_rpmdef,
+                    h->d_block_class, h->d_queue, h->d_rpscratch, h->d_eps, h->d_V2, h->d_rptab,
                     h->d_occ0, h->d_occ, h->d_psi_re, h->d_psi_im, h->d_redtmp, h->d_fp64steps};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -421,6 +422,21 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: Fermi-Dirac occupations need beta > 0");
         if (cfg->precision == NQCD_PREC_FP32_KAHAN)
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: IESH runs NQCD_PREC_FP64 or NQCD_PREC_FP32");
+        if (cfg->nbeads_max > 1) {  // RingPolymerSimulation{AdiabaticIESH}
+            if (cfg->method != NQCD_METHOD_IESH)
+                return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring polymers run IESH, not EhrenfestNA");
+            if (cfg->nbeads_max > kRpIeshMaxBeads || cfg->nelectrons > kRpIeshMaxElectrons)
+                return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ring-polymer IESH takes 2..32 beads and <= 64 electrons");
+            if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ring polymers need beta > 0");
+            if (cfg->save_stride != 0 || cfg->decoherence_C != 0.0)
+                return fail(nullptr, NQCD_ERR_UNSUPPORTED,
+                            "nqcd_create: ring-polymer IESH reports final states only, without decoherence correction");
+            const size_t smem_rp = cfg->precision == NQCD_PREC_FP64
+                                       ? iesh_layout<double>(cfg->nstates, cfg->nelectrons, cfg->nbeads_max).bytes
+                                       : iesh_layout<float>(cfg->nstates, cfg->nelectrons, cfg->nbeads_max).bytes;
+            if (smem_rp > 227 * 1024)
+                return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring-polymer IESH system too large for one CTA");
+        }
     } else if (mdef) {
         if (model != NQCD_MODEL_NEWNS_ANDERSON)
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs on the Newns-Anderson model");
@@ -478,7 +494,9 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
         if (!(cfg->terminate_x >= 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: terminate_x must be >= 0");
     }
     const bool rp_mdef = mdef && cfg->nbeads_max > 1;
-    const int64_t ndof = (rp || rp_mdef) ? (int64_t)cfg->nbeads_max : (int64_t)cfg->ndofs * cfg->natoms;
+    const bool rp_iesh = iesh && cfg->nbeads_max > 1;
+    const int64_t ndof = (rp || rp_mdef) ? (int64_t)cfg->nbeads_max
+                                         : (int64_t)cfg->ndofs * cfg->natoms * (rp_iesh ? cfg->nbeads_max : 1);
     int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? 5 : (iesh ? 6 : 4))));
     if (cfg->nparams < need_params || !cfg->params)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: too few model parameters");
@@ -569,7 +587,10 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     NQCD_CREATE(dalloc(&h->d_nhops, cap));
     NQCD_CREATE(dalloc(&h->d_nfrust, cap));
     NQCD_CREATE(dalloc(&h->d_nsteps, cap));
-    if (rp_mdef) NQCD_CREATE(dalloc(&h->d_rpmdef, cfg->nbeads_max * cfg->nbeads_max + 4 * cfg->nbeads_max));
+    if (rp_mdef || rp_iesh) {
+        h->rp_beads = cfg->nbeads_max;
+        NQCD_CREATE(dalloc(&h->d_rptab, cfg->nbeads_max * cfg->nbeads_max + 4 * cfg->nbeads_max));
+    }
     if (!mdef && !iesh) {  // FSSH, Ehrenfest, RPSH: per-trajectory FP64-electronics step counts
         NQCD_CREATE(dalloc(&h->d_fp64steps, cap));
         NQCD_CREATE(cudaMemset(h->d_fp64steps, 0, cap * sizeof(int32_t)));
@@ -785,7 +806,7 @@ int nqcd_sample_initial(nqcd_handle* h, int64_t ntraj, const nqcd_sampler* posit
     if (!h) return NQCD_ERR_ARG;
     if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: ntraj outside 1..ntraj_max");
     if (!position || !velocity) return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: position and velocity samplers are required");
-    if (h->cfg.method == NQCD_METHOD_RPSH)
+    if (h->cfg.method == NQCD_METHOD_RPSH || h->rp_beads > 1)
         return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_sample_initial: ring-polymer beads take nqcd_set_initial");
     if (h->cfg.method != NQCD_METHOD_MDEF && h->cfg.init_kind == NQCD_INIT_GIVEN)
         return fail(h, NQCD_ERR_ARG, "nqcd_sample_initial: NQCD_INIT_GIVEN needs nqcd_set_initial");
@@ -1141,6 +1162,19 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.energy = h->d_energy;
         q.obs_partial = nsave > 0 ? h->d_partial : nullptr;
         q.counters = h->d_counts + 8;
+        q.nbeads = h->rp_beads;
+        if (h->rp_beads > 1) {
+            // ring polymer: normal modes and full-step Cayley matrices of the free ring polymer
+            // (cayley_propagator(half=false), ring_polymer.jl:71-82, omega_n = nbeads / beta)
+            const int nb = h->rp_beads;
+            std::vector<double> tab((size_t)nb * nb + 4 * (size_t)nb);
+            nm_transform_matrix(nb, tab.data());
+            cayley_matrices(nb, h->cfg.beta, dt, tab.data() + (size_t)nb * nb);
+            NQCD_CUDA(h, cudaMemcpyAsync(h->d_rptab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+            q.rp_U = h->d_rptab;
+            q.rp_cay = h->d_rptab + (size_t)nb * nb;
+            q.omega_n = nb / h->cfg.beta;
+        }
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         e = h->cfg.precision == NQCD_PREC_FP64 ? launch_iesh_fp64(q, s) : launch_iesh_fp32(q, s);
     } else if (mdef) {
@@ -1168,11 +1202,11 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
                 c[2] = c[2] * sc;
                 c[3] = (c[3] + 1.0) * sc;
             }
-            NQCD_CUDA(h, cudaMemcpyAsync(h->d_rpmdef, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+            NQCD_CUDA(h, cudaMemcpyAsync(h->d_rptab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s));
             NQCD_CUDA(h, cudaMemsetAsync(h->d_energy, 0, 2 * N * sizeof(double), s));
             mp.nbeads = nb;
-            mp.rp_U = h->d_rpmdef;
-            mp.rp_half = h->d_rpmdef + (size_t)nb * nb;
+            mp.rp_U = h->d_rptab;
+            mp.rp_half = h->d_rptab + (size_t)nb * nb;
             mp.energy = nullptr;
             mp.obs_partial = nullptr;
         }

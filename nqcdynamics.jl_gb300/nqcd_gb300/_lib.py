@@ -282,10 +282,12 @@ class Engine:
 
     def get_final_iesh(self, nstates: int, nelectrons: int):
         """IESH final state: orbitals psi (ntraj, nstates, nelectrons) and
-        occupations (ntraj, nelectrons) in electron order."""
+        occupations (ntraj, nelectrons) in electron order; r, v (ntraj, 3), or
+        (ntraj, nbeads, 3) for a ring polymer."""
         n = self.ntraj
-        r = np.empty((n, 3))
-        v = np.empty((n, 3))
+        nb = self.cfg.nbeads_max if self.cfg.nbeads_max > 1 else 1
+        r = np.empty((n, 3 * nb))
+        v = np.empty((n, 3 * nb))
         pre = np.empty((n, nelectrons, nstates))
         pim = np.empty((n, nelectrons, nstates))
         occ = np.empty((n, nelectrons), np.int32)
@@ -296,6 +298,8 @@ class Engine:
         self._check(self.lib.nqcd_get_final(self.h, dptr(r), dptr(v), dptr(pre), dptr(pim), iptr(occ),
                                             iptr(nh), iptr(nf), iptr(ns), dptr(en)))
         psi = (pre + 1j * pim).transpose(0, 2, 1).copy()
+        if nb > 1:
+            r, v = r.reshape(n, nb, 3), v.reshape(n, nb, 3)
         return dict(r=r, v=v, psi=psi, state=occ, nhops=nh, nfrustrated=nf, nsteps=ns, energy=en)
 
     def mdef_evaluate(self, x):

@@ -9,6 +9,8 @@ Names, argument meanings and error behaviour follow the reference:
   Simulation[DiabaticMDEF](atoms, model; friction_method, temperature)   mdef.jl:79-100
   Simulation[AdiabaticIESH](atoms, model; rescaling, estimate_probability)   iesh.jl:72-87
   Simulation[EhrenfestNA](atoms, model)           EhrenfestMethods/ehrenfest_na.jl:30-32
+  RingPolymerSimulation[DiabaticMDEF](atoms, model, n_beads; friction_method, temperature)   rpmdef.jl:5-27
+  RingPolymerSimulation[AdiabaticIESH](atoms, model, n_beads; rescaling, temperature)   rpiesh.jl:3-18
   AndersonHolstein(impurity, bath; coupling, fermi_level, nelectrons),
   TrapezoidalRule, ShenviGaussLegendre, GaussianBroadening      (NQCModels, NQCCalculators)
   FermiDiracState(fermi_level, temperature; statetype)          (NQCDistributions)
@@ -330,12 +332,29 @@ class Simulation(metaclass=_MethodIndexed):
 
 
 class RingPolymerSimulation(metaclass=_MethodIndexed):
-    """RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature) and
+    """RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature),
     RingPolymerSimulation[DiabaticMDEF](atoms, model, n_beads; friction_method,
-    temperature) (rpmdef.jl:5-27)."""
+    temperature) (rpmdef.jl:5-27) and
+    RingPolymerSimulation[AdiabaticIESH](atoms, model, n_beads; rescaling,
+    estimate_probability, temperature) (rpiesh.jl:3-18)."""
 
     def __init__(self, atoms: Atoms, model: Model, n_beads, method=FSSH, rescaling: str = "standard",
-                 temperature: float = 0.0, friction_method=None):
+                 temperature: float = 0.0, friction_method=None, estimate_probability: bool = True,
+                 decoherence=None):
+        if method is AdiabaticIESH:
+            if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON_3D:
+                raise NotImplementedError("ring-polymer IESH runs on AndersonHolstein(AdsorbateMetal3D(...), bath)")
+            if decoherence is not None:
+                raise NotImplementedError("ring-polymer IESH runs without decoherence correction")
+            if not temperature > 0:
+                raise ValueError("ring polymers need a positive temperature")
+            if len(atoms) != 1 or not 2 <= int(n_beads) <= 32:
+                raise ValueError("one adsorbate atom with three degrees of freedom and 2..32 beads")
+            self.atoms, self.model = atoms, model
+            self.method = AdiabaticIESH(rescaling, estimate_probability, None)
+            self.temperature = float(temperature)
+            self.n_beads = int(n_beads)
+            return
         if method is DiabaticMDEF:
             if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON:
                 raise NotImplementedError("ring-polymer MDEF runs on AndersonHolstein(DisplacedHarmonic(...), bath)")
@@ -493,6 +512,8 @@ class DynamicalDistribution:
             return np.full((ntraj, n), float(arr))
         if arr.shape == self.size or arr.size == n:
             return np.broadcast_to(arr.reshape(-1, order="F"), (ntraj, n)).copy()
+        if arr.shape == (ntraj,) + tuple(self.size):  # one Julia-shaped array per trajectory: column-major
+            return arr.transpose(0, *range(arr.ndim - 1, 0, -1)).reshape(ntraj, -1).copy()
         if arr.ndim >= 1 and arr.shape[0] == ntraj:
             return arr.reshape(ntraj, -1).copy()
         raise ValueError("cannot interpret distribution specification")
@@ -675,7 +696,7 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
     if not isinstance(alg, EnsembleGB300):
         raise TypeError("ensemble_algorithm must be EnsembleGB300")
     if isinstance(sim, RingPolymerSimulation):
-        if isinstance(sim.method, DiabaticMDEF):
+        if isinstance(sim.method, (DiabaticMDEF, AdiabaticIESH)):
             return _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, dt, saveat, seed, rng)
         raise NotImplementedError("ring-polymer surface hopping runs through run_ring_polymer_ensemble")
     if isinstance(getattr(sim, "method", None), (DiabaticMDEF, AdiabaticIESH, EhrenfestNA)):
@@ -807,7 +828,10 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
     ntraj = int(trajectories)
     rp = isinstance(sim, RingPolymerSimulation)
     if rp and save_stride:
-        raise NotImplementedError("ring-polymer MDEF reports final states (OutputFinal) on the GPU path")
+        raise NotImplementedError("ring polymers report final states (OutputFinal, OutputTotalEnergy) on the GPU path")
+    if rp and not mdef and abs(distribution.electronic.β * sim.temperature - 1.0) > 1e-12:
+        raise NotImplementedError("ring-polymer IESH on the GPU path takes the Fermi-Dirac temperature equal to the "
+                                  "ring-polymer temperature")
     rng = rng if rng is not None else np.random.default_rng(alg.seed if seed is None else seed)
     r0 = nuclear.sample("r", ntraj, rng)
     v0 = nuclear.sample("v", ntraj, rng)
@@ -841,7 +865,7 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
             elif name == "OutputImpurityPopulation" and not mdef:
                 result[name] = ob[:, 2]
             elif name in ("OutputFinal", "OutputTotalEnergy", "OutputSurfaceHops"):
-                if final is None:
+                if final is None:  # ring polymers: r, v (ntraj, nbeads, ...)
                     final = eng.get_final(sim.n_beads if rp else 1) if mdef else \
                         eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
                 if name == "OutputFinal":

@@ -92,10 +92,11 @@ def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0,
 
 
 def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max_hops=0, exact=0, traj_offset=0,
-                        method=None):
+                        method=None, nbeads=0):
     """C5: IESH on the three-dimensional Newns-Anderson adsorbate, Fermi-Dirac
     initial occupations (method=L.METHOD_EHRENFEST_NA: EhrenfestNA on the same
-    system)."""
+    system; nbeads > 1: RingPolymerSimulation{AdiabaticIESH} with that many
+    beads)."""
     P = wl["params"]
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision, cfg.rescaling = (method or L.METHOD_IESH), L.MODEL_NEWNS_ANDERSON_3D, \
@@ -114,4 +115,5 @@ def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max
     cfg.max_hops = max_hops
     cfg.exact_hop_probability = exact
     cfg.traj_offset = traj_offset
+    cfg.nbeads_max = nbeads
     return L.Engine(cfg, [params, masses, eps, V])

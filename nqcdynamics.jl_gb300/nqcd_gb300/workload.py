@@ -114,6 +114,37 @@ def newns_anderson_iesh(ntraj: int, *, nstates: int = 80, nelectrons: int = 40, 
                 nelectrons=nelectrons, r0=r0, v0=v0, dt=0.1 * AU_PER_FS)
 
 
+def newns_anderson_rpiesh(ntraj: int, nbeads: int, **kw):
+    """Ring-polymer IESH workload: the IESH scattering workload's positions and
+    velocities become the centroids, and the beads spread about them as a
+    free ring polymer at the electronic temperature T: with
+    beta_n = beta / nbeads and omega_n = nbeads / beta, the internal normal
+    modes (eigenvectors of the cyclic bead Laplacian, eigenvalues
+    4 sin^2(k pi / nbeads)) are Gaussian with variance
+    1 / (beta_n m omega_n^2 4 sin^2(k pi / nbeads)), and the bead velocities
+    are thermal at beta_n about the centroid velocity.  r0, v0:
+    (ntraj, nbeads, 3), every centroid exactly the workload's value."""
+    wl = newns_anderson_iesh(ntraj, **kw)
+    B = nbeads
+    m, beta = wl["mass"], wl["beta"]
+    bn, wn = beta / B, B / beta
+    rng = np.random.default_rng([kw.get("seed", SEED), kw.get("traj_offset", 0), 6])
+    lap = 2.0 * np.eye(B) - np.roll(np.eye(B), 1, axis=1) - np.roll(np.eye(B), -1, axis=1)
+    lam, E = np.linalg.eigh(lap)
+    sd = np.zeros(B)
+    internal = lam > 1e-9
+    sd[internal] = 1.0 / np.sqrt(bn * m * wn * wn * lam[internal])
+    q = rng.standard_normal((ntraj, 3, B)) * sd
+    dr = np.einsum("bk,tdk->tbd", E, q)
+    dv = rng.standard_normal((ntraj, B, 3)) / np.sqrt(bn * m)
+    dr -= dr.mean(axis=1, keepdims=True)
+    dv -= dv.mean(axis=1, keepdims=True)
+    wl["r0"] = wl["r0"][:, None, :] + dr
+    wl["v0"] = wl["v0"][:, None, :] + dv
+    wl["nbeads"] = B
+    return wl
+
+
 # ---------------------------------------------------------------------------
 # Algorithmic work of the reference algorithm per nuclear step of one
 # trajectory (two electronic states), counted operation by operation from

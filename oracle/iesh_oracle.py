@@ -308,3 +308,144 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
     nimp = impurity_population_ehrenfest_na(psi, Z) if ehrenfest_na else impurity_population(psi, Z, state)
     return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, Z=Z, w=w, initial_state=states,
                 energy=np.stack([e0, e1], axis=1), nimp=nimp, nfull=nfull)
+
+
+def spring_energy(r, mass, beta):
+    """get_spring_energy (ring_polymer.jl:85-107): m omega_n^2 / 2 sum over
+    neighbouring beads (cyclic) of |r_b - r_b+1|^2, omega_n = nbeads / beta."""
+    B = r.shape[1]
+    wn = B / beta
+    d = r - np.roll(r, -1, axis=1)
+    return 0.5 * mass * wn * wn * np.sum(d * d, axis=(1, 2))
+
+
+def run_rpiesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, estimate=True,
+               initial_state=None):
+    """RingPolymerSimulation{AdiabaticIESH} (rpiesh.jl) with BCBWavefunction
+    (bcb_wavefunction.jl:37-69).  r0, v0: (ntraj, nbeads, 3).
+
+    Step: v' = v + dt/2 k; full Cayley step of the free ring polymer in
+    normal modes (cayley_propagator(half=false), ring_polymer.jl:71-82,
+    omega_n = nbeads / beta); bead forces from each bead's own eigenstates
+    summed over the shared occupied set (rpiesh.jl:20-37); v = v' + dt/2 k;
+    orbitals propagated with the centroid velocity of the step's START and the
+    centroid eigenvalues and couplings of the step's END (the calculator
+    cache holds the end positions when propagate_wavefunction! reads it,
+    bcb_wavefunction.jl:59-68, SurfaceHoppingMethods.jl:81-103).  Hops use
+    the final centroid velocity and couplings (iesh.jl:231-298); an accepted
+    hop shifts every bead's velocity by the same -gamma d / m and a frustrated
+    :vinversion hop inverts the centroid velocity along d in every bead
+    (rpsh.jl:30-50).  Fermi-Dirac occupations come from the centroid
+    eigenvalues (iesh.jl:99-128).  Energy: kinetic + sum over beads of
+    U0 + occupied eigenvalues (rpiesh.jl:39-52) + spring energy."""
+    import oracle as O
+
+    n, B, _ = r0.shape
+    N = model.nstates
+    traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
+    r = np.asarray(r0, np.float64).copy()
+    v = np.asarray(v0, np.float64).copy()
+    U = O.nm_transform(B)  # U[j, k]: bead j, mode k
+    C = O.cayley(B, beta, dt)
+
+    def free(r, v):
+        q = np.einsum("tbd,bk->tkd", r, U)
+        p = np.einsum("tbd,bk->tkd", v, U)
+        q2 = C[None, :, 0, 0, None] * q + C[None, :, 0, 1, None] * p
+        p2 = C[None, :, 1, 0, None] * q + C[None, :, 1, 1, None] * p
+        return np.einsum("tkd,bk->tbd", q2, U), np.einsum("tkd,bk->tbd", p2, U)
+
+    def beads(r):
+        w, Z = np.linalg.eigh(model.hamiltonian(r.reshape(n * B, 3)))
+        return w.reshape(n, B, N), (Z[:, 0, :] ** 2).reshape(n, B, N)
+
+    def accel(r, state):
+        _, z2 = beads(r)
+        occsum = np.take_along_axis(z2, np.repeat(state[:, None, :], B, axis=1), axis=2).sum(2)
+        gh = model.grad_h(r.reshape(n * B, 3)).reshape(n, B, 3)
+        gu = model.grad_U0(r.reshape(n * B, 3)).reshape(n, B, 3)
+        return -(gu + gh * occsum[:, :, None]) / mass
+
+    def energy(r, v, state):
+        w, _ = beads(r)
+        band = np.take_along_axis(w, np.repeat(state[:, None, :], B, axis=1), axis=2).sum(2)
+        pot = (model.U0(r.reshape(n * B, 3)).reshape(n, B) + band).sum(1)
+        return 0.5 * mass * np.sum(v * v, axis=(1, 2)) + pot + spring_energy(r, mass, beta)
+
+    Zc = np.tile(np.eye(N), (n, 1, 1))
+    wc, Zc = eigen_continuous(model, r.mean(1), Zc)
+    states = sample_fermi_dirac(wc, ne, beta, seed, traj) if initial_state is None else np.array(initial_state)
+    psi = np.zeros((n, N, ne), np.complex128)
+    for t in range(n):
+        psi[t, states[t], np.arange(ne)] = 1.0
+    state = states.copy()
+    hops = [[] for _ in range(n)]
+    nfr = np.zeros(n, np.int32)
+    k = accel(r, state)
+    e0 = energy(r, v, state)
+    idx = np.arange(N)
+    for step in range(1, nsteps + 1):
+        vc_prev = v.mean(1)
+        vt = v + (dt / 2) * k
+        r, vt = free(r, vt)
+        k = accel(r, state)
+        v = vt + (dt / 2) * k
+        rc = r.mean(1)
+        wc, Zc = eigen_continuous(model, rc, Zc)
+        gh = model.grad_h(rc)
+        z0 = Zc[:, 0, :]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            base = z0[:, :, None] * z0[:, None, :] / (wc[:, None, :] - wc[:, :, None])
+        base[:, idx, idx] = 0.0
+        Heff = np.zeros((n, N, N), np.complex128)
+        Heff[:, idx, idx] = wc
+        Heff -= 1j * np.einsum("ta,ta->t", vc_prev, gh)[:, None, None] * base
+        mu, Uh = np.linalg.eigh(Heff)
+        psi = np.einsum("tij,tj,tkj->tik", Uh, np.exp(-1j * mu * dt), Uh.conj()) @ psi
+        vc = v.mean(1)
+        vd = np.einsum("ta,ta->t", vc, gh)[:, None, None] * base
+        wh = uniform(seed, traj, step, RNG_HOP)
+        rnd = u53(wh[0], wh[1])
+        for t in range(n):
+            st = state[t]
+            unocc = np.array([s for s in range(N) if s not in set(st.tolist())])
+            detS = np.linalg.det(psi[t][st, :])
+            pref = 2 * dt / abs(detS) ** 2
+            vdd = np.zeros((N, ne))
+            for nn in range(ne):
+                vdd[unocc, nn] -= vd[t][unocc, st[nn]]
+            if estimate and pref * np.abs(vdd).sum() * (abs(detS.real) + abs(detS.imag)) < rnd[t]:
+                continue
+            prob = np.zeros((N, ne))
+            for nn in range(ne):
+                for m in unocc:
+                    s2 = st.copy()
+                    s2[nn] = m
+                    prob[m, nn] = pref * (detS * np.conj(np.linalg.det(psi[t][s2, :]))).real * vdd[m, nn]
+            prob = np.clip(prob, 0, 1)
+            cum, new = 0.0, None
+            for nn in range(ne):
+                for m in unocc:
+                    cum += prob[m, nn]
+                    if rnd[t] < cum:
+                        new = (nn, m)
+                        break
+                if new:
+                    break
+            if new is None:
+                continue
+            nn, m = new
+            old = st[nn]
+            accept = True
+            if rescaling != 2:
+                d = gh[t] * z0[t, m] * z0[t, old] / (wc[t, old] - wc[t, m])
+                vc_new, accept = rescale_velocity(vc[t], d, mass, wc[t, m] - wc[t, old], rescaling)
+                v[t] += (vc_new - vc[t])[None, :]  # the same shift in every bead
+            if accept:
+                state[t, nn] = m
+                hops[t].append((step, int(old), int(m)))
+            else:
+                nfr[t] += 1
+    e1 = energy(r, v, state)
+    return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, initial_state=states,
+                energy=np.stack([e0, e1], axis=1))

@@ -192,3 +192,59 @@ def test_metal_simulation_arguments_are_checked():
     with pytest.raises(ValueError):  # time series need saveat
         N.run_dynamics(sim, (0.0, 10.0), nuc * N.FermiDiracState(0.0, 1e-3), output=N.OutputKineticEnergy,
                        trajectories=2, ensemble_algorithm=N.EnsembleGB300("fp32"))
+
+
+def _rpiesh_cfg(**kw):
+    wl = workload.newns_anderson_iesh(4, nstates=20, nelectrons=10)
+    P = wl["params"]
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = L.METHOD_IESH, L.MODEL_NEWNS_ANDERSON_3D, L.PREC_FP64
+    cfg.ndofs, cfg.natoms, cfg.nstates, cfg.nelectrons = 3, 1, 20, 10
+    params = np.array([P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"]])
+    masses = np.array([wl["mass"]])
+    eps, V = np.ascontiguousarray(wl["eps"]), np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 6, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta, cfg.ntraj_max, cfg.init_kind, cfg.nbeads_max = wl["beta"], 4, L.INIT_FERMI_DIRAC, 8
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg, [params, masses, eps, V]
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("method", "ehrenfest_na", -6), ("nbeads_max", 33, -1), ("save_stride", 5, -6), ("decoherence_C", 0.1, -6),
+    ("beta", 0.0, -1),
+])
+def test_create_validates_ring_polymer_iesh(field, value, code):
+    # RingPolymerSimulation{AdiabaticIESH}: IESH with nbeads_max > 1; checked before any device work
+    if value == "ehrenfest_na":
+        value = L.METHOD_EHRENFEST_NA
+    cfg, keep = _rpiesh_cfg(**{field: value})
+    lib = L.load()
+    h = C.c_void_p()
+    rc = lib.nqcd_create(C.byref(cfg), C.byref(h))
+    assert rc == code, (field, rc, lib.nqcd_last_error(None))
+    assert not h.value
+
+
+def test_ring_polymer_iesh_maps_to_the_abi():
+    _, m = _iesh_sim()
+    sim = N.RingPolymerSimulation[N.AdiabaticIESH](N.Atoms(1837.0), m, 8, temperature=1 / 1052.6,
+                                                   rescaling="vinversion")
+    cfg, _ = api._metal_config(sim, 16, N.EnsembleGB300("fp64"), 0)
+    assert cfg.method == L.METHOD_IESH and cfg.rescaling == 1 and cfg.nelectrons == 40
+    with pytest.raises(ValueError):
+        N.RingPolymerSimulation[N.AdiabaticIESH](N.Atoms(1837.0), m, 33, temperature=0.001)
+    with pytest.raises(NotImplementedError):
+        N.RingPolymerSimulation[N.AdiabaticIESH](N.Atoms(1837.0), m, 4, temperature=0.001,
+                                                 decoherence=N.DecoherenceCorrectionEDC())
+    # per-trajectory arrays in Julia's (ndofs, natoms, nbeads) shape flatten column-major
+    r = np.arange(2 * 3 * 4, dtype=float).reshape(2, 3, 1, 4)
+    d = N.DynamicalDistribution(r, r, (3, 1, 4))
+    flat = d.sample("r", 2, np.random.default_rng(0))
+    np.testing.assert_array_equal(flat[1], r[1].reshape(-1, order="F"))
+    # the Fermi-Dirac temperature must be the ring polymer's on the GPU path
+    dist = d * N.FermiDiracState(0.0, 2e-3)
+    with pytest.raises(NotImplementedError):
+        N.run_dynamics(sim, (0.0, 1.0), dist, output=N.OutputFinal, trajectories=2,
+                       ensemble_algorithm=N.EnsembleGB300("fp64"), dt=0.1)

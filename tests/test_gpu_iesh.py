@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 
 def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_DIRAC, max_hops=32, save_stride=0,
-              exact=0, method=L.METHOD_IESH, decoherence=0.0):
+              exact=0, method=L.METHOD_IESH, decoherence=0.0, nbeads=0, traj_offset=0):
     P = wl["params"]
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision, cfg.rescaling = method, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
@@ -41,6 +41,8 @@ def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_D
     cfg.save_stride = save_stride
     cfg.exact_hop_probability = exact
     cfg.decoherence_C = decoherence
+    cfg.nbeads_max = nbeads  # > 1: RingPolymerSimulation{AdiabaticIESH}
+    cfg.traj_offset = traj_offset
     return L.Engine(cfg, [params, masses, eps, V])
 
 

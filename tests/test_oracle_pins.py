@@ -538,3 +538,59 @@ def test_rpmdef_oracle_reduces_to_baoab_for_one_bead():
     x2, v2 = MO.run_mdef(model, x0=wl["x0"], v0=wl["v0"], **kw)
     np.testing.assert_array_equal(x1[:, 0], x2)
     np.testing.assert_array_equal(v1[:, 0], v2)
+
+
+def _rpiesh_case(n, nbeads, z0, **kw):
+    IO = _iesh()
+    from nqcd_gb300 import workload as WL
+
+    wl = WL.newns_anderson_rpiesh(n, nbeads, z0=z0, **kw)
+    P = wl["params"]
+    model = IO.Metal3D(kxy=P["kxy"], A=P["A"], a=P["a"], delta=P["delta"], B=P["B"], b=P["b"], eps=wl["eps"],
+                       V=wl["V"])
+    return IO, wl, model
+
+
+def test_rpiesh_spring_energy_known_answer():
+    # get_spring_energy (ring_polymer.jl:85-107): m omega_n^2 / 2 times the sum of squared
+    # neighbour distances around the ring; four beads on a unit square give 4
+    IO = _iesh()
+    r = np.array([[[0.0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]]])
+    beta, m = 8.0, 3.0
+    assert IO.spring_energy(r, m, beta)[0] == pytest.approx(0.5 * m * (4 / beta) ** 2 * 4, rel=1e-15)
+    r2 = np.array([[[0.0, 0, 0], [2, 0, 0]]])  # two beads: the pair counted once each way
+    assert IO.spring_energy(r2, m, beta)[0] == pytest.approx(0.5 * m * (2 / beta) ** 2 * 8, rel=1e-15)
+
+
+def test_rpiesh_oracle_one_bead_moves_the_nucleus_as_iesh():
+    """With one bead the full Cayley step of the free ring polymer is the drift
+    r + dt v, so BCBWavefunction moves the nucleus exactly as
+    VerletwithElectronics; the orbitals differ only in the velocity used by the
+    propagator (the step's start for BCBWavefunction, its end for
+    VerletwithElectronics).  Far from the surface no hop happens."""
+    IO, wl, model = _rpiesh_case(3, 1, 12.0, nstates=20, nelectrons=10)
+    C = O.cayley(1, wl["beta"], wl["dt"])
+    np.testing.assert_array_equal(C[0], [[1.0, wl["dt"]], [0.0, 1.0]])
+    kw = dict(mass=wl["mass"], ne=10, beta=wl["beta"], dt=wl["dt"], nsteps=100, seed=2)
+    a = IO.run_rpiesh(model, r0=wl["r0"], v0=wl["v0"], **kw)
+    b = IO.run_iesh(model, r0=wl["r0"][:, 0, :], v0=wl["v0"][:, 0, :], **kw)
+    assert all(len(h) == 0 for h in a["hops"]) and all(len(h) == 0 for h in b["hops"])
+    np.testing.assert_array_equal(a["initial_state"], b["initial_state"])
+    np.testing.assert_allclose(a["r"][:, 0, :], b["r"], rtol=1e-14, atol=1e-14)
+    np.testing.assert_allclose(a["v"][:, 0, :], b["v"], rtol=1e-14, atol=1e-16)
+    np.testing.assert_allclose(a["energy"], b["energy"], rtol=1e-13)
+    np.testing.assert_allclose(a["psi"], b["psi"], atol=1e-6)
+
+
+def test_rpiesh_oracle_conserves_ring_polymer_energy():
+    # no hops far from the surface: kinetic + bead potentials + springs is conserved by the
+    # symplectic BCB step to O(dt^2); orbitals stay orthonormal
+    IO, wl, model = _rpiesh_case(3, 4, 12.0, nstates=16, nelectrons=8)
+    res = IO.run_rpiesh(model, mass=wl["mass"], ne=8, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"], dt=wl["dt"],
+                        nsteps=400, seed=5)
+    assert all(len(h) == 0 for h in res["hops"])
+    e0, e1 = res["energy"][:, 0], res["energy"][:, 1]
+    assert np.all(np.abs(e1 - e0) < 1e-6 * np.abs(e0))
+    for t in range(3):
+        g = res["psi"][t].conj().T @ res["psi"][t]
+        assert np.abs(g - np.eye(8)).max() < 1e-10
