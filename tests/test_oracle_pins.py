@@ -594,3 +594,25 @@ def test_rpiesh_oracle_conserves_ring_polymer_energy():
     for t in range(3):
         g = res["psi"][t].conj().T @ res["psi"][t]
         assert np.abs(g - np.eye(8)).max() < 1e-10
+
+
+def test_rpiesh_workload_is_a_thermal_free_ring_polymer():
+    """The ring-polymer IESH workload keeps every centroid at the classical
+    workload's value and spreads the beads as the free ring polymer at
+    beta_n = beta / nbeads: the mean spring energy per internal mode and
+    Cartesian direction is 1 / (2 beta_n), and the bead velocities about the
+    centroid have variance 1 / (beta_n m) times (nbeads - 1) / nbeads."""
+    IO = _iesh()
+    from nqcd_gb300 import workload as WL
+
+    n, B = 4000, 8
+    wl = WL.newns_anderson_rpiesh(n, B)
+    base = WL.newns_anderson_iesh(n)
+    np.testing.assert_allclose(wl["r0"].mean(1), base["r0"], atol=1e-12)
+    np.testing.assert_allclose(wl["v0"].mean(1), base["v0"], atol=1e-15)
+    bn, m = wl["beta"] / B, wl["mass"]
+    spring = IO.spring_energy(wl["r0"], m, wl["beta"])  # m omega_n^2 / 2 sum |r_b - r_b+1|^2
+    expect = 3 * (B - 1) / (2 * bn)
+    assert spring.mean() == pytest.approx(expect, rel=0.02)
+    dv = wl["v0"] - wl["v0"].mean(1, keepdims=True)
+    assert dv.var() == pytest.approx((B - 1) / B / (bn * m), rel=0.02)
