@@ -452,7 +452,7 @@ def secondary(args, dist):
                                             ("surrogate_sub", L.PREC_FP32, nsub, nsub_steps, True),
                                             ("fp32", L.PREC_FP32, n, nsteps, False),
                                             ("surrogate", L.PREC_FP32, n, nsteps, True)):
-                eng = C.mdef_newns_anderson(L, wl, nt, prec, surrogate=sur, judge_every=50 if sur else 0,
+                eng = C.mdef_newns_anderson(L, wl, nt, prec, surrogate=sur, exact_friction_every=50 if sur else 0,
                                             save_stride=stride, traj_offset=rank_off * n)
                 if sur:
                     eng.mlp_set(*mlp)

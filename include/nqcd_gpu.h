@@ -121,7 +121,7 @@ typedef struct nqcd_config {
     double gap_fp64;      /* fast path: propagate electronics in FP64 when the adiabatic gap is below this */
     int64_t traj_offset;  /* global index of trajectory 0 (Philox counter), for sharded ensembles */
     int32_t use_friction_surrogate; /* MDEF fast path: friction from the trained network inside its domain */
-    int32_t judge_every;  /* MDEF with surrogate: exact friction every judge_every steps (0 = never) */
+    int32_t exact_friction_every; /* MDEF with surrogate: exact friction every k steps (0 = never) */
     int32_t nelectrons;   /* IESH: electrons (occupied one-electron states) */
     int32_t exact_hop_probability; /* IESH: 1 = no estimate screen (estimate_probability = false) */
     int32_t reserved[2];

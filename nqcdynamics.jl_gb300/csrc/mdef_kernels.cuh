@@ -68,7 +68,7 @@ struct MdefParams {
     uint64_t seed;
     int32_t save_stride, nsave;
     int32_t use_mlp;        // fast path: friction from the surrogate inside its domain
-    int32_t judge_every;    // fast path with surrogate: exact friction every k steps (0 = never)
+    int32_t exact_friction_every;    // fast path with surrogate: exact friction every k steps (0 = never)
     MlpWeights mlp;
     double* x;              // [ntraj] in/out
     double* v;              // [ntraj] in/out
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         bool use_net = false;
         if constexpr (std::is_same<R, float>::value) {
             use_net = p.use_mlp && (float)x >= p.mlp.lo && (float)x <= p.mlp.hi &&
-                      !(p.judge_every > 0 && step % p.judge_every == 0);
+                      !(p.exact_friction_every > 0 && step % p.exact_friction_every == 0);
         }
         if (use_net) {
             lamv = (double)mlp_friction(p.mlp, (float)x);

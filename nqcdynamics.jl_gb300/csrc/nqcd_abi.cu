@@ -364,7 +364,7 @@ MdefParams mdef_params(nqcd_handle* h, int64_t N, double dt, int32_t nsteps, uin
     m.save_stride = stride;
     m.nsave = nsave;
     m.use_mlp = (h->cfg.use_friction_surrogate && h->cfg.precision != NQCD_PREC_FP64) ? 1 : 0;
-    m.judge_every = h->cfg.judge_every;
+    m.exact_friction_every = h->cfg.exact_friction_every;
     m.mlp = mlp_view(h->mlp);
     m.x = h->d_r;
     m.v = h->d_v;

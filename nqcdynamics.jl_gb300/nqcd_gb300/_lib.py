@@ -62,7 +62,7 @@ class nqcd_config(C.Structure):
         ("gap_fp64", C.c_double),
         ("traj_offset", C.c_int64),
         ("use_friction_surrogate", C.c_int32),
-        ("judge_every", C.c_int32),
+        ("exact_friction_every", C.c_int32),
         ("nelectrons", C.c_int32),
         ("exact_hop_probability", C.c_int32),
         ("reserved", C.c_int32 * 2),

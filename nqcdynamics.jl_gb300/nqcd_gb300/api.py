@@ -634,7 +634,7 @@ class EnsembleGB300:
     max_hops: int = 16
     seed: int = 20261203
     friction_surrogate: Any = None  # MDEF: (weights, meta) of a trained network, or None
-    judge_every: int = 0
+    exact_friction_every: int = 0
     device_sampling: bool = False   # draw the nuclear initial conditions on the GPU (nqcd_sample_initial)
 
 
@@ -779,7 +779,7 @@ def _metal_config(sim, ntraj, alg, save_stride):
         params = np.array([imp.k, imp.g, imp.delta, model.fermi_level, sim.friction_method.σ])
         cfg.beta = 1.0 / sim.temperature
         cfg.use_friction_surrogate = int(alg.friction_surrogate is not None)
-        cfg.judge_every = alg.judge_every
+        cfg.exact_friction_every = alg.exact_friction_every
     else:
         params = np.array([imp.kxy, imp.A, imp.a, imp.delta, imp.B, imp.b])
         cfg.rescaling = 0 if ena else L.RESCALE[sim.method.rescaling]

@@ -68,7 +68,7 @@ def rpsh_inputs(ntraj, bmax=32, mass=2000.0, x0=-9.5, seed=WL.SEED, traj_offset=
     return r0, v0, nb, models
 
 
-def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0, save_stride=0, traj_offset=0,
+def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, exact_friction_every=0, save_stride=0, traj_offset=0,
                         nbeads=0):
     """C4: MDEF (electronic-friction Langevin) on the Newns-Anderson model
     (nbeads > 1: ring-polymer MDEF with that many beads)."""
@@ -85,7 +85,7 @@ def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, judge_every=0,
     cfg.ntraj_max = ntraj
     cfg.save_stride = save_stride
     cfg.use_friction_surrogate = int(surrogate)
-    cfg.judge_every = judge_every
+    cfg.exact_friction_every = exact_friction_every
     cfg.traj_offset = traj_offset
     cfg.nbeads_max = nbeads
     return L.Engine(cfg, [params, masses, eps, V])

@@ -24,7 +24,7 @@ from nqcd_gb300 import workload as WL
 pytestmark = pytest.mark.gpu
 
 
-def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, judge_every=0, nbeads=0):
+def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, exact_friction_every=0, nbeads=0):
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON, precision
     cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 1 + len(wl["eps"])
@@ -38,7 +38,7 @@ def make_mdef(wl, ntraj, precision=L.PREC_FP64, save_stride=0, surrogate=False, 
     cfg.ntraj_max = ntraj
     cfg.save_stride = save_stride
     cfg.use_friction_surrogate = int(surrogate)
-    cfg.judge_every = judge_every
+    cfg.exact_friction_every = exact_friction_every
     cfg.nbeads_max = nbeads
     return L.Engine(cfg, [params, masses, eps, V])
 
@@ -81,8 +81,8 @@ def test_mdef_fp64_trajectories_match_oracle():
     np.testing.assert_allclose(fin["v"][:, 0], v, rtol=1e-8, atol=1e-12)
 
 
-def run_relax(wl, n, prec, nsteps, stride, surrogate=False, judge_every=0, mlp=None):
-    eng = make_mdef(wl, n, prec, save_stride=stride, surrogate=surrogate, judge_every=judge_every)
+def run_relax(wl, n, prec, nsteps, stride, surrogate=False, exact_friction_every=0, mlp=None):
+    eng = make_mdef(wl, n, prec, save_stride=stride, surrogate=surrogate, exact_friction_every=exact_friction_every)
     try:
         if mlp is not None:
             eng.mlp_set(*mlp)
@@ -162,7 +162,7 @@ def test_friction_surrogate_trains_and_serves():
     # the network reproduces the exact friction over its domain
     assert np.max(np.abs(pred - G)) < 0.02 * G.max(), (loss, np.max(np.abs(pred - G)), G.max())
     exact, st_e, e_e = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
-    surr, st_s, e_s = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, judge_every=50, mlp=mlp)
+    surr, st_s, e_s = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, exact_friction_every=50, mlp=mlp)
     total = n * nsteps
     assert st_s.surrogate_friction_evals + st_s.exact_friction_evals == total
     assert st_s.surrogate_friction_evals > 0.9 * total
