@@ -616,3 +616,37 @@ def test_rpiesh_workload_is_a_thermal_free_ring_polymer():
     assert spring.mean() == pytest.approx(expect, rel=0.02)
     dv = wl["v0"] - wl["v0"].mean(1, keepdims=True)
     assert dv.var() == pytest.approx((B - 1) / B / (bn * m), rel=0.02)
+
+
+def test_tsit5_tableau_satisfies_the_order_five_conditions():
+    """The Tsit5 tableau (Tsitouras, Comput. Math. Appl. 62, 770 (2011)), shared
+    by the oracle and the kernels through csrc/nqcd_math.h, satisfies the row
+    sums c_i = sum_j a_ij, the first-same-as-last property (the weights are the
+    last row, c_6 = c_7 = 1) and all 17 Butcher order conditions up to order 5."""
+    import re
+    from pathlib import Path
+
+    src = (Path(__file__).resolve().parent.parent / "nqcdynamics.jl_gb300" / "csrc" / "nqcd_math.h").read_text()
+    body = src[src.index("struct Tsit5"):]
+    body = body[: body.index("};")]
+    val = {k: float(v) for k, v in re.findall(r"(\w+) = (-?[0-9.eE+-]+);", body)}
+    A = np.zeros((7, 7))
+    for (i, j) in [(i, j) for i in range(2, 8) for j in range(1, i)]:
+        A[i - 1, j - 1] = val[f"a{i}{j}"]
+    c = A.sum(axis=1)
+    for i in range(2, 6):
+        assert c[i - 1] == pytest.approx(val[f"c{i}"], abs=1e-15)
+    assert c[5] == pytest.approx(1.0, abs=1e-14) and c[6] == pytest.approx(1.0, abs=1e-14)
+    b = A[6]
+    Ac, Ac2, Ac3 = A @ c, A @ c**2, A @ c**3
+    AAc = A @ Ac
+    conditions = [
+        (b.sum(), 1.0), (b @ c, 1 / 2),
+        (b @ c**2, 1 / 3), (b @ Ac, 1 / 6),
+        (b @ c**3, 1 / 4), (b @ (c * Ac), 1 / 8), (b @ Ac2, 1 / 12), (b @ AAc, 1 / 24),
+        (b @ c**4, 1 / 5), (b @ (c**2 * Ac), 1 / 10), (b @ (c * Ac2), 1 / 15), (b @ (c * AAc), 1 / 30),
+        (b @ Ac**2, 1 / 20), (b @ Ac3, 1 / 20), (b @ (A @ (c * Ac)), 1 / 40), (b @ (A @ Ac2), 1 / 60),
+        (b @ (A @ AAc), 1 / 120),
+    ]
+    for k, (got, want) in enumerate(conditions):
+        assert got == pytest.approx(want, abs=5e-14), (k, got, want)
