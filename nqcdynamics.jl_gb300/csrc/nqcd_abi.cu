@@ -1408,16 +1408,22 @@ int nqcd_train_friction_mlp(nqcd_handle* h, double x_lo, double x_hi, int64_t np
         if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_train_friction_mlp: allocation");
     }
     double *dx = nullptr, *dF = nullptr, *dG = nullptr, *dL = nullptr;
-    NQCD_CUDA(h, dalloc(&dx, npoints));
-    NQCD_CUDA(h, dalloc(&dF, npoints));
-    NQCD_CUDA(h, dalloc(&dG, npoints));
-    NQCD_CUDA(h, dalloc(&dL, npoints));
-    auto release = [&]() {
+    auto release = [&]() {  // cudaFree(nullptr) is a no-op
         cudaFree(dx);
         cudaFree(dF);
         cudaFree(dG);
         cudaFree(dL);
     };
+    {
+        cudaError_t ea = dalloc(&dx, npoints);
+        if (ea == cudaSuccess) ea = dalloc(&dF, npoints);
+        if (ea == cudaSuccess) ea = dalloc(&dG, npoints);
+        if (ea == cudaSuccess) ea = dalloc(&dL, npoints);
+        if (ea != cudaSuccess) {
+            release();
+            return cuda_fail(h, ea, "nqcd_train_friction_mlp: allocation");
+        }
+    }
     uniform_positions_kernel<<<(unsigned)((npoints + 255) / 256), 256, 0, s>>>(dx, npoints, x_lo, x_hi, seed);
     int rc = mdef_eval_device(h, dx, npoints, dF, dG);  // training data from the method itself
     if (rc) {
