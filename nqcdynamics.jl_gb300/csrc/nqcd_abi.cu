@@ -1476,6 +1476,9 @@ int nqcd_mlp_get(nqcd_handle* h, float* params, double* meta) {
 int nqcd_mlp_set(nqcd_handle* h, const float* params, const double* meta) {
     if (!h || !params || !meta) return NQCD_ERR_ARG;
     if (h->cfg.method != NQCD_METHOD_MDEF) return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_mlp_set: MDEF handles only");
+    if (!isfinite(meta[0]) || !(meta[1] > 0.0 && meta[1] < 1e300) || !isfinite(meta[2]) || !isfinite(meta[3]) ||
+        !(meta[3] > meta[2]))
+        return fail(h, NQCD_ERR_ARG, "nqcd_mlp_set: need finite shift, scale > 0 and a domain lo < hi");
     if (!h->mlp.master) {
         cudaError_t e = mlp_alloc(h->mlp, 65536);
         if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_mlp_set: allocation");
@@ -1565,8 +1568,11 @@ int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
     double* sink64 = nullptr;
     float* sink32 = nullptr;
     cudaEvent_t a, b;
-    if (cudaMalloc(&sink64, 1024 * sizeof(double)) != cudaSuccess || cudaMalloc(&sink32, 1024 * sizeof(float)) != cudaSuccess)
-        return cuda_fail(nullptr, cudaGetLastError(), "nqcd_measure_fma_peaks: alloc");
+    if (cudaMalloc(&sink64, 1024 * sizeof(double)) != cudaSuccess || cudaMalloc(&sink32, 1024 * sizeof(float)) != cudaSuccess) {
+        const cudaError_t ea = cudaGetLastError();
+        cudaFree(sink64);  // no-op when null
+        return cuda_fail(nullptr, ea, "nqcd_measure_fma_peaks: alloc");
+    }
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     const int threads = 256;
