@@ -266,7 +266,9 @@ int nqcd_train_friction_mlp(nqcd_handle* h, double x_lo, double x_hi, int64_t np
 
 /* Surrogate network parameters as FP32, packed W1[64] b1[64] W2[64*64] b2[64]
  * W3[64] b3[1] (4353 values): get from / set into the handle (set also fixes
- * the input normalisation x -> (x - shift) * scale and the domain). */
+ * the input normalisation x -> (x - shift) * scale and the domain [lo, hi]
+ * from shift_scale_lo_hi; NQCD_ERR_ARG unless shift is finite, scale > 0 and
+ * lo < hi). */
 #define NQCD_MLP_NPARAMS 4353
 int nqcd_mlp_get(nqcd_handle* h, float* params, double* shift_scale_lo_hi);
 int nqcd_mlp_set(nqcd_handle* h, const float* params, const double* shift_scale_lo_hi);
