@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 104
+#define NQCD_ABI_VERSION 105
 
 enum nqcd_status {
     NQCD_OK = 0,
