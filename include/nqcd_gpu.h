@@ -169,13 +169,13 @@ int nqcd_version(void);
 
 /* Create an engine for one Simulation (reference: Simulation/RingPolymerSimulation
  * constructors, src/simulations.jl:12-73, with the method of
- * src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:206-213).  Allocates device
+ * src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:38-45).  Allocates device
  * memory for cfg->ntraj_max trajectories. */
 int nqcd_create(const nqcd_config* cfg, nqcd_handle** out);
 
 /* Initial conditions for `ntraj` trajectories (reference: Selection /
  * sample_distribution, src/Ensembles/selections.jl:70-99, and
- * DynamicsVariables, fssh.jl:215-233).  r0, v0: (ndofs, natoms[, nbeads], ntraj).
+ * DynamicsVariables, fssh.jl:47-65).  r0, v0: (ndofs, natoms[, nbeads], ntraj).
  * sig_re/sig_im/state0 are read only for NQCD_INIT_GIVEN (else may be NULL).
  * IESH: state0 holds the occupied states (nelectrons, ntraj), 0-based and
  * distinct, the orbitals start as unit vectors on them (iesh.jl:89-97);

@@ -45,8 +45,8 @@ __device__ __forceinline__ void warp_save_popcorr(const FsshParams& p, int isave
 }
 
 // diag(U sigma' U^T), sigma' = Re(sigma) with diagonal replaced by the
-// occupied state (fssh.jl:300-310).
-// Ehrenfest (ehrenfest.jl:79-89): the density matrix itself on the diagonal.
+// occupied state (fssh.jl:132-142).
+// Ehrenfest (ehrenfest.jl:75-83): the density matrix itself on the diagonal.
 template <typename R>
 __device__ __forceinline__ void diabatic_pop2(const Sig2<R>& sg, int s, const R Z[4], double pop[2],
                                               bool ehrenfest = false) {
@@ -62,7 +62,7 @@ __device__ __forceinline__ void diabatic_pop2(const Sig2<R>& sg, int s, const R 
     pop[1] = M10 * U10 + M11 * U11;
 }
 
-// Ehrenfest force weight (ehrenfest.jl:50-69): sum_m sum_n A_nm Re sigma_nm
+// Ehrenfest force weight (ehrenfest.jl:50-68): sum_m sum_n A_nm Re sigma_nm
 // for a symmetric 2x2 A = (A00, A01, A11), in the reference's loop order
 // (m outer, n inner); Re sigma_10 = Re sigma_01 = x.
 template <typename R>
@@ -70,7 +70,7 @@ __device__ __forceinline__ R ehrenfest_weight(R A00, R A01, R A11, const Sig2<R>
     return ((A00 * sg.p + A01 * sg.x) + A01 * sg.x) + A11 * sg.q;
 }
 
-// Ehrenfest potential energy (ehrenfest.jl:92-101): sum_i Re sigma_ii E_i.
+// Ehrenfest potential energy (ehrenfest.jl:85-95): sum_i Re sigma_ii E_i.
 template <typename R>
 __device__ __forceinline__ double ehrenfest_potential(const Sig2<R>& sg, const R w[2]) {
     return (double)sg.p * (double)w[0] + (double)sg.q * (double)w[1];
@@ -78,7 +78,7 @@ __device__ __forceinline__ double ehrenfest_potential(const Sig2<R>& sg, const R
 
 // Initial electronic variables: adiabatic pure state, or a diabatic pure
 // state rotated to the adiabatic basis with the occupied state sampled from
-// its populations (fssh.jl:215-233; density_matrix_dynamics.jl:37-75).
+// its populations (fssh.jl:47-65; density_matrix_dynamics.jl:37-75).
 template <typename R>
 __device__ __forceinline__ void init_electronics2(const FsshParams& p, int64_t i, int64_t gid, const R Z[4],
                                                   Sig2<R>& sg, int& state) {

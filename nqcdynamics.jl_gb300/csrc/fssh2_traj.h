@@ -6,12 +6,12 @@
 // Reference algorithm (NQCDynamics.jl):
 //   BABwithTsit5.perform_step!      src/DynamicsMethods/IntegrationAlgorithms/bab_electronics.jl:61-91
 //   step_B!/step_A!                 src/DynamicsMethods/IntegrationAlgorithms/steps.jl:3-8
-//   DoubleBuffer/update_parameters! src/DynamicsMethods/electronic_dynamics.jl:106-144
-//   DensityMatrixODEProblem f!      src/DynamicsMethods/electronic_dynamics.jl:195-207
+//   DoubleBuffer/update_parameters! src/DynamicsMethods/electronic_dynamics.jl:15-53
+//   DensityMatrixODEProblem f!      src/DynamicsMethods/electronic_dynamics.jl:104-130
 //   commutator!                     src/DynamicsUtils/density_matrix_dynamics.jl:29-33
-//   FSSH acceleration!              src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:235-242
-//   fewest_switches_probability!    src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:264-276
-//   select_new_state                src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:278-289
+//   FSSH acceleration!              src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:67-74
+//   fewest_switches_probability!    src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:86-108
+//   select_new_state                src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:110-121
 //   rescale_velocity!               src/DynamicsMethods/SurfaceHoppingMethods/surface_hopping.jl:64-168
 //
 // Two precisions share the code:
@@ -72,7 +72,7 @@ NQCD_HD Sig2<R> rhs2(R E0, R E1, R D, const Sig2<R>& u) {
 }
 
 // Plain path: interpolation exactly as interpolate_eigenvalues! /
-// interpolate_dynamical_coupling! (electronic_dynamics.jl:146-170).
+// interpolate_dynamical_coupling! (electronic_dynamics.jl:55-79).
 struct Interp64 {
     double E0c, E1c, Dc, dE0, dE1, dD, tc, den;
     NQCD_HD Interp64(const EBuf<double>& b)

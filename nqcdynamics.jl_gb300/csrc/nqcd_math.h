@@ -69,7 +69,7 @@ NQCD_HD u32x4 philox4x32_10(u32x4 ctr, uint32_t k0, uint32_t k1) {
 // block, so one draw per (trajectory, step, stream) costs one block.
 enum RngStream : uint32_t {
     RNG_HOP = 1,        // uniform for the hop test (fssh.jl:112, iesh.jl:393)
-    RNG_INIT_STATE = 2, // uniform for sampling the initial adiabatic state (fssh.jl:222)
+    RNG_INIT_STATE = 2, // uniform for sampling the initial adiabatic state (fssh.jl:54)
     RNG_NOISE = 3,      // Gaussian Wiener increments for MDEF (mdef_baoab.jl:164)
     RNG_INIT_FD = 4,    // Fermi-Dirac occupation sampling (DynamicsUtils.jl:194-208)
     RNG_INIT_POSITION = 5, // device-side initial positions (selections.jl:24-101); counter z = degree of freedom

@@ -1,6 +1,6 @@
 // Model Hamiltonians of the ensemble hot path, restated from their published
 // definitions (the reference takes them from the un-vendored NQCModels
-// package; call sites: src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:236,
+// package; call sites: src/DynamicsMethods/SurfaceHoppingMethods/fssh.jl:67-74,
 // src/DynamicsMethods/ClassicalMethods/mdef.jl:110, iesh.jl:192).
 //
 //  * Tully's models 1-3: J. C. Tully, J. Chem. Phys. 93, 1061 (1990).

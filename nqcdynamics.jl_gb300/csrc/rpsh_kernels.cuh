@@ -4,8 +4,8 @@
 //   BCBwithTsit5.perform_step!   src/DynamicsMethods/IntegrationAlgorithms/bcb_electronics.jl:53-97
 //   step_C! (Cayley free step)   src/DynamicsMethods/IntegrationAlgorithms/steps.jl:10-17
 //   cayley_propagator            src/RingPolymers/ring_polymer.jl:71-82
-//   RPSH rescaling / inversion   src/DynamicsMethods/SurfaceHoppingMethods/rpsh.jl:127-147
-//   hopping with centroid data   SurfaceHoppingMethods.jl:403-425, fssh.jl:254-289
+//   RPSH rescaling / inversion   src/DynamicsMethods/SurfaceHoppingMethods/rpsh.jl:30-50
+//   hopping with centroid data   SurfaceHoppingMethods.jl:81-103, fssh.jl:86-121
 //   TerminatingCallback          src/DynamicsUtils/callbacks.jl:29
 //
 // Uneven ensembles: trajectories carry their own bead count (one of the

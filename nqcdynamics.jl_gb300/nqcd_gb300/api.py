@@ -3,8 +3,8 @@
 Names, argument meanings and error behaviour follow the reference:
 
   Atoms, TullyModelOne/Two/Three, SpinBoson + OhmicSpectralDensity   (NQCModels / NQCBase)
-  Simulation[FSSH](atoms, model; rescaling)       src/simulations.jl:12-44, fssh.jl:206-213
-  Simulation[Ehrenfest](atoms, model)             EhrenfestMethods/ehrenfest.jl:41-43
+  Simulation[FSSH](atoms, model; rescaling)       src/simulations.jl:12-44, fssh.jl:38-45
+  Simulation[Ehrenfest](atoms, model)             EhrenfestMethods/ehrenfest.jl:39-41
   RingPolymerSimulation[FSSH](atoms, model, n_beads; temperature)   simulations.jl:46-73, rpsh.jl:5-7
   Simulation[DiabaticMDEF](atoms, model; friction_method, temperature)   mdef.jl:79-100
   Simulation[AdiabaticIESH](atoms, model; rescaling, estimate_probability)   iesh.jl:72-87

@@ -13,8 +13,8 @@ hopping on a Newns-Anderson (AndersonHolstein) metal:
   select_new_state                      iesh.jl:318-335
   iesh_check_hop! / iesh_execute_hop!   iesh.jl:390-407
   rescale_velocity!                     surface_hopping.jl:64-99
-  sample_fermi_dirac_distribution       src/DynamicsUtils/DynamicsUtils.jl:407-421
-  set_unoccupied_states!                DynamicsUtils.jl:375-384
+  sample_fermi_dirac_distribution       src/DynamicsUtils/DynamicsUtils.jl:194-208
+  set_unoccupied_states!                DynamicsUtils.jl:162-171
 
 Electronic structure as the reference's cache computes it: dense
 eigen-decomposition (LAPACK) with eigenvector signs fixed by continuity with
@@ -129,7 +129,7 @@ def rescale_velocity(v, d, mass, dE, rescaling):
 
 
 def sample_fermi_dirac(energies, ne, beta, seed, traj_ids):
-    """Metropolis occupations: Ne electrons in N states (DynamicsUtils.jl:407-421)."""
+    """Metropolis occupations: Ne electrons in N states (DynamicsUtils.jl:194-208)."""
     n, N = energies.shape
     states = np.tile(np.arange(ne), (n, 1))
     for it in range(N * ne):

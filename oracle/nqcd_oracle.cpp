@@ -143,12 +143,12 @@ inline double adi_elem(const Cache& c, int I, int i, int j) {
     return c.adi[3 * I + 1];
 }
 
-// FSSH acceleration: a_I = -(Z^T dH_I Z)_ss / m_I   (fssh.jl:235-242)
+// FSSH acceleration: a_I = -(Z^T dH_I Z)_ss / m_I   (fssh.jl:67-74)
 void acceleration(const Cache& c, int ndof, const double* mass, int s, double* k) {
     for (int I = 0; I < ndof; ++I) k[I] = -adi_elem(c, I, s, s) / mass[I];
 }
 
-// Ehrenfest acceleration (ehrenfest.jl:50-69): a_I = -sum_m sum_n
+// Ehrenfest acceleration (ehrenfest.jl:50-68): a_I = -sum_m sum_n
 // (Z^T dH_I Z)_nm Re sigma_nm / m_I, the sum in the reference's loop order
 // (m outer, n inner); the models here have no separate state-independent
 // derivative (the spin-boson bath term is on the diagonal of dH_I).
@@ -163,7 +163,7 @@ void acceleration_ehrenfest(const Cache& c, int ndof, const double* mass, const 
     }
 }
 
-// Ehrenfest potential energy (ehrenfest.jl:92-101): sum_i Re sigma_ii E_i.
+// Ehrenfest potential energy (ehrenfest.jl:85-95): sum_i Re sigma_ii E_i.
 double ehrenfest_potential(const Cache& c, const cx sig[NS][NS]) {
     double pe = sig[0][0].re * c.w[0];
     for (int i = 1; i < NS; ++i) pe = pe + sig[i][i].re * c.w[i];
@@ -171,7 +171,7 @@ double ehrenfest_potential(const Cache& c, const cx sig[NS][NS]) {
 }
 
 // ---------------------------------------------------------------------------
-// Electronic density-matrix ODE (electronic_dynamics.jl:106-221)
+// Electronic density-matrix ODE (electronic_dynamics.jl:15-140)
 // ---------------------------------------------------------------------------
 struct ElecParams {
     double E[NS];
@@ -182,7 +182,7 @@ struct DoubleBuffer {
     ElecParams cur, next;
 };
 
-// update_parameters! (electronic_dynamics.jl:129-144)
+// update_parameters! (electronic_dynamics.jl:38-53, 132-140)
 void update_parameters(DoubleBuffer& b, const Cache& c, int ndof, const double* v, double t) {
     std::swap(b.cur, b.next);
     for (int i = 0; i < NS; ++i) b.next.E[i] = c.w[i];
@@ -194,7 +194,7 @@ void update_parameters(DoubleBuffer& b, const Cache& c, int ndof, const double* 
     b.next.t = t;
 }
 
-// f!(du, u, p, t) = -i [A(t), u] with A = diag(E(t)) - i D(t)   (electronic_dynamics.jl:197-207)
+// f!(du, u, p, t) = -i [A(t), u] with A = diag(E(t)) - i D(t)   (electronic_dynamics.jl:106-116)
 void density_rhs(const DoubleBuffer& b, double t, const cx u[NS][NS], cx du[NS][NS]) {
     double s = (t - b.cur.t) / (b.next.t - b.cur.t);
     if (s != s) s = 0.0;
@@ -275,7 +275,7 @@ void electronic_macro_step(const DoubleBuffer& b, double t, double h, double dts
 // ---------------------------------------------------------------------------
 // Surface hopping (surface_hopping.jl, fssh.jl)
 // ---------------------------------------------------------------------------
-int select_new_state(const double* cum, int n, int s, double u) {  // fssh.jl:278-289
+int select_new_state(const double* cum, int n, int s, double u) {  // fssh.jl:110-121
     for (int i = 0; i < n; ++i)
         if (i != s && cum[i] > u) return i;
     return s;
@@ -319,8 +319,8 @@ bool rescale_velocity(const oracle_fssh_args& a, Traj& tr, const double* mass, i
     return true;
 }
 
-// diabatic population of FSSH (fssh.jl:300-310): diag(U sigma' U^T) with the
-// occupied state on the diagonal of sigma'; Ehrenfest (ehrenfest.jl:79-89):
+// diabatic population of FSSH (fssh.jl:132-142): diag(U sigma' U^T) with the
+// occupied state on the diagonal of sigma'; Ehrenfest (ehrenfest.jl:75-83):
 // sigma' = Re sigma.
 void diabatic_population(const Traj& tr, double pop[NS], bool ehrenfest = false) {
     double sp[NS][NS];
@@ -351,7 +351,7 @@ double kinetic_energy(const std::vector<double>& v, const double* mass) {
     return ke / 2.0;
 }
 
-// Initial electronic variables (fssh.jl:215-233, density_matrix_dynamics.jl:37-75)
+// Initial electronic variables (fssh.jl:47-65, density_matrix_dynamics.jl:37-75)
 void init_electronics(const oracle_fssh_args& a, int64_t gid, Traj& tr) {
     if (a.init_kind == 0) return;
     for (int i = 0; i < NS; ++i)
@@ -414,7 +414,7 @@ void run_one_fssh(const oracle_fssh_args& a, const Model& m, int64_t it, oracle_
     tr.cache.Zprev[1] = 0.0;
     tr.cache.Zprev[2] = 0.0;
     tr.cache.Zprev[3] = 1.0;
-    // DensityMatrixODEProblem parameters start zeroed at t = 0 (electronic_dynamics.jl:209-218)
+    // DensityMatrixODEProblem parameters start zeroed at t = 0 (electronic_dynamics.jl:118-127)
     memset(&tr.buf, 0, sizeof(tr.buf));
 
     // initialize!: update_cache!(r); k = a(r, state) or a(r, sigma)   (bab_electronics.jl:48-59)
@@ -468,7 +468,7 @@ void run_one_fssh(const oracle_fssh_args& a, const Model& m, int64_t it, oracle_
             }
             continue;
         }
-        // HoppingCallback (surface_hopping.jl:2-16, fssh.jl:254-289)
+        // HoppingCallback (surface_hopping.jl:2-16, fssh.jl:86-121)
         double prob[NS] = {0.0, 0.0};
         const int s = tr.state;
         double inv_ss = 1.0 / tr.sig[s][s].re;
@@ -542,7 +542,7 @@ struct RPTables {
 };
 
 // Per-bead FSSH force on the active state: -(Z^T dH Z)_ss / m for each bead
-// (fssh.jl:235-242 applied bead-wise).  The eigenvector sign cancels in the
+// (fssh.jl:67-74 applied bead-wise).  The eigenvector sign cancels in the
 // diagonal element, so each bead is diagonalised without phase tracking.
 double bead_accel(const Model& m, double x, int s, double mass, double* w_s) {
     double V[3], D[3], w[2], Z[4];
@@ -653,7 +653,7 @@ void run_one_rpsh(const oracle_fssh_args& a, const Model& m, const RPTables& tb,
         t = nqcd::snap_time(t + h, a.t1);
         step += 1;
 
-        // HoppingCallback with centroid quantities (rpsh.jl, fssh.jl:254-289)
+        // HoppingCallback with centroid quantities (rpsh.jl, fssh.jl:86-121)
         const int s = tr.state;
         double prob[NS] = {0.0, 0.0};
         double inv_ss = 1.0 / tr.sig[s][s].re;
@@ -676,7 +676,7 @@ void run_one_rpsh(const oracle_fssh_args& a, const Model& m, const RPTables& tb,
                 double disc = bb * bb - 4.0 * aa * cc;
                 if (disc < 0.0) {
                     accept = false;
-                    if (a.rescaling == 1) {  // rpsh.jl:136-147
+                    if (a.rescaling == 1) {  // rpsh.jl:39-50
                         double nrm = sqrt(0.0 + d * d);
                         double dn = d / nrm;
                         double vcom = 0.0;
@@ -688,7 +688,7 @@ void run_one_rpsh(const oracle_fssh_args& a, const Model& m, const RPTables& tb,
                 } else {
                     double root = sqrt(disc);
                     double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
-                    double dv = gamma * d / mass;  // rpsh.jl:127-134
+                    double dv = gamma * d / mass;  // rpsh.jl:30-37
                     for (int j = 0; j < nb; ++j) v[j] = v[j] - dv;
                 }
             }

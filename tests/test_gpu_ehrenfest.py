@@ -2,7 +2,7 @@
 
 Simulation{Ehrenfest} runs the FSSH integrator (BABwithTsit5,
 bab_electronics.jl:61-91) with the mean-field force of the step's initial
-density matrix (ehrenfest.jl:50-69) and no hopping.  Plain FP64 path:
+density matrix (ehrenfest.jl:50-68) and no hopping.  Plain FP64 path:
 bit-identical to the CPU oracle (positions, velocities, density matrices,
 energies) for Tully models 1-3 and the spin-boson model, population
 correlation and population-resolved scattering to rounding of the sums.

@@ -413,7 +413,7 @@ def test_ehrenfest_reference_algorithm_comparison():
 @pytest.mark.parametrize("kind,p0,x0,t1", [(1, 20.0, -8.0, 1600.0), (2, 30.0, -8.0, 1100.0)])
 def test_ehrenfest_through_the_coupling_region(kind, p0, x0, t1):
     """Ehrenfest (BAB + Tsit5 electronics, force from the step's initial
-    density matrix, ehrenfest.jl:50-69) through the avoided crossing at
+    density matrix, ehrenfest.jl:50-68) through the avoided crossing at
     dt = 0.1: second-order agreement with the high-accuracy integration."""
     pytest.importorskip("scipy")
     m = 2000.0
