@@ -650,3 +650,34 @@ def test_tsit5_tableau_satisfies_the_order_five_conditions():
     ]
     for k, (got, want) in enumerate(conditions):
         assert got == pytest.approx(want, abs=5e-14), (k, got, want)
+
+
+def test_iesh_force_is_the_gradient_of_the_adiabatic_energy():
+    """Finite-difference consistency of the IESH acceleration (iesh.jl:190-207;
+    rpiesh.jl:20-37 applies the same formula to each bead), as the reference
+    checks acceleration!
+    against FiniteDiff gradients (test/Dynamics/utils.jl:9-62): with
+    dH = dh e0 e0^T the force -(grad U0 + grad h sum_occ z0_k^2) equals
+    -grad(U0 + sum_occ l_k) at positions near the surface, for random
+    occupied sets."""
+    IO = _iesh()
+    from nqcd_gb300 import workload as WL
+
+    wl = WL.newns_anderson_iesh(1, nstates=24, nelectrons=12)
+    P = wl["params"]
+    model = IO.Metal3D(kxy=P["kxy"], A=P["A"], a=P["a"], delta=P["delta"], B=P["B"], b=P["b"], eps=wl["eps"],
+                       V=wl["V"])
+    rng = np.random.default_rng(11)
+
+    def energy(r, occ):
+        w = np.linalg.eigh(model.hamiltonian(r[None]))[0][0]
+        return model.U0(r[None])[0] + w[occ].sum()
+
+    for _ in range(8):
+        r = np.array([rng.normal(0, 0.3), rng.normal(0, 0.3), rng.uniform(1.5, 4.0)])
+        occ = np.sort(rng.choice(24, 12, replace=False))
+        Z = np.linalg.eigh(model.hamiltonian(r[None]))[1][0]
+        force = -(model.grad_U0(r[None])[0] + model.grad_h(r[None])[0] * np.sum(Z[0, occ] ** 2))
+        h = 1e-5
+        fd = np.array([-(energy(r + h * e, occ) - energy(r - h * e, occ)) / (2 * h) for e in np.eye(3)])
+        np.testing.assert_allclose(force, fd, rtol=1e-6, atol=1e-10)
