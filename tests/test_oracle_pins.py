@@ -681,3 +681,116 @@ def test_iesh_force_is_the_gradient_of_the_adiabatic_energy():
         h = 1e-5
         fd = np.array([-(energy(r + h * e, occ) - energy(r - h * e, occ)) / (2 * h) for e in np.eye(3)])
         np.testing.assert_allclose(force, fd, rtol=1e-6, atol=1e-10)
+
+
+def _rpsh_continuous(r0, v0, *, mass, beta, dt, nsteps, seed, traj, substeps=2):
+    """Independent integration of ring-polymer FSSH on Tully model 1: the
+    continuous equations of motion! (rpsh.jl:12-28) integrated by RK4 with
+    `substeps` sub-steps per dt, hop checks at the end of every step with the
+    engine's Philox uniform (fewest_switches_probability!, fssh.jl:86-121,
+    centroid velocity and coupling, SurfaceHoppingMethods.jl:81-103) and
+    centroid momentum rescaling of every bead (surface_hopping.jl:64-99,
+    rpsh.jl:30-50).  Beads feel -d/dx of their own eigenvalue of the occupied
+    state and the springs omega_n^2 (2 x_j - x_j+1 - x_j-1), omega_n =
+    nbeads / beta.  The adiabatic basis is the 2x2 rotation by
+    theta = atan2(V12, V11) / 2, continuous because V12 > 0, with the lower
+    state (sin theta, -cos theta): far left it is the identity, the oracle's
+    starting gauge."""
+    import iesh_oracle as IO
+
+    A, Bp, C, D = TULLY[1]
+    B = len(r0)
+    wn2 = (B / beta) ** 2
+
+    def model(x):
+        e = np.exp(-Bp * np.abs(x))
+        a = np.sign(x) * A * (1.0 - e)
+        da = A * Bp * e
+        c = C * np.exp(-D * x * x)
+        dc = -2.0 * D * x * c
+        return a, c, da, dc
+
+    def centroid(x, v):
+        a, c, da, dc = model(np.mean(x))
+        rho = np.hypot(a, c)
+        th = 0.5 * np.arctan2(c, a)
+        z0 = np.array([np.sin(th), -np.cos(th)])
+        z1 = np.array([np.cos(th), np.sin(th)])
+        Dm = np.array([[da, dc], [dc, -da]])
+        d01 = (z0 @ Dm @ z1) / (2.0 * rho)  # (Z^T dH Z)_01 / (w1 - w0)
+        return np.array([-rho, rho]), d01, np.mean(v)
+
+    def rhs(x, v, sig, s):
+        a, c, da, dc = model(x)
+        dw = (a * da + c * dc) / np.hypot(a, c)  # d/dx of the upper eigenvalue; the lower is -dw
+        acc = (dw if s == 0 else -dw) / mass - wn2 * (2 * x - np.roll(x, 1) - np.roll(x, -1))
+        w, d01, vc = centroid(x, v)
+        Vm = np.array([[w[0], -1j * vc * d01], [1j * vc * d01, w[1]]])  # diag(w) - i v d, d10 = -d01
+        return v, acc, -1j * (Vm @ sig - sig @ Vm)
+
+    x, v = np.array(r0, float), np.array(v0, float)
+    sig = np.array([[1.0, 0.0], [0.0, 0.0]], complex)
+    s, hops = 0, []
+    h = dt / substeps
+    for step in range(1, nsteps + 1):
+        for _ in range(substeps):
+            k1 = rhs(x, v, sig, s)
+            k2 = rhs(x + h / 2 * k1[0], v + h / 2 * k1[1], sig + h / 2 * k1[2], s)
+            k3 = rhs(x + h / 2 * k2[0], v + h / 2 * k2[1], sig + h / 2 * k2[2], s)
+            k4 = rhs(x + h * k3[0], v + h * k3[1], sig + h * k3[2], s)
+            x = x + h / 6 * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0])
+            v = v + h / 6 * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1])
+            sig = sig + h / 6 * (k1[2] + 2 * k2[2] + 2 * k3[2] + k4[2])
+        w, d01, vc = centroid(x, v)
+        m = 1 - s
+        dsm = d01 if s == 0 else -d01
+        p = min(max(2.0 * vc * (sig[m, s] / sig[s, s]).real * dsm * dt, 0.0), 1.0)
+        wh = IO.uniform(seed, np.array([traj], np.uint64), step, IO.RNG_HOP)
+        u = IO.u53(wh[0], wh[1])[0]
+        if u < p:
+            d = -dsm  # d[new, old]
+            aa, bb, cc = 0.5 * d * d / mass, d * vc, w[m] - w[s]
+            disc = bb * bb - 4 * aa * cc
+            if disc >= 0:
+                root = np.sqrt(disc)
+                gam = (bb + root) / (2 * aa) if bb < 0 else (bb - root) / (2 * aa)
+                v = v - gam * d / mass
+                hops.append((step, s, m))
+                s = m
+    return x, v, sig, s, hops
+
+
+def test_rpsh_oracle_matches_a_continuous_integration():
+    """The reference's BCBwithTsit5 test (test/Dynamics/bcbwithtsit5.jl:24-36):
+    ring-polymer FSSH on Tully 1 with 10 beads at T = 1e-3, p = 20, beads at
+    -5 + N(0, 1), the same random stream for both integrations, agreement to
+    rtol 1e-3.  Here the oracle's BCBwithTsit5 restatement is compared with an
+    independent fine-step integration of the continuous equations."""
+    import ctypes
+
+    # the restated Tully 1 equals the oracle's model
+    for xx in (-3.0, -0.4, 0.0, 0.7, 2.5):
+        V, Dd = _tully_vd(1, xx)
+        A, Bp, C, D = TULLY[1]
+        e = np.exp(-Bp * abs(xx))
+        np.testing.assert_allclose([V[0, 0], V[0, 1], Dd[0, 0], Dd[0, 1]],
+                                   [np.sign(xx) * A * (1 - e), C * np.exp(-D * xx * xx), A * Bp * e,
+                                    -2 * D * xx * C * np.exp(-D * xx * xx)], rtol=1e-12, atol=1e-15)
+    B, n, mass, beta, dt, nsteps, seed = 10, 4, 2000.0, 1000.0, 0.1, 10000, 1
+    rng = np.random.default_rng(1)
+    r0 = -5.0 + rng.standard_normal((n, B))
+    v0 = np.full((n, B), 20.0 / mass)
+    o = O.run_rpsh(model=1, params=TULLY[1], mass=mass, r0=r0, v0=v0, nbeads=np.full(n, B, np.int32), beta=beta,
+                   t0=0.0, t1=nsteps * dt, dt=dt, seed=seed)
+    nhop = 0
+    for t in range(n):
+        x, v, sig, s, hops = _rpsh_continuous(r0[t], v0[t], mass=mass, beta=beta, dt=dt, nsteps=nsteps, seed=seed,
+                                               traj=t)
+        log = [tuple(h) for h in o["hop_log"][t] if h[0] >= 0]
+        assert log == hops, (t, log, hops)
+        nhop += len(hops)
+        assert o["state"][t] == s
+        np.testing.assert_allclose(o["r"][t], x, rtol=1e-3)
+        np.testing.assert_allclose(o["v"][t], v, rtol=1e-3)
+        np.testing.assert_allclose(o["sigma"][t], sig, atol=1e-3)
+    assert nhop > 0  # the comparison covers hops
