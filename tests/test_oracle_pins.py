@@ -259,14 +259,14 @@ def _iesh():
 
 
 def test_iesh_unoccupied_known_answers():
-    # iesh.jl:71-78 (1-based there): occupied 1:15 -> 16:31, occupied 6:20 -> 1:5, 21:31
+    # test/Dynamics/iesh.jl:66-80 (1-based there): occupied 1:15 -> 16:31, occupied 6:20 -> 1:5, 21:31
     IO = _iesh()
     assert IO.unoccupied(list(range(15)), 31) == list(range(15, 31))
     assert IO.unoccupied(list(range(5, 20)), 31) == list(range(5)) + list(range(20, 31))
 
 
 def test_iesh_overlap_and_akj_known_answers():
-    # iesh.jl:87-110: overlap of the initial orbitals is the identity; with every
+    # test/Dynamics/iesh.jl:87-109: overlap of the initial orbitals is the identity; with every
     # electron in state 1 only the first column is ones; A_kj(state, state) = 1
     IO = _iesh()
     n, ne = 31, 15
@@ -279,7 +279,7 @@ def test_iesh_overlap_and_akj_known_answers():
 
 
 def _narrow_band_model(IO, M=30):
-    # the band of iesh.jl:17-25: Gamma = 6.4e-3, W = 3 Gamma, TrapezoidalRule(M, -W, W)
+    # the band of test/Dynamics/iesh.jl:17-25: Gamma = 6.4e-3, W = 3 Gamma, TrapezoidalRule(M, -W, W)
     G = 6.4e-3
     W = 3 * G
     eps = np.linspace(-W, W, M)
@@ -288,7 +288,7 @@ def _narrow_band_model(IO, M=30):
 
 
 def test_iesh_fermi_dirac_zero_temperature_fills_lowest_states():
-    # iesh.jl:39-44: at 0 K the sampled occupations are the lowest nelectrons states
+    # test/Dynamics/iesh.jl:39-44: at 0 K the sampled occupations are the lowest nelectrons states
     IO = _iesh()
     model = _narrow_band_model(IO)
     n = 16
@@ -299,7 +299,7 @@ def test_iesh_fermi_dirac_zero_temperature_fills_lowest_states():
 
 
 def test_iesh_fermi_dirac_statistics():
-    # iesh.jl:51-69: sample averages of the occupations match the Fermi function
+    # test/Dynamics/iesh.jl:44-64: sample averages of the occupations match the Fermi function
     # (isapprox on vectors: norm of the difference within 0.2 of the norm)
     IO = _iesh()
     model = _narrow_band_model(IO)
@@ -324,7 +324,7 @@ def test_iesh_fermi_dirac_statistics():
 
 
 def test_iesh_hop_rescaling_conserves_energy():
-    # iesh.jl:122-152: after a successful hop dKE = -dE (rtol 1e-3)
+    # test/Dynamics/iesh.jl:122-152: after a successful hop dKE = -dE (rtol 1e-3)
     IO = _iesh()
     rng = np.random.default_rng(4)
     mass = np.array([2000.0, 2000.0, 2000.0])
