@@ -766,8 +766,6 @@ def test_rpsh_oracle_matches_a_continuous_integration():
     -5 + N(0, 1), the same random stream for both integrations, agreement to
     rtol 1e-3.  Here the oracle's BCBwithTsit5 restatement is compared with an
     independent fine-step integration of the continuous equations."""
-    import ctypes
-
     # the restated Tully 1 equals the oracle's model
     for xx in (-3.0, -0.4, 0.0, 0.7, 2.5):
         V, Dd = _tully_vd(1, xx)
