@@ -248,3 +248,74 @@ def test_ring_polymer_iesh_maps_to_the_abi():
     with pytest.raises(NotImplementedError):
         N.run_dynamics(sim, (0.0, 1.0), dist, output=N.OutputFinal, trajectories=2,
                        ensemble_algorithm=N.EnsembleGB300("fp64"), dt=0.1)
+
+
+def _mdef_cfg(**kw):
+    wl = workload.newns_anderson_mdef(4, M=40)
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON, L.PREC_FP64
+    cfg.ndofs, cfg.natoms, cfg.nstates = 1, 1, 41
+    params = np.array([wl["k"], wl["g"], wl["delta"], wl["mu"], wl["sigma"]])
+    masses = np.array([wl["mass"]])
+    eps, V = np.ascontiguousarray(wl["eps"]), np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 5, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta, cfg.ntraj_max = wl["beta"], 4
+    keep = [params, masses, eps, V]
+    for k, v in kw.items():
+        if k in ("eps", "V"):  # replace a bath array
+            arr = np.ascontiguousarray(v, dtype=np.float64)
+            keep.append(arr)
+            setattr(cfg, "bath_a" if k == "eps" else "bath_b", L.dptr(arr))
+        else:
+            setattr(cfg, k, v)
+    return cfg, keep
+
+
+@pytest.mark.parametrize("which,field,value,code", [
+    ("iesh", "nelectrons", 0, -1), ("iesh", "nelectrons", 20, -1), ("iesh", "nstates", 30, -1),
+    ("iesh", "precision", L.PREC_FP32_KAHAN, -6), ("iesh", "init_kind", L.INIT_ADIABATIC_PURE, -1),
+    ("iesh", "decoherence_C", -1.0, -1), ("iesh", "ndofs", 1, -6), ("iesh", "nparams", 5, -1),
+    ("mdef", "beta", 0.0, -1), ("mdef", "nbeads_max", 33, -1), ("mdef", "save_stride", 4, None),
+    ("mdef", "nbath", 0, -1), ("mdef", "eps", "descending", -1), ("mdef", "V", "zero", -1),
+    ("mdef", "decoherence_C", 0.1, -6), ("mdef", "ndofs", 3, -6),
+])
+def test_create_validates_metal_models(which, field, value, code):
+    # IESH (nqcd_create's IESH block) and MDEF (its MDEF block): every rejection happens before
+    # any device work, so on a machine without a GPU an accepted config reports NQCD_ERR_CUDA
+    if which == "iesh":
+        cfg, keep = _rpiesh_cfg(nbeads_max=0, **{field: value})
+    else:
+        if value == "descending":
+            value = np.linspace(0.5, -0.5, 40)
+        elif value == "zero":
+            value = np.zeros(40)
+        cfg, keep = _mdef_cfg(**{field: value})
+    if which == "mdef" and field == "save_stride":
+        cfg.nbeads_max = 4  # ring-polymer MDEF reports final states only
+        code = -6
+    lib = L.load()
+    h = C.c_void_p()
+    rc = lib.nqcd_create(C.byref(cfg), C.byref(h))
+    assert rc == code, (which, field, rc, lib.nqcd_last_error(None))
+    assert not h.value
+
+
+@pytest.mark.parametrize("make", ["mdef", "mdef_rp", "iesh", "iesh_rp"])
+def test_valid_metal_configs_pass_validation(make):
+    # the unmodified configurations of the validation tests above are accepted: they reach the
+    # device (NQCD_ERR_CUDA without a GPU, a handle with one)
+    import torch
+
+    if make.startswith("mdef"):
+        cfg, keep = _mdef_cfg(nbeads_max=4 if make == "mdef_rp" else 0)
+    else:
+        cfg, keep = _rpiesh_cfg(nbeads_max=8 if make == "iesh_rp" else 0)
+    lib = L.load()
+    h = C.c_void_p()
+    rc = lib.nqcd_create(C.byref(cfg), C.byref(h))
+    if torch.cuda.is_available():
+        assert rc == 0
+        lib.nqcd_destroy(h)
+    else:
+        assert rc == -2 and b"no CUDA device" in lib.nqcd_last_error(None), lib.nqcd_last_error(None)
