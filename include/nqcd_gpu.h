@@ -325,10 +325,13 @@ int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
  *            [ntraj] out or NULL
  *  stream: cudaStream_t (NULL = default stream); the call only enqueues.
  * Returns NQCD_ERR_ARG (message in errbuf, if given) when nmodes * ntraj >
- * NQCD_NOALLOC_SCRATCH_DOUBLES.  The first call on a device looks up the
- * scratch array's device address (cudaGetSymbolAddress) and caches it: make
- * that first call before any stream capture.  All calls share the scratch
- * array, so calls whose kernels overlap on the GPU race. */
+ * NQCD_NOALLOC_SCRATCH_DOUBLES, when t0, t1 or dt is not finite, t1 < t0,
+ * dt <= 0, the run needs 2^31 - 2 steps or more, or dt is too small to advance
+ * the clock.  Every call looks up the scratch array's device address in the
+ * current context (cudaGetSymbolAddress, which allocates nothing); the first
+ * call in a context may also load the library's device code, so make that
+ * first call before any stream capture.  All calls share the scratch array,
+ * so calls whose kernels overlap on the GPU race. */
 #define NQCD_NOALLOC_SCRATCH_DOUBLES 1048576
 int nqcd_fssh_spinboson_fp64_noalloc(int64_t ntraj, int32_t nmodes, const double* d_bath_c,
                                      const double* d_bath_omega2, const double* d_mass, double eps, double delta,

@@ -21,49 +21,51 @@
 #include <stdio.h>
 #include <string.h>
 
-#include <mutex>
-
 #include "../../include/nqcd_gpu.h"
 #include "engine_params.h"
+#include "nqcd_math.h"
 #include "nqcd_models.h"
 
 namespace {
 
 __device__ __align__(256) double g_noalloc_scratch[NQCD_NOALLOC_SCRATCH_DOUBLES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-double* g_scratch_addr[kMaxDevices] = {nullptr};
-
 int noalloc_fail(char* errbuf, int32_t len, int code, const char* msg, const char* detail = "") {
     if (errbuf && len > 0) snprintf(errbuf, (size_t)len, "nqcd_fssh_spinboson_fp64_noalloc: %s%s", msg, detail);
     return code;
 }
 
-// Device address of g_noalloc_scratch on the current device.  In host code
+// Device address of g_noalloc_scratch in the current context.  In host code
 // the symbol's name is only a host-side stand-in, so the device address is
-// looked up with cudaGetSymbolAddress once per device, with that device
-// current, and cached.
+// looked up with cudaGetSymbolAddress, with the caller's device current.  It
+// is looked up on every call (the lookup allocates nothing): after a device
+// reset, or in another context on the same device, the module loads at a new
+// address, so a cached address could go stale.
 int scratch_address(double** out, char* errbuf, int32_t len) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
         cudaGetLastError();
-        return noalloc_fail(errbuf, len, NQCD_ERR_CUDA, "cudaGetDevice: ", cudaGetErrorString(e));
+        return noalloc_fail(errbuf, len, NQCD_ERR_CUDA, "cudaGetSymbolAddress: ", cudaGetErrorString(e));
     }
-    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(errbuf, len, NQCD_ERR_UNSUPPORTED, "device ordinal >= 64");
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return noalloc_fail(errbuf, len, NQCD_ERR_CUDA, "cudaGetSymbolAddress: ", cudaGetErrorString(e));
-        }
-        g_scratch_addr[dev] = static_cast<double*>(p);
-    }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<double*>(p);
     return NQCD_OK;
+}
+
+// Number of nuclear steps the kernel takes from t0 to t1 (its clock: whole
+// steps of dt, a shortened last step, a time within 100 ulp of t1 snapped to
+// t1), or -1 once it exceeds max_steps.  A dt below the spacing of doubles
+// near t never advances the clock; the cap turns that into a rejection
+// instead of a kernel that never ends.
+int64_t bounded_step_count(double t0, double t1, double dt, int64_t max_steps) {
+    int64_t n = 0;
+    double t = t0;
+    while (t < t1) {
+        if (++n > max_steps) return -1;
+        double h = (t1 - t) < dt ? (t1 - t) : dt;
+        t = nqcd::snap_time(t + h, t1);
+    }
+    return n;
 }
 
 }  // namespace
@@ -86,8 +88,15 @@ extern "C" int nqcd_fssh_spinboson_fp64_noalloc(int64_t ntraj, int32_t nmodes, c
         return noalloc_fail(errbuf, errbuf_len, NQCD_ERR_ARG, "null device buffer");
     if (rescaling < 0 || rescaling > 2 || diabatic_state < 0 || diabatic_state > 1)
         return noalloc_fail(errbuf, errbuf_len, NQCD_ERR_ARG, "rescaling must be 0..2 and diabatic_state 0..1");
-    if (!(dt > 0.0) || !(t1 >= t0))
-        return noalloc_fail(errbuf, errbuf_len, NQCD_ERR_ARG, "need dt > 0 and t0 <= t1");
+    if (!(dt > 0.0) || !(t1 >= t0) || !isfinite(t0) || !isfinite(t1))
+        return noalloc_fail(errbuf, errbuf_len, NQCD_ERR_ARG, "need dt > 0 and finite t0 <= t1");
+    // the kernel counts steps in 32-bit integers; the span bounds the count
+    // before the clock is stepped through on the host
+    if (!((t1 - t0) / dt < 2147483646.0))
+        return noalloc_fail(errbuf, errbuf_len, NQCD_ERR_ARG, "more than 2^31 - 2 steps");
+    if (bounded_step_count(t0, t1, dt, (int64_t)((t1 - t0) / dt) + 2) < 0)
+        return noalloc_fail(errbuf, errbuf_len, NQCD_ERR_ARG,
+                            "dt is below the spacing of doubles between t0 and t1, so the clock would not advance");
 
     double* scratch = nullptr;
     int rc = scratch_address(&scratch, errbuf, errbuf_len);

@@ -331,10 +331,15 @@ int ensure_stage(nqcd_handle* h, int64_t n) {
     return NQCD_OK;
 }
 
+// Steps of the reference's clock from t0 to t1 (whole steps of dt, a
+// shortened last step, a time within 100 ulp of t1 snapped to t1).  The count
+// stops at (t1 - t0) / dt + 2, which only a clock that no longer advances (dt
+// below the spacing of doubles near t) reaches; the caller rejects it.
 int64_t count_steps(double t0, double t1, double dt) {
     int64_t n = 0;
     double t = t0;
-    while (t < t1 && n < (int64_t)1 << 40) {
+    const int64_t cap = (int64_t)((t1 - t0) / dt) + 2;
+    while (t < t1 && n <= cap) {
         double hh = (t1 - t) < dt ? (t1 - t) : dt;
         t = snap_time(t + hh, t1);
         ++n;
@@ -869,10 +874,10 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     // FSSH and RPSH step like the reference's integrator (a last partial step
     // up to t1); MDEF and IESH take whole steps of dt only
     const double span = (t1 - t0) / dt;
-    if ((mdef || iesh) && !(span < 2147483647.0))
-        return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
+    if (!(span < 2147483645.0)) return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
     const int64_t nsteps = (mdef || iesh) ? (int64_t)llround(span) : count_steps(t0, t1, dt);
-    if (nsteps > 0x7fffffff) return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
+    if (nsteps > (int64_t)span + 2)
+        return fail(h, NQCD_ERR_ARG, "nqcd_run: dt is below the spacing of doubles between t0 and t1");
     const int stride = h->cfg.save_stride;
     const int nsave = stride > 0 ? (int)(nsteps / stride + 1) : 0;
     if ((mdef || iesh) && fabs((double)nsteps * dt - (t1 - t0)) > 1e-9 * (fabs(t1 - t0) + dt))

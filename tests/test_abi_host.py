@@ -87,6 +87,55 @@ def test_null_arguments():
     lib.nqcd_destroy(None)  # no-op
 
 
+def _noalloc(lib):
+    f = lib.nqcd_fssh_spinboson_fp64_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int32,
+                  C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_void_p, C.c_char_p, C.c_int32]
+    return f
+
+
+_NOALLOC_OK = dict(ntraj=100, nmodes=100, c=8, w2=8, m=8, rescaling=0, state=0, r=8, v=8, sig=8, st=8,
+                   t0=0.0, t1=20.0, dt=0.05)
+
+
+@pytest.mark.parametrize("change,message", [
+    (dict(ntraj=0), b"must be positive"),
+    (dict(nmodes=0), b"must be positive"),
+    (dict(ntraj=1048576 // 100 + 1), b"exceeds the fixed scratch"),
+    (dict(c=None), b"null device buffer"),
+    (dict(w2=None), b"null device buffer"),
+    (dict(m=None), b"null device buffer"),
+    (dict(r=None), b"null device buffer"),
+    (dict(v=None), b"null device buffer"),
+    (dict(sig=None), b"null device buffer"),
+    (dict(st=None), b"null device buffer"),
+    (dict(rescaling=3), b"rescaling must be"),
+    (dict(rescaling=-1), b"rescaling must be"),
+    (dict(state=2), b"diabatic_state"),
+    (dict(dt=0.0), b"finite t0 <= t1"),
+    (dict(dt=float("nan")), b"finite t0 <= t1"),
+    (dict(t1=-1.0), b"finite t0 <= t1"),
+    (dict(t1=float("inf")), b"finite t0 <= t1"),
+    (dict(t0=float("-inf")), b"finite t0 <= t1"),
+    (dict(t0=float("nan")), b"finite t0 <= t1"),
+    (dict(t1=1.0, dt=1e-300), b"more than 2^31"),
+    # a span of 1e4 steps whose clock never moves: 1000 is below half the spacing of doubles at 1e20
+    (dict(t0=1e20, t1=1e20 + 1e7, dt=1000.0), b"clock would not advance"),
+])
+def test_noalloc_rejects_arguments_before_device_work(change, message):
+    """Each rejection of the allocation-free entry point answers NQCD_ERR_ARG
+    before any device work: the dummy device pointers are never touched."""
+    a = dict(_NOALLOC_OK, **change)
+    err = C.create_string_buffer(256)
+    rc = _noalloc(L.load())(a["ntraj"], a["nmodes"], a["c"], a["w2"], a["m"], 0.0, 1.0, a["rescaling"], a["state"],
+                            a["r"], a["v"], a["sig"], a["st"], None, None, None, a["t0"], a["t1"], a["dt"], 1, None,
+                            err, 256)
+    assert rc == -1, (change, rc, err.value)
+    assert message in err.value, err.value
+
+
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(L.EngineUnavailable):
         L.load(tmp_path / "absent.so")

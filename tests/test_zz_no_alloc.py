@@ -92,12 +92,3 @@ def test_noalloc_matches_handle_api_twice():
         for key in ("r", "v", "sig_re", "sig_im", "state", "nhops", "nfrustrated", "nsteps"):
             np.testing.assert_array_equal(b[key], a[key], err_msg=key)
 
-
-def test_noalloc_rejects_oversize_ensembles():
-    fn = _bind(L.load())
-    err = C.create_string_buffer(256)
-    # nmodes * ntraj one past the fixed scratch: rejected before any device work (the pointers are never used)
-    ntraj = 1048576 // NMODES + 1
-    rc = fn(ntraj, NMODES, 8, 8, 8, 0.0, 1.0, 0, 0, 8, 8, 8, 8, None, None, None, 0.0, 1.0, 0.05, 1, None, err, 256)
-    assert rc == -1
-    assert b"exceeds the fixed scratch" in err.value
