@@ -309,9 +309,10 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         step += 1;
 
         // hop test
+        // real(sigma[m, s] / sigma[s, s]) by Julia's complex division; the
+        // imaginary part of sigma[s, s] is exactly zero for two states
         const int s = state;
-        R inv = R(1) / (s == 0 ? sg.p : sg.q);
-        R re = sg.x * inv;
+        R re = cdiv_real(sg.x, s == 0 ? -sg.y : sg.y, s == 0 ? sg.p : sg.q, 0.0);
         R nsm = s == 0 ? nac : -nac;
         R prob = clamp01<R>(R(0) + R(2) * (R)v * re * nsm * dtR);
         double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
@@ -646,9 +647,10 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
         step += 1;
 
         // hop test
+        // real(sigma[m, s] / sigma[s, s]) by Julia's complex division; the
+        // imaginary part of sigma[s, s] is exactly zero for two states
         const int s = state;
-        R inv = R(1) / (s == 0 ? sg.p : sg.q);
-        R re = sg.x * inv;
+        R re = cdiv_real(sg.x, s == 0 ? -sg.y : sg.y, s == 0 ? sg.p : sg.q, 0.0);
         R prob;
         {
             double acc = 0.0;

@@ -158,6 +158,58 @@ struct Tsit5 {
     static constexpr double a76 = 2.324710524099774;
 };
 
+// ---------------------------------------------------------------------------
+// Real part of the complex quotient (a + ib) / (c + id), rounded as Julia's
+// `/` for Complex{Float64} rounds it.  That operator is the robust complex
+// division of Baudin and Smith ("A Robust Complex Division in Scilab",
+// arXiv:1210.4539, 2012), restated here from the paper:
+//   1. scale (a, b) and (c, d) by powers of two when the larger magnitude of
+//      a pair is at or above half the largest double, or at or below
+//      2 * (smallest normal) / eps; the scale factor s undoes it at the end;
+//   2. pivot on the larger of |c|, |d|: r = d/c, t = 1/(c + d r) when
+//      |d| <= |c|, else the roles of (a, b) and (c, d) are swapped;
+//   3. the real part is (a + b r) t, with b r split as a t + (b t) r when it
+//      underflows to zero, and (a + d (b/c)) t when r itself is zero.
+// The reference's fewest-switches probability uses it as
+// real(sigma[m, s] / sigma[s, s]) (fssh.jl:96-108).  With d = 0 (the
+// diagonal of a two-state density matrix, whose imaginary part stays exactly
+// zero) it reduces to a * (1/c) for normal operands.
+// ---------------------------------------------------------------------------
+NQCD_HD double cdiv_real_part(double A, double B, double C, double D, double r, double t) {
+    if (r != 0.0) {
+        double br = B * r;
+        return br != 0.0 ? (A + br) * t : A * t + (B * t) * r;
+    }
+    return (A + D * (B / C)) * t;
+}
+
+NQCD_HD double cdiv_real(double a, double b, double c, double d) {
+    const double halfov = 0x1.fffffffffffffp+1022;  // largest double / 2
+    const double twoun = 0x1p-969;                  // 2 * smallest normal / eps
+    const double bs = 0x1p+105;                     // 2 / eps^2
+    double absa = fabs(a), absb = fabs(b), absc = fabs(c), absd = fabs(d);
+    double ab = absa >= absb ? absa : absb;
+    double cd = absc >= absd ? absc : absd;
+    double s = 1.0;
+    if (ab >= halfov || ab <= twoun || cd >= halfov || cd <= twoun) {
+        if (ab >= halfov) { a = 0.5 * a; b = 0.5 * b; s = 2.0; }
+        if (cd >= halfov) { c = 0.5 * c; d = 0.5 * d; s = s * 0.5; }
+        if (ab <= twoun) { a = a * bs; b = b * bs; s = s / bs; }
+        if (cd <= twoun) { c = c * bs; d = d * bs; s = s * bs; }
+    }
+    double re;
+    if (fabs(d) <= fabs(c)) {
+        double r = d / c;
+        double t = 1.0 / (c + d * r);
+        re = cdiv_real_part(a, b, c, d, r, t);
+    } else {
+        double r = c / d;
+        double t = 1.0 / (d + c * r);
+        re = cdiv_real_part(b, a, d, c, r, t);
+    }
+    return re * s;
+}
+
 // Time snapping used by the reference's ODE integrator after each step:
 // a time within 100 eps of the stop time is set to the stop time.
 NQCD_HD double snap_time(double t, double tstop) {

@@ -299,8 +299,8 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
         step += 1;
 
         const int s = state;
-        double inv = 1.0 / (s == 0 ? sg.p : sg.q);
-        double re = sg.x * inv;
+        // real(sigma[m, s] / sigma[s, s]) by Julia's complex division
+        double re = cdiv_real(sg.x, s == 0 ? -sg.y : sg.y, s == 0 ? sg.p : sg.q, 0.0);
         double nsm = s == 0 ? nac : -nac;
         double prob = clamp01<double>(0.0 + 2.0 * vc * re * nsm * p.dt);
         double u = rng_uniform(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);

@@ -471,10 +471,10 @@ void run_one_fssh(const oracle_fssh_args& a, const Model& m, int64_t it, oracle_
         // HoppingCallback (surface_hopping.jl:2-16, fssh.jl:86-121)
         double prob[NS] = {0.0, 0.0};
         const int s = tr.state;
-        double inv_ss = 1.0 / tr.sig[s][s].re;
         for (int mm = 0; mm < NS; ++mm) {
             if (mm == s) continue;
-            double re = tr.sig[mm][s].re * inv_ss;
+            // real(sigma[m, s] / sigma[s, s]): Julia's Complex{Float64} division (fssh.jl:101)
+            double re = nqcd::cdiv_real(tr.sig[mm][s].re, tr.sig[mm][s].im, tr.sig[s][s].re, tr.sig[s][s].im);
             for (int I = 0; I < ndof; ++I)
                 prob[mm] = prob[mm] + 2.0 * tr.v[I] * re * nac_elem(tr.cache, I, s, mm) * a.dt;
         }
@@ -656,10 +656,10 @@ void run_one_rpsh(const oracle_fssh_args& a, const Model& m, const RPTables& tb,
         // HoppingCallback with centroid quantities (rpsh.jl, fssh.jl:86-121)
         const int s = tr.state;
         double prob[NS] = {0.0, 0.0};
-        double inv_ss = 1.0 / tr.sig[s][s].re;
         for (int mm = 0; mm < NS; ++mm) {
             if (mm == s) continue;
-            double re = tr.sig[mm][s].re * inv_ss;
+            // real(sigma[m, s] / sigma[s, s]): Julia's Complex{Float64} division (fssh.jl:101)
+            double re = nqcd::cdiv_real(tr.sig[mm][s].re, tr.sig[mm][s].im, tr.sig[s][s].re, tr.sig[s][s].im);
             prob[mm] = prob[mm] + 2.0 * vc * re * nac_elem(tr.cache, 0, s, mm) * a.dt;
         }
         for (int i = 0; i < NS; ++i) prob[i] = std::min(std::max(prob[i], 0.0), 1.0);
@@ -795,6 +795,8 @@ extern "C" void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint
 }
 
 extern "C" double oracle_exp(double x) { return nqcd::nqcd_exp(x); }
+
+extern "C" double oracle_cdiv_real(double a, double b, double c, double d) { return nqcd::cdiv_real(a, b, c, d); }
 
 extern "C" double oracle_uniform(uint64_t seed, uint64_t traj, uint32_t step, uint32_t stream) {
     return nqcd::rng_uniform(seed, traj, step, stream);

@@ -76,6 +76,8 @@ def lib() -> C.CDLL:
         L.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.oracle_exp.restype = C.c_double
         L.oracle_exp.argtypes = [C.c_double]
+        L.oracle_cdiv_real.restype = C.c_double
+        L.oracle_cdiv_real.argtypes = [C.c_double] * 4
         L.oracle_uniform.restype = C.c_double
         L.oracle_uniform.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32]
         L.oracle_tully.argtypes = [C.c_int32, DP, C.c_double, DP, DP]
@@ -93,6 +95,11 @@ def _d(a):
 
 def _i(a):
     return None if a is None else a.ctypes.data_as(IP)
+
+
+def cdiv_real(a: float, b: float, c: float, d: float) -> float:
+    """real((a + ib) / (c + id)) by the restated Julia Complex{Float64} division."""
+    return lib().oracle_cdiv_real(a, b, c, d)
 
 
 def philox(ctr, key):

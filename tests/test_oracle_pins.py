@@ -175,6 +175,65 @@ def test_density_matrix_stays_hermitian_and_normalised():
     np.testing.assert_allclose(np.trace(s, axis1=1, axis2=2).real, 1.0, atol=1e-8)
 
 
+def _exact_real_quotient(a, b, c, d):
+    from fractions import Fraction as F
+
+    a, b, c, d = map(F, (a, b, c, d))
+    return (a * c + b * d) / (c * c + d * d)
+
+
+def test_complex_division_follows_the_robust_algorithm():
+    """real(z / w) as Julia divides Complex{Float64} (Baudin and Smith 2012):
+    within a few roundings of the exact quotient for ordinary operands, exactly
+    a * (1 / c) for a real denominator, and finite where the textbook formula
+    (a c + b d) / (c^2 + d^2) overflows or underflows."""
+    rng = np.random.default_rng(5)
+    for _ in range(2000):
+        a, b, c, d = rng.standard_normal(4) * 10.0 ** rng.integers(-5, 5, 4)
+        got = O.cdiv_real(a, b, c, d)
+        ex = float(_exact_real_quotient(a, b, c, d))
+        # a few roundings of the summands a c and b d (their sum may cancel)
+        scale = (abs(a * c) + abs(b * d)) / (c * c + d * d)
+        assert abs(got - ex) <= 4 * np.spacing(scale), (a, b, c, d, got, ex)
+    for a, b, c in [(0.3, -0.2, 0.7), (-1e-3, 5e-4, 0.999), (0.5, 0.0, 0.5), (0.0, 0.4, 0.6)]:
+        assert O.cdiv_real(a, b, c, 0.0) == a * (1.0 / c)
+    # pairs near the overflow and underflow thresholds, where the scaling steps act
+    for a, b, c, d in [(1e308, 1e308, 1e308, 1e308), (1e-310, 3e-311, 2e-310, -1e-310), (1.0, 1.0, 1e300, 1e-300),
+                       (1e-300, 1e-300, 1e-300, 1e-300), (2.0 ** -1000, 1.0, 2.0 ** -1000, 2.0 ** 1000)]:
+        got = O.cdiv_real(a, b, c, d)
+        ex = float(_exact_real_quotient(a, b, c, d))
+        assert math.isfinite(got)
+        assert abs(got - ex) <= 4 * np.spacing(abs(ex)) + 2 ** -1074, (a, b, c, d, got, ex)
+
+
+def test_two_state_density_matrix_diagonal_stays_exactly_real():
+    """The oracle carries the full complex 2x2 density matrix through the
+    reference's commutator (electronic_dynamics.jl:106-116,
+    density_matrix_dynamics.jl:29-33).  Its diagonal stays exactly real: the
+    real part of [A, sigma]_ss is (E_s p - D y) - (p E_s - y D), zero in
+    floating point.  So real(sigma[m, s] / sigma[s, s]) divides by an exactly
+    real sigma[s, s], and the kernels, which carry the diagonal as real
+    numbers, divide by (p, 0)."""
+    n = 48
+    rng = np.random.default_rng(9)
+    for kind in (1, 2, 3):
+        r0 = np.full((n, 1), -10.0)
+        v0 = rng.uniform(8.0, 30.0, (n, 1)) / 2000.0
+        for t1 in (700.0, 1500.0, 3000.0):
+            o = O.run_fssh(model=kind, params=TULLY[kind], ndof=1, mass=2000.0, r0=r0, v0=v0, t0=0.0, t1=t1, dt=1.0,
+                           seed=3)
+            assert np.all(o["sigma"][:, 0, 0].imag == 0.0) and np.all(o["sigma"][:, 1, 1].imag == 0.0)
+        assert o["nhops"].sum() > 0
+    nm = 20
+    w = np.linspace(0.1, 3.0, nm)
+    c = 0.3 * w
+    o = O.run_fssh(model=10, params=(0.0, 1.0), ndof=nm, mass=1.0, r0=rng.standard_normal((n, nm)),
+                   v0=rng.standard_normal((n, nm)), t0=0.0, t1=8.0, dt=0.05, seed=4, init_kind=2, init_state=0,
+                   bath_c=c, bath_w2=w * w)
+    assert o["nhops"].sum() > 0
+    assert np.all(o["sigma"][:, 0, 0].imag == 0.0) and np.all(o["sigma"][:, 1, 1].imag == 0.0)
+
+
 def test_rpsh_energy_and_termination():
     # test/Dynamics/fssh.jl:210-233: RPSH on Tully 2 conserves the ring-polymer energy to rtol 1e-2
     n, nb = 32, 5
