@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 105
+#define NQCD_ABI_VERSION 106
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -118,7 +118,9 @@ typedef struct nqcd_config {
     int32_t save_stride;  /* population correlation every save_stride steps (0 = off) */
     int32_t max_hops;     /* hop-log capacity per trajectory (0 = no log) */
     double terminate_x;   /* ring polymer: stop a trajectory once |centroid x| > terminate_x (0 = off) */
-    double gap_fp64;      /* fast path: propagate electronics in FP64 when the adiabatic gap is below this */
+    double gap_fp64;      /* fast path: propagate electronics in FP64 when the adiabatic gap is below this;
+                             IESH: solve adjacent roots closer than this again in FP64 and form the
+                             couplings between them from the FP64 roots (0 = off) */
     int64_t traj_offset;  /* global index of trajectory 0 (Philox counter), for sharded ensembles */
     int32_t use_friction_surrogate; /* MDEF fast path: friction from the trained network inside its domain */
     int32_t exact_friction_every; /* MDEF with surrogate: exact friction every k steps (0 = never) */
@@ -128,6 +130,11 @@ typedef struct nqcd_config {
     double decoherence_C; /* IESH: energy-based decoherence correction (DecoherenceCorrectionEDC(C),
                              decoherence_corrections.jl:21-39, applied after every step as the callback
                              of iesh.jl:424-441); 0 = none (the reference's default), 0.1 = EDC() */
+    double surrogate_tolerance; /* MDEF with surrogate: on each exact_friction_every-th step the network is
+                             judged against the exact friction (mdef.jl:131-140); a relative error
+                             |net - exact| / max(|exact|, 0.1 max friction of the domain) above this
+                             switches the trajectory to exact friction for the rest of the run
+                             (<= 0: 0.1) */
 } nqcd_config;
 
 typedef struct nqcd_outputs {
@@ -159,7 +166,12 @@ typedef struct nqcd_stats {
     int64_t hop_evaluations;          /* IESH: steps whose hop probabilities were evaluated in full */
     int64_t propagator_terms;         /* IESH: Chebyshev terms summed over trajectory steps */
     int64_t electronics_fp64_steps;   /* FSSH, Ehrenfest, RPSH fast paths: steps whose electronics ran in
-                                         FP64 because the adiabatic gap was below gap_fp64 */
+                                         FP64 because the adiabatic gap was below gap_fp64; IESH fast
+                                         path: steps with adjacent roots refined in FP64 */
+    int64_t surrogate_judged;         /* MDEF with surrogate: steps where network and exact friction were compared */
+    int64_t surrogate_rejected;       /* MDEF with surrogate: trajectories switched to exact friction by the judge */
+    double surrogate_max_rel_error;   /* MDEF with surrogate: largest judged relative error */
+    double surrogate_mean_rel_error;  /* MDEF with surrogate: mean judged relative error */
 } nqcd_stats;
 
 typedef struct nqcd_handle nqcd_handle;
@@ -287,8 +299,9 @@ int nqcd_get_hop_log(nqcd_handle* h, int32_t* log);
  * skip): nonfinite[t] = 1 where a final position or velocity is not finite
  * (the trajectories counted in nqcd_stats.flagged), fp64_steps[t] = steps of
  * a fast path whose electronics ran in FP64 because the adiabatic gap was
- * below gap_fp64 (0 on the plain path and for MDEF/IESH).  Frustrated-hop
- * counts come from nqcd_get_final. */
+ * below gap_fp64, or (IESH) whose near-degenerate roots were refined in FP64
+ * (0 on the plain path and for MDEF).  Frustrated-hop counts come from
+ * nqcd_get_final. */
 int nqcd_get_status(nqcd_handle* h, int32_t* nonfinite, int32_t* fp64_steps);
 
 /* Message of the last failed call on this handle (or of the last failed

@@ -44,7 +44,7 @@ export EnsembleGB300, install_keyed_hop_stream!, with_keyed_hops, keyed_fermi_di
 # C ABI (include/nqcd_gpu.h)
 # ---------------------------------------------------------------------------
 
-const ABI_VERSION = Int32(105)
+const ABI_VERSION = Int32(106)
 
 const METHOD_FSSH = Int32(1)
 const METHOD_RPSH = Int32(2)
@@ -105,6 +105,7 @@ struct NqcdConfig
     exact_hop_probability::Int32
     reserved::NTuple{2,Int32}
     decoherence_C::Float64
+    surrogate_tolerance::Float64
 end
 
 struct NqcdOutputs
@@ -133,6 +134,10 @@ struct NqcdStats
     hop_evaluations::Int64
     propagator_terms::Int64
     electronics_fp64_steps::Int64
+    surrogate_judged::Int64
+    surrogate_rejected::Int64
+    surrogate_max_rel_error::Float64
+    surrogate_mean_rel_error::Float64
 end
 
 struct NqcdSampler
@@ -142,7 +147,7 @@ struct NqcdSampler
     b::Float64
 end
 
-zero_stats() = NqcdStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+zero_stats() = NqcdStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0.0)
 
 """
     config(; method, model, ndofs, natoms, nstates, ..., keep)
@@ -155,7 +160,7 @@ function config(; method, model, ndofs, natoms, nstates, params, masses, keep, p
                 rescaling=Int32(0), nbeads_max=0, bath_a=Float64[], bath_b=Float64[], beta=0.0, ntraj_max,
                 init_kind=INIT_ADIABATIC_PURE, init_state=0, save_stride=0, max_hops=0, terminate_x=0.0,
                 gap_fp64=1e-3, traj_offset=0, use_friction_surrogate=0, exact_friction_every=0, nelectrons=0,
-                exact_hop_probability=0, decoherence_C=0.0)
+                exact_hop_probability=0, decoherence_C=0.0, surrogate_tolerance=0.0)
     p = collect(Float64, params)
     m = collect(Float64, masses)
     a = collect(Float64, bath_a)
@@ -165,7 +170,8 @@ function config(; method, model, ndofs, natoms, nstates, params, masses, keep, p
     return NqcdConfig(method, model, precision, rescaling, ndofs, natoms, nstates, nbeads_max, length(p), ptr(p),
                       length(a), ptr(a), ptr(b), ptr(m), beta, ntraj_max, init_kind, init_state, save_stride,
                       max_hops, terminate_x, gap_fp64, traj_offset, use_friction_surrogate, exact_friction_every,
-                      nelectrons, exact_hop_probability, (Int32(0), Int32(0)), decoherence_C)
+                      nelectrons, exact_hop_probability, (Int32(0), Int32(0)), decoherence_C,
+                      surrogate_tolerance)
 end
 
 const LIBHANDLE = Ref{Ptr{Cvoid}}(C_NULL)

@@ -108,6 +108,11 @@ struct IeshParams {
     double* energy;                 // [2][ntraj] total energy at start and end, or null
     double* obs_partial;            // [ntraj][nsave][4]: z, kinetic, impurity population, potential
     unsigned long long* counters;   // [0] full hop evaluations, [1] Chebyshev terms, [2] unconverged roots
+    // FP32 path: adjacent roots closer than gap_fp64 are solved again in FP64 and the couplings
+    // between them, z0_i z0_j / (l_j - l_i), formed from the FP64 roots; fp64_steps[ti] counts the
+    // steps that needed it (null: not counted)
+    double gap_fp64;
+    int32_t* fp64_steps;
 };
 
 template <typename R>
@@ -441,6 +446,10 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     const double Lpad = fabs(p.eps[0]) + fabs(p.eps[M - 1]) + 1.0 + p.sumV2;
     // thread i < N owns root i and warm-starts it from the previous step
     R lam_own = R(0);
+    // FP32 path: w64 holds, during the step loop, the FP64 roots of near-degenerate pairs (NaN for
+    // the others) and fp64_now whether this step refined any
+    bool fp64_now = false;
+    int nfp64 = 0;
     auto roots = [&]() {  // after a barrier that published misc[4] = h
         const double hz = misc[4];
         if (tid < N) {
@@ -450,7 +459,42 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             z2[tid] = zz;
             z0[tid] = sqrt(zz);
         }
-        __syncthreads();
+        if constexpr (std::is_same<R, float>::value) {
+            // near-degeneracy fallback: a root whose neighbour lies closer than gap_fp64 is solved
+            // again in FP64 (warm start from the FP32 root), which fixes the small gap that divides
+            // its couplings.  Two roots closer than the threshold are both flagged: each has the
+            // other as a neighbour, and a root whose neighbours are both at least the threshold
+            // away is at least that far from every root.
+            __syncthreads();
+            bool flag = false;
+            if (tid < N && p.gap_fp64 > 0.0) {
+                const double lo = tid > 0 ? (double)lam[tid] - (double)lam[tid - 1] : 1e300;
+                const double hi = tid + 1 < N ? (double)lam[tid + 1] - (double)lam[tid] : 1e300;
+                flag = (lo < hi ? lo : hi) < p.gap_fp64;
+                double l64 = (double)lam_own;
+                if (flag) {
+                    double zz64;
+                    secular_root<double>(p.eps, p.V2, M, tid, hz, fabs(hz) + Lpad, l64, zz64, nonconv);
+                    z0[tid] = (R)sqrt(zz64);
+                    z2[tid] = (R)zz64;
+                }
+                w64[tid] = flag ? l64 : __longlong_as_double(0x7ff8000000000000ll);
+            }
+            fp64_now = __syncthreads_or(flag) != 0;
+            nfp64 += fp64_now ? 1 : 0;
+        } else {
+            __syncthreads();
+        }
+    };
+    // coupling denominator l_j - l_i: from the FP64 roots where both were refined
+    auto gap = [&](int i, int j) -> R {
+        if constexpr (std::is_same<R, float>::value) {
+            if (fp64_now) {
+                const double a = w64[i], b = w64[j];
+                if (a == a && b == b) return (R)(b - a);
+            }
+        }
+        return lam[j] - lam[i];
     };
     // ---- ring polymer ----
     // mean over the beads of warp 0 (the same value in every lane)
@@ -637,6 +681,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     if (warp == 0) publish_levels(hz, dhz);
     __syncthreads();
     roots();
+    nfp64 = 0;  // the count is of integration steps
     const double z_fd = RP ? misc[14] : r[2];  // where the Fermi-Dirac eigenvalues are taken
     if (p.init_kind == IESH_INIT_FERMI_DIRAC) {
         // Metropolis over occupations with the Boltzmann ratio (DynamicsUtils.jl:194-208).
@@ -825,7 +870,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         // ---- propagator (wavefunction_dynamics.jl:15-58) ----
         for (int q = tid; q < N * N; q += nthr) {
             const int j = q / N, i = q - j * N;
-            At[j * Np + i] = i == j ? R(0) : z0[i] * z0[j] / (lam[j] - lam[i]);
+            At[j * Np + i] = i == j ? R(0) : z0[i] * z0[j] / gap(i, j);
         }
         __syncthreads();
         const double w = misc[6];
@@ -1178,7 +1223,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     bool accept = true;
                     if (p.rescaling != RESCALE_OFF) {
                         // d[new, old] = dh A[new][old]; only its z component is nonzero
-                        const double dz = dhz * (double)z0[nw] * (double)z0[old] / ((double)lam[old] - (double)lam[nw]);
+                        const double dz = dhz * (double)z0[nw] * (double)z0[old] / (double)gap(nw, old);
                         const double aa = (dz * dz / mass) / 2.0;
                         const double vz = RP ? misc[13] : v[2];  // hopping velocity: the centroid's
                         const double bb = dz * vz;
@@ -1283,6 +1328,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         if (p.nhops) p.nhops[ti] = nh;
         if (p.nfrustrated) p.nfrustrated[ti] = nf;
         if (p.nsteps_out) p.nsteps_out[ti] = p.nsteps;
+        if (p.fp64_steps) p.fp64_steps[ti] = nfp64;
         if (p.energy) {
             p.energy[ti] = e0;
             p.energy[NT + ti] = e1;

@@ -53,6 +53,7 @@ struct MlpWeights {
     const __nv_bfloat16* b3;  // [1]
     float x_shift, x_scale;   // input normalisation
     float lo, hi;             // training domain (outside: exact friction)
+    float floor;              // judge: relative errors are taken against max(|exact|, floor)
 };
 
 struct MdefParams {
@@ -69,12 +70,15 @@ struct MdefParams {
     int32_t save_stride, nsave;
     int32_t use_mlp;        // fast path: friction from the surrogate inside its domain
     int32_t exact_friction_every;    // fast path with surrogate: exact friction every k steps (0 = never)
+    double judge_tol;       // relative error of a judged network value that retires the network for the trajectory
     MlpWeights mlp;
     double* x;              // [ntraj] in/out
     double* v;              // [ntraj] in/out
     double* energy;         // [2][ntraj] (initial, final) or null
     double* obs_partial;    // [nwarps_total][nsave][4] (<x>, <x^2>, <KE>, <Lambda>)
-    unsigned long long* counters;  // [0] exact friction evaluations, [1] surrogate evaluations, [2] non-converged roots
+    unsigned long long* counters;  // [0] exact friction evaluations, [1] surrogate evaluations, [2] non-converged roots,
+                                   // [8] judged steps, [9] rejected trajectories, [10] largest judged relative
+                                   // error (bits of a non-negative double), [11] sum of judged relative errors (double)
     double* friction_out;   // optional: exact friction at x (single evaluation mode), [ntraj]
     double* force_out;      // optional: force at x, [ntraj]
     // ring polymers (RingPolymerSimulation{DiabaticMDEF}, rpmdef_kernel): x, v are [bead][ntraj]
@@ -273,23 +277,35 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         ++isave;
     };
     save(0.0);
-    unsigned long long n_exact = 0, n_mlp = 0;
+    unsigned long long n_exact = 0, n_mlp = 0, n_judged = 0;
+    bool net_on = p.use_mlp != 0;  // the judge retires the network for this trajectory
+    double err_max = 0.0, err_sum = 0.0;
     for (int step = 1; step <= p.nsteps; ++step) {
         v = v + (half * dt) * k;  // B
         x = x + (half * dt) * v;  // A
         double lamv;
-        bool use_net = false;
+        bool in_domain = false, judge = false;
         if constexpr (std::is_same<R, float>::value) {
-            use_net = p.use_mlp && (float)x >= p.mlp.lo && (float)x <= p.mlp.hi &&
-                      !(p.exact_friction_every > 0 && step % p.exact_friction_every == 0);
+            in_domain = net_on && (float)x >= p.mlp.lo && (float)x <= p.mlp.hi;
+            judge = in_domain && p.exact_friction_every > 0 && step % p.exact_friction_every == 0;
         }
-        if (use_net) {
+        // x is the same in every lane of the warp, so these branches are warp-uniform
+        if (in_domain && !judge) {
             lamv = (double)mlp_friction(p.mlp, (float)x);
             ++n_mlp;
         } else {
             double Fm;
             mdef_electronic<R>(p, sh, wib, lam, x, true, Fm, lamv);
             ++n_exact;
+            if (judge) {  // the exact friction (mdef.jl:131-140) judges the network at this step
+                const double net = (double)mlp_friction(p.mlp, (float)x);
+                const double ref = fabs(lamv) > (double)p.mlp.floor ? fabs(lamv) : (double)p.mlp.floor;
+                const double err = fabs(net - lamv) / ref;
+                ++n_judged;
+                err_sum += err;
+                err_max = err > err_max ? err : err_max;
+                if (!(err <= p.judge_tol)) net_on = false;
+            }
         }
         if constexpr (std::is_same<R, float>::value) {
             // O step in FP32: c2 = sqrt(1 - c1^2) as sqrt(-expm1(-2 gamma dt)), accurate for small gamma dt
@@ -325,6 +341,13 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
     if (p.counters) {
         atomicAdd(p.counters + 0, n_exact);
         atomicAdd(p.counters + 1, n_mlp);
+        if (n_judged) {
+            atomicAdd(p.counters + 8, n_judged);
+            if (p.use_mlp && !net_on) atomicAdd(p.counters + 9, 1ull);
+            // non-negative doubles order as their bit patterns
+            atomicMax(p.counters + 10, (unsigned long long)__double_as_longlong(err_max));
+            atomicAdd(reinterpret_cast<double*>(p.counters + 11), err_sum);
+        }
     }
 }
 

@@ -391,6 +391,7 @@ MlpWeights mlp_view(const MlpState& s) {
     w.x_scale = (float)s.scale;
     w.lo = (float)s.lo;
     w.hi = (float)s.hi;
+    w.floor = (float)s.friction_floor;
     return w;
 }
 

@@ -30,6 +30,7 @@ struct MlpState {
     unsigned long long* step_counter = nullptr;  // device: Adam step (graph replays advance it)
     int* batch_index = nullptr;  // device scratch: minibatch sample indices
     double shift = 0.0, scale = 1.0, lo = 0.0, hi = 0.0;
+    double friction_floor = 0.0;  // judge: 0.1 x the largest exact friction on a grid of the domain
     bool trained = false;
 };
 

@@ -240,7 +240,8 @@ struct nqcd_handle {
     double* d_redtmp = nullptr;  // chunk sums of the partial reduction
     int64_t redtmp_cap = 0;
     double* d_popcorr = nullptr;
-    unsigned long long* d_counts = nullptr;  // [0..3] scatter, [4..7] stats
+    unsigned long long* d_counts = nullptr;  // [0..3] scatter, [4..7] stats, [8..11] method counters,
+                                             // [12] FP64-electronics steps, [16..19] surrogate judge
     double* d_stage = nullptr;               // staging for layout gathers
     int64_t stage_cap = 0;
     // ring polymers: normal-mode tables per instantiated bead count, bead-count classes
@@ -370,6 +371,7 @@ MdefParams mdef_params(nqcd_handle* h, int64_t N, double dt, int32_t nsteps, uin
     m.nsave = nsave;
     m.use_mlp = (h->cfg.use_friction_surrogate && h->cfg.precision != NQCD_PREC_FP64) ? 1 : 0;
     m.exact_friction_every = h->cfg.exact_friction_every;
+    m.judge_tol = h->cfg.surrogate_tolerance > 0.0 ? h->cfg.surrogate_tolerance : 0.1;
     m.mlp = mlp_view(h->mlp);
     m.x = h->d_r;
     m.v = h->d_v;
@@ -473,6 +475,8 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
             return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: unknown model");
         if (cfg->nstates != 2) return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: only two-state models");
     }
+    if (!(cfg->surrogate_tolerance < 1e300) || cfg->surrogate_tolerance != cfg->surrogate_tolerance)
+        return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: surrogate_tolerance must be finite");
     if (!(cfg->decoherence_C >= 0.0 && cfg->decoherence_C < 1e300))
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: decoherence_C must be finite and >= 0");
     if (cfg->decoherence_C != 0.0 && cfg->method != NQCD_METHOD_IESH)
@@ -596,13 +600,13 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
         h->rp_beads = cfg->nbeads_max;
         NQCD_CREATE(dalloc(&h->d_rptab, cfg->nbeads_max * cfg->nbeads_max + 4 * cfg->nbeads_max));
     }
-    if (!mdef && !iesh) {  // FSSH, Ehrenfest, RPSH: per-trajectory FP64-electronics step counts
+    if (!mdef) {  // FSSH, Ehrenfest, RPSH, IESH: per-trajectory counts of steps with FP64 electronics
         NQCD_CREATE(dalloc(&h->d_fp64steps, cap));
         NQCD_CREATE(cudaMemset(h->d_fp64steps, 0, cap * sizeof(int32_t)));
     }
     if (cfg->max_hops > 0) NQCD_CREATE(dalloc(&h->d_hoplog, (int64_t)cfg->max_hops * 3 * cap));
     NQCD_CREATE(dalloc(&h->d_energy, 2 * cap));
-    NQCD_CREATE(dalloc(&h->d_counts, 16));
+    NQCD_CREATE(dalloc(&h->d_counts, 24));
     if (mdef || iesh) {
         std::vector<double> eps(cfg->bath_a, cfg->bath_a + cfg->nbath), V2(cfg->nbath);
         for (int k = 0; k < cfg->nbath; ++k) V2[k] = cfg->bath_b[k] * cfg->bath_b[k];
@@ -916,7 +920,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_v, h->d_v0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_sig, h->d_sig0, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_state, h->d_state0, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
-    NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 16 * sizeof(unsigned long long), s));
+    NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 24 * sizeof(unsigned long long), s));
     if (h->d_fp64steps) NQCD_CUDA(h, cudaMemsetAsync(h->d_fp64steps, 0, N * sizeof(int32_t), s));
     if (h->d_hoplog) {
         int64_t nl = (int64_t)h->cfg.max_hops * 3 * N;
@@ -1167,6 +1171,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.energy = h->d_energy;
         q.obs_partial = nsave > 0 ? h->d_partial : nullptr;
         q.counters = h->d_counts + 8;
+        q.gap_fp64 = h->cfg.precision == NQCD_PREC_FP64 ? 0.0 : h->cfg.gap_fp64;
+        q.fp64_steps = h->d_fp64steps;
         q.nbeads = h->rp_beads;
         if (h->rp_beads > 1) {
             // ring polymer: normal modes and full-step Cayley matrices of the free ring polymer
@@ -1258,7 +1264,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     }
     NQCD_CUDA(h, cudaEventRecord(h->ev1, s));
 
-    unsigned long long counts[16];
+    unsigned long long counts[24];
     int64_t d2h = 0;
     NQCD_CUDA(h, cudaMemcpyAsync(counts, h->d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
     d2h += sizeof(counts);
@@ -1294,6 +1300,13 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         stats->frustrated = (int64_t)counts[6];
         stats->flagged = (int64_t)counts[7];
         stats->electronics_fp64_steps = h->d_fp64steps ? (int64_t)counts[12] : 0;
+        stats->surrogate_judged = mdef ? (int64_t)counts[16] : 0;
+        stats->surrogate_rejected = mdef ? (int64_t)counts[17] : 0;
+        double emax = 0.0, esum = 0.0;
+        memcpy(&emax, &counts[18], sizeof(double));
+        memcpy(&esum, &counts[19], sizeof(double));
+        stats->surrogate_max_rel_error = mdef ? emax : 0.0;
+        stats->surrogate_mean_rel_error = (mdef && counts[16] > 0) ? esum / (double)counts[16] : 0.0;
         stats->device_ms = ms;
         stats->kernel_ms = kms;
         stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
@@ -1390,6 +1403,28 @@ int nqcd_mdef_evaluate(nqcd_handle* h, int64_t n, const double* x, double* force
     return NQCD_OK;
 }
 
+// Friction floor of the surrogate's judge: 0.1 x the largest exact friction
+// on 257 evenly spaced points of the network's domain (relative errors of
+// judged values are taken against max(|exact|, floor), so that a region of
+// vanishing friction does not turn rounding into a rejection).
+static int mlp_set_friction_floor(nqcd_handle* h) {
+    const int64_t n = 257;
+    int rc = ensure_stage(h, 3 * n);
+    if (rc) return rc;
+    std::vector<double> xs(n), G(n);
+    for (int64_t i = 0; i < n; ++i) xs[i] = h->mlp.lo + (h->mlp.hi - h->mlp.lo) * (double)i / (double)(n - 1);
+    double *dx = h->d_stage, *dF = h->d_stage + n, *dG = h->d_stage + 2 * n;
+    NQCD_CUDA(h, cudaMemcpyAsync(dx, xs.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    rc = mdef_eval_device(h, dx, n, dF, dG);
+    if (rc) return rc;
+    NQCD_CUDA(h, cudaMemcpyAsync(G.data(), dG, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
+    double gmax = 0.0;
+    for (double g : G) gmax = fabs(g) > gmax ? fabs(g) : gmax;
+    h->mlp.friction_floor = gmax > 0.0 ? 0.1 * gmax : 1e-300;
+    return NQCD_OK;
+}
+
 __global__ void uniform_positions_kernel(double* x, int64_t n, double lo, double hi, uint64_t seed) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = lo + (hi - lo) * rng_uniform(seed, (uint64_t)i, 0u, 9u);
@@ -1460,6 +1495,8 @@ int nqcd_train_friction_mlp(nqcd_handle* h, double x_lo, double x_hi, int64_t np
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     release();
     if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_train_friction_mlp: training");
+    rc = mlp_set_friction_floor(h);
+    if (rc) return rc;
     h->mlp.trained = true;
     return NQCD_OK;
 }
@@ -1495,6 +1532,8 @@ int nqcd_mlp_set(nqcd_handle* h, const float* params, const double* meta) {
     h->mlp.scale = meta[1];
     h->mlp.lo = meta[2];
     h->mlp.hi = meta[3];
+    int rc = mlp_set_friction_floor(h);
+    if (rc) return rc;
     h->mlp.trained = true;
     return NQCD_OK;
 }

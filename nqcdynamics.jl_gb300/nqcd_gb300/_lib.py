@@ -67,6 +67,7 @@ class nqcd_config(C.Structure):
         ("exact_hop_probability", C.c_int32),
         ("reserved", C.c_int32 * 2),
         ("decoherence_C", C.c_double),
+        ("surrogate_tolerance", C.c_double),
     ]
 
 
@@ -99,6 +100,10 @@ class nqcd_stats(C.Structure):
         ("hop_evaluations", C.c_int64),
         ("propagator_terms", C.c_int64),
         ("electronics_fp64_steps", C.c_int64),
+        ("surrogate_judged", C.c_int64),
+        ("surrogate_rejected", C.c_int64),
+        ("surrogate_max_rel_error", C.c_double),
+        ("surrogate_mean_rel_error", C.c_double),
     ]
 
 

@@ -634,7 +634,8 @@ class EnsembleGB300:
     max_hops: int = 16
     seed: int = 20261203
     friction_surrogate: Any = None  # MDEF: (weights, meta) of a trained network, or None
-    exact_friction_every: int = 0
+    exact_friction_every: int = 0   # MDEF surrogate: judge the network against the exact friction every k steps
+    surrogate_tolerance: float = 0.1  # judged relative error that retires the network for a trajectory
     device_sampling: bool = False   # draw the nuclear initial conditions on the GPU (nqcd_sample_initial)
 
 
@@ -780,6 +781,7 @@ def _metal_config(sim, ntraj, alg, save_stride):
         cfg.beta = 1.0 / sim.temperature
         cfg.use_friction_surrogate = int(alg.friction_surrogate is not None)
         cfg.exact_friction_every = alg.exact_friction_every
+        cfg.surrogate_tolerance = alg.surrogate_tolerance
     else:
         params = np.array([imp.kxy, imp.A, imp.a, imp.delta, imp.B, imp.b])
         cfg.rescaling = 0 if ena else L.RESCALE[sim.method.rescaling]
@@ -788,6 +790,7 @@ def _metal_config(sim, ntraj, alg, save_stride):
             cfg.decoherence_C = sim.method.decoherence.C
         cfg.nelectrons = model.nelectrons
         cfg.max_hops = alg.max_hops
+        cfg.gap_fp64 = alg.gap_fp64  # FP32 path: FP64 refinement of near-degenerate roots
     masses = np.ascontiguousarray(sim.atoms.masses, dtype=np.float64)
     cfg.nparams, cfg.params, cfg.masses = len(params), L.dptr(params), L.dptr(masses)
     cfg.nbath, cfg.bath_a, cfg.bath_b = len(model.eps), L.dptr(model.eps), L.dptr(model.V)

@@ -92,11 +92,12 @@ def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, exact_friction
 
 
 def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max_hops=0, exact=0, traj_offset=0,
-                        method=None, nbeads=0):
+                        method=None, nbeads=0, gap_fp64=1e-3):
     """C5: IESH on the three-dimensional Newns-Anderson adsorbate, Fermi-Dirac
     initial occupations (method=L.METHOD_EHRENFEST_NA: EhrenfestNA on the same
     system; nbeads > 1: RingPolymerSimulation{AdiabaticIESH} with that many
-    beads)."""
+    beads).  The FP32 path refines adjacent roots closer than gap_fp64 in
+    FP64 (the near-degeneracy fallback)."""
     P = wl["params"]
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision, cfg.rescaling = (method or L.METHOD_IESH), L.MODEL_NEWNS_ANDERSON_3D, \
@@ -116,4 +117,5 @@ def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max
     cfg.exact_hop_probability = exact
     cfg.traj_offset = traj_offset
     cfg.nbeads_max = nbeads
+    cfg.gap_fp64 = gap_fp64
     return L.Engine(cfg, [params, masses, eps, V])

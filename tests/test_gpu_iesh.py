@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 
 def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_DIRAC, max_hops=32, save_stride=0,
-              exact=0, method=L.METHOD_IESH, decoherence=0.0, nbeads=0, traj_offset=0):
+              exact=0, method=L.METHOD_IESH, decoherence=0.0, nbeads=0, traj_offset=0, gap_fp64=0.0):
     P = wl["params"]
     cfg = L.nqcd_config()
     cfg.method, cfg.model, cfg.precision, cfg.rescaling = method, L.MODEL_NEWNS_ANDERSON_3D, precision, rescaling
@@ -43,6 +43,7 @@ def make_iesh(wl, ntraj, precision=L.PREC_FP64, rescaling=0, init=L.INIT_FERMI_D
     cfg.decoherence_C = decoherence
     cfg.nbeads_max = nbeads  # > 1: RingPolymerSimulation{AdiabaticIESH}
     cfg.traj_offset = traj_offset
+    cfg.gap_fp64 = gap_fp64
     return L.Engine(cfg, [params, masses, eps, V])
 
 
@@ -162,3 +163,41 @@ def test_iesh_decoherence_edc_fp64_matches_oracle():
     assert np.max(np.abs(plain["psi"] - fin["psi"])) > 1e-3
     norms = np.linalg.norm(fin["psi"], axis=1)
     np.testing.assert_allclose(norms, 1.0, atol=1e-10)
+
+
+def test_iesh_fp32_near_degeneracy_fallback():
+    """The FP32 path's FP64 near-degeneracy fallback: two bath levels 1e-6
+    apart put adjacent roots closer than gap_fp64 = 1e-3 at every step; those
+    roots are solved again in FP64 and the couplings between them formed from
+    the FP64 roots.  Every step of every trajectory is counted
+    (nqcd_get_status, nqcd_stats.electronics_fp64_steps), nothing is counted
+    with the fallback off or on the plain path, and the FP32 run stays within
+    FP32 tolerance of the plain FP64 path."""
+    n, nsteps = 64, 200
+    wl = WL.newns_anderson_iesh(n, nstates=40, nelectrons=20, z0=3.0)
+    eps = wl["eps"].copy()
+    k = len(eps) // 2
+    eps[k] = eps[k - 1] + 1e-6
+    wl["eps"] = eps
+    res = {}
+    for name, prec, gap in (("fp64", L.PREC_FP64, 1e-3), ("fp32", L.PREC_FP32, 1e-3), ("fp32_off", L.PREC_FP32, 0.0)):
+        eng = make_iesh(wl, n, precision=prec, gap_fp64=gap)
+        try:
+            eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]))
+            _, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 21)
+            fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+            fin["hop_log"] = eng.get_hop_log(eng.cfg.max_hops)
+            res[name] = (fin, st, eng.get_status()["fp64_steps"])
+        finally:
+            eng.close()
+    (f64, s64, c64), (f32, s32, c32), (foff, soff, coff) = res["fp64"], res["fp32"], res["fp32_off"]
+    assert np.all(c32 == nsteps) and s32.electronics_fp64_steps == n * nsteps
+    assert np.all(c64 == 0) and np.all(coff == 0) and soff.electronics_fp64_steps == 0
+    print("max |psi - psi_fp64|: fallback", np.abs(f32["psi"] - f64["psi"]).max(), "off",
+          np.abs(foff["psi"] - f64["psi"]).max())
+    # trajectories whose hop sequences agree (the FP32 path may flip a near-tie hop)
+    same = np.array([np.array_equal(a[a[:, 0] >= 0], b[b[:, 0] >= 0]) for a, b in zip(f32["hop_log"], f64["hop_log"])])
+    assert same.mean() > 0.9
+    np.testing.assert_allclose(f32["r"][same], f64["r"][same], rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(f32["v"][same], f64["v"][same], rtol=1e-3, atol=1e-7)
+    np.testing.assert_allclose(f32["energy"][:, 1].mean(), f64["energy"][:, 1].mean(), rtol=1e-4)

@@ -174,6 +174,50 @@ def test_friction_surrogate_trains_and_serves():
     assert st_s.kernel_ms < 0.8 * st_e.kernel_ms, (st_s.kernel_ms, st_e.kernel_ms)
 
 
+def test_surrogate_judge_retires_a_mistrained_network():
+    """The exact friction (mdef.jl:131-140) judges the network on every k-th
+    step inside its domain.  A network trained on another system (band
+    coupling 0.03 instead of 0.02, about 2.25 x the friction) fails its first
+    judged step in every trajectory and is retired there, so the relaxation
+    stays within 2 % of the exact run; the network trained on this system
+    passes the judge with small errors and keeps serving."""
+    n, nsteps, stride, every = 2048, 400, 20, 4
+    wl = WL.newns_anderson_mdef(n, M=200)
+    other = WL.newns_anderson_mdef(8, M=200, coupling=0.03)
+    lo, hi = -1.5, 2.5
+    nets = {}
+    for name, w in (("good", wl), ("wrong", other)):
+        eng = make_mdef(w, 8, L.PREC_FP32)
+        try:
+            eng.train_friction_mlp(lo, hi, 20000, 150, 1024, 3e-3, 11)
+            nets[name] = eng.mlp_get()
+        finally:
+            eng.close()
+    exact, _, e_e = run_relax(wl, n, L.PREC_FP32, nsteps, stride)
+    good, st_g, e_g = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, exact_friction_every=every,
+                                mlp=nets["good"])
+    bad, st_b, e_b = run_relax(wl, n, L.PREC_FP32, nsteps, stride, surrogate=True, exact_friction_every=every,
+                               mlp=nets["wrong"])
+    print("judge good:", st_g.surrogate_judged, st_g.surrogate_rejected, st_g.surrogate_mean_rel_error,
+          st_g.surrogate_max_rel_error, "wrong:", st_b.surrogate_judged, st_b.surrogate_rejected,
+          st_b.surrogate_mean_rel_error, st_b.surrogate_max_rel_error)
+    # the mistrained network is caught on its first judged step (a trajectory
+    # that starts outside the domain is judged when it first enters it)
+    assert st_b.surrogate_judged == st_b.surrogate_rejected
+    assert st_b.surrogate_rejected >= 0.97 * n
+    assert st_b.surrogate_max_rel_error > 0.5
+    assert st_b.surrogate_friction_evals <= n * (every - 1)
+    de, se = energy_drop(e_e)
+    db, sb = energy_drop(e_b)
+    assert abs(db - de) <= 0.02 * abs(de) + 2 * se, (de, db, se)
+    np.testing.assert_allclose(bad[:, 2], exact[:, 2], rtol=0.02)
+    # the network trained on this system passes and keeps serving
+    assert st_g.surrogate_judged > 0.2 * n * nsteps / every
+    assert st_g.surrogate_rejected < 0.02 * n
+    assert st_g.surrogate_mean_rel_error < 0.02
+    assert st_g.surrogate_friction_evals > 0.7 * n * nsteps
+
+
 def rp_initial(wl, n, B):
     x0 = np.repeat(wl["x0"][:, None], B, axis=1) + 0.02 * np.sin(2 * np.pi * np.arange(B) / B)[None]
     v0 = np.repeat(wl["v0"][:, None], B, axis=1)
