@@ -92,6 +92,7 @@ struct IeshParams {
     int32_t save_stride, nsave, max_hops;
     int64_t ntraj, traj_offset;
     double dt;
+    double h_last;                  // length of the last step (dt unless the span is not a whole number of steps)
     int32_t nsteps;
     uint64_t seed;
     double cheb_tol;                // truncation of the Chebyshev series
@@ -417,7 +418,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     const int64_t ti = blockIdx.x;
     const int64_t NT = p.ntraj;
     const uint64_t gid = (uint64_t)(p.traj_offset + ti);
-    const double mass = p.mass, inv_mass = 1.0 / p.mass, dt = p.dt, half = dt / 2.0;
+    const double mass = p.mass, inv_mass = 1.0 / p.mass, dt = p.dt;
     unsigned long long* nonconv = p.counters ? p.counters + 2 : nullptr;
 
     for (int k = tid; k < Np; k += nthr) {
@@ -833,17 +834,20 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     unsigned long long nfull = 0, nterms = 0;
     for (int step = 1; step <= p.nsteps; ++step) {
         // ---- velocity Verlet (verlet_with_electronics.jl:55-63) ----
+        // the integrator's dt (the shortened last step reaches t1); the hop probability and the
+        // decoherence correction read get_proposed_dt, the full dt
+        const double hs = step == p.nsteps ? p.h_last : dt, hh = hs / 2.0;
         double vt[3];
         double vzc0 = 0.0;  // ring polymer: centroid v_z at the step's start
         if (warp == 0) {
 #pragma unroll
-            for (int d = 0; d < 3; ++d) vt[d] = v[d] + half * k[d];
+            for (int d = 0; d < 3; ++d) vt[d] = v[d] + hh * k[d];
             if constexpr (RP) {
                 vzc0 = bead_mean(v[2]);
                 free_step(r, vt);
             } else {
 #pragma unroll
-                for (int d = 0; d < 3; ++d) r[d] = r[d] + dt * vt[d];
+                for (int d = 0; d < 3; ++d) r[d] = r[d] + hs * vt[d];
             }
             publish_levels(hz, dhz);
         }
@@ -854,7 +858,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         if (warp == 0) {
             accel(dhz);
 #pragma unroll
-            for (int d = 0; d < 3; ++d) v[d] = vt[d] + half * k[d];
+            for (int d = 0; d < 3; ++d) v[d] = vt[d] + hh * k[d];
             // v . grad h: the couplings are d_alpha = dh/dalpha A
             if constexpr (RP) {
                 const double vzc = bead_mean(v[2]);
@@ -889,11 +893,11 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             // covers the rounding of the bound in the working precision
             const double cen = 0.5 * (ehi + elo);
             const double hw = 0.5 * (ehi - elo) * (1.0 + (std::is_same<R, float>::value ? 1e-5 : 1e-12)) + 1e-300;
-            const int K = iesh_bessel_warp(hw * dt, p.cheb_tol, Jc, inv);
+            const int K = iesh_bessel_warp(hw * hs, p.cheb_tol, Jc, inv);
             for (int q = lane; q < kIeshMaxTerms; q += 32) Jr[q] = (R)(2.0 * Jc[q]);
             if (lane == 0) {
                 double sn, cs;
-                sincos(cen * dt, &sn, &cs);  // exp(-i c dt) = cs - i sn
+                sincos(cen * hs, &sn, &cs);  // exp(-i c h) = cs - i sn
                 misc[0] = (double)K;
                 misc[1] = sn;
                 misc[2] = cs;

@@ -65,6 +65,7 @@ struct MdefParams {
     double mass;
     int64_t ntraj, traj_offset;
     double dt;
+    double h_last;          // length of the last step (dt unless the span is not a whole number of steps)
     int32_t nsteps;
     uint64_t seed;
     int32_t save_stride, nsave;
@@ -281,8 +282,10 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
     bool net_on = p.use_mlp != 0;  // the judge retires the network for this trajectory
     double err_max = 0.0, err_sum = 0.0;
     for (int step = 1; step <= p.nsteps; ++step) {
-        v = v + (half * dt) * k;  // B
-        x = x + (half * dt) * v;  // A
+        // the integrator's dt: the shortened last step reaches t1 (mdef_baoab.jl:163-180)
+        const double hs = step == p.nsteps ? p.h_last : dt;
+        v = v + (half * hs) * k;  // B
+        x = x + (half * hs) * v;  // A
         double lamv;
         bool in_domain = false, judge = false;
         if constexpr (std::is_same<R, float>::value) {
@@ -309,7 +312,7 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         }
         if constexpr (std::is_same<R, float>::value) {
             // O step in FP32: c2 = sqrt(1 - c1^2) as sqrt(-expm1(-2 gamma dt)), accurate for small gamma dt
-            float gdt = (float)lamv * inv_m_f * dt_f;
+            float gdt = (float)lamv * inv_m_f * (float)hs;
             if (gdt < 0.f) gdt = 0.f;
             const float c1 = expf(-gdt);
             const float c2 = sqrtf(-expm1f(-2.f * gdt));
@@ -318,16 +321,16 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         } else {
             double gam = lamv / m;  // friction / (sqrt m sqrt m)
             if (gam < 0.0) gam = 0.0;
-            double c1 = exp(-gam * dt);
+            double c1 = exp(-gam * hs);
             double c2 = sqrt(1.0 - c1 * c1);
             double xi = noise_normal(p.seed, gid, (uint32_t)step);
             v = c1 * v + c2 * (sqrt(T / m) * xi);  // O
         }
-        x = x + (half * dt) * v;                // A
+        x = x + (half * hs) * v;                // A
         double Fn, dummy;
         mdef_electronic<R>(p, sh, wib, lam, x, false, Fn, dummy);
         k = -Fn / m;
-        v = v + (half * dt) * k;  // B
+        v = v + (half * hs) * k;  // B
         if (p.save_stride > 0 && step % p.save_stride == 0) save(lamv);
     }
     const double e1 = p.energy ? total_energy() : 0.0;

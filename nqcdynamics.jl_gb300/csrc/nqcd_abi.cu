@@ -365,6 +365,7 @@ MdefParams mdef_params(nqcd_handle* h, int64_t N, double dt, int32_t nsteps, uin
     m.ntraj = N;
     m.traj_offset = h->cfg.traj_offset;
     m.dt = dt;
+    m.h_last = dt;
     m.nsteps = nsteps;
     m.seed = seed;
     m.save_stride = stride;
@@ -875,17 +876,31 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     const int64_t N = h->ntraj;
     const bool mdef = h->cfg.method == NQCD_METHOD_MDEF;
     const bool iesh = h->cfg.method == NQCD_METHOD_IESH || h->cfg.method == NQCD_METHOD_EHRENFEST_NA;
-    // FSSH and RPSH step like the reference's integrator (a last partial step
-    // up to t1); MDEF and IESH take whole steps of dt only
+    // FSSH and RPSH step like the reference's integrator (its FP64 clock, a
+    // last partial step up to t1).  MDEF and IESH take steps of dt and, when
+    // t1 - t0 is not a whole number of steps, a shortened last step h_last
+    // that reaches t1 (ring polymers need whole steps: their Cayley matrices
+    // are built for dt).
     const double span = (t1 - t0) / dt;
     if (!(span < 2147483645.0)) return fail(h, NQCD_ERR_ARG, "nqcd_run: too many steps");
-    const int64_t nsteps = (mdef || iesh) ? (int64_t)llround(span) : count_steps(t0, t1, dt);
+    int64_t nsteps = 0;
+    double h_last = dt;
+    if (mdef || iesh) {
+        nsteps = (int64_t)llround(span);
+        if (fabs((double)nsteps * dt - (t1 - t0)) > 1e-9 * (fabs(t1 - t0) + dt)) {
+            if (h->cfg.nbeads_max > 1)
+                return fail(h, NQCD_ERR_ARG, "nqcd_run: ring-polymer MDEF and IESH need t1 - t0 to be a whole "
+                                              "number of steps");
+            nsteps = (int64_t)floor(span) + 1;
+            h_last = (t1 - t0) - (double)(nsteps - 1) * dt;
+        }
+    } else {
+        nsteps = count_steps(t0, t1, dt);
+    }
     if (nsteps > (int64_t)span + 2)
         return fail(h, NQCD_ERR_ARG, "nqcd_run: dt is below the spacing of doubles between t0 and t1");
     const int stride = h->cfg.save_stride;
     const int nsave = stride > 0 ? (int)(nsteps / stride + 1) : 0;
-    if ((mdef || iesh) && fabs((double)nsteps * dt - (t1 - t0)) > 1e-9 * (fabs(t1 - t0) + dt))
-        return fail(h, NQCD_ERR_ARG, "nqcd_run: MDEF and IESH need t1 - t0 to be a whole number of steps");
     const int64_t lanes = mdef ? 32 : (iesh ? 1 : fssh2_lanes_per_traj(h->cfg.model, h->cfg.precision));
     const int64_t blocks = (N * lanes + 127) / 128;
     // rows of observable partial sums: one per warp (FSSH, MDEF) or per trajectory (IESH)
@@ -1154,6 +1169,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.ntraj = N;
         q.traj_offset = h->cfg.traj_offset;
         q.dt = dt;
+        q.h_last = h_last;
         q.nsteps = (int32_t)nsteps;
         q.seed = seed;
         // series tail below the rounding of each path's arithmetic
@@ -1190,6 +1206,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         e = h->cfg.precision == NQCD_PREC_FP64 ? launch_iesh_fp64(q, s) : launch_iesh_fp32(q, s);
     } else if (mdef) {
         MdefParams mp = mdef_params(h, N, dt, (int32_t)nsteps, seed, stride, nsave);
+        mp.h_last = h_last;
         if (mp.use_mlp && !h->mlp.trained)
             return fail(h, NQCD_ERR_STATE, "nqcd_run: use_friction_surrogate needs nqcd_train_friction_mlp or nqcd_mlp_set");
         // steps and hop counters are not written by MDEF; observables need zeroed partials

@@ -186,7 +186,7 @@ def apply_decoherence_edc(psi, C, occupied, dt, E, ekin):
 
 
 def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, max_hops=16,
-             estimate=True, initial_state=None, ehrenfest_na=False, decoherence_C=0.0):
+             estimate=True, initial_state=None, ehrenfest_na=False, decoherence_C=0.0, h_last=None):
     """estimate: the reference's estimate_probability screen (iesh.jl:251-254).
     initial_state: given occupations (ntraj, ne) instead of Fermi-Dirac sampling.
     ehrenfest_na: Simulation{EhrenfestNA} instead (ehrenfest_na.jl): the same
@@ -195,7 +195,12 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
     Re(psi_ne conj(psi_me)) = -dh |sum_n z0_n psi_ne|^2 summed over e
     (ehrenfest_na.jl:74-90; A = dh z0 z0^T for this model), and no hops.
     decoherence_C > 0: DecoherenceCorrectionEDC(C) applied to every electron's
-    column after each step's hop (iesh.jl:424-441)."""
+    column after each step's hop (iesh.jl:424-441).
+    h_last: length of the last step when the time span is not a whole number
+    of steps.  The integrator takes the shortened step (Verlet and propagator,
+    verlet_with_electronics.jl:42-69 read integrator.dt); the hop probability
+    and the decoherence correction read get_proposed_dt, the full dt
+    (iesh.jl:390-398, 430-441)."""
     n = r0.shape[0]
     N = model.nstates
     traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
@@ -229,11 +234,12 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
     e0 = energy(w, psi)
     nfull = 0
     for step in range(1, nsteps + 1):
-        vt = v + (dt / 2) * k
-        r = r + dt * vt
+        hs = h_last if (h_last is not None and step == nsteps) else dt  # this step's length
+        vt = v + (hs / 2) * k
+        r = r + hs * vt
         w, Z = eigen_continuous(model, r, Z)
         k = accel(w, Z, r, state, psi)
-        v = vt + (dt / 2) * k
+        v = vt + (hs / 2) * k
         gh = model.grad_h(r)
         z0 = Z[:, 0, :]
         lam_diff = w[:, None, :] - w[:, :, None]  # l_j - l_i
@@ -247,7 +253,7 @@ def run_iesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, 
         Heff[:, idx, idx] = w
         Heff -= 1j * vd
         mu, U = np.linalg.eigh(Heff)
-        P = np.einsum("tij,tj,tkj->tik", U, np.exp(-1j * mu * dt), U.conj())
+        P = np.einsum("tij,tj,tkj->tik", U, np.exp(-1j * mu * hs), U.conj())
         psi = P @ psi
         if ehrenfest_na:
             continue

@@ -141,9 +141,13 @@ def electronic(model, x, beta, sigma, want_friction=True):
 
 
 def run_mdef(model: NewnsAnderson, *, mass, beta, sigma, x0, v0, dt, nsteps, seed, traj_offset=0,
-             friction_fn=None):
+             friction_fn=None, h_last=None):
     """BAOAB with friction in the tensor's eigenbasis (1 DoF: a scalar).
-    friction_fn(x) may replace the exact friction (surrogate runs)."""
+    friction_fn(x) may replace the exact friction (surrogate runs).
+    h_last: length of the last step when the time span is not a whole number
+    of steps; every sub-step of BAOAB reads the integrator's dt, the
+    shortened one on the last step (mdef_baoab.jl:163-180, steps.jl:41-69),
+    and the noise dW / sqrt(dt) is a standard normal whatever the step."""
     x = np.asarray(x0, np.float64).copy()
     v = np.asarray(v0, np.float64).copy()
     traj = np.arange(len(x), dtype=np.uint64) + np.uint64(traj_offset)
@@ -151,20 +155,21 @@ def run_mdef(model: NewnsAnderson, *, mass, beta, sigma, x0, v0, dt, nsteps, see
     half = 0.5
     k = -electronic(model, x, beta, sigma, want_friction=False)["F"] / mass
     for step in range(1, nsteps + 1):
-        v = v + (half * dt) * k                         # B
-        x = x + (half * dt) * v                         # A
+        hs = h_last if (h_last is not None and step == nsteps) else dt  # this step's length
+        v = v + (half * hs) * k                         # B
+        x = x + (half * hs) * v                         # A
         if friction_fn is None:
             lam = electronic(model, x, beta, sigma)["friction"]
         else:
             lam = friction_fn(x)
         gam = np.maximum(lam / mass, 0.0)               # Lambda / (sqrt m sqrt m), clamp(gamma, 0, Inf)
-        c1 = np.exp(-gam * dt)
+        c1 = np.exp(-gam * hs)
         c2 = np.sqrt(1.0 - c1 * c1)
         noise = np.sqrt(T / mass) * normal(seed, traj, step)
         v = c1 * v + c2 * noise                         # O
-        x = x + (half * dt) * v                         # A
+        x = x + (half * hs) * v                         # A
         k = -electronic(model, x, beta, sigma, want_friction=False)["F"] / mass
-        v = v + (half * dt) * k                         # B
+        v = v + (half * hs) * k                         # B
     return x, v
 
 

@@ -201,3 +201,26 @@ def test_iesh_fp32_near_degeneracy_fallback():
     np.testing.assert_allclose(f32["r"][same], f64["r"][same], rtol=1e-4, atol=1e-5)
     np.testing.assert_allclose(f32["v"][same], f64["v"][same], rtol=1e-3, atol=1e-7)
     np.testing.assert_allclose(f32["energy"][:, 1].mean(), f64["energy"][:, 1].mean(), rtol=1e-4)
+
+
+def test_iesh_fp64_shortened_last_step_matches_oracle():
+    """A time span that is not a whole number of steps: Verlet and the
+    propagator take the shortened last step (integrator.dt,
+    verlet_with_electronics.jl:42-69), the hop probability keeps the proposed
+    full dt (iesh.jl:390-398); identical hop sequences, r, v and orbitals to
+    1e-8 of the oracle."""
+    n, whole = 8, 300
+    wl = WL.newns_anderson_iesh(n, nstates=20, nelectrons=10, z0=3.0)
+    t1 = (whole + 0.6) * wl["dt"]
+    eng = make_iesh(wl, n)
+    try:
+        eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]))
+        _, st = eng.run(0.0, t1, wl["dt"], 3)
+        fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+        fin["hop_log"] = eng.get_hop_log(eng.cfg.max_hops)
+    finally:
+        eng.close()
+    assert st.traj_steps == n * (whole + 1)
+    o = IO.run_iesh(oracle_model(wl), mass=wl["mass"], ne=10, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"],
+                    dt=wl["dt"], nsteps=whole + 1, seed=3, h_last=t1 - whole * wl["dt"])
+    compare_with_oracle(fin, o, n)

@@ -81,6 +81,27 @@ def test_mdef_fp64_trajectories_match_oracle():
     np.testing.assert_allclose(fin["v"][:, 0], v, rtol=1e-8, atol=1e-12)
 
 
+def test_mdef_fp64_shortened_last_step_matches_oracle():
+    """A time span that is not a whole number of steps: the last BAOAB step is
+    shortened to reach t1, as the reference's integrator does (every sub-step
+    reads integrator.dt, mdef_baoab.jl:163-180), to 1e-8 of the oracle."""
+    n, whole = 32, 100
+    wl = WL.newns_anderson_mdef(n, M=40)
+    t1 = (whole + 0.37) * wl["dt"]
+    eng = make_mdef(wl, n)
+    try:
+        eng.set_initial(wl["x0"].reshape(n, 1).copy(), wl["v0"].reshape(n, 1).copy())
+        _, st = eng.run(0.0, t1, wl["dt"], 99)
+        fin = eng.get_final(1)
+    finally:
+        eng.close()
+    assert st.traj_steps == n * (whole + 1)
+    x, v = MO.run_mdef(oracle_model(wl), mass=wl["mass"], beta=wl["beta"], sigma=wl["sigma"], x0=wl["x0"],
+                       v0=wl["v0"], dt=wl["dt"], nsteps=whole + 1, seed=99, h_last=t1 - whole * wl["dt"])
+    np.testing.assert_allclose(fin["r"][:, 0], x, rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(fin["v"][:, 0], v, rtol=1e-8, atol=1e-12)
+
+
 def run_relax(wl, n, prec, nsteps, stride, surrogate=False, exact_friction_every=0, mlp=None):
     eng = make_mdef(wl, n, prec, save_stride=stride, surrogate=surrogate, exact_friction_every=exact_friction_every)
     try:
