@@ -319,6 +319,15 @@ int nqcd_unpin_host(void* ptr);
  * (TFLOP/s, 2 flops per FMA) with a register-resident FMA chain kernel. */
 int nqcd_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
 
+/* Tensor-core self-test (no counterpart in the reference): D = A B for
+ * A 128 x 80, B 80 x 80 (row-major host arrays, D 128 x 80) on the fifth-
+ * generation tensor cores, kind::tf32 with the accumulator in tensor memory;
+ * passes = 1 rounds A and B to tf32, passes = 3 splits each into tf32 high
+ * and low parts (3xTF32, near fp32 accuracy).  The shape is the one of the
+ * IESH propagator terms.  NQCD_ERR_TIMEOUT if the device wait for the
+ * product gave up. */
+int nqcd_tensor_selftest(int32_t passes, const float* A, const float* B, float* D);
+
 /* Allocation-free plain FP64 spin-boson FSSH ensemble.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory while
  * they run (a Julia host whose CUDA.jl pool owns the device memory, a service

@@ -34,6 +34,7 @@ ENGINE_UNITS = {
     "noalloc.cu": [],
     "mlp.cu": [],
     "kernels_iesh.cu": [],
+    "tensor.cu": [],
 }
 
 
