@@ -16,6 +16,7 @@ struct FsshParams {
     const double* bath_c;     // [ndof] (spin-boson)
     const double* bath_w2;    // [ndof] (spin-boson)
     double sum_c2_over_m;     // sum_j c_j^2 / m_j (spin-boson fast path)
+    float sum_c2_over_m_f;    // the same in FP32 (the fast kernel's hop rescaling)
     // method
     int32_t rescaling;
     int32_t ehrenfest;        // 1: Ehrenfest (mean-field force from sigma, no hopping), 0: FSSH

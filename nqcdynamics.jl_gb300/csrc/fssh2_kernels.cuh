@@ -129,19 +129,28 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<dou
 // weights (sa, sb) = (sa1, sb1) on the first step (the buffer starts at
 // t = 0) and (0, 1) afterwards, which is what the FP64 clock gives; below the
 // gap threshold the FP64 sub-integrator runs on the same relative times.
+// The FP64 sub-integration of a near-degenerate step.  Not inlined, so that
+// none of its conversions to and from FP64 is scheduled into the FP32 path of
+// the steps that do not take it (the FP64 pipe of this GPU runs at 1/64 of
+// the FP32 rate).
+static __device__ __noinline__ void electronics2_fp64_step(const EBuf<float>& buf, bool first, float h, double t0, double dt,
+                                                    Sig2<float>& sg) {
+    const double hd = h;
+    const double tn = first ? t0 + hd : hd, t = first ? t0 : 0.0;
+    EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, 0.0, buf.E0n, buf.E1n, buf.Dn, tn};
+    Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
+    Interp64 fn(b64);
+    electronic_macro_step2<double>(fn, t, hd, dt / 5.0, s64);
+    sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
+}
+
 template <typename P>  // FsshParams or RpshParams
 __device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>& buf, bool first, float h, float gap,
                                                    Sig2<float>& sg, int& nfp64) {
     const float dtsub = p.dtsub;
     if (gap < p.gap_fp64) {
         ++nfp64;  // steps integrated with the FP64 electronics (per-trajectory status)
-        const double hd = h;
-        const double tn = first ? p.t0 + hd : hd, t = first ? p.t0 : 0.0;
-        EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, 0.0, buf.E0n, buf.E1n, buf.Dn, tn};
-        Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
-        Interp64 fn(b64);
-        electronic_macro_step2<double>(fn, t, hd, p.dt / 5.0, s64);
-        sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
+        electronics2_fp64_step(buf, first, h, p.t0, p.dt, sg);
     } else {
         InterpS32 fn(buf, first ? p.sa1 : 0.f, first ? p.sb1 : 1.f);
         electronic_macro_step2_fast(fn, h, dtsub, sg);

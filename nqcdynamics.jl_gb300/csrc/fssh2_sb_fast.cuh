@@ -185,24 +185,28 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
             const float sgn = ns < s ? 1.0f : -1.0f;  // d(new, old) = sgn * c_I * dscale
             bool accept = true;
             if (p.rescaling != RESCALE_OFF) {
-                double aa = 0.5 * (double)dscale * (double)dscale * p.sum_c2_over_m;
-                double bb = (double)sgn * (double)dscale * (double)cv;
-                double cc = (double)w[ns] - (double)w[s];
-                double disc = bb * bb - 4.0 * aa * cc;
-                if (disc < 0.0) {
+                // rescale_velocity! (surface_hopping.jl:64-99) in FP32, the precision of this path:
+                // a = |d|^2/(2m) summed, b = d.v, c = E_new - E_old, disc = b^2 - 4ac.  (FP64 here
+                // cost about ten FP64-pipe instructions per warp and step on average: a warp takes
+                // the branch whenever one of its eight trajectories attempts a hop.)
+                const float aa = 0.5f * dscale * dscale * p.sum_c2_over_m_f;
+                const float bb = sgn * dscale * cv;
+                const float cc = w[ns] - w[s];
+                const float disc = fmaf(bb, bb, -4.0f * aa * cc);
+                if (disc < 0.f) {
                     accept = false;
                     if (p.rescaling == RESCALE_VINVERSION) {
                         // v -= 2 (v.n) n with n = d/|d|, |d|^2 = dscale^2 sum c^2; v.d = sgn dscale c.v
-                        double c2 = 0.0;
-                        for (int I = 0; I < nd; ++I) c2 += (double)bath[I].x * bath[I].x;
-                        float coef = (float)(2.0 * (double)cv / c2);  // 2 (v.d) d_I / |d|^2 = coef * c_I
+                        float c2 = 0.f;
+                        for (int I = 0; I < nd; ++I) c2 = fmaf(bath[I].x, bath[I].x, c2);
+                        const float coef = 2.0f * cv / c2;  // 2 (v.d) d_I / |d|^2 = coef * c_I
 #pragma unroll
                         for (int j = 0; j < NPL; ++j) v[j].add(-coef * bath[lane_g + G * j].x);
                     }
                 } else {
-                    double root = sqrt(disc);
-                    double gamma = bb < 0.0 ? (bb + root) / (2.0 * aa) : (bb - root) / (2.0 * aa);
-                    float coef = (float)(gamma * (double)sgn * (double)dscale);  // gamma d_I / m_I = coef c_I / m_I
+                    const float root = sqrtf(disc);
+                    const float gamma = bb < 0.f ? (bb + root) / (2.0f * aa) : (bb - root) / (2.0f * aa);
+                    const float coef = gamma * sgn * dscale;  // gamma d_I / m_I = coef c_I / m_I
 #pragma unroll
                     for (int j = 0; j < NPL; ++j) {
                         float4 b = bath[lane_g + G * j];

@@ -953,6 +953,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.bath_c = h->d_bath_c;
     p.bath_w2 = h->d_bath_w2;
     p.sum_c2_over_m = h->sum_c2_over_m;
+    p.sum_c2_over_m_f = (float)h->sum_c2_over_m;
     p.rescaling = h->cfg.rescaling;
     p.ehrenfest = h->cfg.method == NQCD_METHOD_EHRENFEST ? 1 : 0;
     p.init_kind = h->cfg.init_kind;
