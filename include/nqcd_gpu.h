@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 106
+#define NQCD_ABI_VERSION 107
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -294,6 +294,25 @@ int nqcd_mlp_loss_grad(nqcd_handle* h, int64_t n, const double* x, const double*
 /* Accepted hops of the last run, [ntraj][max_hops][3] = (step, from, to), -1 padded
  * (DynamicsOutputs.OutputSurfaceHops, src/DynamicsOutputs.jl:235-243). */
 int nqcd_get_hop_log(nqcd_handle* h, int32_t* log);
+
+/* Launch shapes of the fast kernels (no counterpart in the reference: the
+ * thread/warp-per-trajectory mapping that the project's autotuner,
+ * nqcd_gb300/autotune.py, picks by timing the candidates on the GPU).  Zero
+ * fields keep the defaults.  Results do not depend on the mapping except
+ * through the order of floating-point sums inside a trajectory. */
+typedef struct nqcd_mapping {
+    int32_t sb_lanes;    /* fast spin-boson kernel: lanes per trajectory, 4 or 8 (0 = 4; 8 needs
+                            NQCD_PREC_FP32_KAHAN and at most 128 modes) */
+    int32_t sb_block;    /* fast spin-boson kernel: threads per block, 64, 128 or 256 (0 = 128) */
+    int32_t rp_lanes[4]; /* fast ring-polymer kernels: lanes per trajectory for 4, 8, 16 and 32 beads
+                            (0 = 4; 4 beads: 1, 2, 4; 8: 2, 4, 8; 16: 4, 8, 16; 32: 4, 8, 16, 32) */
+    int32_t reserved[2];
+} nqcd_mapping;
+
+/* Set the handle's launch shapes for the following runs; NQCD_ERR_ARG for a
+ * shape outside the lists above, NQCD_ERR_UNSUPPORTED for 8 spin-boson lanes
+ * without Kahan accumulation or with more than 128 modes. */
+int nqcd_set_mapping(nqcd_handle* h, const nqcd_mapping* m);
 
 /* Per-trajectory status of the last nqcd_run (host arrays of ntraj, NULL to
  * skip): nonfinite[t] = 1 where a final position or velocity is not finite

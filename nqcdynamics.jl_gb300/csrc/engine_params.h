@@ -53,6 +53,9 @@ struct FsshParams {
     double* popcorr_partial;  // [nwarps][nsave][4]
     unsigned long long* scatter;  // [4]
     int32_t* fp64_steps;      // [ntraj] fast paths: steps whose electronics ran in FP64 (gap below gap_fp64)
+    // launch shape of the fast spin-boson kernel (nqcd_set_mapping; 0 = default)
+    int32_t sb_group;         // lanes per trajectory: 4 or 8
+    int32_t sb_block;         // threads per block: 64, 128 or 256
 };
 
 // Host launchers (one translation unit per precision).
@@ -61,9 +64,10 @@ cudaError_t launch_fssh2_fp32(const FsshParams& p, cudaStream_t s);
 cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s);
 
 // Threads per trajectory of the kernel that runs (model, precision): the
-// fast spin-boson kernel spreads the bath over a group of 4 lanes.
-inline int fssh2_lanes_per_traj(int model, int precision) {
-    return (model == 10 /* MODEL_SPINBOSON */ && precision != 0 /* FP64 */) ? 4 : 1;
+// fast spin-boson kernel spreads the bath over a group of sb_group lanes (4
+// unless the mapping says 8).
+inline int fssh2_lanes_per_traj(int model, int precision, int sb_group = 4) {
+    return (model == 10 /* MODEL_SPINBOSON */ && precision != 0 /* FP64 */) ? (sb_group == 8 ? 8 : 4) : 1;
 }
 // out[k] = sum over rows p of partial[p][k], deterministic: rows are summed in
 // fixed chunks in parallel (tmp: [reduce_chunks(nparts, width)][width]) and the

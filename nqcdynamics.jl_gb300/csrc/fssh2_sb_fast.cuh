@@ -21,6 +21,8 @@
 // Reference algorithm: fssh2_traj.h (same steps, same random stream).
 #pragma once
 
+#include <type_traits>
+
 #include "fssh2_kernels.cuh"
 
 namespace nqcd {
@@ -34,15 +36,16 @@ __device__ __forceinline__ float group_sum(float x) {
     return x;
 }
 
-constexpr int kSbFastBlock = 128;
-constexpr int kSbGroup = 4;
+constexpr int kSbFastBlock = 128;   // default threads per block
+constexpr int kSbFastBlockMax = 256;
+constexpr int kSbGroup = 4;         // default lanes per trajectory
 
+// G lanes per trajectory (4, or 8 in the variants the autotuner may pick).
 // Ehr = true: Ehrenfest (mean-field force from the density matrix, no
 // hopping); a template parameter so that the surface-hopping instantiation
 // keeps its register allocation.
-template <typename Acc, int NPL, bool Ehr>
-__global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshParams p) {
-    constexpr int G = kSbGroup;
+template <typename Acc, int G, int NPL, bool Ehr>
+__global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const FsshParams p) {
     extern __shared__ float4 bath[];  // (c, w2, 1/m, c^2/m) per mode
     const int nd = p.ndof;
     for (int I = threadIdx.x; I < G * NPL; I += blockDim.x) {
@@ -260,31 +263,39 @@ __global__ void __launch_bounds__(kSbFastBlock) fssh2_sb_fast_kernel(const FsshP
     if (p.scatter) atomicAdd(p.scatter + (p.r[i] > 0.0 ? 2 : 0) + state, 1ull);
 }
 
-template <typename Acc, int NPL>
+template <typename Acc, int G, int NPL>
 cudaError_t launch_sb_fast_npl(const FsshParams& p, cudaStream_t s) {
-    int64_t threads = p.ntraj * kSbGroup;
-    int64_t blocks = (threads + kSbFastBlock - 1) / kSbFastBlock;
-    size_t shmem = sizeof(float4) * kSbGroup * NPL;
+    const int block = p.sb_block > 0 ? p.sb_block : kSbFastBlock;
+    int64_t threads = p.ntraj * G;
+    int64_t blocks = (threads + block - 1) / block;
+    size_t shmem = sizeof(float4) * G * NPL;
     if (p.ehrenfest)
-        fssh2_sb_fast_kernel<Acc, NPL, true><<<(unsigned)blocks, kSbFastBlock, shmem, s>>>(p);
+        fssh2_sb_fast_kernel<Acc, G, NPL, true><<<(unsigned)blocks, block, shmem, s>>>(p);
     else
-        fssh2_sb_fast_kernel<Acc, NPL, false><<<(unsigned)blocks, kSbFastBlock, shmem, s>>>(p);
+        fssh2_sb_fast_kernel<Acc, G, NPL, false><<<(unsigned)blocks, block, shmem, s>>>(p);
     return cudaGetLastError();
 }
+
+// Lane group of 8 (Kahan accumulators), instantiated in their own translation unit.
+cudaError_t launch_sb_fast_g8_kahan(const FsshParams& p, cudaStream_t s);
 
 // modes per lane rounded up to an instantiated size
 template <typename Acc>
 cudaError_t launch_sb_fast(const FsshParams& p, cudaStream_t s) {
     if (p.ntraj <= 0) return cudaSuccess;
+    if (p.sb_group == 8) {
+        if constexpr (std::is_same<Acc, AccKahan>::value) return launch_sb_fast_g8_kahan(p, s);
+        return cudaErrorInvalidValue;
+    }
     int need = (p.ndof + kSbGroup - 1) / kSbGroup;
-    if (need <= 1) return launch_sb_fast_npl<Acc, 1>(p, s);
-    if (need <= 2) return launch_sb_fast_npl<Acc, 2>(p, s);
-    if (need <= 4) return launch_sb_fast_npl<Acc, 4>(p, s);
-    if (need <= 8) return launch_sb_fast_npl<Acc, 8>(p, s);
-    if (need <= 16) return launch_sb_fast_npl<Acc, 16>(p, s);
-    if (need <= 25) return launch_sb_fast_npl<Acc, 25>(p, s);
-    if (need <= 32) return launch_sb_fast_npl<Acc, 32>(p, s);
-    if (need <= 64) return launch_sb_fast_npl<Acc, 64>(p, s);
+    if (need <= 1) return launch_sb_fast_npl<Acc, 4, 1>(p, s);
+    if (need <= 2) return launch_sb_fast_npl<Acc, 4, 2>(p, s);
+    if (need <= 4) return launch_sb_fast_npl<Acc, 4, 4>(p, s);
+    if (need <= 8) return launch_sb_fast_npl<Acc, 4, 8>(p, s);
+    if (need <= 16) return launch_sb_fast_npl<Acc, 4, 16>(p, s);
+    if (need <= 25) return launch_sb_fast_npl<Acc, 4, 25>(p, s);
+    if (need <= 32) return launch_sb_fast_npl<Acc, 4, 32>(p, s);
+    if (need <= 64) return launch_sb_fast_npl<Acc, 4, 64>(p, s);
     return cudaErrorInvalidValue;
 }
 

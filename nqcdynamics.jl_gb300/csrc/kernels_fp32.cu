@@ -19,35 +19,28 @@ cudaError_t launch_fssh2_fp32_kahan(const FsshParams& p, cudaStream_t s) {
     return launch_tully_fast(p, s);
 }
 
-// Fast ring-polymer kernels, one per bead count (see rpsh_group_kernel).
-template <int Q, int GL>
-static int rpsh_group_grid_t() {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, rpsh_group_kernel<Q, GL>, kRpshBlock, 0);
-    return sms * (per > 0 ? per : 1);
-}
-
+// Fast ring-polymer kernels, one per bead count (see rpsh_group_kernel): the
+// default lane-group shapes here, the other shapes a mapping may select in
+// kernels_tune.cu.
 #define NQCD_RP_SHAPES(X) X(1, 1) X(1, 2) X(1, 4) X(5, 1) X(2, 4) X(5, 2) X(4, 4) X(8, 4)
 
-int rpsh_group_grid(int beads) {
+int rpsh_group_grid(int beads, int lanes) {
 #define X(Q, GL) \
-    if (beads == Q * GL) return rpsh_group_grid_t<Q, GL>();
+    if (beads == Q * GL && (lanes == 0 || lanes == GL)) return rpsh_group_grid_t<Q, GL>();
     NQCD_RP_SHAPES(X)
 #undef X
-    return 0;
+    return rpsh_group_grid_tuned(beads, lanes);
 }
 
-cudaError_t launch_rpsh_group(int beads, const RpshParams& p, int blocks, cudaStream_t s) {
+cudaError_t launch_rpsh_group(int beads, int lanes, const RpshParams& p, int blocks, cudaStream_t s) {
 #define X(Q, GL)                                                    \
-    if (beads == Q * GL) {                                          \
+    if (beads == Q * GL && (lanes == 0 || lanes == GL)) {           \
         rpsh_group_kernel<Q, GL><<<blocks, kRpshBlock, 0, s>>>(p); \
         return cudaGetLastError();                                  \
     }
     NQCD_RP_SHAPES(X)
 #undef X
-    return cudaErrorInvalidValue;
+    return launch_rpsh_group_tuned(beads, lanes, p, blocks, s);
 }
 #undef NQCD_RP_SHAPES
 

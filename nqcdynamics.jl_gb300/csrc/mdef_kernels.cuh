@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
     }
     double x = p.x[i], v = p.v[i];
     const double m = p.mass, T = 1.0 / p.beta, dt = p.dt, half = 0.5;
-    const float inv_m_f = (float)(1.0 / m), dt_f = (float)dt, sig_f = (float)sqrt(T / m);
+    const float inv_m_f = (float)(1.0 / m), sig_f = (float)sqrt(T / m);
     double F, fr;
     mdef_electronic<R>(p, sh, wib, lam, x, p.friction_out != nullptr, F, fr);
     if (p.force_out || p.friction_out) {  // single-evaluation mode (force/friction tables, training data)

@@ -26,9 +26,7 @@ using namespace nqcd;
 
 namespace nqcd {
 int rpsh_grid_fp64();
-int rpsh_group_grid(int beads);
 cudaError_t launch_rpsh_fp64(const RpshParams& p, int blocks, cudaStream_t s);
-cudaError_t launch_rpsh_group(int beads, const RpshParams& p, int blocks, cudaStream_t s);
 cudaError_t launch_mdef_fp64(const MdefParams& p, cudaStream_t s);
 cudaError_t launch_mdef_fp32(const MdefParams& p, cudaStream_t s);
 cudaError_t launch_iesh_fp64(const IeshParams& p, cudaStream_t s);
@@ -211,6 +209,7 @@ __global__ void fma_peak_kernel(T* sink, int iters, T seed) {
 // ---------------------------------------------------------------------------
 struct nqcd_handle {
     nqcd_config cfg;
+    nqcd_mapping map = {};  // launch shapes (nqcd_set_mapping); zeros: defaults
     std::string err;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
@@ -346,6 +345,18 @@ int64_t count_steps(double t0, double t1, double dt) {
         ++n;
     }
     return n;
+}
+
+// Lanes per trajectory of the fast ring-polymer kernel of a bead count under
+// the handle's mapping (0: the default shape).
+int rp_lanes_of(const nqcd_handle* h, int beads) {
+    switch (beads) {
+        case 4: return h->map.rp_lanes[0];
+        case 8: return h->map.rp_lanes[1];
+        case 16: return h->map.rp_lanes[2];
+        case 32: return h->map.rp_lanes[3];
+        default: return 0;
+    }
 }
 
 // MDEF launch parameters of a handle (device pointers of the handle).
@@ -901,10 +912,15 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         return fail(h, NQCD_ERR_ARG, "nqcd_run: dt is below the spacing of doubles between t0 and t1");
     const int stride = h->cfg.save_stride;
     const int nsave = stride > 0 ? (int)(nsteps / stride + 1) : 0;
-    const int64_t lanes = mdef ? 32 : (iesh ? 1 : fssh2_lanes_per_traj(h->cfg.model, h->cfg.precision));
-    const int64_t blocks = (N * lanes + 127) / 128;
+    const int64_t lanes =
+        mdef ? 32 : (iesh ? 1 : fssh2_lanes_per_traj(h->cfg.model, h->cfg.precision, h->map.sb_lanes));
+    // the fast spin-boson kernel's block size follows the mapping; the other kernels use 128 threads
+    const bool sb_fast = !mdef && !iesh && h->cfg.method != NQCD_METHOD_RPSH &&
+                         h->cfg.model == NQCD_MODEL_SPINBOSON && h->cfg.precision != NQCD_PREC_FP64;
+    const int64_t blk = sb_fast && h->map.sb_block > 0 ? h->map.sb_block : 128;
+    const int64_t blocks = (N * lanes + blk - 1) / blk;
     // rows of observable partial sums: one per warp (FSSH, MDEF) or per trajectory (IESH)
-    const int64_t nwarps = iesh ? N : blocks * 4;
+    const int64_t nwarps = iesh ? N : blocks * (blk / 32);
     if (nsave > 0 && nwarps * nsave * 4 > h->partial_cap) {
         if (h->d_partial) cudaFree(h->d_partial);
         if (h->d_popcorr) cudaFree(h->d_popcorr);
@@ -954,6 +970,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.bath_w2 = h->d_bath_w2;
     p.sum_c2_over_m = h->sum_c2_over_m;
     p.sum_c2_over_m_f = (float)h->sum_c2_over_m;
+    p.sb_group = h->map.sb_lanes;
+    p.sb_block = h->map.sb_block;
     p.rescaling = h->cfg.rescaling;
     p.ehrenfest = h->cfg.method == NQCD_METHOD_EHRENFEST ? 1 : 0;
     p.init_kind = h->cfg.init_kind;
@@ -1024,7 +1042,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         // persistent grid; blocks start on classes in proportion to their estimated work
         int grid = plain ? rpsh_grid_fp64() : 0;
         for (int k = 0; k < h->nclass && !plain; ++k) {
-            const int gk = rpsh_group_grid(h->class_beads[k]);
+            const int gk = rpsh_group_grid(h->class_beads[k], rp_lanes_of(h, h->class_beads[k]));
             grid = gk > grid ? gk : grid;
         }
         if (grid > kMaxRpGrid) grid = kMaxRpGrid;
@@ -1134,7 +1152,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
                 for (int q = 0; q < h->nclass; ++q) present |= h->class_beads[q] == kRpCounts[c];
                 if (!present) continue;
                 NQCD_CUDA(h, cudaStreamWaitEvent(h->rp_streams[k], h->rp_fork, 0));
-                e = launch_rpsh_group(kRpCounts[c], rq, rpsh_group_grid(kRpCounts[c]), h->rp_streams[k]);
+                const int ln = rp_lanes_of(h, kRpCounts[c]);
+                e = launch_rpsh_group(kRpCounts[c], ln, rq, rpsh_group_grid(kRpCounts[c], ln), h->rp_streams[k]);
                 if (e != cudaSuccess) break;
                 NQCD_CUDA(h, cudaEventRecord(h->rp_join[k], h->rp_streams[k]));
                 NQCD_CUDA(h, cudaStreamWaitEvent(s, h->rp_join[k], 0));
@@ -1569,6 +1588,28 @@ int nqcd_mlp_loss_grad(nqcd_handle* h, int64_t n, const double* x, const double*
     NQCD_CUDA(h, cudaStreamSynchronize(h->stream));
     if (grad) memcpy(grad, g.data(), kMlpN * sizeof(float));
     if (loss) *loss = g[kMlpN];
+    return NQCD_OK;
+}
+
+int nqcd_set_mapping(nqcd_handle* h, const nqcd_mapping* m) {
+    if (!h || !m) return NQCD_ERR_ARG;
+    if (m->sb_lanes != 0 && m->sb_lanes != 4 && m->sb_lanes != 8)
+        return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: sb_lanes must be 0, 4 or 8");
+    if (m->sb_block != 0 && m->sb_block != 64 && m->sb_block != 128 && m->sb_block != 256)
+        return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: sb_block must be 0, 64, 128 or 256");
+    static const int kAllowed[4][4] = {{1, 2, 4, 0}, {2, 4, 8, 0}, {4, 8, 16, 0}, {4, 8, 16, 32}};
+    for (int q = 0; q < 4; ++q) {
+        bool ok = m->rp_lanes[q] == 0;
+        for (int a = 0; a < 4; ++a) ok |= kAllowed[q][a] != 0 && m->rp_lanes[q] == kAllowed[q][a];
+        if (!ok) return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: rp_lanes outside the shapes of its bead count");
+    }
+    if (m->sb_lanes == 8) {
+        const bool sb = h->cfg.model == NQCD_MODEL_SPINBOSON && h->cfg.method != NQCD_METHOD_RPSH;
+        if (sb && (h->cfg.precision != NQCD_PREC_FP32_KAHAN || h->cfg.nbath > 128))
+            return fail(h, NQCD_ERR_UNSUPPORTED,
+                        "nqcd_set_mapping: 8 lanes per trajectory need NQCD_PREC_FP32_KAHAN and at most 128 modes");
+    }
+    h->map = *m;
     return NQCD_OK;
 }
 

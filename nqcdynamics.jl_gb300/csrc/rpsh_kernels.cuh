@@ -712,6 +712,24 @@ cudaError_t launch_rpsh_plain(const RpshParams& p, int blocks, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// Persistent grid of a lane-group kernel: SMs x resident blocks.
+template <int Q, int GL>
+int rpsh_group_grid_t() {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, rpsh_group_kernel<Q, GL>, kRpshBlock, 0);
+    return sms * (per > 0 ? per : 1);
+}
+
+// Lane-group shapes: lanes = 0 takes the default of the bead count; another
+// power of two dividing it (at most 32) selects that shape.  0 when no
+// kernel exists for the shape.
+int rpsh_group_grid(int beads, int lanes);
+cudaError_t launch_rpsh_group(int beads, int lanes, const RpshParams& p, int blocks, cudaStream_t s);
+int rpsh_group_grid_tuned(int beads, int lanes);
+cudaError_t launch_rpsh_group_tuned(int beads, int lanes, const RpshParams& p, int blocks, cudaStream_t s);
+
 // Lane-group shape (beads per lane Q, lanes per trajectory GL) of a bead count.
 inline void rpsh_group_shape(int beads, int& Q, int& GL) {
     switch (beads) {

@@ -116,6 +116,25 @@ class nqcd_sampler(C.Structure):
 SAMPLE_FIXED, SAMPLE_NORMAL, SAMPLE_UNIFORM = 0, 1, 2
 
 
+class nqcd_mapping(C.Structure):
+    """Launch shapes of the fast kernels (nqcd_gpu.h, nqcd_set_mapping)."""
+
+    _fields_ = [("sb_lanes", C.c_int32), ("sb_block", C.c_int32), ("rp_lanes", C.c_int32 * 4),
+                ("reserved", C.c_int32 * 2)]
+
+
+RP_LANE_BEADS = (4, 8, 16, 32)  # bead counts of nqcd_mapping.rp_lanes
+
+
+def mapping(sb_lanes=0, sb_block=0, rp_lanes=None):
+    """nqcd_mapping from keyword values; rp_lanes: {bead count: lanes}."""
+    m = nqcd_mapping()
+    m.sb_lanes, m.sb_block = int(sb_lanes), int(sb_block)
+    for q, b in enumerate(RP_LANE_BEADS):
+        m.rp_lanes[q] = int((rp_lanes or {}).get(b, 0))
+    return m
+
+
 def samplers(specs):
     """ctypes array of nqcd_sampler from (kind, a, b) triples."""
     arr = (nqcd_sampler * len(specs))()
@@ -135,6 +154,7 @@ EXPORTED = [
     "nqcd_get_hop_log",
     "nqcd_get_status",
     "nqcd_set_trajectory_models",
+    "nqcd_set_mapping",
     "nqcd_mdef_evaluate",
     "nqcd_train_friction_mlp",
     "nqcd_mlp_get",
@@ -145,6 +165,7 @@ EXPORTED = [
     "nqcd_pin_host",
     "nqcd_unpin_host",
     "nqcd_measure_fma_peaks",
+    "nqcd_tensor_selftest",
 ]
 
 
@@ -185,6 +206,8 @@ def load(path: Path | str | None = None) -> C.CDLL:
     lib.nqcd_get_hop_log.argtypes = [C.c_void_p, IP]
     lib.nqcd_get_status.argtypes = [C.c_void_p, IP, IP]
     lib.nqcd_set_trajectory_models.argtypes = [C.c_void_p, IP]
+    lib.nqcd_set_mapping.argtypes = [C.c_void_p, C.POINTER(nqcd_mapping)]
+    lib.nqcd_tensor_selftest.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.nqcd_mdef_evaluate.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP]
     lib.nqcd_train_friction_mlp.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32, C.c_int32,
                                             C.c_double, C.c_uint64, DP]
@@ -339,6 +362,12 @@ class Engine:
         self._check(self.lib.nqcd_mlp_loss_grad(self.h, len(x), dptr(x), dptr(t), C.byref(loss),
                                                 g.ctypes.data_as(C.POINTER(C.c_float))))
         return loss.value, g
+
+    def set_mapping(self, m):
+        """Launch shapes for the following runs (nqcd_mapping or a dict of mapping() keywords)."""
+        if isinstance(m, dict):
+            m = mapping(**m)
+        self._check(self.lib.nqcd_set_mapping(self.h, C.byref(m)))
 
     def set_trajectory_models(self, models):
         self._check(self.lib.nqcd_set_trajectory_models(self.h, iptr(np.ascontiguousarray(models, np.int32))))

@@ -35,6 +35,7 @@ ENGINE_UNITS = {
     "mlp.cu": [],
     "kernels_iesh.cu": [],
     "tensor.cu": [],
+    "kernels_tune.cu": [],
 }
 
 

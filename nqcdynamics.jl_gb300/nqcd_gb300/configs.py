@@ -32,6 +32,26 @@ def tully_fssh(L, ntraj, precision, model=1, mass=2000.0, rescaling=0, max_hops=
     return L.Engine(cfg, [p, m])
 
 
+def spinboson_fssh(L, w, c, ntraj, nmodes, precision, save_stride=0, traj_offset=0, method=None):
+    """C2: FSSH (or Ehrenfest) on the Ohmic spin-boson model, unit masses,
+    diabatic pure state 1 (frequencies w, couplings c)."""
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = method or L.METHOD_FSSH, L.MODEL_SPINBOSON, precision
+    cfg.ndofs, cfg.natoms, cfg.nstates = 1, nmodes, 2
+    params = np.array([0.0, 1.0])
+    masses = np.ones(nmodes)
+    c = np.ascontiguousarray(c, np.float64)
+    w = np.ascontiguousarray(w, np.float64)
+    cfg.nparams, cfg.params, cfg.masses = 2, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = nmodes, L.dptr(c), L.dptr(w)
+    cfg.ntraj_max = ntraj
+    cfg.init_kind, cfg.init_state = L.INIT_DIABATIC_PURE, 0
+    cfg.save_stride = save_stride
+    cfg.gap_fp64 = 1e-3
+    cfg.traj_offset = traj_offset
+    return L.Engine(cfg, [params, masses, c, w])
+
+
 def tully_inputs(ntraj, x0=-10.0, p0=10.0, mass=2000.0):
     return np.full((ntraj, 1), x0), np.full((ntraj, 1), p0 / mass)
 

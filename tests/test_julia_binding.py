@@ -60,7 +60,8 @@ def julia_struct(name):
 
 
 @pytest.mark.parametrize("cname,jname", [("nqcd_config", "NqcdConfig"), ("nqcd_outputs", "NqcdOutputs"),
-                                         ("nqcd_stats", "NqcdStats"), ("nqcd_sampler", "NqcdSampler")])
+                                         ("nqcd_stats", "NqcdStats"), ("nqcd_sampler", "NqcdSampler"),
+                                         ("nqcd_mapping", "NqcdMapping")])
 def test_julia_structs_mirror_the_header(cname, jname):
     c = c_struct(cname)
     j = julia_struct(jname)
