@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 107
+#define NQCD_ABI_VERSION 108
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -306,7 +306,11 @@ typedef struct nqcd_mapping {
     int32_t sb_block;    /* fast spin-boson kernel: threads per block, 64, 128 or 256 (0 = 128) */
     int32_t rp_lanes[4]; /* fast ring-polymer kernels: lanes per trajectory for 4, 8, 16 and 32 beads
                             (0 = 4; 4 beads: 1, 2, 4; 8: 2, 4, 8; 16: 4, 8, 16; 32: 4, 8, 16, 32) */
-    int32_t reserved[2];
+    int32_t iesh_cores;  /* IESH FP32 path, products of the propagator's Chebyshev terms: 0 = fifth-generation
+                            tensor cores (tcgen05, the orbitals split into tf32 high and low parts) where
+                            nstates is a multiple of 16 up to 80 and 2 nelectrons <= 128, else CUDA cores;
+                            1 = CUDA cores (FP32 register tiles) */
+    int32_t reserved;
 } nqcd_mapping;
 
 /* Set the handle's launch shapes for the following runs; NQCD_ERR_ARG for a

@@ -59,6 +59,7 @@
 #include "fssh2_traj.h"
 #include "nqcd_math.h"
 #include "secular.h"
+#include "tc_mma.cuh"
 
 namespace nqcd {
 
@@ -114,6 +115,9 @@ struct IeshParams {
     // steps that needed it (null: not counted)
     double gap_fp64;
     int32_t* fp64_steps;
+    // FP32 path: the propagator's products on the tensor cores (tcgen05, iesh_tc_shape); counters[3]
+    // counts waits for them that gave up
+    int32_t tensor;
 };
 
 template <typename R>
@@ -124,9 +128,15 @@ struct alignas(2 * sizeof(R)) Cx {
 // Dynamic shared memory layout of one CTA (identical on host and device).
 struct IeshLayout {
     int N, Ne, Nu, Np, Nep, B;
+    bool tc;  // tensor-core propagator: o_tc replaces At, phiB and out
     size_t o_eps, o_V2, o_lam, o_z2, o_z0, o_w64, o_At, o_phiA, o_phiB, o_out, o_J, o_Jr, o_inv, o_fdu, o_fdi, o_occ,
-        o_unocc, o_piv, o_red, o_misc, o_rph, o_rpq, bytes;
+        o_unocc, o_piv, o_red, o_misc, o_rph, o_rpq, o_tc, tc_sa, bytes;
 };
+
+// The tensor-core propagator handles N states and Ne electrons when N is a
+// multiple of 16 (the MMA's N), at most 80 (three N-column TMEM regions fit
+// the 256 columns of a CTA that shares its SM), and 2 Ne <= 128 (the MMA's M).
+NQCD_HD bool iesh_tc_shape(int N, int Ne) { return N % 16 == 0 && N >= 16 && N <= 80 && Ne >= 1 && 2 * Ne <= 128; }
 
 NQCD_HD size_t iesh_take(size_t& o, size_t bytes) {
     size_t at = o;
@@ -136,9 +146,12 @@ NQCD_HD size_t iesh_take(size_t& o, size_t bytes) {
 
 // B > 1: ring polymer of B beads (per-bead levels and sums, normal-mode scratch).
 template <typename R>
-NQCD_HD IeshLayout iesh_layout(int N, int Ne, int B = 1) {
+NQCD_HD IeshLayout iesh_layout(int N, int Ne, int B = 1, bool tc = false) {
     IeshLayout L;
     L.B = B;
+    L.tc = tc;
+    L.o_tc = 0;
+    L.tc_sa = 0;
     L.N = N;
     L.Ne = Ne;
     L.Nu = N - Ne;
@@ -151,12 +164,29 @@ NQCD_HD IeshLayout iesh_layout(int N, int Ne, int B = 1) {
     L.o_z2 = iesh_take(o, sizeof(R) * L.Np);
     L.o_z0 = iesh_take(o, sizeof(R) * L.Np);
     L.o_w64 = iesh_take(o, sizeof(double) * L.Np);
-    L.o_At = iesh_take(o, sizeof(R) * L.Np * L.Np);
-    L.o_phiA = iesh_take(o, 2 * sizeof(R) * L.Np * L.Nep);
     const size_t pb = 2 * sizeof(R) * (size_t)L.Np * L.Nep;
     const size_t lu = 2 * sizeof(R) * (size_t)L.Nep * (L.Nep + L.Nu);  // S^T and the right-hand sides
-    L.o_phiB = iesh_take(o, lu > pb ? lu : pb);
-    L.o_out = iesh_take(o, 2 * sizeof(R) * L.Np * L.Nep);
+    if (tc) {
+        // [A operand high | A operand low | B operand], tf32 in 4-byte words, K-major core
+        // matrices: the orbital block transposed (2 Ne rows: re, im of each electron) and the
+        // coupling matrix (N rows).  The MMA reads 128 A rows; rows past 2 Ne fall in the next
+        // buffer (their products land in accumulator rows that are never read), so the region
+        // reaches 128 rows past the low buffer's start.  The hop test's LU workspace shares it.
+        L.o_At = 0;
+        L.o_phiA = iesh_take(o, pb);
+        const size_t sa = (size_t)((2 * Ne + 7) / 8 * 8) * N * 4, sb = (size_t)N * N * 4;
+        size_t tr = sa + (sa + sb > (size_t)128 * N * 4 ? sa + sb : (size_t)128 * N * 4);
+        if (lu > tr) tr = lu;
+        L.tc_sa = sa;
+        L.o_tc = iesh_take(o, tr);
+        L.o_phiB = L.o_tc;
+        L.o_out = L.o_tc;
+    } else {
+        L.o_At = iesh_take(o, sizeof(R) * L.Np * L.Np);
+        L.o_phiA = iesh_take(o, pb);
+        L.o_phiB = iesh_take(o, lu > pb ? lu : pb);
+        L.o_out = iesh_take(o, pb);
+    }
     L.o_J = iesh_take(o, sizeof(double) * kIeshMaxTerms);
     L.o_Jr = iesh_take(o, sizeof(R) * kIeshMaxTerms);
     L.o_inv = iesh_take(o, sizeof(double) * kIeshInv);
@@ -383,7 +413,7 @@ __device__ inline double iesh_wall(const IeshParams& p, double z) {  // exp(-a z
 template <typename R, bool RP>
 __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, RP ? p.nbeads : 1);
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, RP ? p.nbeads : 1, p.tensor != 0);
     R* eps = (R*)(smem + L.o_eps);
     R* V2 = (R*)(smem + L.o_V2);
     R* lam = (R*)(smem + L.o_lam);
@@ -428,7 +458,36 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         z2[k] = R(0);
         z0[k] = R(0);
     }
-    for (int q = tid; q < Np * Np; q += nthr) At[q] = R(0);
+    constexpr bool kF32 = std::is_same<R, float>::value;
+    // tensor-core propagator (FP32 path): operands in shared memory, accumulator, phi_{k-2} and the
+    // series sum in TMEM columns of this CTA
+    const bool tcp = kF32 && L.tc;
+    unsigned char* aop_hi = smem + L.o_tc;  // A operand: the orbital block transposed, rows 2 e + (re, im)
+    unsigned char* aop_lo = aop_hi + L.tc_sa;
+    unsigned char* bop = aop_hi + 2 * L.tc_sa;  // B operand: the coupling matrix A (tf32), row i, k = j
+    __shared__ __align__(8) uint64_t tc_bar;
+    __shared__ uint32_t tc_slot;
+    __shared__ int tc_fail;
+    uint32_t tmem = 0, tc_phase = 0;
+    // TMEM columns: a power of two >= 3 N (256 at N = 80: two CTAs share an SM's 512)
+    uint32_t tc_cols = 32;
+    while (tc_cols < 3u * (uint32_t)L.N) tc_cols <<= 1;
+    if constexpr (kF32) {
+        if (tcp) {
+            if (tid == 0) {
+                tc::mbar_init(&tc_bar, 1);
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+                tc_fail = 0;
+            }
+            if (warp == 0) tc::tmem_alloc(&tc_slot, tc_cols);
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            tmem = tc_slot;
+        }
+    }
+    if (!tcp)
+        for (int q = tid; q < Np * Np; q += nthr) At[q] = R(0);
     for (int q = tid; q < Np * Nep; q += nthr) {
         phiA[q] = {R(0), R(0)};
         phiB[q] = {R(0), R(0)};
@@ -497,6 +556,9 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         }
         return lam[j] - lam[i];
     };
+    // A_ij = z0_i z0_j / (l_j - l_i): from the step's matrix, or formed here where the tensor-core layout
+    // keeps only its tf32 copy
+    auto coup = [&](int i, int j) -> R { return tcp ? z0[i] * z0[j] / gap(i, j) : At[j * Np + i]; };
     // ---- ring polymer ----
     // mean over the beads of warp 0 (the same value in every lane)
     auto bead_mean = [&](double x) {
@@ -872,9 +934,26 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             }
         }
         // ---- propagator (wavefunction_dynamics.jl:15-58) ----
-        for (int q = tid; q < N * N; q += nthr) {
-            const int j = q / N, i = q - j * N;
-            At[j * Np + i] = i == j ? R(0) : z0[i] * z0[j] / gap(i, j);
+        if (tcp) {
+            // the coupling matrix rounded to tf32 as the B operand (row i, k = j); rounding to
+            // nearest keeps it antisymmetric, so H_eff stays Hermitian.  Consecutive threads take
+            // consecutive rows: their 16-byte stores fill one core matrix each (no bank conflicts)
+            for (int q = tid; q < N * (N / 4); q += nthr) {
+                const int j4 = q / N, i = q - j4 * N;
+                float4 a;
+                float* av = &a.x;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int j = 4 * j4 + t;
+                    av[t] = i == j ? 0.f : tc::to_tf32((float)(z0[i] * z0[j] / gap(i, j)));
+                }
+                *(float4*)(bop + tc::smem_kmajor_offset(i, 4 * j4, N)) = a;
+            }
+        } else {
+            for (int q = tid; q < N * N; q += nthr) {
+                const int j = q / N, i = q - j * N;
+                At[j * Np + i] = i == j ? R(0) : z0[i] * z0[j] / gap(i, j);
+            }
         }
         __syncthreads();
         const double w = misc[6];
@@ -882,7 +961,14 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         double elo = 1e300, ehi = -1e300;
         if (tid < N) {
             R sacc = R(0);
-            for (int j = 0; j < N; ++j) sacc += fabs(At[j * Np + tid]);
+            if (tcp) {  // row sums of the matrix the tensor cores multiply with
+                for (int j4 = 0; j4 < N / 4; ++j4) {
+                    const float4 a = *(const float4*)(bop + tc::smem_kmajor_offset(tid, 4 * j4, N));
+                    sacc += (R)(fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(a.w));
+                }
+            } else {
+                for (int j = 0; j < N; ++j) sacc += fabs(At[j * Np + tid]);
+            }
             const double rad = fabs(w) * (double)sacc;
             elo = (double)lam[tid] - rad;
             ehi = (double)lam[tid] + rad;
@@ -913,101 +999,259 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             if (tid == 0 && nonconv) atomicAdd(nonconv, 1ull);
         } else {
             nterms += (unsigned long long)K;
-            const R s = (R)misc[10];
-            const R cenr = (R)misc[8], ihwr = (R)misc[9];
-            R dl[4];
+            if (tcp) {
+                if constexpr (kF32) {
+                    // Chebyshev terms on the tensor cores: D = Phi^T A^T (M = 2 Ne orbital components
+                    // padded to 128, N = N states, K = N states) with Phi split into tf32 high and low
+                    // parts (two products) and A in tf32.  Thread (warp w, lane l) owns accumulator row
+                    // tn = 32 (w % 4) + l, i.e. component tcmp (0 re, 1 im) of electron te, and the
+                    // states s0 .. s0 + N/2 - 1 of its half (w / 4); the partner component is lane
+                    // l ^ 1.  TMEM columns: [0, N) D, [N, 2N) phi_{k-2}, [2N, 3N) the series sum.
+                    // phi_{k-1} is read back as the high + low tf32 pair the tensor cores multiply
+                    // (2^-22 relative), so the whole of Ht phi_{k-1} has that precision.
+                    const float st = (float)misc[10];
+                    const float cenf = (float)misc[8], ihwf = (float)misc[9];
+                    const int tq = warp & 3, NH = N >> 1, s0 = (warp >> 2) * NH;
+                    const int tn = 32 * tq + lane, te = tn >> 1, tcmp = tn & 1;
+                    const bool twarp = 32 * tq < 2 * Ne;  // warp-uniform: the warp holds orbital rows
+                    const bool trow = tn < 2 * Ne;
+                    const uint32_t tl = tmem + ((uint32_t)(32 * tq) << 16);
+                    const uint32_t cD = 0, cP = (uint32_t)N, cO = 2u * (uint32_t)N;
+                    const float sgn = tcmp ? -1.f : 1.f;
+                    // phi_{k-1} of this thread's states i0 .. i0 + 7 from the A operand (zero off the rows)
+                    auto get_a = [&](int i0, float (&v)[8]) {
+                        if (!trow) {
 #pragma unroll
-            for (int rr = 0; rr < 4; ++rr) dl[rr] = (lam[i0 + RG * rr] - cenr) * ihwr;
-            if (tile_on) {
-                const R j0 = (R)misc[11];
+                            for (int t = 0; t < 8; ++t) v[t] = 0.f;
+                            return;
+                        }
+                        const uint32_t o0 = tc::smem_kmajor_offset(tn, i0, N), o1 = tc::smem_kmajor_offset(tn, i0 + 4, N);
+                        const float4 h0 = *(const float4*)(aop_hi + o0), h1 = *(const float4*)(aop_hi + o1);
+                        const float4 l0 = *(const float4*)(aop_lo + o0), l1 = *(const float4*)(aop_lo + o1);
+                        v[0] = h0.x + l0.x; v[1] = h0.y + l0.y; v[2] = h0.z + l0.z; v[3] = h0.w + l0.w;
+                        v[4] = h1.x + l1.x; v[5] = h1.y + l1.y; v[6] = h1.z + l1.z; v[7] = h1.w + l1.w;
+                    };
+                    // A operand (rows tn, k = states i0 .. i0 + 7) from 8 values, high and low tf32 parts
+                    auto put_a = [&](int i0, const float (&v)[8]) {
+                        if (!trow) return;
+                        float4 h0, h1, l0, l1;
+                        float* hv0 = &h0.x; float* hv1 = &h1.x; float* lv0 = &l0.x; float* lv1 = &l1.x;
 #pragma unroll
-                for (int rr = 0; rr < 4; ++rr)
+                        for (int t = 0; t < 4; ++t) {
+                            hv0[t] = tc::to_tf32(v[t]);
+                            lv0[t] = tc::to_tf32(v[t] - hv0[t]);
+                            hv1[t] = tc::to_tf32(v[4 + t]);
+                            lv1[t] = tc::to_tf32(v[4 + t] - hv1[t]);
+                        }
+                        const uint32_t o0 = tc::smem_kmajor_offset(tn, i0, N), o1 = tc::smem_kmajor_offset(tn, i0 + 4, N);
+                        *(float4*)(aop_hi + o0) = h0;
+                        *(float4*)(aop_hi + o1) = h1;
+                        *(float4*)(aop_lo + o0) = l0;
+                        *(float4*)(aop_lo + o1) = l1;
+                    };
+                    // phi_0 = psi; series sum J_0 phi_0
+                    if (twarp) {
+                        const float j0 = (float)misc[11];
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
-                        const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
-                        const Cx<R> x = phiA[ix];
-                        outb[ix] = {j0 * x.re, j0 * x.im};
-                    }
-            }
-            for (int kk = 1; kk <= K; ++kk) {
-                // phi_k = 2 Ht phi_{k-1} - phi_{k-2}: dst holds phi_{k-2} on entry and
-                // each thread reads back only its own tile before overwriting it
-                const Cx<R>* src = (kk & 1) ? phiA : phiB;
-                Cx<R>* dst = (kk & 1) ? phiB : phiA;
-                __syncthreads();
-                if (tile_on) {
-                    R ar[4][4], ai[4][4];
+                        for (int q = 0; q < 5; ++q) {
+                            if (8 * q >= NH) break;
+                            float v[8], o[8];
 #pragma unroll
-                    for (int rr = 0; rr < 4; ++rr)
-#pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) ar[rr][cc] = ai[rr][cc] = R(0);
-                    for (int j = 0; j < N; ++j) {
-                        const R* aj = At + j * Np + i0;
-                        const Cx<R>* pj = src + j * Nep + c0;
-                        R av[4];
-                        Cx<R> pv[4];
-#pragma unroll
-                        for (int rr = 0; rr < 4; ++rr) av[rr] = aj[RG * rr];
-#pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) pv[cc] = pj[CG * cc];
-#pragma unroll
-                        for (int rr = 0; rr < 4; ++rr)
-#pragma unroll
-                            for (int cc = 0; cc < 4; ++cc) {
-                                ar[rr][cc] += av[rr] * pv[cc].re;
-                                ai[rr][cc] += av[rr] * pv[cc].im;
+                            for (int t = 0; t < 8; ++t) {
+                                const Cx<R> x = phiA[(s0 + 8 * q + t) * Nep + (trow ? te : 0)];
+                                v[t] = trow ? (tcmp ? x.im : x.re) : 0.f;
+                                o[t] = j0 * v[t];
                             }
+                            tc::st8(tl + cO + s0 + 8 * q, o);
+                            put_a(s0 + 8 * q, v);
+                        }
+                        tc::wait_st();
                     }
-                    const R jk = Jr[kk];
-                    const int ph = kk & 3;
+                    tc::fence_proxy_async();
+                    tc::fence_before_sync();
+                    __syncthreads();
+                    constexpr uint32_t kPolls = 1u << 20;  // a product takes about a microsecond
+                    for (int kk = 1; kk <= K; ++kk) {
+                        if (tid == 0) {
+                            tc::fence_after_sync();
+                            const uint32_t idesc = tc::idesc_f32acc(tc::kTypeTF32, 128, N);
+                            const uint32_t sbo = (uint32_t)N * 32u, ah = tc::smem_u32(aop_hi),
+                                           al = tc::smem_u32(aop_lo), bb = tc::smem_u32(bop);
+                            for (int ks = 0; ks < N / 8; ++ks)
+                                tc::mma<tc::kTypeTF32>(tmem + cD, tc::smem_desc(ah + 256u * ks, 128, sbo),
+                                                       tc::smem_desc(bb + 256u * ks, 128, sbo), idesc, ks > 0);
+                            for (int ks = 0; ks < N / 8; ++ks)
+                                tc::mma<tc::kTypeTF32>(tmem + cD, tc::smem_desc(al + 256u * ks, 128, sbo),
+                                                       tc::smem_desc(bb + 256u * ks, 128, sbo), idesc, true);
+                            tc::commit(&tc_bar);
+                        }
+                        const bool ok = tc::mbar_wait(&tc_bar, tc_phase, kPolls);
+                        tc_phase ^= 1u;
+                        if (__syncthreads_or(!ok)) {  // record and stop the series; psi keeps the partial sum
+                            if (tid == 0) tc_fail = 1;
+                            break;
+                        }
+                        tc::fence_after_sync();
+                        if (twarp) {
+                            const float jk = (float)Jr[kk];
+                            const int ph = kk & 3;
 #pragma unroll
+                            for (int q = 0; q < 5; ++q) {
+                                if (8 * q >= NH) break;
+                                const int i0 = s0 + 8 * q;
+                                float d[8], p2[8], o[8], nw[8], p1[8];
+                                get_a(i0, p1);
+                                tc::ld8(tl + cD + i0, d);
+                                if (kk > 1) tc::ld8(tl + cP + i0, p2);
+                                tc::ld8(tl + cO + i0, o);
+                                tc::wait_ld();
+#pragma unroll
+                                for (int t = 0; t < 8; ++t) {
+                                    // Ht phi = dl phi - i s (A phi): the partner lane holds the other component
+                                    const float dp = __shfl_xor_sync(0xffffffffu, d[t], 1);
+                                    const float dl = (lam[i0 + t] - cenf) * ihwf;
+                                    const float hv = dl * p1[t] + sgn * st * dp;
+                                    nw[t] = kk == 1 ? hv : 2.f * hv - p2[t];
+                                    const float np = __shfl_xor_sync(0xffffffffu, nw[t], 1);
+                                    // series sum += 2 J_k (-i)^k phi_k
+                                    if (ph == 0) o[t] += jk * nw[t];
+                                    else if (ph == 1) o[t] += sgn * jk * np;
+                                    else if (ph == 2) o[t] -= jk * nw[t];
+                                    else o[t] -= sgn * jk * np;
+                                    p2[t] = p1[t];
+                                }
+                                tc::st8(tl + cP + i0, p2);
+                                tc::st8(tl + cO + i0, o);
+                                put_a(i0, nw);
+                            }
+                            tc::wait_st();
+                        }
+                        tc::fence_proxy_async();
+                        tc::fence_before_sync();
+                        __syncthreads();
+                    }
+                    tc::fence_after_sync();
+                    // psi = exp(-i c h) sum
+                    const float snf = (float)misc[1], csf = (float)misc[2];
+                    if (twarp) {
+#pragma unroll
+                        for (int q = 0; q < 5; ++q) {
+                            if (8 * q >= NH) break;
+                            const int i0 = s0 + 8 * q;
+                            float o[8];
+                            tc::ld8(tl + cO + i0, o);
+                            tc::wait_ld();
+#pragma unroll
+                            for (int t = 0; t < 8; ++t) {
+                                const float op = __shfl_xor_sync(0xffffffffu, o[t], 1);
+                                const float val = tcmp ? o[t] * csf - op * snf : o[t] * csf + op * snf;
+                                if (trow) {
+                                    Cx<R>& c = phiA[(i0 + t) * Nep + te];
+                                    if (tcmp) c.im = val; else c.re = val;
+                                }
+                            }
+                        }
+                    }
+                    tc::fence_before_sync();
+                    __syncthreads();
+                }
+            } else {
+                const R s = (R)misc[10];
+                const R cenr = (R)misc[8], ihwr = (R)misc[9];
+                R dl[4];
+    #pragma unroll
+                for (int rr = 0; rr < 4; ++rr) dl[rr] = (lam[i0 + RG * rr] - cenr) * ihwr;
+                if (tile_on) {
+                    const R j0 = (R)misc[11];
+    #pragma unroll
                     for (int rr = 0; rr < 4; ++rr)
-#pragma unroll
+    #pragma unroll
                         for (int cc = 0; cc < 4; ++cc) {
                             const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
-                            const Cx<R> cur = src[ix];
-                            // Ht phi = dl phi - i s (A phi)
-                            const R hre = dl[rr] * cur.re + s * ai[rr][cc];
-                            const R him = dl[rr] * cur.im - s * ar[rr][cc];
-                            Cx<R> nw;
-                            if (kk == 1) {
-                                nw = {hre, him};
-                            } else {
-                                const Cx<R> pr = dst[ix];
-                                nw = {R(2) * hre - pr.re, R(2) * him - pr.im};
-                            }
-                            dst[ix] = nw;
-                            Cx<R> o = outb[ix];
-                            if (ph == 0) {
-                                o.re += jk * nw.re;
-                                o.im += jk * nw.im;
-                            } else if (ph == 1) {  // (-i) nw
-                                o.re += jk * nw.im;
-                                o.im -= jk * nw.re;
-                            } else if (ph == 2) {
-                                o.re -= jk * nw.re;
-                                o.im -= jk * nw.im;
-                            } else {  // (+i) nw
-                                o.re -= jk * nw.im;
-                                o.im += jk * nw.re;
-                            }
-                            outb[ix] = o;
+                            const Cx<R> x = phiA[ix];
+                            outb[ix] = {j0 * x.re, j0 * x.im};
                         }
                 }
-            }
-            __syncthreads();
-            const R snr = (R)misc[1], csr = (R)misc[2];
-            if (tile_on) {
-#pragma unroll
-                for (int rr = 0; rr < 4; ++rr)
-#pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
-                        const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
-                        const Cx<R> o = outb[ix];
-                        phiA[ix] = {o.re * csr + o.im * snr, o.im * csr - o.re * snr};
+                for (int kk = 1; kk <= K; ++kk) {
+                    // phi_k = 2 Ht phi_{k-1} - phi_{k-2}: dst holds phi_{k-2} on entry and
+                    // each thread reads back only its own tile before overwriting it
+                    const Cx<R>* src = (kk & 1) ? phiA : phiB;
+                    Cx<R>* dst = (kk & 1) ? phiB : phiA;
+                    __syncthreads();
+                    if (tile_on) {
+                        R ar[4][4], ai[4][4];
+    #pragma unroll
+                        for (int rr = 0; rr < 4; ++rr)
+    #pragma unroll
+                            for (int cc = 0; cc < 4; ++cc) ar[rr][cc] = ai[rr][cc] = R(0);
+                        for (int j = 0; j < N; ++j) {
+                            const R* aj = At + j * Np + i0;
+                            const Cx<R>* pj = src + j * Nep + c0;
+                            R av[4];
+                            Cx<R> pv[4];
+    #pragma unroll
+                            for (int rr = 0; rr < 4; ++rr) av[rr] = aj[RG * rr];
+    #pragma unroll
+                            for (int cc = 0; cc < 4; ++cc) pv[cc] = pj[CG * cc];
+    #pragma unroll
+                            for (int rr = 0; rr < 4; ++rr)
+    #pragma unroll
+                                for (int cc = 0; cc < 4; ++cc) {
+                                    ar[rr][cc] += av[rr] * pv[cc].re;
+                                    ai[rr][cc] += av[rr] * pv[cc].im;
+                                }
+                        }
+                        const R jk = Jr[kk];
+                        const int ph = kk & 3;
+    #pragma unroll
+                        for (int rr = 0; rr < 4; ++rr)
+    #pragma unroll
+                            for (int cc = 0; cc < 4; ++cc) {
+                                const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
+                                const Cx<R> cur = src[ix];
+                                // Ht phi = dl phi - i s (A phi)
+                                const R hre = dl[rr] * cur.re + s * ai[rr][cc];
+                                const R him = dl[rr] * cur.im - s * ar[rr][cc];
+                                Cx<R> nw;
+                                if (kk == 1) {
+                                    nw = {hre, him};
+                                } else {
+                                    const Cx<R> pr = dst[ix];
+                                    nw = {R(2) * hre - pr.re, R(2) * him - pr.im};
+                                }
+                                dst[ix] = nw;
+                                Cx<R> o = outb[ix];
+                                if (ph == 0) {
+                                    o.re += jk * nw.re;
+                                    o.im += jk * nw.im;
+                                } else if (ph == 1) {  // (-i) nw
+                                    o.re += jk * nw.im;
+                                    o.im -= jk * nw.re;
+                                } else if (ph == 2) {
+                                    o.re -= jk * nw.re;
+                                    o.im -= jk * nw.im;
+                                } else {  // (+i) nw
+                                    o.re -= jk * nw.im;
+                                    o.im += jk * nw.re;
+                                }
+                                outb[ix] = o;
+                            }
                     }
+                }
+                __syncthreads();
+                const R snr = (R)misc[1], csr = (R)misc[2];
+                if (tile_on) {
+    #pragma unroll
+                    for (int rr = 0; rr < 4; ++rr)
+    #pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) {
+                            const int ix = (i0 + RG * rr) * Nep + c0 + CG * cc;
+                            const Cx<R> o = outb[ix];
+                            phiA[ix] = {o.re * csr + o.im * snr, o.im * csr - o.re * snr};
+                        }
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
 
         if (!ena) {  // EhrenfestNA: no hopping
@@ -1143,7 +1387,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             // sum |v.d| over unoccupied rows and electrons (the estimate's sum(abs, v_dot_d))
             for (int q = tid - 32; q < Nu * Ne; q += nthr - 32) {
                 const int mm = q / Ne, n = q - mm * Ne;
-                sabs += fabs(At[occ[n] * Np + unocc[mm]]);
+                sabs += fabs(coup(unocc[mm], occ[n]));
             }
         }
         double sumabs;
@@ -1203,7 +1447,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 // p_mn = 2 dt Re(Y_nm) (v.d)_mn, (v.d)_mn = -w A[m][state n]
                 const int m = unocc[mm];
                 for (int n = 0; n < Ne; ++n) {
-                    const double vdd = -wh * (double)At[occ[n] * Np + m];
+                    const double vdd = -wh * (double)coup(m, occ[n]);
                     const double pr = clamp01<double>(2.0 * dt * (double)Rh[n * Nu + mm].re * vdd);
                     Rh[n * Nu + mm].re = (R)pr;
                 }
@@ -1342,6 +1586,14 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             atomicAdd(p.counters + 1, nterms);
         }
     }
+    if constexpr (kF32) {
+        if (tcp) {
+            if (tid == 0 && tc_fail && p.counters) atomicAdd(p.counters + 3, 1ull);
+            tc::fence_before_sync();
+            __syncthreads();
+            if (warp == 0) tc::tmem_dealloc(tmem, tc_cols);
+        }
+    }
 }
 
 template <typename R>
@@ -1360,7 +1612,7 @@ cudaError_t launch_iesh(const IeshParams& p, cudaStream_t s) {
     if (p.ntraj <= 0) return cudaSuccess;
     const bool rp = p.nbeads > 1;
     if (rp && (p.nbeads > kRpIeshMaxBeads || p.nelec > kRpIeshMaxElectrons)) return cudaErrorInvalidValue;
-    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, rp ? p.nbeads : 1);
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, rp ? p.nbeads : 1, p.tensor != 0);
     cudaError_t e = cudaFuncSetAttribute(rp ? rpiesh_kernel<R> : iesh_kernel<R>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
     if (e != cudaSuccess) return e;

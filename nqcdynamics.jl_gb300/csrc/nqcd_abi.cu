@@ -1209,6 +1209,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.counters = h->d_counts + 8;
         q.gap_fp64 = h->cfg.precision == NQCD_PREC_FP64 ? 0.0 : h->cfg.gap_fp64;
         q.fp64_steps = h->d_fp64steps;
+        q.tensor = (h->cfg.precision != NQCD_PREC_FP64 && h->map.iesh_cores == 0 &&
+                    iesh_tc_shape(q.nstates, q.nelec)) ? 1 : 0;
         q.nbeads = h->rp_beads;
         if (h->rp_beads > 1) {
             // ring polymer: normal modes and full-step Cayley matrices of the free ring polymer
@@ -1351,6 +1353,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         stats->d2h_bytes = d2h;
         stats->kernel_launches = launches;
     }
+    if (iesh && counts[11] > 0)
+        return fail(h, NQCD_ERR_TIMEOUT, "nqcd_run: a wait for the tensor-core propagator gave up");
     if (counts[7] > 0) return fail(h, NQCD_ERR_NAN, "nqcd_run: non-finite final positions or velocities");
     return NQCD_OK;
 }
@@ -1603,6 +1607,8 @@ int nqcd_set_mapping(nqcd_handle* h, const nqcd_mapping* m) {
         for (int a = 0; a < 4; ++a) ok |= kAllowed[q][a] != 0 && m->rp_lanes[q] == kAllowed[q][a];
         if (!ok) return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: rp_lanes outside the shapes of its bead count");
     }
+    if (m->iesh_cores != 0 && m->iesh_cores != 1)
+        return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: iesh_cores must be 0 (tensor cores) or 1 (CUDA cores)");
     if (m->sb_lanes == 8) {
         const bool sb = h->cfg.model == NQCD_MODEL_SPINBOSON && h->cfg.method != NQCD_METHOD_RPSH;
         if (sb && (h->cfg.precision != NQCD_PREC_FP32_KAHAN || h->cfg.nbath > 128))

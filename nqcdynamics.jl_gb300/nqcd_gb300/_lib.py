@@ -120,16 +120,17 @@ class nqcd_mapping(C.Structure):
     """Launch shapes of the fast kernels (nqcd_gpu.h, nqcd_set_mapping)."""
 
     _fields_ = [("sb_lanes", C.c_int32), ("sb_block", C.c_int32), ("rp_lanes", C.c_int32 * 4),
-                ("reserved", C.c_int32 * 2)]
+                ("iesh_cores", C.c_int32), ("reserved", C.c_int32)]
 
 
 RP_LANE_BEADS = (4, 8, 16, 32)  # bead counts of nqcd_mapping.rp_lanes
 
 
-def mapping(sb_lanes=0, sb_block=0, rp_lanes=None):
-    """nqcd_mapping from keyword values; rp_lanes: {bead count: lanes}."""
+def mapping(sb_lanes=0, sb_block=0, rp_lanes=None, iesh_cores=0):
+    """nqcd_mapping from keyword values; rp_lanes: {bead count: lanes};
+    iesh_cores: 0 tensor cores, 1 CUDA cores for the IESH propagator."""
     m = nqcd_mapping()
-    m.sb_lanes, m.sb_block = int(sb_lanes), int(sb_block)
+    m.sb_lanes, m.sb_block, m.iesh_cores = int(sb_lanes), int(sb_block), int(iesh_cores)
     for q, b in enumerate(RP_LANE_BEADS):
         m.rp_lanes[q] = int((rp_lanes or {}).get(b, 0))
     return m
