@@ -9,8 +9,9 @@ workload:
   spin-boson FSSH, Kahan-accumulated fast kernel: lanes per trajectory
       (4, 8) x threads per block (64, 128, 256);
   ring-polymer FSSH: lanes per trajectory of each bead count's kernel
-      (4 beads: 1, 2, 4; 8: 2, 4, 8; 16: 4, 8, 16; 32: 4, 8, 16, 32), each
-      timed on an ensemble of that bead count alone.
+      (4 beads: 1, 2, 4; 8: 2, 4, 8; 16: 4, 8, 16; 32: 4, 8, 16, 32), by
+      coordinate descent on the mixed C3 ensemble (the four kernels run
+      concurrently, so a shape is judged by the whole ensemble's time).
 
 The committed cache (tuned/mappings.json) holds the sweeps measured on a
 GB300; NQCD_TUNE_CACHE names another file.  `mapping_for` returns the cached
@@ -81,27 +82,35 @@ def tune_spinboson(L, ntraj=100_000, nmodes=100, t1=20.0, dt=0.05, repeats=3):
     return dict(sb_lanes=best["sb_lanes"], sb_block=best["sb_block"]), rows
 
 
-def tune_rpsh(L, ntraj=20_000, repeats=2):
-    """Sweep of the ring-polymer fast kernels: for each bead count, an
-    ensemble of that bead count alone (Tully 1-3 round robin, C3's momenta,
-    termination at |x| > 10); returns (best rp_lanes dict, sweep rows)."""
-    r0, v0, _, models = C.rpsh_inputs(ntraj)
-    best, rows = {}, []
-    for beads, cands in RP_LANES.items():
-        nb = np.full(ntraj, beads, np.int32)
-        eng = C.rpsh_tully(L, ntraj, L.PREC_FP32)
-        try:
-            eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0), nbeads=nb)
-            eng.set_trajectory_models(np.ascontiguousarray(models))
-            timing = {}
-            for lanes in cands:
-                eng.set_mapping(dict(rp_lanes={beads: lanes}))
-                ms = _best_kernel_ms(eng, lambda: eng.run(0.0, 20000.0, 1.0, WL.SEED), repeats)
-                timing[lanes] = ms
-                rows.append(dict(beads=beads, lanes=lanes, kernel_ms=ms))
-            best[beads] = min(timing, key=timing.get)
-        finally:
-            eng.close()
+def tune_rpsh(L, ntraj=50_000, repeats=2):
+    """Sweep of the ring-polymer fast kernels on the mixed ensemble of C3
+    (Tully 1-3 round robin, bead counts 4-32 mixed, C3's momenta,
+    termination at |x| > 10), where the four bead-count kernels run
+    concurrently and share the SMs: coordinate descent from the defaults,
+    one bead count at a time over its lane groups with the others fixed.
+    Returns (best rp_lanes dict, sweep rows)."""
+    r0, v0, nb, models = C.rpsh_inputs(ntraj)
+    eng = C.rpsh_tully(L, ntraj, L.PREC_FP32)
+    best = {b: 4 for b in RP_LANES}
+    rows = []
+    try:
+        eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0), nbeads=np.ascontiguousarray(nb))
+        eng.set_trajectory_models(np.ascontiguousarray(models))
+        timed = {}
+
+        def time_of(mp):
+            key = tuple(sorted(mp.items()))
+            if key not in timed:
+                eng.set_mapping(dict(rp_lanes=mp))
+                timed[key] = _best_kernel_ms(eng, lambda: eng.run(0.0, 20000.0, 1.0, WL.SEED), repeats)
+                rows.append(dict(rp_lanes={str(k): v for k, v in mp.items()}, kernel_ms=timed[key]))
+            return timed[key]
+
+        for beads, cands in RP_LANES.items():
+            trial = {lanes: time_of(dict(best, **{beads: lanes})) for lanes in cands}
+            best[beads] = min(trial, key=trial.get)
+    finally:
+        eng.close()
     return dict(rp_lanes=best), rows
 
 
@@ -111,7 +120,7 @@ TUNERS = {"spinboson": tune_spinboson, "rpsh": tune_rpsh}
 def workload_key(workload: str, **kw) -> str:
     if workload == "spinboson":
         return f"spinboson_modes{kw.get('nmodes', 100)}_traj{kw.get('ntraj', 100_000)}"
-    return "rpsh_tully123"
+    return f"rpsh_tully123_mixed_traj{kw.get('ntraj', 50_000)}"
 
 
 def tune(L, workload: str, **kw) -> dict:
