@@ -69,6 +69,8 @@ def parse():
                     choices=["spinboson", "tully1", "rpsh", "mdef", "iesh", "ehrenfest", "ehrenfest_na", "rpmdef",
                              "rpiesh"])
     ap.add_argument("--nsteps", type=int, default=0, help="secondary workloads: nuclear steps of the fast path")
+    ap.add_argument("--iesh-cores", type=int, default=0, choices=[0, 1],
+                    help="IESH/EhrenfestNA/ring-polymer IESH FP32 propagator: 0 tensor cores, 1 CUDA cores")
     return ap.parse_args()
 
 
@@ -529,6 +531,7 @@ def secondary(args, dist):
             fin = {}
             for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
                 eng = C.iesh_newns_anderson(L, wl, nt, prec, traj_offset=rank_off * n, nbeads=B)
+                eng.set_mapping(dict(iesh_cores=args.iesh_cores))
                 eng.set_initial(np.ascontiguousarray(wl["r0"][:nt]), np.ascontiguousarray(wl["v0"][:nt]))
                 sub = name != "fp32"
                 res[name] = _timed(eng, lambda: eng.run(0.0, nsteps * wl["dt"], wl["dt"], seed),
@@ -587,6 +590,7 @@ def secondary(args, dist):
             for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
                 eng = C.iesh_newns_anderson(L, wl, nt, prec, save_stride=stride, traj_offset=rank_off * n,
                                             method=L.METHOD_EHRENFEST_NA if wk == "ehrenfest_na" else L.METHOD_IESH)
+                eng.set_mapping(dict(iesh_cores=args.iesh_cores))
                 eng.set_initial(np.ascontiguousarray(wl["r0"][:nt]), np.ascontiguousarray(wl["v0"][:nt]))
                 ob = np.zeros((nsteps // stride + 1) * 4)
                 sub = name != "fp32"
@@ -603,6 +607,7 @@ def secondary(args, dist):
             terms = st.propagator_terms / max(1, st.traj_steps)
             cfg = {"workload": ("ehrenfest_na" if wk == "ehrenfest_na" else "iesh") + "_newns_anderson_80states_40e_3dof_traj20k_dt0.1fs", "ntraj_per_gpu": n,
                    "nsteps": nsteps, "chebyshev_terms_per_step": terms,
+                   "propagator_products": "CUDA cores" if args.iesh_cores else "tcgen05 tensor cores (tf32 high/low)",
                    "full_hop_evaluations_per_step": st.hop_evaluations / max(1, st.traj_steps)}
             ref_flops = 3.5e7
             kname = "iesh_kernel<float>"

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 108
+#define NQCD_ABI_VERSION 109
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -310,7 +310,9 @@ typedef struct nqcd_mapping {
                             tensor cores (tcgen05, the orbitals split into tf32 high and low parts) where
                             nstates is a multiple of 16 up to 80 and 2 nelectrons <= 128, else CUDA cores;
                             1 = CUDA cores (FP32 register tiles) */
-    int32_t reserved;
+    int32_t rp_one_launch; /* fast ring-polymer path: 0 = one persistent kernel per bead count, concurrent
+                              on forked streams; 1 = one persistent launch serving every bead count
+                              (default lane groups) with a refill over all classes */
 } nqcd_mapping;
 
 /* Set the handle's launch shapes for the following runs; NQCD_ERR_ARG for a

@@ -44,7 +44,7 @@ export EnsembleGB300, install_keyed_hop_stream!, with_keyed_hops, keyed_fermi_di
 # C ABI (include/nqcd_gpu.h)
 # ---------------------------------------------------------------------------
 
-const ABI_VERSION = Int32(108)
+const ABI_VERSION = Int32(109)
 
 const METHOD_FSSH = Int32(1)
 const METHOD_RPSH = Int32(2)
@@ -152,7 +152,7 @@ struct NqcdMapping
     sb_block::Int32
     rp_lanes::NTuple{4,Int32}
     iesh_cores::Int32
-    reserved::Int32
+    rp_one_launch::Int32
 end
 
 zero_stats() = NqcdStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0.0)

@@ -41,4 +41,46 @@ cudaError_t launch_rpsh_group_tuned(int beads, int lanes, const RpshParams& p, i
 }
 #undef NQCD_RP_TUNED_SHAPES
 
+// One persistent launch for every bead count (the mapping's rp_one_launch):
+// each block starts on the class the host gave it and then helps the other
+// classes as their queues drain (a refill of the whole grid), calling the
+// class loop of its bead count's default lane-group shape.  The loops are
+// not inlined, so each keeps its own register allocation, but the launch
+// reserves the registers of the largest for every warp; the autotuner times
+// this against the concurrent per-bead-count kernels.
+template <int Q, int GL>
+static __device__ __noinline__ void rp_serve_class_call(const RpshParams& p, int cls) {
+    rp_serve_class<Q, GL>(p, cls);
+}
+
+__global__ void __launch_bounds__(kRpshBlock) rpsh_one_launch_kernel(const RpshParams p) {
+    int cls = p.block_class[blockIdx.x];
+    for (int visited = 0; visited < p.nclass; ++visited, cls = (cls + 1) % p.nclass) {
+        switch (p.class_beads[cls]) {
+            case 1: rp_serve_class_call<1, 1>(p, cls); break;
+            case 2: rp_serve_class_call<1, 2>(p, cls); break;
+            case 4: rp_serve_class_call<1, 4>(p, cls); break;
+            case 5: rp_serve_class_call<5, 1>(p, cls); break;
+            case 8: rp_serve_class_call<2, 4>(p, cls); break;
+            case 10: rp_serve_class_call<5, 2>(p, cls); break;
+            case 16: rp_serve_class_call<4, 4>(p, cls); break;
+            case 32: rp_serve_class_call<8, 4>(p, cls); break;
+            default: break;  // the host admits only these bead counts
+        }
+    }
+}
+
+int rpsh_one_launch_grid() {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, rpsh_one_launch_kernel, kRpshBlock, 0);
+    return sms * (per > 0 ? per : 1);
+}
+
+cudaError_t launch_rpsh_one(const RpshParams& p, int blocks, cudaStream_t s) {
+    rpsh_one_launch_kernel<<<blocks, kRpshBlock, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
 }  // namespace nqcd

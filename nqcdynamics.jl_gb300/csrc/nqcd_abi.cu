@@ -1040,8 +1040,9 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
                 return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_run: ring-polymer free step is not circulant");
         }
         // persistent grid; blocks start on classes in proportion to their estimated work
-        int grid = plain ? rpsh_grid_fp64() : 0;
-        for (int k = 0; k < h->nclass && !plain; ++k) {
+        const bool one = !plain && h->map.rp_one_launch;
+        int grid = plain ? rpsh_grid_fp64() : (one ? rpsh_one_launch_grid() : 0);
+        for (int k = 0; k < h->nclass && !plain && !one; ++k) {
             const int gk = rpsh_group_grid(h->class_beads[k], rp_lanes_of(h, h->class_beads[k]));
             grid = gk > grid ? gk : grid;
         }
@@ -1055,7 +1056,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
             total += cost[k];
         }
         std::vector<int32_t> bc(grid, 0);
-        if (!plain) {
+        if (!plain && !one) {
             // each bead-count kernel serves only its own classes: block b starts
             // at class b mod nclass and takes the next one of its bead count,
             // which spreads a kernel's blocks evenly over its classes
@@ -1140,6 +1141,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         if (plain) {
             e = launch_rpsh_fp64(rq, grid, s);
+        } else if (one) {
+            e = launch_rpsh_one(rq, grid, s);
         } else {
             // one persistent kernel per bead count present, each with the grid
             // that fills the GPU, concurrently on forked streams and largest
@@ -1607,6 +1610,8 @@ int nqcd_set_mapping(nqcd_handle* h, const nqcd_mapping* m) {
         for (int a = 0; a < 4; ++a) ok |= kAllowed[q][a] != 0 && m->rp_lanes[q] == kAllowed[q][a];
         if (!ok) return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: rp_lanes outside the shapes of its bead count");
     }
+    if (m->rp_one_launch != 0 && m->rp_one_launch != 1)
+        return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: rp_one_launch must be 0 or 1");
     if (m->iesh_cores != 0 && m->iesh_cores != 1)
         return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: iesh_cores must be 0 (tensor cores) or 1 (CUDA cores)");
     if (m->sb_lanes == 8) {

@@ -728,6 +728,9 @@ int rpsh_group_grid_t() {
 int rpsh_group_grid(int beads, int lanes);
 cudaError_t launch_rpsh_group(int beads, int lanes, const RpshParams& p, int blocks, cudaStream_t s);
 int rpsh_group_grid_tuned(int beads, int lanes);
+// One persistent launch serving every bead count (kernels_tune.cu).
+int rpsh_one_launch_grid();
+cudaError_t launch_rpsh_one(const RpshParams& p, int blocks, cudaStream_t s);
 cudaError_t launch_rpsh_group_tuned(int beads, int lanes, const RpshParams& p, int blocks, cudaStream_t s);
 
 // Lane-group shape (beads per lane Q, lanes per trajectory GL) of a bead count.

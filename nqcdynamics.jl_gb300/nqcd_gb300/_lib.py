@@ -120,17 +120,19 @@ class nqcd_mapping(C.Structure):
     """Launch shapes of the fast kernels (nqcd_gpu.h, nqcd_set_mapping)."""
 
     _fields_ = [("sb_lanes", C.c_int32), ("sb_block", C.c_int32), ("rp_lanes", C.c_int32 * 4),
-                ("iesh_cores", C.c_int32), ("reserved", C.c_int32)]
+                ("iesh_cores", C.c_int32), ("rp_one_launch", C.c_int32)]
 
 
 RP_LANE_BEADS = (4, 8, 16, 32)  # bead counts of nqcd_mapping.rp_lanes
 
 
-def mapping(sb_lanes=0, sb_block=0, rp_lanes=None, iesh_cores=0):
+def mapping(sb_lanes=0, sb_block=0, rp_lanes=None, iesh_cores=0, rp_one_launch=0):
     """nqcd_mapping from keyword values; rp_lanes: {bead count: lanes};
-    iesh_cores: 0 tensor cores, 1 CUDA cores for the IESH propagator."""
+    iesh_cores: 0 tensor cores, 1 CUDA cores for the IESH propagator;
+    rp_one_launch: 1 serves every bead count from one persistent launch."""
     m = nqcd_mapping()
     m.sb_lanes, m.sb_block, m.iesh_cores = int(sb_lanes), int(sb_block), int(iesh_cores)
+    m.rp_one_launch = int(rp_one_launch)
     for q, b in enumerate(RP_LANE_BEADS):
         m.rp_lanes[q] = int((rp_lanes or {}).get(b, 0))
     return m

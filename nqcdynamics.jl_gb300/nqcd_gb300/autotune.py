@@ -11,7 +11,8 @@ workload:
   ring-polymer FSSH: lanes per trajectory of each bead count's kernel
       (4 beads: 1, 2, 4; 8: 2, 4, 8; 16: 4, 8, 16; 32: 4, 8, 16, 32), by
       coordinate descent on the mixed C3 ensemble (the four kernels run
-      concurrently, so a shape is judged by the whole ensemble's time).
+      concurrently, so a shape is judged by the whole ensemble's time), and
+      against it one persistent launch serving every bead count.
 
 The committed cache (tuned/mappings.json) holds the sweeps measured on a
 GB300; NQCD_TUNE_CACHE names another file.  `mapping_for` returns the cached
@@ -109,8 +110,15 @@ def tune_rpsh(L, ntraj=50_000, repeats=2):
         for beads, cands in RP_LANES.items():
             trial = {lanes: time_of(dict(best, **{beads: lanes})) for lanes in cands}
             best[beads] = min(trial, key=trial.get)
+        # one persistent launch for every bead count (default lane groups) against the
+        # concurrent per-bead-count kernels
+        eng.set_mapping(dict(rp_one_launch=1))
+        one_ms = _best_kernel_ms(eng, lambda: eng.run(0.0, 20000.0, 1.0, WL.SEED), repeats)
+        rows.append(dict(rp_one_launch=1, kernel_ms=one_ms))
     finally:
         eng.close()
+    if one_ms < time_of(best):
+        return dict(rp_one_launch=1), rows
     return dict(rp_lanes=best), rows
 
 

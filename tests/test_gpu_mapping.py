@@ -77,11 +77,36 @@ def test_rpsh_lane_groups_give_the_same_scattering():
             assert np.all(np.abs(sc - ref) <= 4 * sig + 1e-3), (beads, lanes, sc, ref)
 
 
+def test_rpsh_one_launch_is_bitwise_the_per_bead_count_kernels():
+    """One persistent launch serving every bead count runs each trajectory
+    with the same lane-group shape as the concurrent per-bead-count kernels,
+    and the random stream is keyed by trajectory, so the results are bitwise
+    equal whatever order the queues hand trajectories out in."""
+    n = 6000
+    r0, v0, nb, models = C.rpsh_inputs(n)
+    out = {}
+    for one in (0, 1):
+        eng = C.rpsh_tully(L, n, L.PREC_FP32, max_hops=8)
+        try:
+            eng.set_mapping(dict(rp_one_launch=one))
+            eng.set_initial(np.ascontiguousarray(r0), np.ascontiguousarray(v0), nbeads=np.ascontiguousarray(nb))
+            eng.set_trajectory_models(np.ascontiguousarray(models))
+            eng.run(0.0, 20000.0, 1.0, 9)
+            fin = eng.get_final(32)
+            fin["hop_log"] = eng.get_hop_log(8)
+            out[one] = fin
+        finally:
+            eng.close()
+    for key in ("r", "v", "state", "nhops", "nsteps", "hop_log"):
+        np.testing.assert_array_equal(out[1][key], out[0][key], err_msg=key)
+
+
 def test_mapping_rejects_unknown_shapes():
     w, c, _, _ = WL.spin_boson_inputs(8, 100)
     eng = C.spinboson_fssh(L, w, c, 8, 100, L.PREC_FP32)
     try:
-        for bad in (dict(sb_lanes=3), dict(sb_block=96), dict(rp_lanes={4: 8}), dict(rp_lanes={32: 2})):
+        for bad in (dict(sb_lanes=3), dict(sb_block=96), dict(rp_lanes={4: 8}), dict(rp_lanes={32: 2}),
+                    dict(iesh_cores=2), dict(rp_one_launch=2)):
             with pytest.raises(L.EngineError) as e:
                 eng.set_mapping(bad)
             assert e.value.code == L.NQCD_ERR_ARG
