@@ -410,10 +410,12 @@ __device__ inline double iesh_wall(const IeshParams& p, double z) {  // exp(-a z
 // the final centroid velocity, and their velocity change is the same in every
 // bead (rpsh.jl:30-50).  Fermi-Dirac occupations come from the centroid
 // eigenvalues (iesh.jl:99-128).
-template <typename R, bool RP>
+// TC: the tensor-core propagator (R = float only); a separate instantiation so
+// that the CUDA-core kernel keeps its own register allocation.
+template <typename R, bool RP, bool TC>
 __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, RP ? p.nbeads : 1, p.tensor != 0);
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, RP ? p.nbeads : 1, TC);
     R* eps = (R*)(smem + L.o_eps);
     R* V2 = (R*)(smem + L.o_V2);
     R* lam = (R*)(smem + L.o_lam);
@@ -461,7 +463,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     constexpr bool kF32 = std::is_same<R, float>::value;
     // tensor-core propagator (FP32 path): operands in shared memory, accumulator, phi_{k-2} and the
     // series sum in TMEM columns of this CTA
-    const bool tcp = kF32 && L.tc;
+    constexpr bool tcp = kF32 && TC;
     unsigned char* aop_hi = smem + L.o_tc;  // A operand: the orbital block transposed, rows 2 e + (re, im)
     unsigned char* aop_lo = aop_hi + L.tc_sa;
     unsigned char* bop = aop_hi + 2 * L.tc_sa;  // B operand: the coupling matrix A (tf32), row i, k = j
@@ -472,8 +474,8 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     // TMEM columns: a power of two >= 3 N (256 at N = 80: two CTAs share an SM's 512)
     uint32_t tc_cols = 32;
     while (tc_cols < 3u * (uint32_t)L.N) tc_cols <<= 1;
-    if constexpr (kF32) {
-        if (tcp) {
+    if constexpr (tcp) {
+        {
             if (tid == 0) {
                 tc::mbar_init(&tc_bar, 1);
                 asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -999,8 +1001,8 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             if (tid == 0 && nonconv) atomicAdd(nonconv, 1ull);
         } else {
             nterms += (unsigned long long)K;
-            if (tcp) {
-                if constexpr (kF32) {
+            if constexpr (tcp) {
+                {
                     // Chebyshev terms on the tensor cores: D = Phi^T A^T (M = 2 Ne orbital components
                     // padded to 128, N = N states, K = N states) with Phi split into tf32 high and low
                     // parts (two products) and A in tf32.  Thread (warp w, lane l) owns accumulator row
@@ -1586,8 +1588,8 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             atomicAdd(p.counters + 1, nterms);
         }
     }
-    if constexpr (kF32) {
-        if (tcp) {
+    if constexpr (tcp) {
+        {
             if (tid == 0 && tc_fail && p.counters) atomicAdd(p.counters + 3, 1ull);
             tc::fence_before_sync();
             __syncthreads();
@@ -1596,15 +1598,29 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     }
 }
 
-template <typename R>
+template <typename R, bool TC>
 __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) iesh_kernel(const IeshParams p) {
-    iesh_body<R, false>(p);
+    iesh_body<R, false, TC>(p);
 }
 
 // RingPolymerSimulation{AdiabaticIESH}: p.nbeads in 2..kRpIeshMaxBeads, p.nelec <= kRpIeshMaxElectrons
-template <typename R>
+template <typename R, bool TC>
 __global__ void __launch_bounds__(kIeshBlock, iesh_min_blocks<R>()) rpiesh_kernel(const IeshParams p) {
-    iesh_body<R, true>(p);
+    iesh_body<R, true, TC>(p);
+}
+
+template <typename R, bool TC>
+cudaError_t launch_iesh_tc(const IeshParams& p, cudaStream_t s) {
+    const bool rp = p.nbeads > 1;
+    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, rp ? p.nbeads : 1, TC);
+    cudaError_t e = cudaFuncSetAttribute(rp ? rpiesh_kernel<R, TC> : iesh_kernel<R, TC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
+    if (e != cudaSuccess) return e;
+    if (rp)
+        rpiesh_kernel<R, TC><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
+    else
+        iesh_kernel<R, TC><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
+    return cudaGetLastError();
 }
 
 template <typename R>
@@ -1612,15 +1628,13 @@ cudaError_t launch_iesh(const IeshParams& p, cudaStream_t s) {
     if (p.ntraj <= 0) return cudaSuccess;
     const bool rp = p.nbeads > 1;
     if (rp && (p.nbeads > kRpIeshMaxBeads || p.nelec > kRpIeshMaxElectrons)) return cudaErrorInvalidValue;
-    const IeshLayout L = iesh_layout<R>(p.nstates, p.nelec, rp ? p.nbeads : 1, p.tensor != 0);
-    cudaError_t e = cudaFuncSetAttribute(rp ? rpiesh_kernel<R> : iesh_kernel<R>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.bytes);
-    if (e != cudaSuccess) return e;
-    if (rp)
-        rpiesh_kernel<R><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
-    else
-        iesh_kernel<R><<<(unsigned)p.ntraj, kIeshBlock, L.bytes, s>>>(p);
-    return cudaGetLastError();
+    if constexpr (std::is_same<R, float>::value) {
+        if (p.tensor) {
+            if (!iesh_tc_shape(p.nstates, p.nelec)) return cudaErrorInvalidValue;
+            return launch_iesh_tc<float, true>(p, s);
+        }
+    }
+    return launch_iesh_tc<R, false>(p, s);
 }
 
 }  // namespace nqcd

@@ -108,7 +108,7 @@ def tune_rpsh(L, ntraj=50_000, repeats=2):
             return timed[key]
 
         for beads, cands in RP_LANES.items():
-            trial = {lanes: time_of(dict(best, **{beads: lanes})) for lanes in cands}
+            trial = {lanes: time_of({**best, beads: lanes}) for lanes in cands}
             best[beads] = min(trial, key=trial.get)
         # one persistent launch for every bead count (default lane groups) against the
         # concurrent per-bead-count kernels
