@@ -569,12 +569,49 @@ end
 
 output_name(f) = f isa Function ? nameof(f) : nameof(typeof(f))
 
-function check_outputs(outputs)
+const FILE_OUTPUTS = (:OutputTotalEnergy, :OutputSurfaceHops, :OutputPosition, :OutputVelocity)
+
+function check_outputs(outputs, file::Bool)
     for f in outputs
         n = output_name(f)
-        n in (:OutputStateResolvedScattering1D, :PopulationCorrelationFunction, :OutputFinal) ||
-            throw(ArgumentError("EnsembleGB300: output $n is not supported"))
+        if file
+            n in FILE_OUTPUTS || throw(ArgumentError("EnsembleGB300: FileReduction writes $(FILE_OUTPUTS), not $n"))
+        else
+            n in (:OutputStateResolvedScattering1D, :PopulationCorrelationFunction, :OutputFinal) ||
+                throw(ArgumentError("EnsembleGB300: output $n is not supported"))
+        end
     end
+end
+
+"""Per-trajectory outputs for FileReduction (reductions.jl:57-91) from the
+engine's final state (`nqcd_get_final`): the engine keeps each trajectory at
+t0 and t1 only, so `:Time` is `[t0, t1]`, positions and velocities are the
+two arrays at those times (stacked by FileReduction on a trailing axis), the
+total energy the two values, and the hop count a number."""
+function file_batch(h, outputs, t0, t1, shape, r0, v0, trajectories)
+    k = prod(shape)
+    r = zeros(k * trajectories)
+    v = zeros(k * trajectories)
+    nh = zeros(Int32, trajectories)
+    en = zeros(2 * trajectories)
+    GC.@preserve r v nh en check(h, ccall(sym(:nqcd_get_final), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}, Ptr{Int32}, Ptr{Int32},
+         Ptr{Int32}, Ptr{Float64}),
+        h, pointer(r), pointer(v), C_NULL, C_NULL, C_NULL, pointer(nh), C_NULL, C_NULL, pointer(en)))
+    block(x, i) = reshape(x[(i - 1) * k + 1:i * k], shape)
+    batch = Dictionary{Symbol,Any}[]
+    for i in 1:trajectories
+        d = Dictionary{Symbol,Any}([:Time], [[t0, t1]])
+        for f in outputs
+            n = output_name(f)
+            n === :OutputTotalEnergy && insert!(d, n, en[2i - 1:2i])
+            n === :OutputSurfaceHops && insert!(d, n, Int(nh[i]))
+            n === :OutputPosition && insert!(d, n, [block(r0, i), block(r, i)])
+            n === :OutputVelocity && insert!(d, n, [block(v0, i), block(v, i)])
+        end
+        push!(batch, d)
+    end
+    return batch
 end
 
 function SciMLBase.__solve(prob::SciMLBase.AbstractEnsembleProblem,
@@ -585,10 +622,11 @@ function SciMLBase.__solve(prob::SciMLBase.AbstractEnsembleProblem,
                                                "(given through the engine's terminate_x) are not supported"))
     reduction = prob.reduction
     mean = reduction isa NQCDynamics.Ensembles.MeanReduction
-    mean || reduction isa NQCDynamics.Ensembles.SortByTrajectoryReduction ||
+    file = reduction isa NQCDynamics.Ensembles.FileReduction
+    mean || file || reduction isa NQCDynamics.Ensembles.SortByTrajectoryReduction ||
         throw(ArgumentError("EnsembleGB300: reduction $(typeof(reduction)) is not supported"))
     outputs = prob.output_func.functions
-    check_outputs(outputs)
+    check_outputs(outputs, file)
     method = method_code(sim)
     method in (METHOD_FSSH, METHOD_RPSH, METHOD_EHRENFEST) ||
         throw(ArgumentError("EnsembleGB300: this binding marshals the two-state models; IESH and MDEF use " *
@@ -610,6 +648,7 @@ function SciMLBase.__solve(prob::SciMLBase.AbstractEnsembleProblem,
     nsave = stride > 0 ? fld(round(Int, (t1 - t0) / dt), stride) + 1 : 0
     scattering = zeros(2 * 2)
     popcorr = zeros(max(nsave, 1) * 4)
+    batch = nothing
     wall = @elapsed begin
         h = GC.@preserve keep create(cfg)
         try
@@ -626,9 +665,18 @@ function SciMLBase.__solve(prob::SciMLBase.AbstractEnsembleProblem,
                 (Ptr{Cvoid}, Float64, Float64, Float64, UInt64, Ref{NqcdOutputs}, Ref{NqcdStats}),
                 h, t0, t1, dt, ens.seed, out, stats))
             LAST_STATS[] = stats[]
+            if file
+                shape = size(NQCDynamics.DynamicsUtils.get_positions(prob.prob.u0))
+                batch = file_batch(h, outputs, t0, t1, shape, r0, v0, trajectories)
+            end
         finally
             destroy(h)
         end
+    end
+    if file
+        # the reference's own FileReduction writes the HDF5 groups
+        message, _ = reduction(nothing, batch, 1:trajectories)
+        return SciMLBase.EnsembleSolution(message, wall, true)
     end
     times = stride > 0 ? collect(range(t0, step=stride * dt, length=nsave)) : [t0, t1]
     result = Dictionary{Symbol,Any}([:Time], [times])

@@ -13,10 +13,12 @@ from .api import (
     DiabaticMDEF,
     DisplacedHarmonic,
     FermiDiracState,
+    FileReduction,
     GaussianBroadening,
     OutputImpurityPopulation,
     OutputKineticEnergy,
     OutputPosition,
+    OutputVelocity,
     OutputPotentialEnergy,
     ShenviGaussLegendre,
     TrapezoidalRule,

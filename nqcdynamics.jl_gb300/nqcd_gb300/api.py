@@ -29,6 +29,8 @@ because this engine has no CPU path.
 """
 from __future__ import annotations
 
+import os
+
 import math
 from dataclasses import dataclass, field
 from typing import Any
@@ -592,6 +594,10 @@ class OutputPosition:
     pass
 
 
+class OutputVelocity:
+    pass
+
+
 class OutputImpurityPopulation:
     """IESH: population of the impurity state, row 0 of
     iesh_diabatic_population (iesh.jl:351-369), at each save point."""
@@ -607,6 +613,34 @@ class SumReduction:
 
 class SortByTrajectoryReduction:
     pass
+
+
+class FileReduction:
+    """Per-trajectory outputs written to a file, as FileReduction does
+    (src/Ensembles/reductions.jl:57-91): one group `trajectory_<id>` per
+    trajectory (ids from 1) holding one array per output name, `Time`
+    included.  This image has no HDF5 library, so the container is NumPy's
+    .npz with the same paths (`trajectory_3/OutputTotalEnergy`), and the file
+    name takes the .npz extension where the reference's takes .h5.  Outputs
+    that are numbers or arrays per trajectory are written (total energy and
+    positions or velocities at the engine's time points, t0 and t1; hop
+    counts); others raise, as the reference's does for outputs it cannot
+    convert."""
+
+    def __init__(self, filename: str):
+        root, ext = os.path.splitext(filename)
+        self.filename = filename if ext == ".npz" else root + ".npz"
+
+    def write(self, times, per_traj: dict) -> str:
+        n = len(next(iter(per_traj.values())))
+        arrays = {}
+        for i in range(n):
+            g = f"trajectory_{i + 1}"
+            arrays[f"{g}/Time"] = np.asarray(times, np.float64)
+            for name, arr in per_traj.items():
+                arrays[f"{g}/{name}"] = np.asarray(arr[i])
+        np.savez(self.filename, **arrays)
+        return f"Output written to {self.filename}."
 
 
 # ---------------------------------------------------------------------------
@@ -706,8 +740,9 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
         raise TypeError("distribution must be DynamicalDistribution * PureState")
     outputs = output if isinstance(output, (tuple, list)) else (output,)
     reduction = reduction if reduction is not None else MeanReduction()
-    if not isinstance(reduction, (MeanReduction, SumReduction)):
-        raise NotImplementedError("the GPU path reduces on the device: MeanReduction or SumReduction")
+    if not isinstance(reduction, (MeanReduction, SumReduction, FileReduction)):
+        raise NotImplementedError("the GPU path reduces on the device (MeanReduction, SumReduction) or writes "
+                                  "per-trajectory outputs (FileReduction)")
     t0, t1 = float(tspan[0]), float(tspan[1])
     save_stride = 0
     for o in outputs:
@@ -739,6 +774,10 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
             nsteps = int(round((t1 - t0) / dt))
             pc = np.zeros((nsteps // save_stride + 1) * 4 + 4)
         out, stats = eng.run(t0, t1, dt, alg.seed if seed is None else seed, scattering=sc, popcorr=pc)
+        if isinstance(reduction, FileReduction):
+            final = eng.get_final(sim.ndof)
+            start = None if alg.device_sampling else (r0, v0)
+            return reduction.write([t0, t1], _per_trajectory(outputs, final, start, hops=True))
         result: dict[str, Any] = {}
         scale = ntraj if isinstance(reduction, SumReduction) else 1
         final = None
@@ -764,6 +803,28 @@ def run_dynamics(sim, tspan, distribution, *, output, trajectories: int = 1, red
         return result
     finally:
         eng.close()
+
+
+def _per_trajectory(outputs, final, start, hops):
+    """Per-trajectory arrays of FileReduction at the engine's time points
+    (t0, t1): total energy (ntraj, 2), positions and velocities (ntraj, ...,
+    2), surface-hop counts."""
+    per = {}
+    for o in outputs:
+        name = _output_name(o)
+        if name == "OutputTotalEnergy":
+            per[name] = final["energy"]
+        elif name == "OutputSurfaceHops" and hops:
+            per[name] = final["nhops"]
+        elif name in ("OutputPosition", "OutputVelocity") and start is not None:
+            key, q = ("r", 0) if name == "OutputPosition" else ("v", 1)
+            a = np.asarray(start[q], np.float64).reshape(final[key].shape)
+            per[name] = np.stack([a, final[key]], axis=-1)
+        else:
+            raise TypeError(f"Cannot convert output {name} to the file format")
+    if not per:
+        raise TypeError("FileReduction needs at least one per-trajectory output")
+    return per
 
 
 def _metal_config(sim, ntraj, alg, save_stride):
@@ -804,8 +865,9 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
     mdef = isinstance(sim.method, DiabaticMDEF)
     outputs = output if isinstance(output, (tuple, list)) else (output,)
     reduction = reduction if reduction is not None else MeanReduction()
-    if not isinstance(reduction, MeanReduction):
-        raise NotImplementedError("the GPU path reduces on the device: MeanReduction")
+    if not isinstance(reduction, (MeanReduction, FileReduction)):
+        raise NotImplementedError("the GPU path reduces on the device (MeanReduction) or writes per-trajectory "
+                                  "outputs (FileReduction)")
     if mdef:
         nuclear = distribution
         if isinstance(distribution, ProductDistribution):
@@ -821,7 +883,7 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
                                               OutputImpurityPopulation)
                   or isinstance(o, (OutputKineticEnergy, OutputPotentialEnergy, OutputPosition, OutputImpurityPopulation))]
     save_stride = 0
-    if timeseries:
+    if timeseries and not isinstance(reduction, FileReduction):
         if saveat is None:
             raise ValueError("time-series outputs need saveat")
         stride = float(saveat) / dt
@@ -852,6 +914,10 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
         nsteps = int(round((t1 - t0) / dt))
         obs = np.zeros(((nsteps // save_stride + 1) if save_stride else 1) * 4)
         out, stats = eng.run(t0, t1, dt, alg.seed if seed is None else seed, observables=obs)
+        if isinstance(reduction, FileReduction):
+            final = eng.get_final(sim.n_beads if rp else 1) if mdef else \
+                eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
+            return reduction.write([t0, t1], _per_trajectory(outputs, final, (r0, v0), hops=not mdef))
         ob = obs[: out.nsave * 4].reshape(out.nsave, 4)
         result: dict[str, Any] = {}
         if save_stride:

@@ -59,3 +59,50 @@ def test_mdef_run_dynamics_matches_engine():
         eng.close()
     np.testing.assert_array_equal(res["OutputFinal"]["r"], fin["r"])
     np.testing.assert_array_equal(res["OutputPosition"], obs.reshape(-1, 4)[:, 0])
+
+
+def test_file_reduction_writes_each_trajectory(tmp_path):
+    """FileReduction (reductions.jl:57-91) through run_dynamics: one group per
+    trajectory holding the same final state the device reduction averages."""
+    ntraj, nm = 64, 8
+    model = N.SpinBoson(N.OhmicSpectralDensity(2.5, 0.1), nm, 0.0, 1.0)
+    sim = N.Simulation[N.FSSH](N.Atoms(np.ones(nm)), model)
+    rng = np.random.default_rng(5)
+    r0, v0 = rng.normal(size=(ntraj, 1, nm)), rng.normal(size=(ntraj, 1, nm))
+    dist = N.DynamicalDistribution(v0, r0, (1, nm)) * N.PureState(1, N.Diabatic())
+    kw = dict(trajectories=ntraj, dt=0.05, seed=8, ensemble_algorithm=N.EnsembleGB300("fp64"))
+    msg = N.run_dynamics(sim, (0.0, 2.0), dist, output=(N.OutputTotalEnergy, N.OutputSurfaceHops, N.OutputPosition,
+                                                        N.OutputVelocity),
+                         reduction=N.FileReduction(str(tmp_path / "sb.h5")), **kw)
+    assert msg == f"Output written to {tmp_path / 'sb.npz'}."
+    ref = N.run_dynamics(sim, (0.0, 2.0), dist, output=N.OutputFinal, **kw)["OutputFinal"]
+    f = np.load(tmp_path / "sb.npz")
+    for i in range(ntraj):
+        g = f"trajectory_{i + 1}/"
+        np.testing.assert_array_equal(f[g + "Time"], [0.0, 2.0])
+        np.testing.assert_array_equal(f[g + "OutputTotalEnergy"], ref["energy"][i])
+        assert f[g + "OutputSurfaceHops"] == ref["nhops"][i]
+        np.testing.assert_array_equal(f[g + "OutputPosition"][:, 0], r0[i].ravel())
+        np.testing.assert_array_equal(f[g + "OutputPosition"][:, 1], ref["r"][i])
+        np.testing.assert_array_equal(f[g + "OutputVelocity"][:, 1], ref["v"][i])
+
+
+def test_file_reduction_iesh(tmp_path):
+    n, nsteps = 8, 100
+    wl = WL.newns_anderson_iesh(n, z0=4.0)
+    P = wl["params"]
+    model = N.AndersonHolstein(N.AdsorbateMetal3D(P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"]),
+                               N.TrapezoidalRule(79, -0.5, 0.5), coupling=0.04)
+    sim = N.Simulation[N.AdiabaticIESH](N.Atoms(wl["mass"]), model)
+    dist = N.DynamicalDistribution(wl["v0"], wl["r0"], (3, 1)) * N.FermiDiracState(0.0, 1.0 / wl["beta"])
+    kw = dict(trajectories=n, dt=wl["dt"], ensemble_algorithm=N.EnsembleGB300("fp64"), seed=9)
+    N.run_dynamics(sim, (0.0, nsteps * wl["dt"]), dist, output=(N.OutputPosition, N.OutputTotalEnergy,
+                                                                N.OutputSurfaceHops),
+                   reduction=N.FileReduction(str(tmp_path / "iesh")), **kw)
+    ref = N.run_dynamics(sim, (0.0, nsteps * wl["dt"]), dist, output=N.OutputFinal, **kw)["OutputFinal"]
+    f = np.load(tmp_path / "iesh.npz")
+    for i in range(n):
+        g = f"trajectory_{i + 1}/"
+        np.testing.assert_array_equal(f[g + "OutputPosition"][:, 1], ref["r"][i])
+        np.testing.assert_array_equal(f[g + "OutputTotalEnergy"], ref["energy"][i])
+        assert f[g + "OutputSurfaceHops"] == ref["nhops"][i]

@@ -121,3 +121,16 @@ def test_julia_philox_round_structure():
     # the C side, for the record
     assert "c.x = (uint32_t)traj;" in MATH and "c.y = (uint32_t)(traj >> 32);" in MATH
     assert "return (double)(bits >> 11) * 0x1.0p-53;" in MATH
+
+
+def test_julia_file_reduction_writes_through_the_reference():
+    """FileReduction on the Julia side hands per-trajectory Dictionaries to the
+    reference's own FileReduction (reductions.jl:57-91), which writes HDF5; the
+    outputs it takes are the ones the Python mirror writes to .npz."""
+    assert "reduction isa NQCDynamics.Ensembles.FileReduction" in JL
+    assert "message, _ = reduction(nothing, batch, 1:trajectories)" in JL
+    jl = re.search(r"const FILE_OUTPUTS = \((.*?)\)", JL).group(1)
+    names = [x.strip().lstrip(":") for x in jl.split(",")]
+    api = (ROOT / "nqcdynamics.jl_gb300" / "nqcd_gb300" / "api.py").read_text()
+    body = api[api.index("def _per_trajectory"):api.index("def _metal_config")]
+    assert sorted(names) == sorted(set(re.findall(r'"(Output\w+)"', body)))
