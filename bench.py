@@ -430,7 +430,7 @@ def secondary(args, dist):
             r0, v0, nb, models = C.rpsh_inputs(n, traj_offset=rank_off * n)
             from nqcd_gb300 import autotune
 
-            rp_map, rp_src = autotune.mapping_for(L, "rpsh", allow_tune=dist.world == 1)
+            rp_map, rp_src = autotune.mapping_for(L, "rpsh", ntraj=n, allow_tune=dist.world == 1)
             sc = {}
             for name, prec, nt in (("fp64", L.PREC_FP64, nsub), ("fp32_sub", L.PREC_FP32, nsub), ("fp32", L.PREC_FP32, n)):
                 eng = C.rpsh_tully(L, nt, prec, traj_offset=rank_off * n)

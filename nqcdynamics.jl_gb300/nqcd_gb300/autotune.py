@@ -10,7 +10,7 @@ workload:
       (4, 8) x threads per block (64, 128, 256);
   ring-polymer FSSH: lanes per trajectory of each bead count's kernel
       (4 beads: 1, 2, 4; 8: 2, 4, 8; 16: 4, 8, 16; 32: 4, 8, 16, 32), by
-      coordinate descent on the mixed C3 ensemble (the four kernels run
+      coordinate descent on the mixed C3 ensemble of 200 000 trajectories (the four kernels run
       concurrently, so a shape is judged by the whole ensemble's time), and
       against it one persistent launch serving every bead count.
 
@@ -83,12 +83,15 @@ def tune_spinboson(L, ntraj=100_000, nmodes=100, t1=20.0, dt=0.05, repeats=3):
     return dict(sb_lanes=best["sb_lanes"], sb_block=best["sb_block"]), rows
 
 
-def tune_rpsh(L, ntraj=50_000, repeats=2):
-    """Sweep of the ring-polymer fast kernels on the mixed ensemble of C3
-    (Tully 1-3 round robin, bead counts 4-32 mixed, C3's momenta,
+def tune_rpsh(L, ntraj=200_000, repeats=2):
+    """Sweep of the ring-polymer fast kernels on the mixed ring-polymer
+    benchmark ensemble (Tully 1-3 round robin, bead counts 4-32 mixed,
     termination at |x| > 10), where the four bead-count kernels run
     concurrently and share the SMs: coordinate descent from the defaults,
     one bead count at a time over its lane groups with the others fixed.
+    The sweep runs at the ensemble's own size: on a quarter of it the tail
+    of the 32-bead class dominates and favours wider lane groups, which
+    lose throughput on the full ensemble.
     Returns (best rp_lanes dict, sweep rows)."""
     r0, v0, nb, models = C.rpsh_inputs(ntraj)
     eng = C.rpsh_tully(L, ntraj, L.PREC_FP32)
@@ -128,7 +131,7 @@ TUNERS = {"spinboson": tune_spinboson, "rpsh": tune_rpsh}
 def workload_key(workload: str, **kw) -> str:
     if workload == "spinboson":
         return f"spinboson_modes{kw.get('nmodes', 100)}_traj{kw.get('ntraj', 100_000)}"
-    return f"rpsh_tully123_mixed_traj{kw.get('ntraj', 50_000)}"
+    return f"rpsh_tully123_mixed_traj{kw.get('ntraj', 200_000)}"
 
 
 def tune(L, workload: str, **kw) -> dict:
