@@ -608,7 +608,9 @@ def secondary(args, dist):
             cfg = {"workload": ("ehrenfest_na" if wk == "ehrenfest_na" else "iesh") + "_newns_anderson_80states_40e_3dof_traj20k_dt0.1fs", "ntraj_per_gpu": n,
                    "nsteps": nsteps, "chebyshev_terms_per_step": terms,
                    "propagator_products": "CUDA cores" if args.iesh_cores else "tcgen05 tensor cores (tf32 high/low)",
-                   "full_hop_evaluations_per_step": st.hop_evaluations / max(1, st.traj_steps)}
+                   "full_hop_evaluations_per_step": st.hop_evaluations / max(1, st.traj_steps),
+                   "overlap_lu_per_step": st.overlap_factorizations / max(1, st.traj_steps),
+                   "fp64_refined_steps_per_step": st.electronics_fp64_steps / max(1, st.traj_steps)}
             ref_flops = 3.5e7
             kname = "iesh_kernel<float>"
     fast = res["fp32"]

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 109
+#define NQCD_ABI_VERSION 110
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -172,6 +172,9 @@ typedef struct nqcd_stats {
     int64_t surrogate_rejected;       /* MDEF with surrogate: trajectories switched to exact friction by the judge */
     double surrogate_max_rel_error;   /* MDEF with surrogate: largest judged relative error */
     double surrogate_mean_rel_error;  /* MDEF with surrogate: mean judged relative error */
+    int64_t overlap_factorizations;   /* IESH: hop tests that LU-factorized the overlap matrix (all of them
+                                         on the FP64 path; on the FP32 path those that the Gram-matrix
+                                         bound of the estimate did not settle) */
 } nqcd_stats;
 
 typedef struct nqcd_handle nqcd_handle;
@@ -313,6 +316,10 @@ typedef struct nqcd_mapping {
     int32_t rp_one_launch; /* fast ring-polymer path: 0 = one persistent kernel per bead count, concurrent
                               on forked streams; 1 = one persistent launch serving every bead count
                               (default lane groups) with a refill over all classes */
+    int32_t iesh_lu_always; /* IESH FP32 path: 0 = the LU of the overlap matrix runs only in steps where a
+                               bound of the hop estimate from the Gram matrix of the occupied rows does not
+                               already lie below the step's random number (the decision and the results are
+                               those of the LU path); 1 = the LU every step, as iesh.jl:241 */
 } nqcd_mapping;
 
 /* Set the handle's launch shapes for the following runs; NQCD_ERR_ARG for a

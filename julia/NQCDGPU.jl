@@ -44,7 +44,7 @@ export EnsembleGB300, install_keyed_hop_stream!, with_keyed_hops, keyed_fermi_di
 # C ABI (include/nqcd_gpu.h)
 # ---------------------------------------------------------------------------
 
-const ABI_VERSION = Int32(109)
+const ABI_VERSION = Int32(110)
 
 const METHOD_FSSH = Int32(1)
 const METHOD_RPSH = Int32(2)
@@ -138,6 +138,7 @@ struct NqcdStats
     surrogate_rejected::Int64
     surrogate_max_rel_error::Float64
     surrogate_mean_rel_error::Float64
+    overlap_factorizations::Int64
 end
 
 struct NqcdSampler
@@ -153,9 +154,10 @@ struct NqcdMapping
     rp_lanes::NTuple{4,Int32}
     iesh_cores::Int32
     rp_one_launch::Int32
+    iesh_lu_always::Int32
 end
 
-zero_stats() = NqcdStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0.0)
+zero_stats() = NqcdStats(0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0.0, 0.0, 0)
 
 """
     config(; method, model, ndofs, natoms, nstates, ..., keep)

@@ -109,7 +109,8 @@ struct IeshParams {
     int32_t* hop_log;               // [max_hops][3][ntraj]: step, from, to
     double* energy;                 // [2][ntraj] total energy at start and end, or null
     double* obs_partial;            // [ntraj][nsave][4]: z, kinetic, impurity population, potential
-    unsigned long long* counters;   // [0] full hop evaluations, [1] Chebyshev terms, [2] unconverged roots
+    unsigned long long* counters;   // [0] full hop evaluations, [1] Chebyshev terms, [2] unconverged roots,
+                                    // [3] tensor-core waits that gave up, [5] overlap LUs
     // FP32 path: adjacent roots closer than gap_fp64 are solved again in FP64 and the couplings
     // between them, z0_i z0_j / (l_j - l_i), formed from the FP64 roots; fp64_steps[ti] counts the
     // steps that needed it (null: not counted)
@@ -118,6 +119,9 @@ struct IeshParams {
     // FP32 path: the propagator's products on the tensor cores (tcgen05, iesh_tc_shape); counters[3]
     // counts waits for them that gave up
     int32_t tensor;
+    // FP32 path: 1 runs the LU of the overlap matrix every step; 0 skips it where the bound of the
+    // estimate from the occupied Gram matrix is already below the random number
+    int32_t lu_always;
 };
 
 template <typename R>
@@ -130,7 +134,7 @@ struct IeshLayout {
     int N, Ne, Nu, Np, Nep, B;
     bool tc;  // tensor-core propagator: o_tc replaces At, phiB and out
     size_t o_eps, o_V2, o_lam, o_z2, o_z0, o_w64, o_At, o_phiA, o_phiB, o_out, o_J, o_Jr, o_inv, o_fdu, o_fdi, o_occ,
-        o_unocc, o_piv, o_red, o_misc, o_rph, o_rpq, o_tc, tc_sa, bytes;
+        o_unocc, o_piv, o_red, o_misc, o_rph, o_rpq, o_tc, tc_sa, o_dl, bytes;
 };
 
 // The tensor-core propagator handles N states and Ne electrons when N is a
@@ -152,6 +156,7 @@ NQCD_HD IeshLayout iesh_layout(int N, int Ne, int B = 1, bool tc = false) {
     L.tc = tc;
     L.o_tc = 0;
     L.tc_sa = 0;
+    L.o_dl = 0;
     L.N = N;
     L.Ne = Ne;
     L.Nu = N - Ne;
@@ -179,6 +184,7 @@ NQCD_HD IeshLayout iesh_layout(int N, int Ne, int B = 1, bool tc = false) {
         if (lu > tr) tr = lu;
         L.tc_sa = sa;
         L.o_tc = iesh_take(o, tr);
+        L.o_dl = iesh_take(o, sizeof(float) * L.Np);
         L.o_phiB = L.o_tc;
         L.o_out = L.o_tc;
     } else {
@@ -261,6 +267,38 @@ __device__ inline int iesh_bessel_warp(double alpha, double tol, double* J, cons
     return K >= kIeshMaxTerms - 2 ? -1 : K;
 }
 
+// iesh_bessel_warp with fewer FP64 instructions (the FP32 path; the FP64 unit of the GPU issues a
+// warp instruction every few dozen cycles): x^k / k! of lane k as a prefix product over the lanes
+// (5 steps instead of k), and the power series stopped once every lane's term is below 2^-60 of its
+// sum (an integer test of the exponents).  The Miller recurrence beyond alpha = 4 is iesh_bessel_warp's.
+__device__ inline int iesh_bessel_warp_fast(double alpha, double tol, double* J, const double* inv) {
+    if (alpha > 4.0) return iesh_bessel_warp(alpha, tol, J, inv);
+    const int lane = threadIdx.x & 31;
+    const double x = 0.5 * alpha, mx2 = -x * x;
+    const int k = lane;
+    double f = k == 0 ? 1.0 : x * inv[k];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const double g = __shfl_up_sync(0xffffffffu, f, off);
+        if (lane >= off) f *= g;
+    }
+    double t = f, s = f;
+    for (int m = 1; m <= 24; ++m) {
+        t *= mx2 * (inv[m] * inv[m + k]);
+        s += t;
+        const int et = (__double2hiint(t) >> 20) & 0x7ff, es = (__double2hiint(s) >> 20) & 0x7ff;
+        if (__all_sync(0xffffffffu, et + 60 < es || et == 0)) break;
+    }
+    J[k] = s;
+    for (int q = 32 + lane; q < kIeshMaxTerms; q += 32) J[q] = 0.0;
+    __syncwarp();
+    int K = -1;
+    for (int q = lane; q < kIeshMaxTerms; q += 32)
+        if (fabs(J[q]) >= tol) K = q;
+    for (int off = 16; off > 0; off >>= 1) K = max(K, __shfl_xor_sync(0xffffffffu, K, off));
+    return K >= kIeshMaxTerms - 2 ? -1 : K;
+}
+
 // k-th (0-based) unset bit among bits [0, n) of a 128-bit mask.
 __device__ inline int iesh_nth_unset(const unsigned long long* m, int n, int k) {
     for (int w = 0; w < 2; ++w) {
@@ -312,6 +350,52 @@ __device__ inline float iesh_block_sum_f(float x, double* red_) {
     }
     __syncthreads();
     return red[64];
+}
+
+// FP32 form of iesh_block_minmax; every thread receives the block's extremes.
+__device__ inline void iesh_block_minmax_f(float& lo, float& hi, double* red_) {
+    float* red = (float*)red_;
+    for (int off = 16; off > 0; off >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) {
+        red[w] = lo;
+        red[32 + w] = hi;
+    }
+    __syncthreads();
+    for (int q = 0; q < nw; ++q) {
+        lo = fminf(lo, red[q]);
+        hi = fmaxf(hi, red[32 + q]);
+    }
+    __syncthreads();  // red is reused by the next reduction
+}
+
+// Three FP32 block sums at once (one pair of barriers); every thread receives the totals.
+__device__ inline void iesh_block_sum3_f(float& a, float& b, float& c, double* red_) {
+    float* red = (float*)red_;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+        c += __shfl_xor_sync(0xffffffffu, c, off);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) {
+        red[w] = a;
+        red[32 + w] = b;
+        red[64 + w] = c;
+    }
+    __syncthreads();
+    a = b = c = 0.f;
+    for (int q = 0; q < nw; ++q) {  // the same order in every thread
+        a += red[q];
+        b += red[32 + q];
+        c += red[64 + q];
+    }
+    __syncthreads();  // red is reused by the next reduction
 }
 
 __device__ inline void iesh_block_minmax(double& lo, double& hi, double* red) {
@@ -369,6 +453,66 @@ __device__ inline void scaled_mul(T& re, T& im, int& e, T br, T bi, int be) {
 template <typename R>
 constexpr int iesh_min_blocks() {
     return std::is_same<R, float>::value ? 2 : 1;
+}
+
+// Per-thread partial sums of tr X and |X|_F^2 for X = I - G, G = S^H S the Gram matrix of the
+// occupied rows of the orbitals (FP32 path, see the hop-estimate bound in iesh_body): 2 x 2 tiles
+// of G over the upper block triangle, the sum over occupied rows split in four parts held by lanes
+// 4 t .. 4 t + 3.  Out of line, so that its registers do not add to the step loop's.
+static __device__ __noinline__ float2 iesh_gram_partials(const Cx<float>* phiA, const int32_t* occ, int Ne, int Nep) {
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    float trx = 0.f, fx2 = 0.f;
+    const int nbk = (Ne + 1) >> 1, ntile = nbk * (nbk + 1) / 2;
+    for (int base = 0; base < 4 * ntile; base += nthr) {  // the same trip count in every thread
+        const int q = base + tid, part = q & 3;
+        const bool on = q < 4 * ntile;
+        int t = on ? q >> 2 : 0, bi = 0;
+        while (t >= nbk - bi) {  // tile t, row-major over the upper block triangle
+            t -= nbk - bi;
+            ++bi;
+        }
+        const int a0 = 2 * bi, b0 = 2 * (bi + t);
+        float gr[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, gi[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+        if (on)
+            for (int j = part; j < Ne; j += 4) {  // columns a0, a0 + 1 < Nep of row occ[j]
+                const float4* row = (const float4*)(phiA + occ[j] * Nep);
+                const float4 x = row[a0 >> 1], y = row[b0 >> 1];
+                const float xr[2] = {x.x, x.z}, xi[2] = {x.y, x.w};
+                const float yr[2] = {y.x, y.z}, yi[2] = {y.y, y.w};
+#pragma unroll
+                for (int uu = 0; uu < 2; ++uu)
+#pragma unroll
+                    for (int vv = 0; vv < 2; ++vv) {  // conj(x) y
+                        gr[uu][vv] = fmaf(xr[uu], yr[vv], fmaf(xi[uu], yi[vv], gr[uu][vv]));
+                        gi[uu][vv] = fmaf(xr[uu], yi[vv], fmaf(-xi[uu], yr[vv], gi[uu][vv]));
+                    }
+            }
+#pragma unroll
+        for (int uu = 0; uu < 2; ++uu)
+#pragma unroll
+            for (int vv = 0; vv < 2; ++vv)
+#pragma unroll
+                for (int off = 1; off <= 2; off <<= 1) {
+                    gr[uu][vv] += __shfl_xor_sync(0xffffffffu, gr[uu][vv], off);
+                    gi[uu][vv] += __shfl_xor_sync(0xffffffffu, gi[uu][vv], off);
+                }
+        if (on && part == 0)
+#pragma unroll
+            for (int uu = 0; uu < 2; ++uu)
+#pragma unroll
+                for (int vv = 0; vv < 2; ++vv) {
+                    const int a = a0 + uu, b = b0 + vv;
+                    if (a >= Ne || b >= Ne || a > b) continue;
+                    if (a == b) {
+                        const float d = 1.f - gr[uu][vv];
+                        trx += d;
+                        fx2 = fmaf(d, d, fx2);
+                    } else {
+                        fx2 += 2.f * (gr[uu][vv] * gr[uu][vv] + gi[uu][vv] * gi[uu][vv]);
+                    }
+                }
+    }
+    return make_float2(trx, fx2);
 }
 
 // Model functions at height z: h, dh/dz (FP32 on the fast path).
@@ -508,8 +652,11 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     const double Lpad = fabs(p.eps[0]) + fabs(p.eps[M - 1]) + 1.0 + p.sumV2;
     // thread i < N owns root i and warm-starts it from the previous step
     R lam_own = R(0);
-    // FP32 path: w64 holds, during the step loop, the FP64 roots of near-degenerate pairs (NaN for
-    // the others) and fp64_now whether this step refined any
+    // FP32 path: during the step loop the w64 region holds every root as a float pair whi + wlo
+    // (the FP64 root of a refined one, the FP32 root and 0 for the others), and fp64_now tells
+    // whether this step refined any
+    float* whi = (float*)w64;
+    float* wlo = whi + Np;
     bool fp64_now = false;
     int nfp64 = 0;
     auto roots = [&]() {  // after a barrier that published misc[4] = h
@@ -530,17 +677,22 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             __syncthreads();
             bool flag = false;
             if (tid < N && p.gap_fp64 > 0.0) {
-                const double lo = tid > 0 ? (double)lam[tid] - (double)lam[tid - 1] : 1e300;
-                const double hi = tid + 1 < N ? (double)lam[tid + 1] - (double)lam[tid] : 1e300;
-                flag = (lo < hi ? lo : hi) < p.gap_fp64;
-                double l64 = (double)lam_own;
+                // neighbouring roots differ by less than a factor of 2 where it matters, so the
+                // FP32 differences are exact there (Sterbenz)
+                const float lo = tid > 0 ? (float)lam[tid] - (float)lam[tid - 1] : 3.0e38f;
+                const float hi = tid + 1 < N ? (float)lam[tid + 1] - (float)lam[tid] : 3.0e38f;
+                flag = fminf(lo, hi) < (float)p.gap_fp64;
+                float h = (float)lam_own, l = 0.f;
                 if (flag) {
-                    double zz64;
+                    double l64 = (double)lam_own, zz64;
                     secular_root<double>(p.eps, p.V2, M, tid, hz, fabs(hz) + Lpad, l64, zz64, nonconv);
                     z0[tid] = (R)sqrt(zz64);
                     z2[tid] = (R)zz64;
+                    h = (float)l64;
+                    l = (float)(l64 - (double)h);
                 }
-                w64[tid] = flag ? l64 : __longlong_as_double(0x7ff8000000000000ll);
+                whi[tid] = h;
+                wlo[tid] = l;
             }
             fp64_now = __syncthreads_or(flag) != 0;
             nfp64 += fp64_now ? 1 : 0;
@@ -548,19 +700,41 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             __syncthreads();
         }
     };
-    // coupling denominator l_j - l_i: from the FP64 roots where both were refined
+    // coupling denominator l_j - l_i: on a step with refined roots from the float pairs (the high
+    // parts of close roots subtract exactly, the low parts add the FP64 remainder)
     auto gap = [&](int i, int j) -> R {
         if constexpr (std::is_same<R, float>::value) {
-            if (fp64_now) {
-                const double a = w64[i], b = w64[j];
-                if (a == a && b == b) return (R)(b - a);
-            }
+            if (fp64_now) return (whi[j] - whi[i]) + (wlo[j] - wlo[i]);
         }
         return lam[j] - lam[i];
     };
     // A_ij = z0_i z0_j / (l_j - l_i): from the step's matrix, or formed here where the tensor-core layout
     // keeps only its tf32 copy
     auto coup = [&](int i, int j) -> R { return tcp ? z0[i] * z0[j] / gap(i, j) : At[j * Np + i]; };
+    // FP32 path, bound on the hop estimate without the LU.  S = psi[occ, :] (Ne x Ne) and
+    // |det S|^2 = det G with G = S^H S, the Gram matrix of the occupied rows.  X = I - G is
+    // Hermitian; for its eigenvalues |mu| <= rho < 1, log(1 - mu) >= -mu - mu^2 / (2 (1 - rho)), so
+    //     -log |det S|^2 <= tr X + |X|_F^2 / (2 (1 - |X|_F))   when |X|_F < 1,
+    // and with |Re d| + |Im d| <= sqrt(2) |d| the estimate 2 dt sum|v.d| (|Re d| + |Im d|) / |d|^2
+    // of iesh.jl:253-256 is at most 2 sqrt(2) dt sum|v.d| / |det S|.
+    auto gram_partials = [&](float& trx, float& fx2) {
+        if constexpr (kF32) {
+            const float2 g = iesh_gram_partials(phiA, occ, Ne, Nep);
+            trx += g.x;
+            fx2 += g.y;
+        }
+    };
+    // The bound of gram_partials against u.  The margins cover the FP32 sums: each G entry sums
+    // at most 2 Ne products of unit-bounded terms (error below 3e-6 for Ne <= 64), so tr X is off by
+    // less than 2e-4 and |X|_F by less than 3e-4; sum|A| and exp by far less than 1 %.
+    auto estimate_certainly_below = [&](float trx, float fx2, float sabs, double wh_, float u_) -> bool {
+        const float tr = fmaxf(trx, 0.f) * 1.001f + 1e-3f;
+        const float fr = sqrtf(fmaxf(fx2, 0.f)) * 1.001f + 1e-3f;
+        if (!(fr < 0.95f)) return false;
+        const float ld = tr + fr * fr / (2.f * (1.f - fr));  // >= -log |det S|^2
+        const float bound = 2.8285f * (float)dt * fabsf((float)wh_) * sabs * expf(0.5f * ld);
+        return bound * 1.02f < u_;
+    };
     // ---- ring polymer ----
     // mean over the beads of warp 0 (the same value in every lane)
     auto bead_mean = [&](double x) {
@@ -892,26 +1066,28 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         __syncthreads();  // the next step rewrites the roots warp 0 just read
     };
     int isave = 0;
+    if (tid == 0) misc[16] = -1.0;  // no Bessel coefficients cached yet (FP32 path)
     if (p.save_stride > 0 && p.obs_partial) save(isave++);
 
     int nh = 0, nf = 0;
-    unsigned long long nfull = 0, nterms = 0;
+    unsigned long long nterms = 0;
+    unsigned nfull = 0, nlu = 0;  // per trajectory at most one per step
     for (int step = 1; step <= p.nsteps; ++step) {
         // ---- velocity Verlet (verlet_with_electronics.jl:55-63) ----
         // the integrator's dt (the shortened last step reaches t1); the hop probability and the
         // decoherence correction read get_proposed_dt, the full dt
         const double hs = step == p.nsteps ? p.h_last : dt, hh = hs / 2.0;
-        double vt[3];
         double vzc0 = 0.0;  // ring polymer: centroid v_z at the step's start
         if (warp == 0) {
+            if constexpr (RP) vzc0 = bead_mean(v[2]);
+            // v holds the half-step velocity until the second kick
 #pragma unroll
-            for (int d = 0; d < 3; ++d) vt[d] = v[d] + hh * k[d];
+            for (int d = 0; d < 3; ++d) v[d] = v[d] + hh * k[d];
             if constexpr (RP) {
-                vzc0 = bead_mean(v[2]);
-                free_step(r, vt);
+                free_step(r, v);
             } else {
 #pragma unroll
-                for (int d = 0; d < 3; ++d) r[d] = r[d] + hs * vt[d];
+                for (int d = 0; d < 3; ++d) r[d] = r[d] + hs * v[d];
             }
             publish_levels(hz, dhz);
         }
@@ -922,7 +1098,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         if (warp == 0) {
             accel(dhz);
 #pragma unroll
-            for (int d = 0; d < 3; ++d) v[d] = vt[d] + hh * k[d];
+            for (int d = 0; d < 3; ++d) v[d] = v[d] + hh * k[d];
             // v . grad h: the couplings are d_alpha = dh/dalpha A
             if constexpr (RP) {
                 const double vzc = bead_mean(v[2]);
@@ -960,39 +1136,87 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         __syncthreads();
         const double w = misc[6];
         const double wh = RP ? misc[12] : w;  // hops: v . grad h with the final (centroid) velocity
-        double elo = 1e300, ehi = -1e300;
-        if (tid < N) {
-            R sacc = R(0);
-            if (tcp) {  // row sums of the matrix the tensor cores multiply with
-                for (int j4 = 0; j4 < N / 4; ++j4) {
-                    const float4 a = *(const float4*)(bop + tc::smem_kmajor_offset(tid, 4 * j4, N));
-                    sacc += (R)(fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(a.w));
+        if constexpr (kF32) {
+            // FP32 path: the enclosure in FP32 (its margin covers the rounding), the Bessel
+            // coefficients for alpha = hw h rounded up to 1/32 (a wider enclosure is still one), kept
+            // in shared memory while alpha does not change (misc[16] alpha, misc[17] K)
+            float flo = 3.0e38f, fhi = -3.0e38f;
+            if (tid < N) {
+                float sacc = 0.f;
+                if (tcp) {  // row sums of the matrix the tensor cores multiply with
+                    for (int j4 = 0; j4 < N / 4; ++j4) {
+                        const float4 a = *(const float4*)(bop + tc::smem_kmajor_offset(tid, 4 * j4, N));
+                        sacc += fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(a.w);
+                    }
+                } else {
+                    for (int j = 0; j < N; ++j) sacc += fabsf((float)At[j * Np + tid]);
                 }
-            } else {
-                for (int j = 0; j < N; ++j) sacc += fabs(At[j * Np + tid]);
+                const float rad = fabsf((float)w) * sacc;
+                flo = (float)lam[tid] - rad;
+                fhi = (float)lam[tid] + rad;
             }
-            const double rad = fabs(w) * (double)sacc;
-            elo = (double)lam[tid] - rad;
-            ehi = (double)lam[tid] + rad;
-        }
-        iesh_block_minmax(elo, ehi, red);
-        if (warp == 0) {
-            // enclosure [c - hw, c + hw] of the spectrum, widened by a margin that
-            // covers the rounding of the bound in the working precision
-            const double cen = 0.5 * (ehi + elo);
-            const double hw = 0.5 * (ehi - elo) * (1.0 + (std::is_same<R, float>::value ? 1e-5 : 1e-12)) + 1e-300;
-            const int K = iesh_bessel_warp(hw * hs, p.cheb_tol, Jc, inv);
-            for (int q = lane; q < kIeshMaxTerms; q += 32) Jr[q] = (R)(2.0 * Jc[q]);
-            if (lane == 0) {
-                double sn, cs;
-                sincos(cen * hs, &sn, &cs);  // exp(-i c h) = cs - i sn
-                misc[0] = (double)K;
-                misc[1] = sn;
-                misc[2] = cs;
-                misc[8] = cen;
-                misc[9] = 1.0 / hw;
-                misc[10] = w / hw;
-                misc[11] = Jc[0];
+            iesh_block_minmax_f(flo, fhi, red);
+            if (warp == 0) {
+                const float cen = 0.5f * (fhi + flo);
+                const float hw = 0.5f * (fhi - flo) * (1.f + 1e-5f) + 1e-30f;
+                const float aq = ceilf(hw * (float)hs * 32.f) * (1.f / 32.f);
+                if ((double)aq != misc[16]) {  // the same in every lane
+                    const int Kq = iesh_bessel_warp_fast((double)aq, p.cheb_tol, Jc, inv);
+                    for (int q = lane; q < kIeshMaxTerms; q += 32) Jr[q] = (R)(2.0 * Jc[q]);
+                    __syncwarp();
+                    if (lane == 0) {
+                        misc[16] = (double)aq;
+                        misc[17] = (double)Kq;
+                    }
+                }
+                if (lane == 0) {
+                    float sn, cs;
+                    sincosf(cen * (float)hs, &sn, &cs);  // exp(-i c h) = cs - i sn
+                    const float hwq = aq / (float)hs;
+                    misc[0] = misc[17];
+                    misc[1] = (double)sn;
+                    misc[2] = (double)cs;
+                    misc[8] = (double)cen;
+                    misc[9] = (double)(1.f / hwq);
+                    misc[10] = (double)((float)w / hwq);
+                    misc[11] = Jc[0];
+                }
+            }
+        } else {
+        double elo = 1e300, ehi = -1e300;
+            if (tid < N) {
+                R sacc = R(0);
+                if (tcp) {  // row sums of the matrix the tensor cores multiply with
+                    for (int j4 = 0; j4 < N / 4; ++j4) {
+                        const float4 a = *(const float4*)(bop + tc::smem_kmajor_offset(tid, 4 * j4, N));
+                        sacc += (R)(fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(a.w));
+                    }
+                } else {
+                    for (int j = 0; j < N; ++j) sacc += fabs(At[j * Np + tid]);
+                }
+                const double rad = fabs(w) * (double)sacc;
+                elo = (double)lam[tid] - rad;
+                ehi = (double)lam[tid] + rad;
+            }
+            iesh_block_minmax(elo, ehi, red);
+            if (warp == 0) {
+                // enclosure [c - hw, c + hw] of the spectrum, widened by a margin that
+                // covers the rounding of the bound in the working precision
+                const double cen = 0.5 * (ehi + elo);
+                const double hw = 0.5 * (ehi - elo) * (1.0 + (std::is_same<R, float>::value ? 1e-5 : 1e-12)) + 1e-300;
+                const int K = iesh_bessel_warp(hw * hs, p.cheb_tol, Jc, inv);
+                for (int q = lane; q < kIeshMaxTerms; q += 32) Jr[q] = (R)(2.0 * Jc[q]);
+                if (lane == 0) {
+                    double sn, cs;
+                    sincos(cen * hs, &sn, &cs);  // exp(-i c h) = cs - i sn
+                    misc[0] = (double)K;
+                    misc[1] = sn;
+                    misc[2] = cs;
+                    misc[8] = cen;
+                    misc[9] = 1.0 / hw;
+                    misc[10] = w / hw;
+                    misc[11] = Jc[0];
+                }
             }
         }
         __syncthreads();
@@ -1020,6 +1244,10 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     const uint32_t tl = tmem + ((uint32_t)(32 * tq) << 16);
                     const uint32_t cD = 0, cP = (uint32_t)N, cO = 2u * (uint32_t)N;
                     const float sgn = tcmp ? -1.f : 1.f;
+                    // The A operand keeps each component in its partner's row (re of electron e in row
+                    // 2 e + 1, im in row 2 e), so that accumulator row tn holds A times the partner
+                    // component, the one H_t phi needs for component tcmp, without a shuffle.
+                    const int arow = tn ^ 1;
                     // phi_{k-1} of this thread's states i0 .. i0 + 7 from the A operand (zero off the rows)
                     auto get_a = [&](int i0, float (&v)[8]) {
                         if (!trow) {
@@ -1027,7 +1255,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                             for (int t = 0; t < 8; ++t) v[t] = 0.f;
                             return;
                         }
-                        const uint32_t o0 = tc::smem_kmajor_offset(tn, i0, N), o1 = tc::smem_kmajor_offset(tn, i0 + 4, N);
+                        const uint32_t o0 = tc::smem_kmajor_offset(arow, i0, N), o1 = tc::smem_kmajor_offset(arow, i0 + 4, N);
                         const float4 h0 = *(const float4*)(aop_hi + o0), h1 = *(const float4*)(aop_hi + o1);
                         const float4 l0 = *(const float4*)(aop_lo + o0), l1 = *(const float4*)(aop_lo + o1);
                         v[0] = h0.x + l0.x; v[1] = h0.y + l0.y; v[2] = h0.z + l0.z; v[3] = h0.w + l0.w;
@@ -1045,12 +1273,15 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                             hv1[t] = tc::to_tf32(v[4 + t]);
                             lv1[t] = tc::to_tf32(v[4 + t] - hv1[t]);
                         }
-                        const uint32_t o0 = tc::smem_kmajor_offset(tn, i0, N), o1 = tc::smem_kmajor_offset(tn, i0 + 4, N);
+                        const uint32_t o0 = tc::smem_kmajor_offset(arow, i0, N), o1 = tc::smem_kmajor_offset(arow, i0 + 4, N);
                         *(float4*)(aop_hi + o0) = h0;
                         *(float4*)(aop_hi + o1) = h1;
                         *(float4*)(aop_lo + o0) = l0;
                         *(float4*)(aop_lo + o1) = l1;
                     };
+                    // (lam_i - c) / hw of every state, read by the terms as float4 pairs
+                    float* dlt = (float*)(smem + L.o_dl);
+                    for (int i = tid; i < N; i += nthr) dlt[i] = (lam[i] - cenf) * ihwf;
                     // phi_0 = psi; series sum J_0 phi_0
                     if (twarp) {
                         const float j0 = (float)misc[11];
@@ -1095,8 +1326,13 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                         }
                         tc::fence_after_sync();
                         if (twarp) {
+                            // series sum += 2 J_k (-i)^k phi_k: even k add +-2 J_k phi_k to the same
+                            // component, odd k +-2 J_k times the partner component (one shuffle)
                             const float jk = (float)Jr[kk];
                             const int ph = kk & 3;
+                            const bool odd = (kk & 1) != 0;
+                            const float cjk = (ph < 2 ? jk : -jk) * (odd ? sgn : 1.f);
+                            const float sst = sgn * st;
 #pragma unroll
                             for (int q = 0; q < 5; ++q) {
                                 if (8 * q >= NH) break;
@@ -1106,21 +1342,23 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                                 tc::ld8(tl + cD + i0, d);
                                 if (kk > 1) tc::ld8(tl + cP + i0, p2);
                                 tc::ld8(tl + cO + i0, o);
+                                const float4 dl0 = *(const float4*)(dlt + i0), dl1 = *(const float4*)(dlt + i0 + 4);
+                                const float dl[8] = {dl0.x, dl0.y, dl0.z, dl0.w, dl1.x, dl1.y, dl1.z, dl1.w};
                                 tc::wait_ld();
 #pragma unroll
                                 for (int t = 0; t < 8; ++t) {
-                                    // Ht phi = dl phi - i s (A phi): the partner lane holds the other component
-                                    const float dp = __shfl_xor_sync(0xffffffffu, d[t], 1);
-                                    const float dl = (lam[i0 + t] - cenf) * ihwf;
-                                    const float hv = dl * p1[t] + sgn * st * dp;
-                                    nw[t] = kk == 1 ? hv : 2.f * hv - p2[t];
-                                    const float np = __shfl_xor_sync(0xffffffffu, nw[t], 1);
-                                    // series sum += 2 J_k (-i)^k phi_k
-                                    if (ph == 0) o[t] += jk * nw[t];
-                                    else if (ph == 1) o[t] += sgn * jk * np;
-                                    else if (ph == 2) o[t] -= jk * nw[t];
-                                    else o[t] -= sgn * jk * np;
+                                    // Ht phi = dl phi - i s (A phi); d is A times the partner component
+                                    const float hv = fmaf(dl[t], p1[t], sst * d[t]);
+                                    nw[t] = kk == 1 ? hv : fmaf(2.f, hv, -p2[t]);
                                     p2[t] = p1[t];
+                                }
+                                if (odd) {
+#pragma unroll
+                                    for (int t = 0; t < 8; ++t)
+                                        o[t] = fmaf(cjk, __shfl_xor_sync(0xffffffffu, nw[t], 1), o[t]);
+                                } else {
+#pragma unroll
+                                    for (int t = 0; t < 8; ++t) o[t] = fmaf(cjk, nw[t], o[t]);
                                 }
                                 tc::st8(tl + cP + i0, p2);
                                 tc::st8(tl + cO + i0, o);
@@ -1258,6 +1496,26 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
 
         if (!ena) {  // EhrenfestNA: no hopping
         // ---- hop test (iesh.jl:231-335, 390-411) ----
+        // FP32 path: where the bound on the estimate from the occupied Gram matrix already lies
+        // below the random number, the estimate does too and the LU is not needed (the decision
+        // and every result are those of the LU path); sabs_pre is then the step's sum |A_mn|
+        bool lu = true;
+        float sabs_pre = 0.f;
+        if constexpr (kF32) {
+            if (!p.exact_probability && !p.lu_always) {
+                float trx = 0.f, fx2 = 0.f;
+                gram_partials(trx, fx2);
+                for (int q = tid; q < Nu * Ne; q += nthr) {
+                    const int mm = q / Ne, n = q - mm * Ne;
+                    sabs_pre += fabsf(coup(unocc[mm], occ[n]));
+                }
+                iesh_block_sum3_f(trx, fx2, sabs_pre, red);
+                lu = !estimate_certainly_below(trx, fx2, sabs_pre, wh,
+                                               rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP));
+            }
+        }
+        if (lu) {
+        ++nlu;
         // S^T stored by columns: column c of S^T is row occ[c] of psi, Qc[c * Nep + r] = S^T[r][c]
         Cx<R>* Qc = phiB;
         Cx<R>* Rh = phiB + Nep * Nep;  // right-hand sides psi[unocc, :]^T, [Nep][Nu]
@@ -1385,7 +1643,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 det_i = (double)di;
                 det_e = de;
             }
-        } else {
+        } else if (!(kF32 && !p.exact_probability && !p.lu_always)) {  // else the sum is sabs_pre
             // sum |v.d| over unoccupied rows and electrons (the estimate's sum(abs, v_dot_d))
             for (int q = tid - 32; q < Nu * Ne; q += nthr - 32) {
                 const int mm = q / Ne, n = q - mm * Ne;
@@ -1394,7 +1652,8 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         }
         double sumabs;
         if constexpr (std::is_same<R, float>::value)
-            sumabs = fabs(wh) * (double)iesh_block_sum_f(sabs, red);
+            sumabs = fabs(wh) * (double)(!p.exact_probability && !p.lu_always ? sabs_pre
+                                                                              : iesh_block_sum_f(sabs, red));
         else
             sumabs = fabs(wh) * iesh_block_sum((double)sabs, red);
         const double u = std::is_same<R, double>::value
@@ -1514,6 +1773,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 else v[2] = misc[3];
             }
         }
+        }  // lu
         }  // !ena
         if (p.edc_C > 0.0) {
             // DecoherenceCorrectionEDC (decoherence_corrections.jl:21-39, callback
@@ -1584,8 +1844,9 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             p.energy[NT + ti] = e1;
         }
         if (p.counters) {
-            atomicAdd(p.counters + 0, nfull);
+            atomicAdd(p.counters + 0, (unsigned long long)nfull);
             atomicAdd(p.counters + 1, nterms);
+            atomicAdd(p.counters + 5, (unsigned long long)nlu);
         }
     }
     if constexpr (tcp) {

@@ -240,7 +240,8 @@ struct nqcd_handle {
     int64_t redtmp_cap = 0;
     double* d_popcorr = nullptr;
     unsigned long long* d_counts = nullptr;  // [0..3] scatter, [4..7] stats, [8..11] method counters,
-                                             // [12] FP64-electronics steps, [16..19] surrogate judge
+                                             // [12] FP64-electronics steps, [13] IESH overlap LUs,
+                                             // [16..19] surrogate judge
     double* d_stage = nullptr;               // staging for layout gathers
     int64_t stage_cap = 0;
     // ring polymers: normal-mode tables per instantiated bead count, bead-count classes
@@ -1214,6 +1215,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         q.fp64_steps = h->d_fp64steps;
         q.tensor = (h->cfg.precision != NQCD_PREC_FP64 && h->map.iesh_cores == 0 &&
                     iesh_tc_shape(q.nstates, q.nelec)) ? 1 : 0;
+        q.lu_always = h->map.iesh_lu_always;
         q.nbeads = h->rp_beads;
         if (h->rp_beads > 1) {
             // ring polymer: normal modes and full-step Cayley matrices of the free ring polymer
@@ -1338,6 +1340,7 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         stats->unconverged_roots = (int64_t)counts[10];
         stats->hop_evaluations = iesh ? (int64_t)counts[8] : 0;
         stats->propagator_terms = iesh ? (int64_t)counts[9] : 0;
+        stats->overlap_factorizations = iesh ? (int64_t)counts[13] : 0;
         stats->hops = (int64_t)counts[5];
         stats->frustrated = (int64_t)counts[6];
         stats->flagged = (int64_t)counts[7];
@@ -1614,6 +1617,8 @@ int nqcd_set_mapping(nqcd_handle* h, const nqcd_mapping* m) {
         return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: rp_one_launch must be 0 or 1");
     if (m->iesh_cores != 0 && m->iesh_cores != 1)
         return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: iesh_cores must be 0 (tensor cores) or 1 (CUDA cores)");
+    if (m->iesh_lu_always != 0 && m->iesh_lu_always != 1)
+        return fail(h, NQCD_ERR_ARG, "nqcd_set_mapping: iesh_lu_always must be 0 or 1");
     if (m->sb_lanes == 8) {
         const bool sb = h->cfg.model == NQCD_MODEL_SPINBOSON && h->cfg.method != NQCD_METHOD_RPSH;
         if (sb && (h->cfg.precision != NQCD_PREC_FP32_KAHAN || h->cfg.nbath > 128))

@@ -104,6 +104,7 @@ class nqcd_stats(C.Structure):
         ("surrogate_rejected", C.c_int64),
         ("surrogate_max_rel_error", C.c_double),
         ("surrogate_mean_rel_error", C.c_double),
+        ("overlap_factorizations", C.c_int64),
     ]
 
 
@@ -120,19 +121,21 @@ class nqcd_mapping(C.Structure):
     """Launch shapes of the fast kernels (nqcd_gpu.h, nqcd_set_mapping)."""
 
     _fields_ = [("sb_lanes", C.c_int32), ("sb_block", C.c_int32), ("rp_lanes", C.c_int32 * 4),
-                ("iesh_cores", C.c_int32), ("rp_one_launch", C.c_int32)]
+                ("iesh_cores", C.c_int32), ("rp_one_launch", C.c_int32), ("iesh_lu_always", C.c_int32)]
 
 
 RP_LANE_BEADS = (4, 8, 16, 32)  # bead counts of nqcd_mapping.rp_lanes
 
 
-def mapping(sb_lanes=0, sb_block=0, rp_lanes=None, iesh_cores=0, rp_one_launch=0):
+def mapping(sb_lanes=0, sb_block=0, rp_lanes=None, iesh_cores=0, rp_one_launch=0, iesh_lu_always=0):
     """nqcd_mapping from keyword values; rp_lanes: {bead count: lanes};
     iesh_cores: 0 tensor cores, 1 CUDA cores for the IESH propagator;
-    rp_one_launch: 1 serves every bead count from one persistent launch."""
+    rp_one_launch: 1 serves every bead count from one persistent launch;
+    iesh_lu_always: 1 runs the IESH overlap LU every step (0: only where
+    the Gram-matrix bound does not settle the hop estimate)."""
     m = nqcd_mapping()
     m.sb_lanes, m.sb_block, m.iesh_cores = int(sb_lanes), int(sb_block), int(iesh_cores)
-    m.rp_one_launch = int(rp_one_launch)
+    m.rp_one_launch, m.iesh_lu_always = int(rp_one_launch), int(iesh_lu_always)
     for q, b in enumerate(RP_LANE_BEADS):
         m.rp_lanes[q] = int((rp_lanes or {}).get(b, 0))
     return m

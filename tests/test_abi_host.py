@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol():
     lib = L.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.nqcd_version() == 109
+    assert lib.nqcd_version() == 110
 
 
 def _cfg(**kw):

@@ -53,9 +53,11 @@ def oracle_model(wl):
                       V=wl["V"])
 
 
-def run_engine(wl, n, nsteps, seed, state0_arr=None, **kw):
+def run_engine(wl, n, nsteps, seed, state0_arr=None, mapping=None, **kw):
     eng = make_iesh(wl, n, **kw)
     try:
+        if mapping:
+            eng.set_mapping(mapping)
         eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]), state0=state0_arr)
         _, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], seed)
         fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
@@ -111,6 +113,37 @@ def test_iesh_estimate_screen_never_changes_results(precision):
         np.testing.assert_array_equal(a[key], b[key], err_msg=key)
     assert b["stats"].hop_evaluations == n * nsteps
     assert a["stats"].hop_evaluations < b["stats"].hop_evaluations
+
+
+@pytest.mark.parametrize("cores,nbeads,z0", [(0, 0, 3.0), (1, 0, 3.0), (0, 4, 3.0), (0, 0, None)])
+def test_iesh_gram_bound_never_changes_results(cores, nbeads, z0):
+    """FP32 path: the hop tests whose estimate the Gram-matrix bound settles skip the LU of the
+    overlap matrix; every result equals that of the LU in every step (iesh_lu_always = 1).  Through
+    the level crossing (z0 = 3) the orbitals leave the occupied space and many steps still need the
+    LU; on the benchmark's scattering workload almost none do."""
+    n, nsteps = 64, 600
+    kz = {} if z0 is None else dict(z0=z0)
+    wl = WL.newns_anderson_rpiesh(n, nbeads, **kz) if nbeads else WL.newns_anderson_iesh(n, **kz)
+    kw = dict(precision=L.PREC_FP32, nbeads=nbeads)
+    a = run_engine(wl, n, nsteps, 17, mapping=dict(iesh_cores=cores), **kw)
+    b = run_engine(wl, n, nsteps, 17, mapping=dict(iesh_cores=cores, iesh_lu_always=1), **kw)
+    if z0 is not None:
+        assert b["stats"].hops > 0
+    for key in ("r", "v", "psi", "state", "nhops", "nfrustrated", "hop_log", "energy"):
+        np.testing.assert_array_equal(a[key], b[key], err_msg=key)
+    assert a["stats"].hop_evaluations == b["stats"].hop_evaluations
+    assert b["stats"].overlap_factorizations == n * nsteps
+    print("overlap LUs with the bound:", a["stats"].overlap_factorizations, "of", n * nsteps, "z0", z0)
+    assert a["stats"].hop_evaluations <= a["stats"].overlap_factorizations < n * nsteps
+    if z0 is None:
+        assert a["stats"].overlap_factorizations < n * nsteps // 2
+
+
+def test_iesh_fp64_factorizes_every_step():
+    n, nsteps = 8, 100
+    wl = WL.newns_anderson_iesh(n, z0=3.0)
+    fin = run_engine(wl, n, nsteps, 17)
+    assert fin["stats"].overlap_factorizations == n * nsteps
 
 
 @pytest.mark.parametrize("precision,tol", [(L.PREC_FP64, 1e-10), (L.PREC_FP32, 2e-4)])

@@ -106,7 +106,7 @@ def test_mapping_rejects_unknown_shapes():
     eng = C.spinboson_fssh(L, w, c, 8, 100, L.PREC_FP32)
     try:
         for bad in (dict(sb_lanes=3), dict(sb_block=96), dict(rp_lanes={4: 8}), dict(rp_lanes={32: 2}),
-                    dict(iesh_cores=2), dict(rp_one_launch=2)):
+                    dict(iesh_cores=2), dict(rp_one_launch=2), dict(iesh_lu_always=2)):
             with pytest.raises(L.EngineError) as e:
                 eng.set_mapping(bad)
             assert e.value.code == L.NQCD_ERR_ARG
