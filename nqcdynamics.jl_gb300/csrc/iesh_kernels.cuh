@@ -456,61 +456,50 @@ constexpr int iesh_min_blocks() {
 }
 
 // Per-thread partial sums of tr X and |X|_F^2 for X = I - G, G = S^H S the Gram matrix of the
-// occupied rows of the orbitals (FP32 path, see the hop-estimate bound in iesh_body): 2 x 2 tiles
-// of G over the upper block triangle, the sum over occupied rows split in four parts held by lanes
-// 4 t .. 4 t + 3.  Out of line, so that its registers do not add to the step loop's.
+// occupied rows of the orbitals (FP32 path, see the hop-estimate bound in iesh_body): one 2 x 2
+// tile of G per thread over the upper block triangle, summed over all occupied rows.  Out of
+// line, so that its registers do not add to the step loop's.
 static __device__ __noinline__ float2 iesh_gram_partials(const Cx<float>* phiA, const int32_t* occ, int Ne, int Nep) {
-    const int tid = threadIdx.x, nthr = blockDim.x;
     float trx = 0.f, fx2 = 0.f;
     const int nbk = (Ne + 1) >> 1, ntile = nbk * (nbk + 1) / 2;
-    for (int base = 0; base < 4 * ntile; base += nthr) {  // the same trip count in every thread
-        const int q = base + tid, part = q & 3;
-        const bool on = q < 4 * ntile;
-        int t = on ? q >> 2 : 0, bi = 0;
-        while (t >= nbk - bi) {  // tile t, row-major over the upper block triangle
-            t -= nbk - bi;
-            ++bi;
-        }
-        const int a0 = 2 * bi, b0 = 2 * (bi + t);
+    for (int t = threadIdx.x; t < ntile; t += blockDim.x) {
+        // tile t, row-major over the upper block triangle: block row bi starts at
+        // bi nbk - bi (bi - 1) / 2; the float estimate of bi is corrected by the integer tests
+        const float c = 2.f * (float)nbk + 1.f;
+        int bi = (int)((c - sqrtf(c * c - 8.f * (float)t)) * 0.5f);
+        bi = bi < 0 ? 0 : (bi >= nbk ? nbk - 1 : bi);
+        while (bi > 0 && bi * nbk - bi * (bi - 1) / 2 > t) --bi;
+        while (bi + 1 < nbk && (bi + 1) * nbk - (bi + 1) * bi / 2 <= t) ++bi;
+        const int bj = bi + t - (bi * nbk - bi * (bi - 1) / 2);
+        const int a0 = 2 * bi, b0 = 2 * bj;
         float gr[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, gi[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-        if (on)
-            for (int j = part; j < Ne; j += 4) {  // columns a0, a0 + 1 < Nep of row occ[j]
-                const float4* row = (const float4*)(phiA + occ[j] * Nep);
-                const float4 x = row[a0 >> 1], y = row[b0 >> 1];
-                const float xr[2] = {x.x, x.z}, xi[2] = {x.y, x.w};
-                const float yr[2] = {y.x, y.z}, yi[2] = {y.y, y.w};
-#pragma unroll
-                for (int uu = 0; uu < 2; ++uu)
-#pragma unroll
-                    for (int vv = 0; vv < 2; ++vv) {  // conj(x) y
-                        gr[uu][vv] = fmaf(xr[uu], yr[vv], fmaf(xi[uu], yi[vv], gr[uu][vv]));
-                        gi[uu][vv] = fmaf(xr[uu], yi[vv], fmaf(-xi[uu], yr[vv], gi[uu][vv]));
-                    }
-            }
-#pragma unroll
-        for (int uu = 0; uu < 2; ++uu)
-#pragma unroll
-            for (int vv = 0; vv < 2; ++vv)
-#pragma unroll
-                for (int off = 1; off <= 2; off <<= 1) {
-                    gr[uu][vv] += __shfl_xor_sync(0xffffffffu, gr[uu][vv], off);
-                    gi[uu][vv] += __shfl_xor_sync(0xffffffffu, gi[uu][vv], off);
-                }
-        if (on && part == 0)
+        for (int j = 0; j < Ne; ++j) {  // columns a0, a0 + 1 < Nep of row occ[j]
+            const float4* row = (const float4*)(phiA + occ[j] * Nep);
+            const float4 x = row[a0 >> 1], y = row[b0 >> 1];
+            const float xr[2] = {x.x, x.z}, xi[2] = {x.y, x.w};
+            const float yr[2] = {y.x, y.z}, yi[2] = {y.y, y.w};
 #pragma unroll
             for (int uu = 0; uu < 2; ++uu)
 #pragma unroll
-                for (int vv = 0; vv < 2; ++vv) {
-                    const int a = a0 + uu, b = b0 + vv;
-                    if (a >= Ne || b >= Ne || a > b) continue;
-                    if (a == b) {
-                        const float d = 1.f - gr[uu][vv];
-                        trx += d;
-                        fx2 = fmaf(d, d, fx2);
-                    } else {
-                        fx2 += 2.f * (gr[uu][vv] * gr[uu][vv] + gi[uu][vv] * gi[uu][vv]);
-                    }
+                for (int vv = 0; vv < 2; ++vv) {  // conj(x) y
+                    gr[uu][vv] = fmaf(xr[uu], yr[vv], fmaf(xi[uu], yi[vv], gr[uu][vv]));
+                    gi[uu][vv] = fmaf(xr[uu], yi[vv], fmaf(-xi[uu], yr[vv], gi[uu][vv]));
                 }
+        }
+#pragma unroll
+        for (int uu = 0; uu < 2; ++uu)
+#pragma unroll
+            for (int vv = 0; vv < 2; ++vv) {
+                const int a = a0 + uu, b = b0 + vv;
+                if (a >= Ne || b >= Ne || a > b) continue;
+                if (a == b) {
+                    const float d = 1.f - gr[uu][vv];
+                    trx += d;
+                    fx2 = fmaf(d, d, fx2);
+                } else {
+                    fx2 += 2.f * (gr[uu][vv] * gr[uu][vv] + gi[uu][vv] * gi[uu][vv]);
+                }
+            }
     }
     return make_float2(trx, fx2);
 }
@@ -1115,17 +1104,27 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         if (tcp) {
             // the coupling matrix rounded to tf32 as the B operand (row i, k = j); rounding to
             // nearest keeps it antisymmetric, so H_eff stays Hermitian.  Consecutive threads take
-            // consecutive rows: their 16-byte stores fill one core matrix each (no bank conflicts)
+            // consecutive rows: their 16-byte stores fill one core matrix each (no bank conflicts).
+            // The quotient takes the approximate reciprocal (2 ulp, far below the tf32 rounding;
+            // it is odd in the denominator, so the matrix stays antisymmetric)
+            int j4 = tid / N, i = tid - j4 * N;
+            const int sj = nthr / N, si = nthr - sj * N;
             for (int q = tid; q < N * (N / 4); q += nthr) {
-                const int j4 = q / N, i = q - j4 * N;
+                const float zi = (float)z0[i];
                 float4 a;
                 float* av = &a.x;
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int j = 4 * j4 + t;
-                    av[t] = i == j ? 0.f : tc::to_tf32((float)(z0[i] * z0[j] / gap(i, j)));
+                    av[t] = i == j ? 0.f : tc::to_tf32(__fdividef(zi * (float)z0[j], (float)gap(i, j)));
                 }
                 *(float4*)(bop + tc::smem_kmajor_offset(i, 4 * j4, N)) = a;
+                i += si;
+                j4 += sj;
+                if (i >= N) {
+                    i -= N;
+                    ++j4;
+                }
             }
         } else {
             for (int q = tid; q < N * N; q += nthr) {
@@ -1374,20 +1373,31 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     // psi = exp(-i c h) sum
                     const float snf = (float)misc[1], csf = (float)misc[2];
                     if (twarp) {
+                        // the series-sum columns in two batches of loads, each with one wait: a
+                        // wait for TMEM loads takes long while the tensor cores run the other
+                        // CTA's products
 #pragma unroll
-                        for (int q = 0; q < 5; ++q) {
-                            if (8 * q >= NH) break;
-                            const int i0 = s0 + 8 * q;
-                            float o[8];
-                            tc::ld8(tl + cO + i0, o);
+                        for (int b = 0; b < 2; ++b) {
+                            float o[3][8];
+#pragma unroll
+                            for (int g = 0; g < 3; ++g) {
+                                const int q = 3 * b + g;
+                                if (q < 5 && 8 * q < NH) tc::ld8(tl + cO + s0 + 8 * q, o[g]);
+                            }
                             tc::wait_ld();
 #pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                const float op = __shfl_xor_sync(0xffffffffu, o[t], 1);
-                                const float val = tcmp ? o[t] * csf - op * snf : o[t] * csf + op * snf;
-                                if (trow) {
-                                    Cx<R>& c = phiA[(i0 + t) * Nep + te];
-                                    if (tcmp) c.im = val; else c.re = val;
+                            for (int g = 0; g < 3; ++g) {
+                                const int q = 3 * b + g;
+                                if (q >= 5 || 8 * q >= NH) break;
+                                const int i0 = s0 + 8 * q;
+#pragma unroll
+                                for (int t = 0; t < 8; ++t) {
+                                    const float op = __shfl_xor_sync(0xffffffffu, o[g][t], 1);
+                                    const float val = tcmp ? o[g][t] * csf - op * snf : o[g][t] * csf + op * snf;
+                                    if (trow) {
+                                        Cx<R>& c = phiA[(i0 + t) * Nep + te];
+                                        if (tcmp) c.im = val; else c.re = val;
+                                    }
                                 }
                             }
                         }
@@ -1505,9 +1515,9 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             if (!p.exact_probability && !p.lu_always) {
                 float trx = 0.f, fx2 = 0.f;
                 gram_partials(trx, fx2);
-                for (int q = tid; q < Nu * Ne; q += nthr) {
-                    const int mm = q / Ne, n = q - mm * Ne;
-                    sabs_pre += fabsf(coup(unocc[mm], occ[n]));
+                for (int q = tid; q < 4 * Nu; q += nthr) {  // unoccupied state q / 4, a quarter of the electrons
+                    const int m = unocc[q >> 2];
+                    for (int n = q & 3; n < Ne; n += 4) sabs_pre += fabsf(coup(m, occ[n]));
                 }
                 iesh_block_sum3_f(trx, fx2, sabs_pre, red);
                 lu = !estimate_certainly_below(trx, fx2, sabs_pre, wh,

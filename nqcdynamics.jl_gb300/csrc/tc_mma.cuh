@@ -166,10 +166,12 @@ __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Round to tf32 (nearest, ties away), returned in an fp32 container.
+// Round to the nearest tf32 value, ties away from zero (cvt.rna.tf32.f32's rounding), with two
+// integer instructions: add half a tf32 unit to the magnitude bits and clear the 13 low bits.
+// Exact for every finite float whose rounding stays finite; symmetric in the sign, so an
+// antisymmetric matrix stays antisymmetric.
 __device__ __forceinline__ float to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
 }
 
 }  // namespace tc
