@@ -1390,14 +1390,15 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                                 const int q = 3 * b + g;
                                 if (q >= 5 || 8 * q >= NH) break;
                                 const int i0 = s0 + 8 * q;
+                                // states t, t + 1 of electron te: the re lane writes state t and the im
+                                // lane state t + 1, each as one 8-byte element (one shuffle per pair;
+                                // single-component 4-byte stores from lane pairs were far slower)
 #pragma unroll
-                                for (int t = 0; t < 8; ++t) {
-                                    const float op = __shfl_xor_sync(0xffffffffu, o[g][t], 1);
-                                    const float val = tcmp ? o[g][t] * csf - op * snf : o[g][t] * csf + op * snf;
-                                    if (trow) {
-                                        Cx<R>& c = phiA[(i0 + t) * Nep + te];
-                                        if (tcmp) c.im = val; else c.re = val;
-                                    }
+                                for (int t = 0; t < 8; t += 2) {
+                                    const float y = __shfl_xor_sync(0xffffffffu, tcmp ? o[g][t] : o[g][t + 1], 1);
+                                    const float re = tcmp ? y : o[g][t], im = tcmp ? o[g][t + 1] : y;
+                                    if (trow)
+                                        phiA[(i0 + t + tcmp) * Nep + te] = {re * csf + im * snf, im * csf - re * snf};
                                 }
                             }
                         }
