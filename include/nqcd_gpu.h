@@ -70,8 +70,9 @@ enum nqcd_model {
                                       bath_a = bath levels e_k (ascending), bath_b = couplings V_k */
     NQCD_MODEL_NEWNS_ANDERSON_3D = 21 /* AndersonHolstein, one atom (x, y, z) above the metal:
                                       U0 = kxy (x^2+y^2)/2 + A exp(-a z), h = U1 - U0 = delta - B exp(-b z);
-                                      params: kxy, A, a, delta, B, b; bath_a = e_k (ascending),
-                                      bath_b = V_k; nstates = nbath + 1 */
+                                      params: kxy, A, a, delta, B, b (IESH, EhrenfestNA), then mu, sigma
+                                      (MDEF: ndofs = 3, the friction tensor along z); bath_a = e_k
+                                      (ascending), bath_b = V_k; nstates = nbath + 1 */
 };
 
 enum nqcd_precision {
@@ -264,10 +265,12 @@ int nqcd_set_trajectory_models(nqcd_handle* h, const int32_t* models);
 /* MDEF: exact Fermi-weighted force and broadened friction of the model at n
  * positions (host arrays), the quantities of DiabaticMDEF's acceleration! and
  * friction! (src/DynamicsMethods/ClassicalMethods/mdef.jl:102-140), evaluated on
- * the GPU with the handle's precision. */
+ * the GPU with the handle's precision.  For the 3-D adsorbate x holds heights z,
+ * force the z component of the gradient and friction the tensor's zz entry
+ * (its only nonzero one). */
 int nqcd_mdef_evaluate(nqcd_handle* h, int64_t n, const double* x, double* force, double* friction);
 
-/* MDEF friction surrogate (1-64-64-1 network, BF16 weights): generate npoints
+/* MDEF friction surrogate on the one-dimensional model (1-64-64-1 network, BF16 weights): generate npoints
  * exact friction values at positions uniform in [x_lo, x_hi] with the engine,
  * then train the network on the GPU (BF16 tensor-core kernels, FP32 master
  * weights, Adam with the step size decaying from learning_rate to

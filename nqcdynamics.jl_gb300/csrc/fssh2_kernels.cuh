@@ -355,7 +355,8 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
                 nf += 1;
             }
         }
-        if (p.save_stride > 0 && step % p.save_stride == 0) {
+        // save points are the multiples of save_stride: a product, not an integer division per step
+        if (p.save_stride > 0 && step == isave * p.save_stride) {
             double pop[2];
             diabatic_pop2<R>(sg, state, Z, pop, ehr);
             warp_save_popcorr(p, isave++, active, pop0, pop);
@@ -490,7 +491,8 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_fast_kernel(const Fssh
                 nf += 1;
             }
         }
-        if (p.save_stride > 0 && step % p.save_stride == 0) {
+        // save points are the multiples of save_stride: a product, not an integer division per step
+        if (p.save_stride > 0 && step == isave * p.save_stride) {
             float pf[2];
             diabatic_pop2_f(sg, state, Z, pf, ehr);
             warp_save_popcorr_f(p, isave++, active, pop0, pf);
@@ -723,7 +725,8 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
                 nf += 1;
             }
         }
-        if (p.save_stride > 0 && step % p.save_stride == 0) {
+        // save points are the multiples of save_stride: a product, not an integer division per step
+        if (p.save_stride > 0 && step == isave * p.save_stride) {
             double pop[2];
             diabatic_pop2<R>(sg, state, Z, pop, ehr);
             warp_save_popcorr(p, isave++, active, pop0, pop);

@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
                 nf += 1;
             }
         }
-        if (p.save_stride > 0 && step % p.save_stride == 0) {
+        // save points are the multiples of save_stride: a product, not an integer division per step
+        if (p.save_stride > 0 && step == isave * p.save_stride) {
             float pop[2];
             diabatic_pop2_f(sg, state, Z, pop, ehr);
             warp_save_popcorr_f(p, isave++, active && lead, pop0, pop);

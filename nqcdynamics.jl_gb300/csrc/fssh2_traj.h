@@ -250,7 +250,15 @@ NQCD_HD void electronic_macro_step2_fast(const InterpS32& fn, float h, float dts
 // fast path compares in FP32; it differs from the 53-bit draw only below 2^-24).
 NQCD_HD float rng_uniform_f(uint64_t seed, uint64_t traj, uint32_t step, uint32_t stream) {
     u32x4 b = rng_block(seed, traj, step, stream);
+#ifdef __CUDA_ARCH__
+    // (float)(b.x >> 8) without a conversion instruction (conversions issue on this GPU's FP64
+    // unit): the top 23 bits through the exponent bias 2^23, exact, doubled, plus the last bit
+    const uint32_t x = b.x >> 8;
+    const float hi = __uint_as_float(0x4B000000u | (x >> 1)) - 8388608.0f;
+    return fmaf(2.0f, hi, (x & 1u) ? 1.0f : 0.0f) * 0x1.0p-24f;
+#else
     return (float)(b.x >> 8) * 0x1.0p-24f;
+#endif
 }
 
 // clamp(x, 0, 1) with the reference's NaN propagation.

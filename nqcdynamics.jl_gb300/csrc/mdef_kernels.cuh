@@ -61,6 +61,11 @@ struct MdefParams {
     const double* eps;   // [nbath] ascending
     const double* V2;    // [nbath] V_k^2
     double k, g, delta;  // impurity: U0 = k x^2/2, h = k g (g/2 - x) + delta
+    // model3d = 1: the three-dimensional adsorbate (one atom, x, y, z; state [3][ntraj]):
+    // U0 = kxy (x^2 + y^2)/2 + A exp(-a z), h = delta - B exp(-b z).  Its friction tensor
+    // F grad h grad h^T has the one nonzero eigenvalue F (dh/dz)^2 along z.
+    int32_t model3d;
+    double kxy, A, a, B, b;
     double mu, beta, sigma;
     double mass;
     int64_t ntraj, traj_offset;
@@ -120,13 +125,31 @@ __device__ __forceinline__ void fermi_pair(R e, R mu, R beta, R& f, R& df) {
 
 // Electronic structure at x for the warp's trajectory: all roots, force and
 // (optionally) friction.  Roots and weights are also left in shared memory.
-template <typename R>
+template <typename R, bool D3 = false>
 __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib, R lam[kMdefRootsPerLane],
                                 double x, bool want_friction, double& force, double& friction) {
     const int lane = threadIdx.x & 31;
     const int M = p.nbath;
-    const R h = (R)(p.k * p.g * (p.g / 2.0 - x) + p.delta);
-    const R dh = (R)(-p.k * p.g);
+    // x is the height z for the three-dimensional adsorbate; dU0 its derivative of U0
+    R h, dh;
+    double dU0;
+    if constexpr (D3) {
+        if constexpr (std::is_same<R, float>::value) {
+            const float e = expf(-(float)p.b * (float)x);
+            h = (float)p.delta - (float)p.B * e;
+            dh = (float)p.B * (float)p.b * e;
+            dU0 = -p.A * p.a * (double)expf(-(float)p.a * (float)x);
+        } else {
+            const double e = nqcd_exp(-p.b * x);
+            h = p.delta - p.B * e;
+            dh = p.B * p.b * e;
+            dU0 = -p.A * p.a * nqcd_exp(-p.a * x);
+        }
+    } else {
+        h = (R)(p.k * p.g * (p.g / 2.0 - x) + p.delta);
+        dh = (R)(-p.k * p.g);
+        dU0 = p.k * x;
+    }
     const R mu = (R)p.mu, beta = (R)p.beta;
     R Lb = fabs(h) + R(2);
     R accF = R(0);
@@ -145,7 +168,7 @@ __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib,
     }
     // warp sum in the working precision (no FP64 shuffle-adds on the fast path)
     for (int off = 16; off > 0; off >>= 1) accF += __shfl_xor_sync(0xffffffffu, accF, off);
-    force = p.k * x + (double)dh * (double)accF;
+    force = dU0 + (double)dh * (double)accF;
     friction = 0.0;
     if (!want_friction) return;
     __syncwarp();
@@ -218,7 +241,9 @@ __device__ __forceinline__ float noise_normal_f(uint64_t seed, uint64_t traj, ui
     return sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
 }
 
-template <typename R>
+// D3: the three-dimensional adsorbate (p.model3d), a separate instantiation so that the
+// one-dimensional kernel keeps its registers
+template <typename R, bool D3>
 __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams p) {
     __shared__ MdefShared<R> sh;
     for (int k = threadIdx.x; k < p.nbath; k += blockDim.x) {
@@ -238,12 +263,21 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         int idx = lane + 32 * q;
         lam[q] = idx == 0 ? sh.eps[0] - R(1e-3) : (idx <= M ? sh.eps[idx - 1] + R(1e-9) : R(0));
     }
-    double x = p.x[i], v = p.v[i];
+    // x, v: the coordinate the electronic structure depends on (z of the three-dimensional
+    // adsorbate, whose x, y move in the harmonic U0 alone: rx, ry, vx, vy); single-evaluation
+    // mode reads p.x as a list of those coordinates
+    const bool single = p.force_out || p.friction_out;
+    const bool d3 = D3 && !single;
+    const int64_t NT = p.ntraj;
+    double x = p.x[d3 ? 2 * NT + i : i], v = p.v[d3 ? 2 * NT + i : i];
+    double rx = d3 ? p.x[i] : 0.0, ry = d3 ? p.x[NT + i] : 0.0;
+    double vx = d3 ? p.v[i] : 0.0, vy = d3 ? p.v[NT + i] : 0.0;
     const double m = p.mass, T = 1.0 / p.beta, dt = p.dt, half = 0.5;
     const float inv_m_f = (float)(1.0 / m), sig_f = (float)sqrt(T / m);
+    const uint32_t zdof = d3 ? 2u : 0u;  // noise stream of the friction's direction
     double F, fr;
-    mdef_electronic<R>(p, sh, wib, lam, x, p.friction_out != nullptr, F, fr);
-    if (p.force_out || p.friction_out) {  // single-evaluation mode (force/friction tables, training data)
+    mdef_electronic<R, D3>(p, sh, wib, lam, x, p.friction_out != nullptr, F, fr);
+    if (single) {  // single-evaluation mode (force/friction tables, training data)
         if (active && lane == 0) {
             if (p.force_out) p.force_out[i] = F;
             if (p.friction_out) p.friction_out[i] = fr;
@@ -262,6 +296,9 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         }
         double s = (double)acc;
         for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (d3)
+            return 0.5 * m * (vx * vx + vy * vy + v * v) + 0.5 * p.kxy * (rx * rx + ry * ry) +
+                   p.A * (std::is_same<R, float>::value ? (double)expf(-(float)p.a * (float)x) : nqcd_exp(-p.a * x)) + s;
         return 0.5 * m * v * v + 0.5 * p.k * x * x + s;
     };
     const double e0 = p.energy ? total_energy() : 0.0;
@@ -272,7 +309,7 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
             double* dst = p.obs_partial + ((int64_t)(blockIdx.x * kMdefWarps + wib) * p.nsave + isave) * 4;
             dst[0] = x;
             dst[1] = x * x;
-            dst[2] = 0.5 * m * v * v;
+            dst[2] = 0.5 * m * (vx * vx + vy * vy + v * v);
             dst[3] = lamv;
         }
         ++isave;
@@ -286,6 +323,12 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
         const double hs = step == p.nsteps ? p.h_last : dt;
         v = v + (half * hs) * k;  // B
         x = x + (half * hs) * v;  // A
+        if (d3) {  // x, y: harmonic U0, no friction (the O step leaves them)
+            vx = vx + (half * hs) * (-(p.kxy * rx) / m);
+            vy = vy + (half * hs) * (-(p.kxy * ry) / m);
+            rx = rx + (half * hs) * vx;
+            ry = ry + (half * hs) * vy;
+        }
         double lamv;
         bool in_domain = false, judge = false;
         if constexpr (std::is_same<R, float>::value) {
@@ -298,7 +341,7 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
             ++n_mlp;
         } else {
             double Fm;
-            mdef_electronic<R>(p, sh, wib, lam, x, true, Fm, lamv);
+            mdef_electronic<R, D3>(p, sh, wib, lam, x, true, Fm, lamv);
             ++n_exact;
             if (judge) {  // the exact friction (mdef.jl:131-140) judges the network at this step
                 const double net = (double)mlp_friction(p.mlp, (float)x);
@@ -316,27 +359,42 @@ __global__ void __launch_bounds__(32 * kMdefWarps) mdef_kernel(const MdefParams 
             if (gdt < 0.f) gdt = 0.f;
             const float c1 = expf(-gdt);
             const float c2 = sqrtf(-expm1f(-2.f * gdt));
-            const float xi = noise_normal_f(p.seed, gid, (uint32_t)step);
+            const float xi = noise_normal_f(p.seed, gid, (uint32_t)step, zdof);
             v = (double)c1 * v + (double)(c2 * sig_f * xi);
         } else {
             double gam = lamv / m;  // friction / (sqrt m sqrt m)
             if (gam < 0.0) gam = 0.0;
             double c1 = exp(-gam * hs);
             double c2 = sqrt(1.0 - c1 * c1);
-            double xi = noise_normal(p.seed, gid, (uint32_t)step);
+            double xi = noise_normal(p.seed, gid, (uint32_t)step, zdof);
             v = c1 * v + c2 * (sqrt(T / m) * xi);  // O
         }
         x = x + (half * hs) * v;                // A
         double Fn, dummy;
-        mdef_electronic<R>(p, sh, wib, lam, x, false, Fn, dummy);
+        mdef_electronic<R, D3>(p, sh, wib, lam, x, false, Fn, dummy);
         k = -Fn / m;
         v = v + (half * hs) * k;  // B
-        if (p.save_stride > 0 && step % p.save_stride == 0) save(lamv);
+        if (d3) {
+            rx = rx + (half * hs) * vx;
+            ry = ry + (half * hs) * vy;
+            vx = vx + (half * hs) * (-(p.kxy * rx) / m);
+            vy = vy + (half * hs) * (-(p.kxy * ry) / m);
+        }
+        // save points are the multiples of save_stride: a product, not an integer division per step
+        if (p.save_stride > 0 && step == isave * p.save_stride) {
+            save(lamv);
+        }
     }
     const double e1 = p.energy ? total_energy() : 0.0;
     if (!active || lane != 0) return;
-    p.x[i] = x;
-    p.v[i] = v;
+    p.x[d3 ? 2 * NT + i : i] = x;
+    p.v[d3 ? 2 * NT + i : i] = v;
+    if (d3) {
+        p.x[i] = rx;
+        p.x[NT + i] = ry;
+        p.v[i] = vx;
+        p.v[NT + i] = vy;
+    }
     if (p.energy) {
         p.energy[i] = e0;
         p.energy[p.ntraj + i] = e1;
@@ -485,7 +543,10 @@ cudaError_t launch_mdef(const MdefParams& p, cudaStream_t s) {
     if (p.ntraj <= 0) return cudaSuccess;
     if (p.nbath > kMdefMaxBath || p.nbath < 1) return cudaErrorInvalidValue;
     int64_t blocks = (p.ntraj + kMdefWarps - 1) / kMdefWarps;
-    mdef_kernel<R><<<(unsigned)blocks, 32 * kMdefWarps, 0, s>>>(p);
+    if (p.model3d)
+        mdef_kernel<R, true><<<(unsigned)blocks, 32 * kMdefWarps, 0, s>>>(p);
+    else
+        mdef_kernel<R, false><<<(unsigned)blocks, 32 * kMdefWarps, 0, s>>>(p);
     return cudaGetLastError();
 }
 

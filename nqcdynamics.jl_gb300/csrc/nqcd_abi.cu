@@ -367,11 +367,23 @@ MdefParams mdef_params(nqcd_handle* h, int64_t N, double dt, int32_t nsteps, uin
     m.nbath = h->cfg.nbath;
     m.eps = h->d_eps;
     m.V2 = h->d_V2;
-    m.k = h->params[0];
-    m.g = h->params[1];
-    m.delta = h->params[2];
-    m.mu = h->params[3];
-    m.sigma = h->params[4];
+    if (h->cfg.model == NQCD_MODEL_NEWNS_ANDERSON_3D) {
+        m.model3d = 1;
+        m.kxy = h->params[0];
+        m.A = h->params[1];
+        m.a = h->params[2];
+        m.delta = h->params[3];
+        m.B = h->params[4];
+        m.b = h->params[5];
+        m.mu = h->params[6];
+        m.sigma = h->params[7];
+    } else {
+        m.k = h->params[0];
+        m.g = h->params[1];
+        m.delta = h->params[2];
+        m.mu = h->params[3];
+        m.sigma = h->params[4];
+    }
     m.beta = h->cfg.beta;
     m.mass = h->mass0;
     m.ntraj = N;
@@ -458,10 +470,18 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
                 return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: ring-polymer IESH system too large for one CTA");
         }
     } else if (mdef) {
-        if (model != NQCD_MODEL_NEWNS_ANDERSON)
-            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs on the Newns-Anderson model");
-        if (cfg->ndofs * cfg->natoms != 1)
-            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs one adsorbate degree of freedom");
+        const bool m3 = model == NQCD_MODEL_NEWNS_ANDERSON_3D;
+        if (model != NQCD_MODEL_NEWNS_ANDERSON && !m3)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED, "nqcd_create: MDEF runs on the Newns-Anderson models");
+        if (m3 ? (cfg->natoms != 1 || cfg->ndofs != 3) : cfg->ndofs * cfg->natoms != 1)
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED,
+                        "nqcd_create: MDEF runs one degree of freedom (displaced harmonic) or one atom in three "
+                        "dimensions (adsorbate)");
+        if (m3 && (cfg->nparams < 8 || !cfg->params || !(cfg->params[7] > 0.0)))
+            return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: the 3-D adsorbate needs kxy, A, a, delta, B, b, mu, sigma > 0");
+        if (m3 && (cfg->nbeads_max > 1 || cfg->use_friction_surrogate))
+            return fail(nullptr, NQCD_ERR_UNSUPPORTED,
+                        "nqcd_create: MDEF on the 3-D adsorbate runs classical nuclei with the exact friction");
         if (cfg->nbath < 1 || cfg->nbath > kMdefMaxBath || !cfg->bath_a || !cfg->bath_b)
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: MDEF needs 1..512 bath levels and couplings");
         for (int k = 1; k < cfg->nbath; ++k)
@@ -469,7 +489,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
                 return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bath levels must be strictly ascending");
         for (int k = 0; k < cfg->nbath; ++k)
             if (cfg->bath_b[k] == 0.0) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: bath couplings must be nonzero");
-        if (cfg->nparams < 5 || !cfg->params || !(cfg->params[4] > 0.0))
+        if (!m3 && (cfg->nparams < 5 || !cfg->params || !(cfg->params[4] > 0.0)))
             return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: Newns-Anderson needs k, g, delta, mu, sigma > 0");
         if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: MDEF needs beta > 0");
         if (cfg->nbeads_max > 1) {  // RingPolymerSimulation{DiabaticMDEF}
@@ -519,7 +539,7 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
     const bool rp_iesh = iesh && cfg->nbeads_max > 1;
     const int64_t ndof = (rp || rp_mdef) ? (int64_t)cfg->nbeads_max
                                          : (int64_t)cfg->ndofs * cfg->natoms * (rp_iesh ? cfg->nbeads_max : 1);
-    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? 5 : (iesh ? 6 : 4))));
+    int need_params = model == NQCD_MODEL_TULLY2 ? 5 : (model == NQCD_MODEL_TULLY3 ? 3 : (model == NQCD_MODEL_SPINBOSON ? 2 : (mdef ? (model == NQCD_MODEL_NEWNS_ANDERSON_3D ? 8 : 5) : (iesh ? 6 : 4))));
     if (cfg->nparams < need_params || !cfg->params)
         return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: too few model parameters");
     if (mdef || iesh) {
@@ -1485,8 +1505,8 @@ __global__ void cholesky_target_kernel(const double* fric, double* L, int64_t n)
 int nqcd_train_friction_mlp(nqcd_handle* h, double x_lo, double x_hi, int64_t npoints, int32_t epochs, int32_t batch,
                             double learning_rate, uint64_t seed, double* final_loss) {
     if (!h) return NQCD_ERR_ARG;
-    if (h->cfg.method != NQCD_METHOD_MDEF)
-        return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_train_friction_mlp: MDEF handles only");
+    if (h->cfg.method != NQCD_METHOD_MDEF || h->cfg.model != NQCD_MODEL_NEWNS_ANDERSON)
+        return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_train_friction_mlp: MDEF handles of the one-dimensional model only");
     if (!(x_hi > x_lo) || npoints < 16 || epochs < 1 || batch < 16 || batch > 65536 || !(learning_rate > 0))
         return fail(h, NQCD_ERR_ARG, "nqcd_train_friction_mlp: bad domain, sizes or learning rate");
     cudaStream_t s = h->stream;
@@ -1564,7 +1584,8 @@ int nqcd_mlp_get(nqcd_handle* h, float* params, double* meta) {
 
 int nqcd_mlp_set(nqcd_handle* h, const float* params, const double* meta) {
     if (!h || !params || !meta) return NQCD_ERR_ARG;
-    if (h->cfg.method != NQCD_METHOD_MDEF) return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_mlp_set: MDEF handles only");
+    if (h->cfg.method != NQCD_METHOD_MDEF || h->cfg.model != NQCD_MODEL_NEWNS_ANDERSON)
+        return fail(h, NQCD_ERR_UNSUPPORTED, "nqcd_mlp_set: MDEF handles of the one-dimensional model only");
     if (!isfinite(meta[0]) || !(meta[1] > 0.0 && meta[1] < 1e300) || !isfinite(meta[2]) || !isfinite(meta[3]) ||
         !(meta[3] > meta[2]))
         return fail(h, NQCD_ERR_ARG, "nqcd_mlp_set: need finite shift, scale > 0 and a domain lo < hi");

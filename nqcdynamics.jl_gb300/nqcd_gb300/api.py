@@ -291,8 +291,9 @@ class Simulation(metaclass=_MethodIndexed):
         self.model = model
         self.temperature = float(temperature)
         if method is DiabaticMDEF:
-            if not isinstance(model, AndersonHolstein) or model.kind != L.MODEL_NEWNS_ANDERSON:
-                raise NotImplementedError("DiabaticMDEF runs on AndersonHolstein(DisplacedHarmonic(...), bath)")
+            if not isinstance(model, AndersonHolstein):
+                raise NotImplementedError("DiabaticMDEF runs on AndersonHolstein(DisplacedHarmonic(...) or "
+                                          "AdsorbateMetal3D(...), bath)")
             if not isinstance(friction_method, GaussianBroadening):
                 raise ValueError("DiabaticMDEF needs friction_method=GaussianBroadening(sigma)")
             if not temperature > 0:
@@ -838,7 +839,11 @@ def _metal_config(sim, ntraj, alg, save_stride):
     cfg.ndofs, cfg.natoms, cfg.nstates = model.ndofs, 1, model.nstates
     imp = model.impurity
     if mdef:
-        params = np.array([imp.k, imp.g, imp.delta, model.fermi_level, sim.friction_method.σ])
+        if isinstance(imp, AdsorbateMetal3D):  # three coordinates; the friction tensor acts along z
+            params = np.array([imp.kxy, imp.A, imp.a, imp.delta, imp.B, imp.b, model.fermi_level,
+                               sim.friction_method.σ])
+        else:
+            params = np.array([imp.k, imp.g, imp.delta, model.fermi_level, sim.friction_method.σ])
         cfg.beta = 1.0 / sim.temperature
         cfg.use_friction_surrogate = int(alg.friction_surrogate is not None)
         cfg.exact_friction_every = alg.exact_friction_every
@@ -914,8 +919,9 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
         nsteps = int(round((t1 - t0) / dt))
         obs = np.zeros(((nsteps // save_stride + 1) if save_stride else 1) * 4)
         out, stats = eng.run(t0, t1, dt, alg.seed if seed is None else seed, observables=obs)
+        mdef_dofs = sim.n_beads if rp else sim.model.ndofs
         if isinstance(reduction, FileReduction):
-            final = eng.get_final(sim.n_beads if rp else 1) if mdef else \
+            final = eng.get_final(mdef_dofs) if mdef else \
                 eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
             return reduction.write([t0, t1], _per_trajectory(outputs, final, (r0, v0), hops=not mdef))
         ob = obs[: out.nsave * 4].reshape(out.nsave, 4)
@@ -928,14 +934,14 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
             if name == "OutputKineticEnergy":
                 result[name] = ob[:, 2] if mdef else ob[:, 1]
             elif name == "OutputPosition":
-                result[name] = ob[:, 0]  # MDEF: x; IESH: height z
+                result[name] = ob[:, 0]  # MDEF: x (3-D adsorbate: z); IESH: height z
             elif name == "OutputPotentialEnergy" and not mdef:
                 result[name] = ob[:, 3]
             elif name == "OutputImpurityPopulation" and not mdef:
                 result[name] = ob[:, 2]
             elif name in ("OutputFinal", "OutputTotalEnergy", "OutputSurfaceHops"):
                 if final is None:  # ring polymers: r, v (ntraj, nbeads, ...)
-                    final = eng.get_final(sim.n_beads if rp else 1) if mdef else \
+                    final = eng.get_final(mdef_dofs) if mdef else \
                         eng.get_final_iesh(sim.model.nstates, sim.model.nelectrons)
                 if name == "OutputFinal":
                     result[name] = final

@@ -111,6 +111,26 @@ def mdef_newns_anderson(L, wl, ntraj, precision, surrogate=False, exact_friction
     return L.Engine(cfg, [params, masses, eps, V])
 
 
+def mdef_adsorbate3d(L, wl, ntraj, precision, save_stride=0, traj_offset=0, mu=0.0, sigma=0.01):
+    """MDEF on the three-dimensional adsorbate of the IESH system (one atom,
+    x, y, z): the friction tensor has its one nonzero eigenvalue along z."""
+    P = wl["params"]
+    cfg = L.nqcd_config()
+    cfg.method, cfg.model, cfg.precision = L.METHOD_MDEF, L.MODEL_NEWNS_ANDERSON_3D, precision
+    cfg.ndofs, cfg.natoms, cfg.nstates = 3, 1, 1 + len(wl["eps"])
+    params = np.array([P["kxy"], P["A"], P["a"], P["delta"], P["B"], P["b"], mu, sigma])
+    masses = np.array([wl["mass"]])
+    eps = np.ascontiguousarray(wl["eps"])
+    V = np.ascontiguousarray(wl["V"])
+    cfg.nparams, cfg.params, cfg.masses = 8, L.dptr(params), L.dptr(masses)
+    cfg.nbath, cfg.bath_a, cfg.bath_b = len(eps), L.dptr(eps), L.dptr(V)
+    cfg.beta = wl["beta"]
+    cfg.ntraj_max = ntraj
+    cfg.save_stride = save_stride
+    cfg.traj_offset = traj_offset
+    return L.Engine(cfg, [params, masses, eps, V])
+
+
 def iesh_newns_anderson(L, wl, ntraj, precision, rescaling=0, save_stride=0, max_hops=0, exact=0, traj_offset=0,
                         method=None, nbeads=0, gap_fp64=1e-3):
     """C5: IESH on the three-dimensional Newns-Anderson adsorbate, Fermi-Dirac

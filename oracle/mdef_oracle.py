@@ -4,6 +4,8 @@ A numpy FP64 restatement of NQCDynamics.jl's electronic-friction Langevin
 dynamics on the Newns-Anderson (AndersonHolstein) model:
 
   MDEF_BAOAB.perform_step!   src/DynamicsMethods/IntegrationAlgorithms/mdef_baoab.jl:163-180
+                             (one degree of freedom: run_mdef; the 3-D adsorbate with
+                             the friction tensor's eigen-decomposition: run_mdef3d)
   step_O!                    src/DynamicsMethods/IntegrationAlgorithms/steps.jl:41-69
   DiabaticMDEF acceleration! src/DynamicsMethods/ClassicalMethods/mdef.jl:102-124
   friction!                  src/DynamicsMethods/ClassicalMethods/mdef.jl:131-140
@@ -141,13 +143,15 @@ def electronic(model, x, beta, sigma, want_friction=True):
 
 
 def run_mdef(model: NewnsAnderson, *, mass, beta, sigma, x0, v0, dt, nsteps, seed, traj_offset=0,
-             friction_fn=None, h_last=None):
+             friction_fn=None, h_last=None, noise_dof=0):
     """BAOAB with friction in the tensor's eigenbasis (1 DoF: a scalar).
     friction_fn(x) may replace the exact friction (surrogate runs).
     h_last: length of the last step when the time span is not a whole number
     of steps; every sub-step of BAOAB reads the integrator's dt, the
     shortened one on the last step (mdef_baoab.jl:163-180, steps.jl:41-69),
-    and the noise dW / sqrt(dt) is a standard normal whatever the step."""
+    and the noise dW / sqrt(dt) is a standard normal whatever the step.
+    noise_dof: the Philox stream of the degree of freedom (0 for the
+    one-dimensional model)."""
     x = np.asarray(x0, np.float64).copy()
     v = np.asarray(v0, np.float64).copy()
     traj = np.arange(len(x), dtype=np.uint64) + np.uint64(traj_offset)
@@ -165,12 +169,69 @@ def run_mdef(model: NewnsAnderson, *, mass, beta, sigma, x0, v0, dt, nsteps, see
         gam = np.maximum(lam / mass, 0.0)               # Lambda / (sqrt m sqrt m), clamp(gamma, 0, Inf)
         c1 = np.exp(-gam * hs)
         c2 = np.sqrt(1.0 - c1 * c1)
-        noise = np.sqrt(T / mass) * normal(seed, traj, step)
+        noise = np.sqrt(T / mass) * normal(seed, traj, step, dof=noise_dof)
         v = c1 * v + c2 * noise                         # O
         x = x + (half * hs) * v                         # A
         k = -electronic(model, x, beta, sigma, want_friction=False)["F"] / mass
         v = v + (half * hs) * k                         # B
     return x, v
+
+
+def electronic3d(model, r, mu, beta, sigma, want_friction=True):
+    """The 3-D adsorbate (oracle.iesh_oracle.Metal3D, the IESH benchmark system)
+    with DiabaticMDEF: eigen-decomposition of H(r), gradient
+    dU0 + sum_i (d e_i f_i + f'_i d e_i e_i) with d_I e_i = (Z^T d_I H Z)_ii
+    (mdef.jl:102-124), and the friction tensor
+    Lambda_IJ = sum_nm -pi (Z^T d_I H Z)_nm (Z^T d_J H Z)_mn g_sigma(e_n - e_m) f'(e_n)
+    over the three coordinates.  r: (n, 3)."""
+    w, Z = np.linalg.eigh(model.hamiltonian(r))
+    gh = model.grad_h(r)                                   # d_I h; d_I H = d_I h e_0 e_0^T
+    z0 = Z[:, 0, :]
+    dH = gh[:, :, None, None] * (z0[:, None, :, None] * z0[:, None, None, :])  # (n, 3, N, N)
+    deps = np.einsum("tInn->tIn", dH)
+    f = fermi(w, mu, beta)
+    df = dfermi(w, mu, beta)
+    F = model.grad_U0(r) + np.sum(deps * (f + df * w)[:, None, :], axis=2)
+    out = {"w": w, "F": F}
+    if want_friction:
+        de = w[:, :, None] - w[:, None, :]
+        g = np.exp(-0.5 * de * de / sigma**2) / (sigma * np.sqrt(2 * np.pi))
+        out["friction"] = np.einsum("tInm,tJmn,tnm,tn->tIJ", dH, dH, -np.pi * g, df)
+    return out
+
+
+def run_mdef3d(model, *, mass, mu, beta, sigma, r0, v0, dt, nsteps, seed, traj_offset=0, h_last=None):
+    """MDEF_BAOAB on the 3-D adsorbate: B, A, O with the friction tensor's
+    eigen-decomposition (steps.jl:41-69: Lambda / m, eigenvalues clamped at 0,
+    c1 = exp(-gamma dt), c2 = sqrt(1 - c1^2), v <- C c1 C^T v + C c2 C^T noise,
+    one standard normal per degree of freedom I from the Philox stream of dof I),
+    A, B.  r0, v0: (n, 3).  Returns r, v."""
+    r = np.asarray(r0, np.float64).copy()
+    v = np.asarray(v0, np.float64).copy()
+    n = len(r)
+    traj = np.arange(n, dtype=np.uint64) + np.uint64(traj_offset)
+    T = 1.0 / beta
+    k = -electronic3d(model, r, mu, beta, sigma, want_friction=False)["F"] / mass
+    for step in range(1, nsteps + 1):
+        hs = h_last if (h_last is not None and step == nsteps) else dt
+        v = v + (0.5 * hs) * k                                         # B
+        r = r + (0.5 * hs) * v                                         # A
+        gam, C = np.linalg.eigh(electronic3d(model, r, mu, beta, sigma)["friction"] / mass)
+        gam = np.maximum(gam, 0.0)
+        c1 = np.exp(-gam * hs)
+        c2 = np.sqrt(1.0 - c1 * c1)
+        noise = np.sqrt(T / mass) * np.stack([normal(seed, traj, step, dof=I) for I in range(3)], axis=1)
+        v = np.einsum("tij,tj->ti", C, c1 * np.einsum("tji,tj->ti", C, v)) + \
+            np.einsum("tij,tj->ti", C, c2 * np.einsum("tji,tj->ti", C, noise))  # O
+        r = r + (0.5 * hs) * v                                         # A
+        k = -electronic3d(model, r, mu, beta, sigma, want_friction=False)["F"] / mass
+        v = v + (0.5 * hs) * k                                         # B
+    return r, v
+
+
+def energy3d(model, r, v, mass, mu, beta):
+    w, _ = np.linalg.eigh(model.hamiltonian(r))
+    return 0.5 * mass * np.sum(v * v, axis=1) + model.U0(r) + np.sum(w * fermi(w, mu, beta), axis=1)
 
 
 def energy(model, x, v, mass, beta):

@@ -851,3 +851,43 @@ def test_rpsh_oracle_matches_a_continuous_integration():
         np.testing.assert_allclose(o["v"][t], v, rtol=1e-3)
         np.testing.assert_allclose(o["sigma"][t], sig, atol=1e-3)
     assert nhop > 0  # the comparison covers hops
+
+
+def test_mdef3d_oracle_reduces_to_one_dimension():
+    """The 3-D MDEF restatement (friction tensor diagonalised as steps.jl:41-69
+    does) with the atom on the z axis at rest in x, y follows the
+    one-dimensional restatement of the same z-model: x and y stay 0, the
+    tensor's only nonzero eigenvalue is along z, and z takes the noise of
+    degree of freedom 2."""
+    import iesh_oracle as IO
+    import mdef_oracle as MO
+
+    eps = np.linspace(-0.5, 0.5, 30)
+    V = 0.04 * np.sqrt(eps[1] - eps[0]) * np.ones_like(eps)
+    m3 = IO.Metal3D(kxy=2e-3, A=0.05, a=1.2, delta=0.05, B=0.3, b=0.8, eps=eps, V=V)
+
+    class ZModel:
+        mu = 0.0
+
+        def dh(self, z):
+            return m3.B * m3.b * np.exp(-m3.b * z)
+
+        def dU0(self, z):
+            return -m3.A * m3.a * np.exp(-m3.a * z)
+
+        def hamiltonian(self, z):
+            return m3.hamiltonian(np.stack([np.zeros_like(z), np.zeros_like(z), z], axis=1))
+
+    n, mass, beta, sigma, dt = 6, 1837.0, 1000.0, 0.01, 20.0
+    z0 = np.linspace(1.5, 3.5, n)
+    vz0 = np.linspace(-3e-3, 1e-3, n)
+    r0 = np.stack([np.zeros(n), np.zeros(n), z0], axis=1)
+    v0 = np.stack([np.zeros(n), np.zeros(n), vz0], axis=1)
+    r, v = MO.run_mdef3d(m3, mass=mass, mu=0.0, beta=beta, sigma=sigma, r0=r0, v0=v0, dt=dt, nsteps=40, seed=5)
+    z, vz = MO.run_mdef(ZModel(), mass=mass, beta=beta, sigma=sigma, x0=z0, v0=vz0, dt=dt, nsteps=40, seed=5,
+                        noise_dof=2)
+    assert np.all(r[:, :2] == 0.0) and np.all(v[:, :2] == 0.0)
+    np.testing.assert_allclose(r[:, 2], z, rtol=1e-12)
+    np.testing.assert_allclose(v[:, 2], vz, rtol=1e-10, atol=1e-15)
+    lam = MO.electronic3d(m3, r0, 0.0, beta, sigma)["friction"]
+    assert np.all(lam[:, 2, 2] > 0) and np.all(lam[:, :2, :] == 0) and np.all(lam[:, :, :2] == 0)
