@@ -50,7 +50,7 @@ struct FsshParams {
     int32_t* nsteps;          // [ntraj]
     int32_t* hop_log;         // [max_hops][3][ntraj]
     double* energy;           // [2][ntraj]
-    double* popcorr_partial;  // [nwarps][nsave][4]
+    double* popcorr_partial;  // [nwarps][nsave][4] doubles (plain paths) or floats (fast paths)
     unsigned long long* scatter;  // [4]
     int32_t* fp64_steps;      // [ntraj] fast paths: steps whose electronics ran in FP64 (gap below gap_fp64)
     // launch shape of the fast spin-boson kernel (nqcd_set_mapping; 0 = default)
@@ -73,6 +73,8 @@ inline int fssh2_lanes_per_traj(int model, int precision, int sb_group = 4) {
 // fixed chunks in parallel (tmp: [reduce_chunks(nparts, width)][width]) and the
 // chunk sums in ascending order.
 int64_t reduce_chunks(int64_t nparts, int64_t width);
+cudaError_t launch_reduce_partials(const float* partial, int64_t nparts, int64_t width, double* tmp, double* out,
+                                   cudaStream_t s);
 cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* tmp, double* out,
                                    cudaStream_t s);
 

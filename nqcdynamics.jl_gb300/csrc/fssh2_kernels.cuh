@@ -210,10 +210,10 @@ __device__ __forceinline__ void warp_save_popcorr_f(const FsshParams& p, int isa
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) c[q] += __shfl_xor_sync(0xffffffffu, c[q], off);
     if ((threadIdx.x & 31) == 0 && isave < p.nsave) {
+        // FP32 partial sums, one 16-byte store (the fast paths' buffer holds floats; the host
+        // reduction sums them in FP64): no FP32-to-FP64 conversion in the step loop
         int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        double* dst = p.popcorr_partial + (warp * p.nsave + isave) * 4;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) dst[q] = (double)c[q];
+        reinterpret_cast<float4*>(p.popcorr_partial)[warp * p.nsave + isave] = make_float4(c[0], c[1], c[2], c[3]);
     }
 }
 

@@ -571,6 +571,12 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     // misc: [0] K [1] sin(c dt) [2] cos(c dt), then the full-evaluation flag [3] v_z [4] h [5] dh/dz
     //       [6] v . grad h [8] c [9] 1/hw [10] w/hw [11] J_0
     double* misc = (double*)(smem + L.o_misc);
+    // FP32 path: the same step values as floats and ints, written once by their producer so that
+    // their readers convert nothing (conversions issue on this GPU's FP64 unit): mf[1] sin, [2] cos,
+    // [4] h, [5] root bracket |h| + L, [6] v . grad h, [8] c, [9] 1/hw, [10] w/hw, [11] J_0,
+    // [12] final centroid v . grad h, [13] cached alpha; mi[0] K
+    float* mf = (float*)(misc + 20);
+    int* mi = (int*)(misc + 28);
     // ring polymer: rph[b] h, rph[NB + b] dh/dz, rph[2 NB + b] sum of occupied z0^2, rph[3 NB + b] sum of
     // occupied eigenvalues of bead b; rpq [6][NB] normal-mode scratch.  misc[12] v . grad h of the final
     // centroid velocity (hops), [13] final centroid v_z, [14] centroid z
@@ -652,7 +658,10 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         const double hz = misc[4];
         if (tid < N) {
             R zz;
-            secular_root<R>(eps, V2, M, tid, (R)hz, (R)(fabs(hz) + Lpad), lam_own, zz, nonconv);
+            if constexpr (kF32)
+                secular_root<R>(eps, V2, M, tid, mf[4], mf[5], lam_own, zz, nonconv);
+            else
+                secular_root<R>(eps, V2, M, tid, (R)hz, (R)(fabs(hz) + Lpad), lam_own, zz, nonconv);
             lam[tid] = lam_own;
             z2[tid] = zz;
             z0[tid] = sqrt(zz);
@@ -716,12 +725,12 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
     // The bound of gram_partials against u.  The margins cover the FP32 sums: each G entry sums
     // at most 2 Ne products of unit-bounded terms (error below 3e-6 for Ne <= 64), so tr X is off by
     // less than 2e-4 and |X|_F by less than 3e-4; sum|A| and exp by far less than 1 %.
-    auto estimate_certainly_below = [&](float trx, float fx2, float sabs, double wh_, float u_) -> bool {
+    auto estimate_certainly_below = [&](float trx, float fx2, float sabs, float wh_, float u_) -> bool {
         const float tr = fmaxf(trx, 0.f) * 1.001f + 1e-3f;
         const float fr = sqrtf(fmaxf(fx2, 0.f)) * 1.001f + 1e-3f;
         if (!(fr < 0.95f)) return false;
         const float ld = tr + fr * fr / (2.f * (1.f - fr));  // >= -log |det S|^2
-        const float bound = 2.8285f * (float)dt * fabsf((float)wh_) * sabs * expf(0.5f * ld);
+        const float bound = 2.8285f * (float)dt * fabsf(wh_) * sabs * expf(0.5f * ld);
         return bound * 1.02f < u_;
     };
     // ---- ring polymer ----
@@ -750,6 +759,10 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         if (lane == 0) {
             misc[4] = hz_;
             misc[5] = dhz_;
+            if constexpr (kF32) {
+                mf[4] = (float)hz_;
+                mf[5] = (float)(fabs(hz_) + Lpad);
+            }
         }
     };
     // roots of the occupied states of every bead (warp w: beads w, w + 8, ...; lane: electrons lane,
@@ -785,6 +798,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     rph[3 * NB + b] = (double)sl;
                 }
             }
+            if (tid == 0) misc[15] = 0.0;  // the sums hold the current occupations
             __syncthreads();
         }
     };
@@ -1042,12 +1056,31 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             orbital_sums();
             nimp = ena_imp;
         }
+        if constexpr (RP) {
+            // bead eigenvalue sums of the current occupations (a hop of this step changed them)
+            // every thread reads the flag before bead_roots clears it
+            const bool stale = misc[15] != 0.0;
+            __syncthreads();
+            if (stale) bead_roots();
+        }
         if (warp == 0) {
-            const double pe = potential();
+            double pe, ke, zs;
+            if constexpr (RP) {
+                // centroid height, kinetic energy of all beads, sum over beads of U0 and the occupied
+                // eigenvalues (classical_kinetic_energy, DynamicsUtils.jl:122-132; rpiesh.jl:40-52)
+                pe = bead_mean(0.5 * p.kxy * (r[0] * r[0] + r[1] * r[1]) + p.A * iesh_wall<R>(p, r[2]) +
+                               rph[3 * NB + bead]) * (double)NB;
+                ke = bead_mean(kinetic()) * (double)NB;
+                zs = bead_mean(r[2]);
+            } else {
+                pe = potential();
+                ke = kinetic();
+                zs = r[2];
+            }
             if (lane == 0 && isave < p.nsave) {
                 double* dst = p.obs_partial + (ti * p.nsave + isave) * 4;
-                dst[0] = r[2];
-                dst[1] = kinetic();
+                dst[0] = zs;
+                dst[1] = ke;
                 dst[2] = nimp;
                 dst[3] = pe;
             }
@@ -1055,7 +1088,10 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
         __syncthreads();  // the next step rewrites the roots warp 0 just read
     };
     int isave = 0;
-    if (tid == 0) misc[16] = -1.0;  // no Bessel coefficients cached yet (FP32 path)
+    if (tid == 0) {
+        mf[13] = -1.f;    // no Bessel coefficients cached yet (FP32 path)
+        misc[15] = 0.0;   // ring polymer: bead eigenvalue sums current
+    }
     if (p.save_stride > 0 && p.obs_partial) save(isave++);
 
     int nh = 0, nf = 0;
@@ -1095,9 +1131,16 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     misc[6] = vzc0 * dhz;
                     misc[12] = vzc * dhz;
                     misc[13] = vzc;
+                    if constexpr (kF32) {
+                        mf[6] = (float)misc[6];
+                        mf[12] = (float)misc[12];
+                    }
                 }
             } else {
-                if (lane == 0) misc[6] = v[2] * dhz;
+                if (lane == 0) {
+                    misc[6] = v[2] * dhz;
+                    if constexpr (kF32) mf[6] = (float)misc[6];
+                }
             }
         }
         // ---- propagator (wavefunction_dynamics.jl:15-58) ----
@@ -1150,7 +1193,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 } else {
                     for (int j = 0; j < N; ++j) sacc += fabsf((float)At[j * Np + tid]);
                 }
-                const float rad = fabsf((float)w) * sacc;
+                const float rad = fabsf(mf[6]) * sacc;
                 flo = (float)lam[tid] - rad;
                 fhi = (float)lam[tid] + rad;
             }
@@ -1159,26 +1202,25 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 const float cen = 0.5f * (fhi + flo);
                 const float hw = 0.5f * (fhi - flo) * (1.f + 1e-5f) + 1e-30f;
                 const float aq = ceilf(hw * (float)hs * 32.f) * (1.f / 32.f);
-                if ((double)aq != misc[16]) {  // the same in every lane
+                if (aq != mf[13]) {  // the same in every lane
                     const int Kq = iesh_bessel_warp_fast((double)aq, p.cheb_tol, Jc, inv);
                     for (int q = lane; q < kIeshMaxTerms; q += 32) Jr[q] = (R)(2.0 * Jc[q]);
                     __syncwarp();
                     if (lane == 0) {
-                        misc[16] = (double)aq;
-                        misc[17] = (double)Kq;
+                        mf[13] = aq;
+                        mi[0] = Kq;
+                        mf[11] = (float)Jc[0];
                     }
                 }
                 if (lane == 0) {
                     float sn, cs;
                     sincosf(cen * (float)hs, &sn, &cs);  // exp(-i c h) = cs - i sn
                     const float hwq = aq / (float)hs;
-                    misc[0] = misc[17];
-                    misc[1] = (double)sn;
-                    misc[2] = (double)cs;
-                    misc[8] = (double)cen;
-                    misc[9] = (double)(1.f / hwq);
-                    misc[10] = (double)((float)w / hwq);
-                    misc[11] = Jc[0];
+                    mf[1] = sn;
+                    mf[2] = cs;
+                    mf[8] = cen;
+                    mf[9] = 1.f / hwq;
+                    mf[10] = mf[6] / hwq;
                 }
             }
         } else {
@@ -1219,7 +1261,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             }
         }
         __syncthreads();
-        const int K = (int)misc[0];
+        const int K = kF32 ? mi[0] : (int)misc[0];
         if (K < 0) {  // step too long for the series: leave psi unchanged, count as unconverged
             if (tid == 0 && nonconv) atomicAdd(nonconv, 1ull);
         } else {
@@ -1234,8 +1276,8 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     // l ^ 1.  TMEM columns: [0, N) D, [N, 2N) phi_{k-2}, [2N, 3N) the series sum.
                     // phi_{k-1} is read back as the high + low tf32 pair the tensor cores multiply
                     // (2^-22 relative), so the whole of Ht phi_{k-1} has that precision.
-                    const float st = (float)misc[10];
-                    const float cenf = (float)misc[8], ihwf = (float)misc[9];
+                    const float st = mf[10];
+                    const float cenf = mf[8], ihwf = mf[9];
                     const int tq = warp & 3, NH = N >> 1, s0 = (warp >> 2) * NH;
                     const int tn = 32 * tq + lane, te = tn >> 1, tcmp = tn & 1;
                     const bool twarp = 32 * tq < 2 * Ne;  // warp-uniform: the warp holds orbital rows
@@ -1283,7 +1325,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     for (int i = tid; i < N; i += nthr) dlt[i] = (lam[i] - cenf) * ihwf;
                     // phi_0 = psi; series sum J_0 phi_0
                     if (twarp) {
-                        const float j0 = (float)misc[11];
+                        const float j0 = mf[11];
 #pragma unroll
                         for (int q = 0; q < 5; ++q) {
                             if (8 * q >= NH) break;
@@ -1371,7 +1413,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     }
                     tc::fence_after_sync();
                     // psi = exp(-i c h) sum
-                    const float snf = (float)misc[1], csf = (float)misc[2];
+                    const float snf = mf[1], csf = mf[2];
                     if (twarp) {
                         // the series-sum columns in two batches of loads, each with one wait: a
                         // wait for TMEM loads takes long while the tensor cores run the other
@@ -1407,13 +1449,13 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     __syncthreads();
                 }
             } else {
-                const R s = (R)misc[10];
-                const R cenr = (R)misc[8], ihwr = (R)misc[9];
+                const R s = kF32 ? (R)mf[10] : (R)misc[10];
+                const R cenr = kF32 ? (R)mf[8] : (R)misc[8], ihwr = kF32 ? (R)mf[9] : (R)misc[9];
                 R dl[4];
     #pragma unroll
                 for (int rr = 0; rr < 4; ++rr) dl[rr] = (lam[i0 + RG * rr] - cenr) * ihwr;
                 if (tile_on) {
-                    const R j0 = (R)misc[11];
+                    const R j0 = kF32 ? (R)mf[11] : (R)misc[11];
     #pragma unroll
                     for (int rr = 0; rr < 4; ++rr)
     #pragma unroll
@@ -1490,7 +1532,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     }
                 }
                 __syncthreads();
-                const R snr = (R)misc[1], csr = (R)misc[2];
+                const R snr = kF32 ? (R)mf[1] : (R)misc[1], csr = kF32 ? (R)mf[2] : (R)misc[2];
                 if (tile_on) {
     #pragma unroll
                     for (int rr = 0; rr < 4; ++rr)
@@ -1521,7 +1563,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                     for (int n = q & 3; n < Ne; n += 4) sabs_pre += fabsf(coup(m, occ[n]));
                 }
                 iesh_block_sum3_f(trx, fx2, sabs_pre, red);
-                lu = !estimate_certainly_below(trx, fx2, sabs_pre, wh,
+                lu = !estimate_certainly_below(trx, fx2, sabs_pre, RP ? mf[12] : mf[6],
                                                rng_uniform_f(p.seed, gid, (uint32_t)step, RNG_HOP));
             }
         }
@@ -1771,6 +1813,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                         }
                         ++nh;
                         occ[sel_n] = nw;
+                        if constexpr (RP) misc[15] = 1.0;  // the bead eigenvalue sums are stale
                         rebuild_unocc();
                     } else {
                         ++nf;
@@ -1817,11 +1860,19 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             }
             __syncthreads();
         }
-        if (p.save_stride > 0 && p.obs_partial && step % p.save_stride == 0) save(isave++);
+        // save points are the multiples of save_stride: a product, not an integer division per step
+        if (p.save_stride > 0 && step == isave * p.save_stride) {
+            if (p.obs_partial) save(isave++);
+        }
     }
 
     double e1 = 0.0;
     if (ena && p.energy) orbital_sums();
+    if constexpr (RP) {
+        const bool stale = misc[15] != 0.0;  // a hop in the last step; read by all before it is cleared
+        __syncthreads();
+        if (p.energy && stale) bead_roots();
+    }
     if (warp == 0 && p.energy) {
         if constexpr (RP) {
             e1 = rp_energy();  // bead sums of the last step's roots

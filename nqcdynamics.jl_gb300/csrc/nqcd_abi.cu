@@ -76,14 +76,15 @@ __global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
 }
 
 // tmp[c][k] = sum of partial[p][k] over the rows p of chunk c, ascending p.
-__global__ void reduce_chunks_kernel(const double* __restrict__ partial, int64_t nparts, int64_t width,
+template <typename T>
+__global__ void reduce_chunks_kernel(const T* __restrict__ partial, int64_t nparts, int64_t width,
                                      int64_t rows_per_chunk, double* __restrict__ tmp) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= width) return;
     const int64_t p0 = (int64_t)blockIdx.y * rows_per_chunk;
     const int64_t p1 = p0 + rows_per_chunk < nparts ? p0 + rows_per_chunk : nparts;
     double acc = 0.0;
-    for (int64_t q = p0; q < p1; ++q) acc += partial[q * width + k];
+    for (int64_t q = p0; q < p1; ++q) acc += (double)partial[q * width + k];
     tmp[(int64_t)blockIdx.y * width + k] = acc;
 }
 
@@ -460,9 +461,10 @@ int nqcd_create(const nqcd_config* cfg, nqcd_handle** out) {
             if (cfg->nbeads_max > kRpIeshMaxBeads || cfg->nelectrons > kRpIeshMaxElectrons)
                 return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ring-polymer IESH takes 2..32 beads and <= 64 electrons");
             if (!(cfg->beta > 0.0)) return fail(nullptr, NQCD_ERR_ARG, "nqcd_create: ring polymers need beta > 0");
-            if (cfg->save_stride != 0 || cfg->decoherence_C != 0.0)
+            if (cfg->decoherence_C != 0.0)
                 return fail(nullptr, NQCD_ERR_UNSUPPORTED,
-                            "nqcd_create: ring-polymer IESH reports final states only, without decoherence correction");
+                            "nqcd_create: ring-polymer IESH runs without decoherence correction (a ring polymer's "
+                            "eigenvalues are per bead)");
             const size_t smem_rp = cfg->precision == NQCD_PREC_FP64
                                        ? iesh_layout<double>(cfg->nstates, cfg->nelectrons, cfg->nbeads_max).bytes
                                        : iesh_layout<float>(cfg->nstates, cfg->nelectrons, cfg->nbeads_max).bytes;
@@ -1306,7 +1308,13 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
             NQCD_CUDA(h, dalloc(&h->d_redtmp, need));
             h->redtmp_cap = need;
         }
-        NQCD_CUDA(h, launch_reduce_partials(h->d_partial, nwarps, (int64_t)nsave * 4, h->d_redtmp, h->d_popcorr, s));
+        // the fast FSSH / Ehrenfest kernels write FP32 partial sums
+        const bool partial_f32 = !mdef && !iesh && h->cfg.precision != NQCD_PREC_FP64;
+        if (partial_f32)
+            NQCD_CUDA(h, launch_reduce_partials(reinterpret_cast<const float*>(h->d_partial), nwarps, (int64_t)nsave * 4,
+                                                h->d_redtmp, h->d_popcorr, s));
+        else
+            NQCD_CUDA(h, launch_reduce_partials(h->d_partial, nwarps, (int64_t)nsave * 4, h->d_redtmp, h->d_popcorr, s));
         ++launches;
         ++launches;
     }
@@ -1755,8 +1763,9 @@ int64_t reduce_chunks(int64_t nparts, int64_t width) {
     return chunks < nparts ? chunks : (nparts > 0 ? nparts : 1);
 }
 
-cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* tmp, double* out,
-                                   cudaStream_t s) {
+template <typename T>
+static cudaError_t reduce_partials_t(const T* partial, int64_t nparts, int64_t width, double* tmp, double* out,
+                                     cudaStream_t s) {
     const int64_t chunks = reduce_chunks(nparts, width);
     const int64_t rows = (nparts + chunks - 1) / chunks;
     dim3 grid((unsigned)((width + 127) / 128), (unsigned)chunks);
@@ -1765,5 +1774,15 @@ cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_
     if (e != cudaSuccess) return e;
     reduce_partials_kernel<<<(unsigned)((width + 127) / 128), 128, 0, s>>>(tmp, chunks, width, out);
     return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_partials(const double* partial, int64_t nparts, int64_t width, double* tmp, double* out,
+                                   cudaStream_t s) {
+    return reduce_partials_t(partial, nparts, width, tmp, out, s);
+}
+
+cudaError_t launch_reduce_partials(const float* partial, int64_t nparts, int64_t width, double* tmp, double* out,
+                                   cudaStream_t s) {
+    return reduce_partials_t(partial, nparts, width, tmp, out, s);
 }
 }  // namespace nqcd

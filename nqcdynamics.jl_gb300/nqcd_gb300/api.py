@@ -897,8 +897,9 @@ def _run_metal(sim, tspan, distribution, output, trajectories, reduction, alg, d
         save_stride = int(round(stride))
     ntraj = int(trajectories)
     rp = isinstance(sim, RingPolymerSimulation)
-    if rp and save_stride:
-        raise NotImplementedError("ring polymers report final states (OutputFinal, OutputTotalEnergy) on the GPU path")
+    if rp and mdef and save_stride:
+        raise NotImplementedError("ring-polymer MDEF reports final states (OutputFinal, OutputTotalEnergy) on the GPU "
+                                  "path")
     if rp and not mdef and abs(distribution.electronic.β * sim.temperature - 1.0) > 1e-12:
         raise NotImplementedError("ring-polymer IESH on the GPU path takes the Fermi-Dirac temperature equal to the "
                                   "ring-polymer temperature")

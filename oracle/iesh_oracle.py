@@ -326,7 +326,7 @@ def spring_energy(r, mass, beta):
 
 
 def run_rpiesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0, rescaling=0, estimate=True,
-               initial_state=None):
+               initial_state=None, save_stride=0):
     """RingPolymerSimulation{AdiabaticIESH} (rpiesh.jl) with BCBWavefunction
     (bcb_wavefunction.jl:37-69).  r0, v0: (ntraj, nbeads, 3).
 
@@ -343,7 +343,14 @@ def run_rpiesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0
     :vinversion hop inverts the centroid velocity along d in every bead
     (rpsh.jl:30-50).  Fermi-Dirac occupations come from the centroid
     eigenvalues (iesh.jl:99-128).  Energy: kinetic + sum over beads of
-    U0 + occupied eigenvalues (rpiesh.jl:39-52) + spring energy."""
+    U0 + occupied eigenvalues (rpiesh.jl:39-52) + spring energy.
+    save_stride > 0: observables at step 0 and every save_stride steps, after
+    the step's hops, per trajectory (nsave, ntraj, 4): centroid height z,
+    kinetic energy of all beads (classical_kinetic_energy,
+    DynamicsUtils.jl:122-132), impurity population of the centroid
+    eigenstates (iesh.jl:351-369), and the potential of
+    classical_potential_energy (rpiesh.jl:40-52: sum over beads of U0 and
+    the occupied eigenvalues, no spring term)."""
     import oracle as O
 
     n, B, _ = r0.shape
@@ -390,6 +397,17 @@ def run_rpiesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0
     k = accel(r, state)
     e0 = energy(r, v, state)
     idx = np.arange(N)
+    obs = []
+
+    def observe(Zc):
+        w, _ = beads(r)
+        band = np.take_along_axis(w, np.repeat(state[:, None, :], B, axis=1), axis=2).sum(2)
+        pot = (model.U0(r.reshape(n * B, 3)).reshape(n, B) + band).sum(1)
+        ke = 0.5 * mass * np.sum(v * v, axis=(1, 2))
+        obs.append(np.stack([r.mean(1)[:, 2], ke, impurity_population(psi, Zc, state), pot], axis=1))
+
+    if save_stride:
+        observe(Zc)
     for step in range(1, nsteps + 1):
         vc_prev = v.mean(1)
         vt = v + (dt / 2) * k
@@ -452,6 +470,8 @@ def run_rpiesh(model, *, mass, ne, beta, r0, v0, dt, nsteps, seed, traj_offset=0
                 hops[t].append((step, int(old), int(m)))
             else:
                 nfr[t] += 1
+        if save_stride and step % save_stride == 0:
+            observe(Zc)
     e1 = energy(r, v, state)
     return dict(r=r, v=v, psi=psi, state=state, hops=hops, nfrustrated=nfr, initial_state=states,
-                energy=np.stack([e0, e1], axis=1))
+                energy=np.stack([e0, e1], axis=1), obs=np.array(obs) if save_stride else None)

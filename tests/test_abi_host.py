@@ -261,7 +261,7 @@ def _rpiesh_cfg(**kw):
 
 
 @pytest.mark.parametrize("field,value,code", [
-    ("method", "ehrenfest_na", -6), ("nbeads_max", 33, -1), ("save_stride", 5, -6), ("decoherence_C", 0.1, -6),
+    ("method", "ehrenfest_na", -6), ("nbeads_max", 33, -1), ("decoherence_C", 0.1, -6),
     ("beta", 0.0, -1),
 ])
 def test_create_validates_ring_polymer_iesh(field, value, code):

@@ -14,7 +14,7 @@ import pytest
 import iesh_oracle as IO
 from nqcd_gb300 import _lib as L
 from nqcd_gb300 import workload as WL
-from test_gpu_iesh import compare_with_oracle, oracle_model, run_engine
+from test_gpu_iesh import compare_with_oracle, make_iesh, oracle_model, run_engine
 
 pytestmark = pytest.mark.gpu
 
@@ -112,3 +112,28 @@ def test_rpiesh_run_dynamics_matches_engine():
     np.testing.assert_array_equal(fin["v"], eng["v"])
     np.testing.assert_array_equal(fin["state"], eng["state"])
     np.testing.assert_allclose(res["OutputTotalEnergy"], eng["energy"].mean(axis=0), rtol=1e-14)
+
+
+def test_rpiesh_time_series_matches_oracle():
+    """Observables of ring-polymer IESH at save points (the reference's
+    OutputKineticEnergy / OutputPotentialEnergy of a ring polymer: all beads,
+    DynamicsUtils.jl:122-132 and rpiesh.jl:40-52; the centroid height; the
+    impurity population of the centroid eigenstates), after each step's hops,
+    against the oracle; the final energies include steps that ended with a hop."""
+    n, nsteps, stride, B = 8, 300, 25, 4
+    wl = WL.newns_anderson_rpiesh(n, B, nstates=20, nelectrons=10, z0=3.0)
+    eng = make_iesh(wl, n, nbeads=B, save_stride=stride)
+    try:
+        eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]))
+        obs = np.zeros((nsteps // stride + 1) * 4)
+        _, st = eng.run(0.0, nsteps * wl["dt"], wl["dt"], 5, observables=obs)
+        fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+        fin["hop_log"] = eng.get_hop_log(eng.cfg.max_hops)
+        fin["stats"] = st
+    finally:
+        eng.close()
+    o = IO.run_rpiesh(oracle_model(wl), mass=wl["mass"], ne=wl["nelectrons"], beta=wl["beta"], r0=wl["r0"],
+                      v0=wl["v0"], dt=wl["dt"], nsteps=nsteps, seed=5, save_stride=stride)
+    compare_with_oracle(fin, o, n)
+    print("hops:", sum(len(h) for h in o["hops"]))
+    np.testing.assert_allclose(obs.reshape(-1, 4), o["obs"].mean(axis=1), rtol=1e-8, atol=1e-10)
