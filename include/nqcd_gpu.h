@@ -325,6 +325,19 @@ typedef struct nqcd_mapping {
                                those of the LU path); 1 = the LU every step, as iesh.jl:241 */
 } nqcd_mapping;
 
+/* Eigenvalues and eigenvectors of `batch` dense real symmetric n x n matrices
+ * (host arrays; A [batch][n][n], symmetrised as (A + A^T)/2), cyclic Jacobi
+ * in shared memory on the GPU, one CTA per matrix, in NQCD_PREC_FP64 or
+ * NQCD_PREC_FP32: w [batch][n] ascending, Z [batch][n][n] with eigenvector o
+ * of matrix b at Z[(b n + o) n + i] and its largest component positive; sweeps
+ * [batch] (may be NULL) the Jacobi sweeps taken.  The general eigensolver of the
+ * reference's calculators (NQCCalculators get_eigen, LAPACK) for Hamiltonians
+ * without the arrowhead structure the trajectory kernels solve through the
+ * secular equation.  n up to 120 (FP64) or 168 (FP32); NQCD_ERR_UNSUPPORTED
+ * beyond.  Stateless: allocates and frees its device buffers. */
+int nqcd_eigh_batched(int32_t precision, int32_t n, int64_t batch, const double* A, double* w, double* Z,
+                      int32_t* sweeps);
+
 /* Set the handle's launch shapes for the following runs; NQCD_ERR_ARG for a
  * shape outside the lists above, NQCD_ERR_UNSUPPORTED for 8 spin-boson lanes
  * without Kahan accumulation or with more than 128 modes. */

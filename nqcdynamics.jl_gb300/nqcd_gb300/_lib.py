@@ -172,7 +172,25 @@ EXPORTED = [
     "nqcd_unpin_host",
     "nqcd_measure_fma_peaks",
     "nqcd_tensor_selftest",
+    "nqcd_eigh_batched",
 ]
+
+
+def eigh_batched(A, precision=None):
+    """Eigenvalues (ascending) and eigenvectors of real symmetric matrices on
+    the GPU (nqcd_eigh_batched): A (batch, n, n) -> w (batch, n),
+    Z (batch, n, n) with eigenvector o in Z[b, :, o], sweeps (batch,)."""
+    A = np.ascontiguousarray(A, np.float64)
+    batch, n, _ = A.shape
+    w = np.empty((batch, n))
+    Zt = np.empty((batch, n, n))
+    sw = np.empty(batch, np.int32)
+    lib = load()
+    rc = lib.nqcd_eigh_batched(PREC_FP64 if precision is None else precision, n, batch, dptr(A), dptr(w), dptr(Zt),
+                               iptr(sw))
+    if rc:
+        raise EngineError(rc, "nqcd_eigh_batched")
+    return w, Zt.transpose(0, 2, 1).copy(), sw
 
 
 class EngineUnavailable(RuntimeError):
@@ -214,6 +232,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
     lib.nqcd_set_trajectory_models.argtypes = [C.c_void_p, IP]
     lib.nqcd_set_mapping.argtypes = [C.c_void_p, C.POINTER(nqcd_mapping)]
     lib.nqcd_tensor_selftest.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.nqcd_eigh_batched.argtypes = [C.c_int32, C.c_int32, C.c_int64, DP, DP, DP, IP]
     lib.nqcd_mdef_evaluate.argtypes = [C.c_void_p, C.c_int64, DP, DP, DP]
     lib.nqcd_train_friction_mlp.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32, C.c_int32,
                                             C.c_double, C.c_uint64, DP]

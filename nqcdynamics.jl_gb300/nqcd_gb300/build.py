@@ -36,6 +36,7 @@ ENGINE_UNITS = {
     "kernels_iesh.cu": [],
     "tensor.cu": [],
     "kernels_tune.cu": [],
+    "eigh.cu": [],
 }
 
 
