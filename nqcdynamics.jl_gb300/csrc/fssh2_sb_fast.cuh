@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
     EBuf<float> buf = {0.f, 0.f, 0.f, 0.0, 0.f, 0.f, 0.f, 0.0};
     int nh = 0, nf = 0, step = 0, nfp64 = 0;
     float cv = 0.f;
+    float u_pack = 0.f;  // hop uniform of step (batch start + lane_g), see the hop test
     const float dtf = (float)p.dt;
     // the host's step schedule replaces the reference's FP64 clock (no FP64 in the loop)
     while (step < p.nsteps_total) {
@@ -182,7 +183,12 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
         float re = sg.x / (s == 0 ? sg.p : sg.q);
         float nsm = (s == 0 ? 1.0f : -1.0f) * cv * dscale;
         float prob = clamp01<float>(2.0f * re * nsm * dtf);
-        float u = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)step, RNG_HOP);
+        // hop uniforms: every G steps lane g of the group draws the Philox block of step + g, and
+        // a shuffle hands each step its own (the same values as one draw per step, a quarter of
+        // the Philox work)
+        const int kq = (step - 1) & (G - 1);
+        if (kq == 0) u_pack = rng_uniform_f(p.seed, (uint64_t)gid, (uint32_t)(step + lane_g), RNG_HOP);
+        const float u = __shfl_sync(0xffffffffu, u_pack, ((int)threadIdx.x & 31 & ~(G - 1)) | kq);
         if (!ehr && prob > u) {  // Ehrenfest: no hopping
             const int ns = 1 - s;
             const float sgn = ns < s ? 1.0f : -1.0f;  // d(new, old) = sgn * c_I * dscale
