@@ -938,9 +938,11 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             if constexpr (std::is_same<R, double>::value) {
                 l64 = lam[tid];
             } else {
+                // FP64 roots warm-started from the FP32 roots just solved at the same height (a
+                // step or two of Newton instead of a cold start's many)
                 const double h64 = p.delta - p.B * nqcd_exp(-p.b * z_fd);
                 double zz;
-                l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9;
+                l64 = (double)lam_own;
                 secular_root<double>(p.eps, p.V2, M, tid, h64, fabs(h64) + Lpad, l64, zz, nonconv);
             }
             const double wt = nqcd_exp(-p.beta * (l64 - eref));
@@ -955,7 +957,7 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 w64[tid] = lam[tid];
             } else {
                 const double h64 = p.delta - p.B * nqcd_exp(-p.b * z_fd);
-                double zz, l64 = tid == 0 ? p.eps[0] - 1e-3 : p.eps[tid - 1] + 1e-9;
+                double zz, l64 = (double)lam_own;
                 secular_root<double>(p.eps, p.V2, M, tid, h64, fabs(h64) + Lpad, l64, zz, nullptr);
                 w64[tid] = l64;
             }
