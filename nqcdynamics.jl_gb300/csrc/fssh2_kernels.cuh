@@ -152,8 +152,7 @@ __device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>
         ++nfp64;  // steps integrated with the FP64 electronics (per-trajectory status)
         electronics2_fp64_step(buf, first, h, p.t0, p.dt, sg);
     } else {
-        InterpS32 fn(buf, first ? p.sa1 : 0.f, first ? p.sb1 : 1.f);
-        electronic_macro_step2_fast(fn, h, dtsub, sg);
+        electronic_macro_step2_fast(buf, first ? p.sa1 : 0.f, first ? p.sb1 : 1.f, h, dtsub, sg);
     }
 }
 

@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
             cv += b.x * v[j].f();
         }
         cv = group_sum<G>(cv);
-        const float dscale = M01 / gap;  // d_I,01 = c_I * dscale
+        const float dscale = __fdividef(M01, gap);  // d_I,01 = c_I * dscale
         buf.E0c = buf.E0n;
         buf.E1c = buf.E1n;
         buf.Dc = buf.Dn;
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
 
         // hop test (identical in all G lanes of the group)
         const int s = state;
-        float re = sg.x / (s == 0 ? sg.p : sg.q);
+        float re = __fdividef(sg.x, s == 0 ? sg.p : sg.q);
         float nsm = (s == 0 ? 1.0f : -1.0f) * cv * dscale;
         float prob = clamp01<float>(2.0f * re * nsm * dtf);
         // hop uniforms: every G steps lane g of the group draws the Philox block of step + g, and

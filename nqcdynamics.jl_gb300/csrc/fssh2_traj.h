@@ -162,85 +162,95 @@ NQCD_HD void electronic_macro_step2(const F& fn, double t, double h, double dtsu
     }
 }
 
-// Fast path, FP32 only: the macro step [t, t + h] lies inside the DoubleBuffer
-// interval [tc, tn] (equal to it except in the first step of a run that does
-// not start at t = 0), so the interpolation parameter of a stage is
-// sa + sb * sigma with sigma in [0, 1] the position inside the macro step and
-// sa = (t - tc) / (tn - tc), sb = h / (tn - tc) formed once per macro step.
-// No FP64 work per stage.
-struct InterpS32 {
-    float E0c, E1c, Dc, dE0, dE1, dD, sa, sb;
-    NQCD_HD InterpS32(const EBuf<float>& b, double t, double h) : E0c(b.E0c), E1c(b.E1c), Dc(b.Dc),
-        dE0(b.E0n - b.E0c), dE1(b.E1n - b.E1c), dD(b.Dn - b.Dc) {
-        double den = b.tn - b.tc;
-        sa = den != 0.0 ? (float)((t - b.tc) / den) : 0.f;
-        sb = den != 0.0 ? (float)(h / den) : 0.f;
-    }
-    NQCD_HD InterpS32(const EBuf<float>& b, float sa_, float sb_) : E0c(b.E0c), E1c(b.E1c), Dc(b.Dc),
-        dE0(b.E0n - b.E0c), dE1(b.E1n - b.E1c), dD(b.Dn - b.Dc), sa(sa_), sb(sb_) {}
-    NQCD_HD Sig2<float> f(float sigma, const Sig2<float>& u) const {
-        float s = sa + sb * sigma;
-        float D = Dc + dD * s;
-        float E0 = E0c + dE0 * s;
-        float E1 = E1c + dE1 * s;
-        return rhs2<float>(E0, E1, D, u);
-    }
+// Fast path, FP32 only.  rhs2 changes p and q by opposite amounts
+// (dq/dt = -dp/dt = 2 D x exactly, a negation), so a Tsit5 stage needs three
+// derivative components, (dp, dx, dy), and the q update subtracts the p
+// stage sum: the same values as integrating q on its own (negation is exact),
+// with a quarter fewer stage sums.  With G = E0 - E1 the derivative is
+//   dp/dt = -2 D x,   dx/dt = G y + D (p - q),   dy/dt = -G x.
+//
+// The macro step [t, t + h] lies inside the DoubleBuffer interval [tc, tn]
+// (equal to it except in the first step of a run that does not start at
+// t = 0), so a stage at position sigma in [0, 1] of the macro step reads the
+// buffer at s = sa + sb * sigma, with sa = (t - tc) / (tn - tc) and
+// sb = h / (tn - tc) formed on the host.  G and D are linear in s: a sub-step
+// starting at sigma0 forms G = Gb + c Gs for its stage at c once (Gb, Gs) are
+// known, one FMA per stage and quantity, and no FP64.
+struct Deriv3 {
+    float p, x, y;  // dq = -p
 };
 
-// Tsit5 step in macro-step coordinates: stage positions sigma0 + c * hr,
-// step length hr * h in time.
-template <typename F>
-NQCD_HD void tsit5_step2_s(const F& fn, float sigma0, float hr, float h, Sig2<float>& u, Sig2<float>& k1) {
+NQCD_HD Deriv3 rhs_fast(float G, float D, const Sig2<float>& u) {
+    const float m = D * u.x;
+    return {-m - m, fmaf(G, u.y, D * (u.p - u.q)), -(G * u.x)};
+}
+
+// One Tsit5 sub-step of length hs (time) whose stage at c reads
+// G = Gb + c Gs, D = Db + c Ds (FSAL: k1 in, the end point's derivative out).
+NQCD_HD void tsit5_step_fast(float Gb, float Gs, float Db, float Ds, float hs, Sig2<float>& u, Deriv3& k1) {
     typedef Tsit5 TS;
-    const float hs = hr * h;
-    Sig2<float> tmp, k2, k3, k4, k5, k6;
-#define NQCD_TS_COMB_S(dst, EXPR)              \
-    {                                          \
-        dst.p = u.p + hs * (EXPR(p));          \
-        dst.q = u.q + hs * (EXPR(q));          \
-        dst.x = u.x + hs * (EXPR(x));          \
-        dst.y = u.y + hs * (EXPR(y));          \
+    Sig2<float> t;
+    Deriv3 k2, k3, k4, k5, k6;
+#define NQCD_TS_COMB_F(EXPR)              \
+    {                                     \
+        const float sp = (EXPR(p));       \
+        t.p = fmaf(hs, sp, u.p);          \
+        t.q = fmaf(hs, -sp, u.q);         \
+        t.x = fmaf(hs, (EXPR(x)), u.x);   \
+        t.y = fmaf(hs, (EXPR(y)), u.y);   \
     }
+#define NQCD_TS_STAGE(c) rhs_fast(fmaf((float)(c), Gs, Gb), fmaf((float)(c), Ds, Db), t)
 #define E2(c) ((float)TS::a21 * k1.c)
-    NQCD_TS_COMB_S(tmp, E2);
+    NQCD_TS_COMB_F(E2);
 #undef E2
-    k2 = fn.f(sigma0 + (float)TS::c2 * hr, tmp);
+    k2 = NQCD_TS_STAGE(TS::c2);
 #define E3(c) ((float)TS::a31 * k1.c + (float)TS::a32 * k2.c)
-    NQCD_TS_COMB_S(tmp, E3);
+    NQCD_TS_COMB_F(E3);
 #undef E3
-    k3 = fn.f(sigma0 + (float)TS::c3 * hr, tmp);
+    k3 = NQCD_TS_STAGE(TS::c3);
 #define E4(c) ((float)TS::a41 * k1.c + (float)TS::a42 * k2.c + (float)TS::a43 * k3.c)
-    NQCD_TS_COMB_S(tmp, E4);
+    NQCD_TS_COMB_F(E4);
 #undef E4
-    k4 = fn.f(sigma0 + (float)TS::c4 * hr, tmp);
+    k4 = NQCD_TS_STAGE(TS::c4);
 #define E5(c) ((float)TS::a51 * k1.c + (float)TS::a52 * k2.c + (float)TS::a53 * k3.c + (float)TS::a54 * k4.c)
-    NQCD_TS_COMB_S(tmp, E5);
+    NQCD_TS_COMB_F(E5);
 #undef E5
-    k5 = fn.f(sigma0 + (float)TS::c5 * hr, tmp);
+    k5 = NQCD_TS_STAGE(TS::c5);
 #define E6(c)                                                                                                  \
     ((float)TS::a61 * k1.c + (float)TS::a62 * k2.c + (float)TS::a63 * k3.c + (float)TS::a64 * k4.c + \
      (float)TS::a65 * k5.c)
-    NQCD_TS_COMB_S(tmp, E6);
+    NQCD_TS_COMB_F(E6);
 #undef E6
-    k6 = fn.f(sigma0 + hr, tmp);
+    k6 = rhs_fast(Gb + Gs, Db + Ds, t);
 #define E7(c)                                                                                                  \
     ((float)TS::a71 * k1.c + (float)TS::a72 * k2.c + (float)TS::a73 * k3.c + (float)TS::a74 * k4.c + \
      (float)TS::a75 * k5.c + (float)TS::a76 * k6.c)
-    NQCD_TS_COMB_S(tmp, E7);
+    NQCD_TS_COMB_F(E7);
 #undef E7
-#undef NQCD_TS_COMB_S
-    k1 = fn.f(sigma0 + hr, tmp);
-    u = tmp;
+#undef NQCD_TS_STAGE
+#undef NQCD_TS_COMB_F
+    k1 = rhs_fast(Gb + Gs, Db + Ds, t);
+    u = t;
 }
 
-// Fast-path macro step: sub-steps of dtsub (the last one shortened), in FP32.
-NQCD_HD void electronic_macro_step2_fast(const InterpS32& fn, float h, float dtsub, Sig2<float>& u) {
+// Fast-path macro step: sub-steps of dtsub (the last one shortened), in FP32,
+// on the buffer weights (sa, sb) of this step.
+NQCD_HD void electronic_macro_step2_fast(const EBuf<float>& b, float sa, float sb, float h, float dtsub,
+                                         Sig2<float>& u) {
+    const float Gc = b.E0c - b.E1c, dG = (b.E0n - b.E1n) - Gc;
+    const float Dc = b.Dc, dD = b.Dn - b.Dc;
+#ifdef __CUDA_ARCH__
+    // the sub-step count does not hang on the last bits of fs (the snap below)
+    const float fs = __fdividef(dtsub, h);
+#else
     const float fs = dtsub / h;
-    Sig2<float> k1 = fn.f(0.f, u);
+#endif
+    Deriv3 k1 = rhs_fast(fmaf(dG, sa, Gc), fmaf(dD, sa, Dc), u);
     float s0 = 0.f;
     for (int guard = 0; s0 < 1.f && guard < 64; ++guard) {
-        float hr = (1.f - s0) < fs ? (1.f - s0) : fs;
-        tsit5_step2_s(fn, s0, hr, h, u, k1);
+        const float hr = (1.f - s0) < fs ? (1.f - s0) : fs;
+        const float base = fmaf(sb, s0, sa), scale = sb * hr;
+        tsit5_step_fast(fmaf(dG, base, Gc), dG * scale, fmaf(dD, base, Dc), dD * scale, hr * h, u, k1);
         s0 = s0 + hr;
         if (1.f - s0 < 1e-6f) s0 = 1.f;
     }
