@@ -317,6 +317,9 @@ class Engine:
         return out, st
 
     def get_final(self, ndof: int, nstates: int = 2):
+        if self.cfg.method in (METHOD_IESH, METHOD_EHRENFEST_NA):
+            # the C call writes the orbitals (nelectrons x nstates per trajectory) there
+            raise ValueError("IESH and EhrenfestNA handles: use get_final_iesh(nstates, nelectrons)")
         n = self.ntraj
         r = np.empty((n, ndof))
         v = np.empty((n, ndof))
