@@ -1146,29 +1146,39 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
             }
         }
         // ---- propagator (wavefunction_dynamics.jl:15-58) ----
-        if (tcp) {
+        if constexpr (tcp) {
             // the coupling matrix rounded to tf32 as the B operand (row i, k = j); rounding to
-            // nearest keeps it antisymmetric, so H_eff stays Hermitian.  Consecutive threads take
-            // consecutive rows: their 16-byte stores fill one core matrix each (no bank conflicts).
-            // The quotient takes the approximate reciprocal (2 ulp, far below the tf32 rounding;
-            // it is odd in the denominator, so the matrix stays antisymmetric)
-            int j4 = tid / N, i = tid - j4 * N;
-            const int sj = nthr / N, si = nthr - sj * N;
-            for (int q = tid; q < N * (N / 4); q += nthr) {
-                const float zi = (float)z0[i];
-                float4 a;
-                float* av = &a.x;
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const int j = 4 * j4 + t;
-                    av[t] = i == j ? 0.f : tc::to_tf32(__fdividef(zi * (float)z0[j], (float)gap(i, j)));
-                }
-                *(float4*)(bop + tc::smem_kmajor_offset(i, 4 * j4, N)) = a;
-                i += si;
-                j4 += sj;
-                if (i >= N) {
-                    i -= N;
-                    ++j4;
+            // nearest keeps it antisymmetric, so H_eff stays Hermitian.  Thread i of part p
+            // (tid = p N + i) writes row i of the k-blocks p, p + parts, ...: consecutive threads
+            // fill one core matrix with 16-byte stores (no bank conflicts), and the four z0_j and
+            // l_j of a block are one broadcast float4 load each.  The quotient takes the
+            // approximate reciprocal (2 ulp, far below the tf32 rounding; it is odd in the
+            // denominator, so the matrix stays antisymmetric).  The branch on refined roots is
+            // taken once, outside the loop.
+            const int parts = nthr / N, part = tid / N, i = tid - part * N;
+            if (part < parts) {
+                const float zi = z0[i];
+                auto bval = [&](int j, float zj, float g) -> float {
+                    return i == j ? 0.f : tc::to_tf32(__fdividef(zi * zj, g));
+                };
+                if (fp64_now) {  // gaps from the float pairs of the refined roots
+                    for (int j4 = part; j4 < N / 4; j4 += parts) {
+                        const int j0 = 4 * j4;
+                        const float4 zj = *(const float4*)(z0 + j0);
+                        const float4 a = make_float4(bval(j0, zj.x, gap(i, j0)), bval(j0 + 1, zj.y, gap(i, j0 + 1)),
+                                                     bval(j0 + 2, zj.z, gap(i, j0 + 2)), bval(j0 + 3, zj.w, gap(i, j0 + 3)));
+                        *(float4*)(bop + tc::smem_kmajor_offset(i, j0, N)) = a;
+                    }
+                } else {
+                    const float li = lam[i];
+                    for (int j4 = part; j4 < N / 4; j4 += parts) {
+                        const int j0 = 4 * j4;
+                        const float4 zj = *(const float4*)(z0 + j0);
+                        const float4 lj = *(const float4*)(lam + j0);
+                        const float4 a = make_float4(bval(j0, zj.x, lj.x - li), bval(j0 + 1, zj.y, lj.y - li),
+                                                     bval(j0 + 2, zj.z, lj.z - li), bval(j0 + 3, zj.w, lj.w - li));
+                        *(float4*)(bop + tc::smem_kmajor_offset(i, j0, N)) = a;
+                    }
                 }
             }
         } else {

@@ -86,17 +86,21 @@ __device__ __forceinline__ void secular_root(const R* __restrict__ eps, const R*
     // warm start from the previous root if it lies in the bracket
     R d = lam_io - o;
     if (!(d > dlo && d < dhi)) d = R(0.5) * (dlo + dhi);
+    // the pole at the other end of the interval (the origin itself for the outer roots)
+    const R other = o == a ? b : a;
     R fp = R(1);
     bool conv = false;
     for (int it = 0; it < 80; ++it) {
-        R s1 = R(0), s2 = R(0), sa = R(0);
+        R s1 = R(0), s2 = R(0), s3 = R(0), sa = R(0);
 #pragma unroll 4
         for (int k = 0; k < M; ++k) {
             R den = (k == jo) ? d : (o - eps[k]) + d;
             R t = secular_rcp<R>(den);
             R vt = V2[k] * t;
             s1 += vt;
-            s2 += vt * t;
+            const R vt2 = vt * t;
+            s2 += vt2;
+            s3 += vt2 * t;
             sa += fabs(vt);
         }
         R f = (o + d) - h - s1;
@@ -125,6 +129,18 @@ __device__ __forceinline__ void secular_root(const R* __restrict__ eps, const R*
         R ferr = ulp * (fabs(o + d) + fabs(h) + sa);
         if (it >= 16) ferr *= R(8);
         if (fabs(step) <= tol || dhi - dlo <= tol || fabs(f) <= ferr) {
+            conv = true;
+            break;
+        }
+        // The Newton step just taken leaves an error of about |f''/(2 f')| step^2, f'' = -2 s3 at
+        // the previous point.  While the step is at most a tenth of the distance to the nearest
+        // pole, f'' changes along it by less than a factor (1/0.9)^3 < 1.4, so below the tolerance
+        // that bound ends the iteration one evaluation early (a warm start is usually that close).
+        // f' is then carried to the new point to first order, f' + f'' step (the impurity weight
+        // 1/f' is returned; the remainder is of the order of the tolerance).
+        const R pole = fmin(fabs(d), fabs((o + d) - other));
+        if (fabs(step) <= R(0.1) * pole && R(1.4) * fabs(s3) * step * step <= tol * fp) {
+            fp -= R(2) * s3 * step;
             conv = true;
             break;
         }
