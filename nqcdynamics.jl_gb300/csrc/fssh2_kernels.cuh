@@ -167,6 +167,7 @@ struct AccF64 {
     __device__ __forceinline__ double get() const { return x; }
     __device__ __forceinline__ float f() const { return (float)x; }
     __device__ __forceinline__ void add(float inc) { x += (double)inc; }
+    __device__ __forceinline__ void add_prod(float a, float b) { add(a * b); }
 };
 
 struct AccKahan {
@@ -179,6 +180,13 @@ struct AccKahan {
     __device__ __forceinline__ float f() const { return s; }
     __device__ __forceinline__ void add(float inc) {
         float y = __fsub_rn(inc, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    // add(a * b) with the product and the compensation in one rounding (one FMA fewer)
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        float y = __fmaf_rn(a, b, -c);
         float t = __fadd_rn(s, y);
         c = __fsub_rn(__fsub_rn(t, s), y);
         s = t;

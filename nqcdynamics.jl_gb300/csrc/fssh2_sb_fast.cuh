@@ -141,9 +141,9 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
         for (int j = 0; j < NPL; ++j) {
             float4 b = bath[lane_g + G * j];
             float x = r[j].f();
-            float k = -(b.y * x + b.x * Mk) * b.z;
-            v[j].add(half * k);
-            r[j].add(h * v[j].f());
+            const float mk = (b.y * x + b.x * Mk) * b.z;  // minus the force
+            v[j].add_prod(-half, mk);
+            r[j].add_prod(h, v[j].f());
             float xn = r[j].f();
             s0 += b.y * xn * xn;
             cr += b.x * xn;
@@ -163,8 +163,8 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
         for (int j = 0; j < NPL; ++j) {
             float4 b = bath[lane_g + G * j];
             float x = r[j].f();
-            float k = -(b.y * x + b.x * Mk) * b.z;
-            v[j].add(half * k);
+            const float mk = (b.y * x + b.x * Mk) * b.z;
+            v[j].add_prod(-half, mk);
             cv += b.x * v[j].f();
         }
         cv = group_sum<G>(cv);
