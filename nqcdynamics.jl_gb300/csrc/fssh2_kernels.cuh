@@ -133,15 +133,17 @@ __device__ __forceinline__ void electronics2(const FsshParams& p, const EBuf<dou
 // none of its conversions to and from FP64 is scheduled into the FP32 path of
 // the steps that do not take it (the FP64 pipe of this GPU runs at 1/64 of
 // the FP32 rate).
-static __device__ __noinline__ void electronics2_fp64_step(const EBuf<float>& buf, bool first, float h, double t0, double dt,
-                                                    Sig2<float>& sg) {
+// (Arguments and result by value: an address passed to a call that is not inlined would keep the
+// caller's density matrix in local memory for the whole step loop.)
+static __device__ __noinline__ Sig2<float> electronics2_fp64_step(const EBuf<float> buf, bool first, float h, double t0,
+                                                                 double dt, const Sig2<float> sg) {
     const double hd = h;
     const double tn = first ? t0 + hd : hd, t = first ? t0 : 0.0;
     EBuf<double> b64 = {buf.E0c, buf.E1c, buf.Dc, 0.0, buf.E0n, buf.E1n, buf.Dn, tn};
     Sig2<double> s64 = {sg.p, sg.q, sg.x, sg.y};
     Interp64 fn(b64);
     electronic_macro_step2<double>(fn, t, hd, dt / 5.0, s64);
-    sg = {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
+    return {(float)s64.p, (float)s64.q, (float)s64.x, (float)s64.y};
 }
 
 template <typename P>  // FsshParams or RpshParams
@@ -150,7 +152,7 @@ __device__ __forceinline__ void electronics2_sched(const P& p, const EBuf<float>
     const float dtsub = p.dtsub;
     if (gap < p.gap_fp64) {
         ++nfp64;  // steps integrated with the FP64 electronics (per-trajectory status)
-        electronics2_fp64_step(buf, first, h, p.t0, p.dt, sg);
+        sg = electronics2_fp64_step(buf, first, h, p.t0, p.dt, sg);
     } else {
         electronic_macro_step2_fast(buf, first ? p.sa1 : 0.f, first ? p.sb1 : 1.f, h, dtsub, sg);
     }
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
         R a = ehr ? ehrenfest_weight<R>(A[0], A[1], A[2], sg) : (s == 0 ? A[0] : A[2]);
         return (double)(-a / (R)mass);
     };
-    auto pot = [&]() { return ehr ? ehrenfest_potential<R>(sg, w) : (double)w[state]; };
+    auto pot = [&]() { return ehr ? ehrenfest_potential<R>(sg, w) : (double)(state == 0 ? w[0] : w[1]); };
 
     update_cache(x);
     init_electronics2<R>(p, i, gid, Z, sg, state);
@@ -339,7 +341,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_tully_kernel(const FsshParam
                 double d = (double)(ns < s ? nac : -nac);
                 double aa = (0.0 + d * d / mass) / 2.0;
                 double bb = 0.0 + d * v;
-                double cc = (double)w[ns] - (double)w[s];
+                double cc = ns == 1 ? (double)w[1] - (double)w[0] : (double)w[0] - (double)w[1];
                 double disc = bb * bb - 4.0 * aa * cc;
                 if (disc < 0.0) {
                     accept = false;
@@ -587,7 +589,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
     Sig2<R> sg;
     int state;
     init_electronics2<R>(p, i, gid, Z, sg, state);
-    double e0 = ke / 2.0 + (ehr ? ehrenfest_potential<R>(sg, w) : (double)w[state]);
+    double e0 = ke / 2.0 + (ehr ? ehrenfest_potential<R>(sg, w) : (double)(state == 0 ? w[0] : w[1]));
     R Zk[4] = {Z[0], Z[1], Z[2], Z[3]};  // eigenvectors the cached force was computed with
     int sk = state;                      // state the cached force was computed for
     Sig2<R> sgk = sg;                    // Ehrenfest: density matrix the cached force was computed with
@@ -692,7 +694,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
                     bb = bb + d * v[(int64_t)I * N];
                 }
                 aa = aa / 2.0;
-                double cc = (double)w[ns] - (double)w[s];
+                double cc = ns == 1 ? (double)w[1] - (double)w[0] : (double)w[0] - (double)w[1];
                 double disc = bb * bb - 4.0 * aa * cc;
                 if (disc < 0.0) {
                     accept = false;
@@ -753,7 +755,7 @@ __global__ void __launch_bounds__(kFsshBlock) fssh2_spinboson_kernel(const FsshP
             ke1 = ke1 + mj[I] * (vI * vI);
         }
         p.energy[i] = e0;
-        p.energy[N + i] = ke1 / 2.0 + (ehr ? ehrenfest_potential<R>(sg, w) : (double)w[state]);
+        p.energy[N + i] = ke1 / 2.0 + (ehr ? ehrenfest_potential<R>(sg, w) : (double)(state == 0 ? w[0] : w[1]));
     }
     if (p.scatter) atomicAdd(p.scatter + (r[0] > 0.0 ? 2 : 0) + state, 1ull);
 }

@@ -311,7 +311,7 @@ __device__ __noinline__ void rpsh_traj_plain(const RpshParams& p, int cls, int64
                 double d = ns < s ? nac : -nac;
                 double aa = (0.0 + d * d / mass) / 2.0;
                 double bb = 0.0 + d * vc;
-                double cc = w[ns] - w[s];
+                double cc = ns == 1 ? w[1] - w[0] : w[0] - w[1];
                 double disc = bb * bb - 4.0 * aa * cc;
                 if (disc < 0.0) {
                     accept = false;
