@@ -334,7 +334,7 @@ def main():
                 "peak": fp32_peak if chosen != "fp64" else fp64_peak, "unit": "TFLOP/s",
                 # DRAM bytes per launch from the ncu capture in profiles/ (20 000 trajectories,
                 # scaled by the number of trajectories; the kernel keeps its state on chip)
-                "traffic": 1.852e8 * ntraj / 100_000 if chosen == "fp32_kahan" else None,
+                "traffic": 1.761e8 * ntraj / 100_000 if chosen == "fp32_kahan" else None,
                 "traffic_source": "profiles/fssh2_sb_fast_kahan_spinboson100_ncu.md (ncu dram__bytes, scaled)",
                 "peak_source": "measured FMA throughput (project microbenchmark); MEASURED_PEAKS has no CUDA-core entry",
                 "flops_per_traj_step": WL.ref_flops_per_traj_step(nmodes), "kernel": kname,

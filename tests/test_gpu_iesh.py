@@ -258,3 +258,20 @@ def test_iesh_fp64_shortened_last_step_matches_oracle():
     o = IO.run_iesh(oracle_model(wl), mass=wl["mass"], ne=10, beta=wl["beta"], r0=wl["r0"], v0=wl["v0"],
                     dt=wl["dt"], nsteps=whole + 1, seed=3, h_last=t1 - whole * wl["dt"])
     compare_with_oracle(fin, o, n)
+
+
+def test_iesh_get_final_needs_the_orbital_form():
+    """The final state of an IESH handle is the orbitals: the two-state
+    get_final refuses it (the C call would write 40 x 80 orbitals per
+    trajectory into 2 x 2 density-matrix buffers)."""
+    wl = WL.newns_anderson_iesh(4, nstates=16, nelectrons=8)
+    eng = make_iesh(wl, 4)
+    try:
+        eng.set_initial(np.ascontiguousarray(wl["r0"]), np.ascontiguousarray(wl["v0"]))
+        eng.run(0.0, 2 * wl["dt"], wl["dt"], 1)
+        with pytest.raises(ValueError, match="get_final_iesh"):
+            eng.get_final(3)
+        fin = eng.get_final_iesh(wl["nstates"], wl["nelectrons"])
+        assert fin["psi"].shape == (4, 16, 8)
+    finally:
+        eng.close()
