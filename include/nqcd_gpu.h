@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define NQCD_ABI_VERSION 110
+#define NQCD_ABI_VERSION 111
 
 enum nqcd_status {
     NQCD_OK = 0,
@@ -244,6 +244,20 @@ int nqcd_set_initial_device(nqcd_handle* h, int64_t ntraj, const double* d_r0_so
  * Philox4x32-10 keyed by `seed` with counter (trajectory, step, stream). */
 int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out,
              nqcd_stats* stats);
+
+/* nqcd_set_initial(h, ntraj, r0, v0, NULL, NULL, NULL, NULL) followed by
+ * nqcd_run(...) in one call, with the same results: the ensemble solve from
+ * the initial conditions the distribution produced on the host (reference:
+ * src/Ensembles/run_dynamics.jl:91-97).  For the fast spin-boson FSSH and
+ * Ehrenfest kernels (NQCD_PREC_FP32 / NQCD_PREC_FP32_KAHAN, electronic
+ * initial state not NQCD_INIT_GIVEN) the positions and velocities are copied
+ * in chunks of trajectories while earlier chunks already integrate, so the
+ * host-to-device transfer overlaps the dynamics (pinned host buffers make the
+ * copies asynchronous; see nqcd_pin_host); every other configuration runs the
+ * two calls in turn.  r0 and v0 may be reused when the call returns; a later
+ * nqcd_run repeats the run from the same initial conditions. */
+int nqcd_run_host(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, double t0, double t1, double dt,
+                  uint64_t seed, nqcd_outputs* out, nqcd_stats* stats);
 
 /* Final per-trajectory state of the last run (any pointer may be NULL):
  * r, v as in nqcd_set_initial; sig_re/sig_im (nstates, nstates, ntraj);

@@ -44,7 +44,7 @@ export EnsembleGB300, install_keyed_hop_stream!, with_keyed_hops, keyed_fermi_di
 # C ABI (include/nqcd_gpu.h)
 # ---------------------------------------------------------------------------
 
-const ABI_VERSION = Int32(110)
+const ABI_VERSION = Int32(111)
 
 const METHOD_FSSH = Int32(1)
 const METHOD_RPSH = Int32(2)

@@ -56,6 +56,11 @@ struct FsshParams {
     // launch shape of the fast spin-boson kernel (nqcd_set_mapping; 0 = default)
     int32_t sb_group;         // lanes per trajectory: 4 or 8
     int32_t sb_block;         // threads per block: 64, 128 or 256
+    // trajectories [traj_lo, traj_hi) of this launch (the fast spin-boson kernel; the others run
+    // [0, ntraj)); traj_lo is a whole number of blocks, so that every warp keeps the trajectories
+    // and the partial-sum row it has in a launch of all of them.  The launch wrapper shifts the
+    // per-trajectory pointers by traj_lo: the kernel sees trajectories [0, traj_hi).
+    int64_t traj_lo, traj_hi;
 };
 
 // Host launchers (one translation unit per precision).

@@ -59,11 +59,12 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
     }
     __syncthreads();
 
+    // trajectories [0, traj_hi) of the (launch wrapper's shifted) per-trajectory arrays
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane_g = (int)(gt % G);
     const int64_t i0 = gt / G;
-    const bool active = i0 < p.ntraj;
-    const int64_t i = active ? i0 : p.ntraj - 1;
+    const bool active = i0 < p.traj_hi;
+    const int64_t i = active ? i0 : p.traj_hi - 1;  // (the launch's last trajectory: pointers may be shifted)
     const int64_t gid = p.traj_offset + i;
     const int64_t N = p.ntraj;
     const float eps = (float)p.mp[0], Delta = (float)p.mp[1];
@@ -271,10 +272,35 @@ __global__ void __launch_bounds__(kSbFastBlockMax) fssh2_sb_fast_kernel(const Fs
 }
 
 template <typename Acc, int G, int NPL>
-cudaError_t launch_sb_fast_npl(const FsshParams& p, cudaStream_t s) {
+cudaError_t launch_sb_fast_npl(const FsshParams& p0, cudaStream_t s) {
+    FsshParams p = p0;
     const int block = p.sb_block > 0 ? p.sb_block : kSbFastBlock;
-    int64_t threads = p.ntraj * G;
+    const int64_t lo = p.traj_lo, n = p.traj_hi - p.traj_lo;
+    if ((lo * G) % block != 0 || p.traj_hi > p.ntraj || n < 0) return cudaErrorInvalidValue;
+    if (lo > 0) {
+        // trajectories [lo, traj_hi): every per-trajectory array (stride ntraj) from column lo, the
+        // random stream from trajectory traj_offset + lo, the partial sums from the launch's first
+        // warp row (lo is a whole number of blocks: each warp keeps its trajectories and its row)
+        p.r += lo;
+        p.v += lo;
+        p.sigma += lo;
+        p.state += lo;
+        if (p.nhops) p.nhops += lo;
+        if (p.nfrustrated) p.nfrustrated += lo;
+        if (p.nsteps) p.nsteps += lo;
+        if (p.hop_log) p.hop_log += lo;
+        if (p.energy) p.energy += lo;
+        if (p.fp64_steps) p.fp64_steps += lo;
+        if (p.popcorr_partial)  // rows of nsave float4
+            p.popcorr_partial = reinterpret_cast<double*>(reinterpret_cast<float4*>(p.popcorr_partial) +
+                                                          lo * G / 32 * (int64_t)p.nsave);
+        p.traj_offset += lo;
+        p.traj_lo = 0;
+        p.traj_hi = n;
+    }
+    int64_t threads = n * G;
     int64_t blocks = (threads + block - 1) / block;
+    if (blocks == 0) return cudaSuccess;
     size_t shmem = sizeof(float4) * G * NPL;
     if (p.ehrenfest)
         fssh2_sb_fast_kernel<Acc, G, NPL, true><<<(unsigned)blocks, block, shmem, s>>>(p);
@@ -289,7 +315,7 @@ cudaError_t launch_sb_fast_g8_kahan(const FsshParams& p, cudaStream_t s);
 // modes per lane rounded up to an instantiated size
 template <typename Acc>
 cudaError_t launch_sb_fast(const FsshParams& p, cudaStream_t s) {
-    if (p.ntraj <= 0) return cudaSuccess;
+    if (p.ntraj <= 0 || p.traj_hi <= p.traj_lo) return cudaSuccess;
     if (p.sb_group == 8) {
         if constexpr (std::is_same<Acc, AccKahan>::value) return launch_sb_fast_g8_kahan(p, s);
         return cudaErrorInvalidValue;

@@ -115,6 +115,7 @@ extern "C" int nqcd_fssh_spinboson_fp64_noalloc(int64_t ntraj, int32_t nmodes, c
     p.init_kind = NQCD_INIT_DIABATIC_PURE;
     p.init_state = diabatic_state;
     p.ntraj = ntraj;
+    p.traj_hi = ntraj;
     p.t0 = t0;
     p.t1 = t1;
     p.dt = dt;

@@ -38,6 +38,8 @@ namespace {
 // bead counts with an instantiated ring-polymer kernel
 constexpr int kRpCounts[] = {1, 2, 4, 5, 8, 10, 16, 32};
 constexpr int kNumRpCounts = 8;
+// nqcd_run_host: host initial conditions in this many chunks (fewer for small ensembles)
+constexpr int kPipeChunks = 8;
 constexpr int kMaxRpGrid = 8192;
 
 thread_local std::string g_create_error;
@@ -67,6 +69,36 @@ cudaError_t transpose(const double* in, double* out, int64_t n, int64_t m, cudaS
     dim3 block(32, 8);
     dim3 grid((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
     transpose_kernel<<<grid, block, 0, s>>>(in, out, n, m);
+    return cudaGetLastError();
+}
+
+// Rows [0, n) of the row-major n x m block `in` into columns of two column-major arrays with
+// leading dimension ld: out1[c * ld + r] = out2[c * ld + r] = in[r * m + c] (a chunk of
+// trajectories from the host layout into the initial and the working state at once).
+__global__ void transpose2_kernel(const double* __restrict__ in, double* __restrict__ out1, double* __restrict__ out2,
+                                  int64_t n, int64_t m, int64_t ld) {
+    __shared__ double tile[32][33];
+    int64_t bx = (int64_t)blockIdx.x * 32, by = (int64_t)blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        int64_t row = by + j, col = bx + threadIdx.x;
+        if (row < n && col < m) tile[j][threadIdx.x] = in[row * m + col];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        int64_t row = bx + j, col = by + threadIdx.x;  // out[row][col], row < m, col < n
+        if (row < m && col < n) {
+            const double x = tile[threadIdx.x][j];
+            out1[row * ld + col] = x;
+            out2[row * ld + col] = x;
+        }
+    }
+}
+
+cudaError_t transpose2(const double* in, double* out1, double* out2, int64_t n, int64_t m, int64_t ld, cudaStream_t s) {
+    if (n == 0 || m == 0) return cudaSuccess;
+    dim3 block(32, 8);
+    dim3 grid((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
+    transpose2_kernel<<<grid, block, 0, s>>>(in, out1, out2, n, m, ld);
     return cudaGetLastError();
 }
 
@@ -217,6 +249,9 @@ struct nqcd_handle {
     // fast ring polymers: one stream per bead-count kernel, forked from and joined to `stream`
     cudaStream_t rp_streams[kNumRpCounts] = {nullptr};
     cudaEvent_t rp_fork = nullptr, rp_join[kNumRpCounts] = {nullptr};
+    // nqcd_run_host: a copy stream, two compute streams and their events (created on first use)
+    cudaStream_t pipe_copy = nullptr, pipe_run[2] = {nullptr, nullptr};
+    cudaEvent_t pipe_start = nullptr, pipe_ready[kPipeChunks] = {nullptr}, pipe_done[2] = {nullptr, nullptr};
     int64_t cap = 0;
     int64_t ntraj = 0;
     int64_t ndof = 0;  // per trajectory (ndofs * natoms)
@@ -320,6 +355,14 @@ void free_all(nqcd_handle* h) {
         if (h->rp_join[c]) cudaEventDestroy(h->rp_join[c]);
     }
     if (h->rp_fork) cudaEventDestroy(h->rp_fork);
+    if (h->pipe_start) cudaEventDestroy(h->pipe_start);
+    for (int c = 0; c < kPipeChunks; ++c)
+        if (h->pipe_ready[c]) cudaEventDestroy(h->pipe_ready[c]);
+    for (int k = 0; k < 2; ++k) {
+        if (h->pipe_done[k]) cudaEventDestroy(h->pipe_done[k]);
+        if (h->pipe_run[k]) cudaStreamDestroy(h->pipe_run[k]);
+    }
+    if (h->pipe_copy) cudaStreamDestroy(h->pipe_copy);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -901,7 +944,74 @@ int nqcd_get_status(nqcd_handle* h, int32_t* nonfinite, int32_t* fp64_steps) {
     return NQCD_OK;
 }
 
-int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out, nqcd_stats* stats) {
+// nqcd_run_host's fast spin-boson path: the host initial conditions (AoS [ntraj][ndof]) are copied
+// in chunks of whole blocks on a copy stream and transposed into the initial (d_r0, d_v0) and the
+// working (d_r, d_v) state; chunk c runs on compute stream c % 2 once its copy has landed, so the
+// transfer of later chunks overlaps the integration of earlier ones and a chunk's tail overlaps the
+// next one's start.  Each block integrates the same trajectories and writes the same partial-sum
+// rows as in one launch over all of them, so the results are the same.
+static int run_pipelined(nqcd_handle* h, FsshParams p, int64_t lanes, int64_t blk, const double* r_host,
+                         const double* v_host, int64_t* h2d, int* launches) {
+    const int64_t N = h->ntraj, nd = h->ndof;
+    cudaStream_t s = h->stream;
+    if (!h->pipe_copy) {
+        NQCD_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_copy, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            NQCD_CUDA(h, cudaStreamCreateWithFlags(&h->pipe_run[k], cudaStreamNonBlocking));
+            NQCD_CUDA(h, cudaEventCreateWithFlags(&h->pipe_done[k], cudaEventDisableTiming));
+        }
+        NQCD_CUDA(h, cudaEventCreateWithFlags(&h->pipe_start, cudaEventDisableTiming));
+        for (int c = 0; c < kPipeChunks; ++c)
+            NQCD_CUDA(h, cudaEventCreateWithFlags(&h->pipe_ready[c], cudaEventDisableTiming));
+    }
+    int rc = ensure_stage(h, 2 * nd * N);
+    if (rc) return rc;
+    double* stage_r = h->d_stage;
+    double* stage_v = h->d_stage + nd * N;
+    const int64_t per_block = blk / lanes;  // trajectories per block
+    const int64_t nblocks = (N + per_block - 1) / per_block;
+    const int K = (int)(nblocks < kPipeChunks ? nblocks : kPipeChunks);
+    // everything queued on the main stream (resets of counters and outputs) comes first
+    NQCD_CUDA(h, cudaEventRecord(h->pipe_start, s));
+    NQCD_CUDA(h, cudaStreamWaitEvent(h->pipe_copy, h->pipe_start, 0));
+    for (int k = 0; k < 2; ++k) NQCD_CUDA(h, cudaStreamWaitEvent(h->pipe_run[k], h->pipe_start, 0));
+    NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
+    for (int c = 0; c < K; ++c) {
+        const int64_t lo = nblocks * c / K * per_block;
+        const int64_t hi = std::min<int64_t>(nblocks * (c + 1) / K * per_block, N);
+        if (lo >= hi) continue;
+        const size_t bytes = (size_t)((hi - lo) * nd) * sizeof(double);
+        NQCD_CUDA(h, cudaMemcpyAsync(stage_r + lo * nd, r_host + lo * nd, bytes, cudaMemcpyHostToDevice, h->pipe_copy));
+        NQCD_CUDA(h, cudaMemcpyAsync(stage_v + lo * nd, v_host + lo * nd, bytes, cudaMemcpyHostToDevice, h->pipe_copy));
+        NQCD_CUDA(h, transpose2(stage_r + lo * nd, h->d_r0 + lo, h->d_r + lo, hi - lo, nd, N, h->pipe_copy));
+        NQCD_CUDA(h, transpose2(stage_v + lo * nd, h->d_v0 + lo, h->d_v + lo, hi - lo, nd, N, h->pipe_copy));
+        NQCD_CUDA(h, cudaEventRecord(h->pipe_ready[c], h->pipe_copy));
+        *h2d += 2 * (int64_t)bytes;
+        cudaStream_t rs = h->pipe_run[c & 1];
+        NQCD_CUDA(h, cudaStreamWaitEvent(rs, h->pipe_ready[c], 0));
+        p.traj_lo = lo;
+        p.traj_hi = hi;
+        const cudaError_t e = h->cfg.precision == NQCD_PREC_FP32 ? launch_fssh2_fp32(p, rs) : launch_fssh2_fp32_kahan(p, rs);
+        if (e != cudaSuccess) return cuda_fail(h, e, "nqcd_run_host: ensemble kernel launch");
+        *launches += 3;  // two transposes and the chunk's kernel
+    }
+    for (int k = 0; k < 2; ++k) {
+        NQCD_CUDA(h, cudaEventRecord(h->pipe_done[k], h->pipe_run[k]));
+        NQCD_CUDA(h, cudaStreamWaitEvent(s, h->pipe_done[k], 0));
+    }
+    return NQCD_OK;
+}
+
+// Whether nqcd_run_host pipelines this configuration (the fast spin-boson FSSH / Ehrenfest kernel
+// with sampled electronic initial states); the others take nqcd_set_initial + nqcd_run.
+static bool pipelined_config(const nqcd_handle* h) {
+    return (h->cfg.method == NQCD_METHOD_FSSH || h->cfg.method == NQCD_METHOD_EHRENFEST) &&
+           h->cfg.model == NQCD_MODEL_SPINBOSON && h->cfg.precision != NQCD_PREC_FP64 &&
+           h->cfg.init_kind != NQCD_INIT_GIVEN;
+}
+
+static int run_impl(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out,
+                    nqcd_stats* stats, const double* r_host, const double* v_host) {
     if (!h) return NQCD_ERR_ARG;
     if (!h->initial_set) return fail(h, NQCD_ERR_STATE, "nqcd_run: call nqcd_set_initial first");
     if (!(dt > 0.0) || !(t1 >= t0) || !isfinite(t0) || !isfinite(t1))
@@ -970,8 +1080,10 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     }
     NQCD_CUDA(h, cudaEventRecord(h->ev0, s));
     const int64_t nd = h->ndof;
-    NQCD_CUDA(h, cudaMemcpyAsync(h->d_r, h->d_r0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    NQCD_CUDA(h, cudaMemcpyAsync(h->d_v, h->d_v0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (!r_host) {  // (nqcd_run_host writes the working state from the host chunks)
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_r, h->d_r0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        NQCD_CUDA(h, cudaMemcpyAsync(h->d_v, h->d_v0, nd * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_sig, h->d_sig0, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemcpyAsync(h->d_state, h->d_state0, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
     NQCD_CUDA(h, cudaMemsetAsync(h->d_counts, 0, 24 * sizeof(unsigned long long), s));
@@ -1001,6 +1113,8 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
     p.init_state = h->cfg.init_state;
     p.gap_fp64 = (float)h->cfg.gap_fp64;
     p.ntraj = N;
+    p.traj_lo = 0;
+    p.traj_hi = N;
     p.traj_offset = h->cfg.traj_offset;
     p.t0 = t0;
     p.t1 = t1;
@@ -1289,6 +1403,10 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         }
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         e = h->cfg.precision == NQCD_PREC_FP64 ? launch_mdef_fp64(mp, s) : launch_mdef_fp32(mp, s);
+    } else if (r_host) {
+        const int rc = run_pipelined(h, p, lanes, blk, r_host, v_host, &h2d, &launches);
+        if (rc) return rc;
+        --launches;  // counted per chunk
     } else {
         NQCD_CUDA(h, cudaEventRecord(h->evk0, s));
         e = h->cfg.precision == NQCD_PREC_FP64   ? launch_fssh2_fp64(p, s)
@@ -1391,6 +1509,28 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
         return fail(h, NQCD_ERR_TIMEOUT, "nqcd_run: a wait for the tensor-core propagator gave up");
     if (counts[7] > 0) return fail(h, NQCD_ERR_NAN, "nqcd_run: non-finite final positions or velocities");
     return NQCD_OK;
+}
+
+int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqcd_outputs* out, nqcd_stats* stats) {
+    return run_impl(h, t0, t1, dt, seed, out, stats, nullptr, nullptr);
+}
+
+int nqcd_run_host(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, double t0, double t1, double dt,
+                  uint64_t seed, nqcd_outputs* out, nqcd_stats* stats) {
+    if (!h) return NQCD_ERR_ARG;
+    if (!pipelined_config(h)) {
+        const int rc = nqcd_set_initial(h, ntraj, r0, v0, nullptr, nullptr, nullptr, nullptr);
+        return rc ? rc : nqcd_run(h, t0, t1, dt, seed, out, stats);
+    }
+    if (ntraj <= 0 || ntraj > h->cap) return fail(h, NQCD_ERR_ARG, "nqcd_run_host: ntraj outside 1..ntraj_max");
+    if (!r0 || !v0) return fail(h, NQCD_ERR_ARG, "nqcd_run_host: r0 and v0 are required");
+    if (!(dt > 0.0) || !(t1 >= t0) || !isfinite(t0) || !isfinite(t1))
+        return fail(h, NQCD_ERR_ARG, "nqcd_run: need dt > 0 and finite t0 <= t1");
+    // the handle's state as nqcd_set_initial leaves it; the positions and velocities arrive in the run
+    int64_t h2d = 0;
+    const int rc = set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
+    if (rc) return rc;
+    return run_impl(h, t0, t1, dt, seed, out, stats, r0, v0);
 }
 
 int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double* sig_im, int32_t* state,

@@ -156,6 +156,7 @@ EXPORTED = [
     "nqcd_sample_initial",
     "nqcd_set_initial_device",
     "nqcd_run",
+    "nqcd_run_host",
     "nqcd_get_final",
     "nqcd_get_hop_log",
     "nqcd_get_status",
@@ -226,6 +227,8 @@ def load(path: Path | str | None = None) -> C.CDLL:
                                         C.c_uint64]
     lib.nqcd_run.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_uint64,
                              C.POINTER(nqcd_outputs), C.POINTER(nqcd_stats)]
+    lib.nqcd_run_host.argtypes = [C.c_void_p, C.c_int64, DP, DP, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                  C.POINTER(nqcd_outputs), C.POINTER(nqcd_stats)]
     lib.nqcd_get_final.argtypes = [C.c_void_p, DP, DP, DP, DP, IP, IP, IP, IP, DP]
     lib.nqcd_get_hop_log.argtypes = [C.c_void_p, IP]
     lib.nqcd_get_status.argtypes = [C.c_void_p, IP, IP]
@@ -314,6 +317,20 @@ class Engine:
         out.observables = dptr(observables)
         st = nqcd_stats()
         self._check(self.lib.nqcd_run(self.h, t0, t1, dt, seed, C.byref(out), C.byref(st)))
+        return out, st
+
+    def run_host(self, r0, v0, t0, t1, dt, seed, scattering=None, popcorr=None, observables=None):
+        """set_initial(r0, v0) + run(...) in one call (nqcd_run_host): on the fast spin-boson
+        path the host-to-device copy of r0, v0 overlaps the integration of earlier chunks."""
+        ntraj = r0.shape[0]
+        out = nqcd_outputs()
+        out.scattering = dptr(scattering)
+        out.population_correlation = dptr(popcorr)
+        out.observables = dptr(observables)
+        st = nqcd_stats()
+        self._check(self.lib.nqcd_run_host(self.h, ntraj, dptr(r0), dptr(v0), t0, t1, dt, seed, C.byref(out),
+                                           C.byref(st)))
+        self.ntraj = ntraj
         return out, st
 
     def get_final(self, ndof: int, nstates: int = 2):

@@ -35,7 +35,7 @@ def test_library_exports_every_declared_symbol():
     lib = L.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.nqcd_version() == 110
+    assert lib.nqcd_version() == 111
 
 
 def _cfg(**kw):
@@ -83,6 +83,7 @@ def test_null_arguments():
     lib = L.load()
     assert lib.nqcd_create(None, None) == -1
     assert lib.nqcd_run(None, 0.0, 1.0, 1.0, 1, None, None) == -1
+    assert lib.nqcd_run_host(None, 1, None, None, 0.0, 1.0, 1.0, 1, None, None) == -1
     assert lib.nqcd_set_initial(None, 1, None, None, None, None, None, None) == -1
     lib.nqcd_destroy(None)  # no-op
 
