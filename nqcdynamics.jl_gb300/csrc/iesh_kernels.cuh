@@ -1366,9 +1366,16 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                             for (int ks = 0; ks < N / 8; ++ks)
                                 tc::mma<tc::kTypeTF32>(tmem + cD, tc::smem_desc(ah + 256u * ks, 128, sbo),
                                                        tc::smem_desc(bb + 256u * ks, 128, sbo), idesc, ks > 0);
-                            for (int ks = 0; ks < N / 8; ++ks)
-                                tc::mma<tc::kTypeTF32>(tmem + cD, tc::smem_desc(al + 256u * ks, 128, sbo),
-                                                       tc::smem_desc(bb + 256u * ks, 128, sbo), idesc, true);
+                            // The low tf32 part of phi_{k-1} changes the product by at most
+                            // 2^-11 |phi_{k-1}| <= 2^-11 (|T_k| <= 1 on the scaled spectrum, orbitals of
+                            // unit norm), and phi_k's contribution to the sum by |2 J_k| 2^-10: below an
+                            // FP32 unit once |2 J_k| <= 2^-15 (with room for its growth through the
+                            // recurrence, whose later terms weigh less still).  The last terms of the
+                            // series take the high part only.
+                            if (fabsf((float)Jr[kk]) > 0x1p-15f)
+                                for (int ks = 0; ks < N / 8; ++ks)
+                                    tc::mma<tc::kTypeTF32>(tmem + cD, tc::smem_desc(al + 256u * ks, 128, sbo),
+                                                           tc::smem_desc(bb + 256u * ks, 128, sbo), idesc, true);
                             tc::commit(&tc_bar);
                         }
                         const bool ok = tc::mbar_wait(&tc_bar, tc_phase, kPolls);
@@ -1572,7 +1579,11 @@ __device__ __forceinline__ void iesh_body(const IeshParams& p) {
                 gram_partials(trx, fx2);
                 for (int q = tid; q < 4 * Nu; q += nthr) {  // unoccupied state q / 4, a quarter of the electrons
                     const int m = unocc[q >> 2];
-                    for (int n = q & 3; n < Ne; n += 4) sabs_pre += fabsf(coup(m, occ[n]));
+                    // (the approximate quotient: 2 ulp, inside the bound's 2 % margin)
+                    for (int n = q & 3; n < Ne; n += 4) {
+                        const int j = occ[n];
+                        sabs_pre += tcp ? fabsf(__fdividef(z0[m] * z0[j], gap(m, j))) : fabsf(coup(m, j));
+                    }
                 }
                 iesh_block_sum3_f(trx, fx2, sabs_pre, red);
                 lu = !estimate_certainly_below(trx, fx2, sabs_pre, RP ? mf[12] : mf[6],
