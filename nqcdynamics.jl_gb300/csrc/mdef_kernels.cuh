@@ -153,7 +153,10 @@ __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib,
     const R mu = (R)p.mu, beta = (R)p.beta;
     R Lb = fabs(h) + R(2);
     R accF = R(0);
-#pragma unroll
+    // one copy of the root solve, not one per root of the lane: the unrolled copies of both
+    // electronic evaluations of a step outgrew the instruction cache (the warm starts then live in
+    // local memory, two accesses per solve)
+#pragma unroll 1
     for (int q = 0; q < kMdefRootsPerLane; ++q) {
         int i = lane + 32 * q;
         if (i <= M) {
