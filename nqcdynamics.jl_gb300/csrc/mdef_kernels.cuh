@@ -153,20 +153,46 @@ __device__ void mdef_electronic(const MdefParams& p, MdefShared<R>& sh, int wib,
     const R mu = (R)p.mu, beta = (R)p.beta;
     R Lb = fabs(h) + R(2);
     R accF = R(0);
-    // one copy of the root solve, not one per root of the lane: the unrolled copies of both
-    // electronic evaluations of a step outgrew the instruction cache (the warm starts then live in
-    // local memory, two accesses per solve)
+    // the root's Fermi weight in the force, and its eigenpair for the friction
+    auto finish = [&](int q, int i, R l, R z2) {
+        lam[q] = l;
+        R f, df;
+        fermi_pair<R>(l, mu, beta, f, df);
+        accF += z2 * (f + df * l);
+        sh.lam[wib][i] = l;
+        sh.z2[wib][i] = z2;
+    };
+    unsigned long long* nonconv = p.counters ? p.counters + 2 : nullptr;
+    if constexpr (std::is_same<R, float>::value) {
+        // A lane's seven roots one evaluation of f at a time: a lane whose root has converged
+        // starts its next one while the others still iterate (each lane finishes its roots in
+        // the same order and with the same arithmetic as one solve after the other).  One copy
+        // of the solver in the step loop; the warm starts live in local memory.
+        SecularSolve<R> st;
+        int q = 0, i = lane;
+        bool act = i <= M;
+        if (act) secular_begin<R>(sh.eps, M, i, Lb, lam[0], st);
+        while (__any_sync(0xffffffffu, act)) {
+            if (act && secular_eval<R>(sh.eps, sh.V2, M, h, lam[q], st, nonconv)) {
+                finish(q, i, st.o + st.d, R(1) / st.fp);
+                ++q;
+                i = lane + 32 * q;
+                act = q < kMdefRootsPerLane && i <= M;
+                if (act) secular_begin<R>(sh.eps, M, i, Lb, lam[q], st);
+            }
+        }
+    } else {
+        // one copy of the root solve, not one per root of the lane: the unrolled copies of both
+        // electronic evaluations of a step outgrew the instruction cache (the warm starts then
+        // live in local memory, two accesses per solve)
 #pragma unroll 1
-    for (int q = 0; q < kMdefRootsPerLane; ++q) {
-        int i = lane + 32 * q;
-        if (i <= M) {
-            R z2;
-            secular_root<R>(sh.eps, sh.V2, M, i, h, Lb, lam[q], z2, p.counters ? p.counters + 2 : nullptr);
-            R f, df;
-            fermi_pair<R>(lam[q], mu, beta, f, df);
-            accF += z2 * (f + df * lam[q]);
-            sh.lam[wib][i] = lam[q];
-            sh.z2[wib][i] = z2;
+        for (int q = 0; q < kMdefRootsPerLane; ++q) {
+            int i = lane + 32 * q;
+            if (i <= M) {
+                R l = lam[q], z2;
+                secular_root<R>(sh.eps, sh.V2, M, i, h, Lb, l, z2, nonconv);
+                finish(q, i, l, z2);
+            }
         }
     }
     // warp sum in the working precision (no FP64 shuffle-adds on the fast path)
