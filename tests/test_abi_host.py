@@ -369,3 +369,17 @@ def test_valid_metal_configs_pass_validation(make):
         lib.nqcd_destroy(h)
     else:
         assert rc == -2 and b"no CUDA device" in lib.nqcd_last_error(None), lib.nqcd_last_error(None)
+
+
+def test_get_final_refuses_orbital_handles():
+    """An IESH or EhrenfestNA handle's final state is the orbitals: the
+    two-state get_final refuses it before any call into the library (the C
+    call would write nelectrons x nstates values per trajectory into 2 x 2
+    buffers)."""
+    for method in (L.METHOD_IESH, L.METHOD_EHRENFEST_NA):
+        eng = object.__new__(L.Engine)
+        eng.cfg = L.nqcd_config()
+        eng.cfg.method = method
+        eng.ntraj = 4
+        with pytest.raises(ValueError, match="get_final_iesh"):
+            eng.get_final(3)
