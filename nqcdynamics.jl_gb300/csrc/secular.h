@@ -17,15 +17,24 @@
 
 namespace nqcd {
 
+// Host and device: the kernels call these; a host build (the CPU test harness of the solver)
+// takes the IEEE quotient and a plain counter where the device has the approximate reciprocal
+// and an atomic.
+#define NQCD_SECULAR_HD __host__ __device__ __forceinline__
+
 // Reciprocal of a secular-sum denominator.  FP32 (fast paths): the hardware
 // approximate reciprocal (about 1 ulp); its error is of the order of the
 // rounding already allowed for by the stopping test below.
 template <typename R>
-__device__ __forceinline__ R secular_rcp(R d) {
+NQCD_SECULAR_HD R secular_rcp(R d) {
+#ifdef __CUDA_ARCH__
     if constexpr (std::is_same<R, float>::value)
         return __fdividef(1.0f, d);
     else
         return 1.0 / d;
+#else
+    return R(1) / d;
+#endif
 }
 
 // One Newton step of root i's solve: f and f' at o + d (the sums over the poles), the bracket
@@ -33,7 +42,7 @@ __device__ __forceinline__ R secular_rcp(R d) {
 // counted in nonconv); fp is then f' at the returned point.  other = the pole at the far end of
 // the interval (the origin itself for the outer roots), it = steps taken so far.
 template <typename R>
-__device__ __forceinline__ bool secular_newton(const R* __restrict__ eps, const R* __restrict__ V2, int M, R h, int jo,
+NQCD_SECULAR_HD bool secular_newton(const R* __restrict__ eps, const R* __restrict__ V2, int M, R h, int jo,
                                                R o, R other, R& d, R& dlo, R& dhi, R& fp, int& it,
                                                unsigned long long* nonconv) {
     R s1 = R(0), s2 = R(0), s3 = R(0), sa = R(0);
@@ -83,7 +92,13 @@ __device__ __forceinline__ bool secular_newton(const R* __restrict__ eps, const 
         return true;
     }
     if (++it >= 80) {
-        if (nonconv) atomicAdd(nonconv, 1ull);
+        if (nonconv) {
+#ifdef __CUDA_ARCH__
+            atomicAdd(nonconv, 1ull);
+#else
+            ++*nonconv;
+#endif
+        }
         return true;
     }
     return false;
@@ -92,7 +107,7 @@ __device__ __forceinline__ bool secular_newton(const R* __restrict__ eps, const 
 // Solve root i of the secular equation.  o = origin pole, d = offset from it,
 // (dlo, dhi) = bracket of d.  Returns l = o + d and z0^2 = 1/f'.
 template <typename R>
-__device__ __forceinline__ void secular_root(const R* __restrict__ eps, const R* __restrict__ V2, int M, int i, R h,
+NQCD_SECULAR_HD void secular_root(const R* __restrict__ eps, const R* __restrict__ V2, int M, int i, R h,
                                              R Lbound, R& lam_io, R& z2_out, unsigned long long* nonconv) {
     // interval of root i
     const bool first = i == 0, last = i == M;
@@ -168,7 +183,7 @@ struct SecularSolve {
 };
 
 template <typename R>
-__device__ __forceinline__ void secular_warm(SecularSolve<R>& s, R lam) {
+NQCD_SECULAR_HD void secular_warm(SecularSolve<R>& s, R lam) {
     s.d = lam - s.o;
     if (!(s.d > s.dlo && s.d < s.dhi)) s.d = R(0.5) * (s.dlo + s.dhi);
     s.other = s.o == s.a ? s.b : s.a;
@@ -176,7 +191,7 @@ __device__ __forceinline__ void secular_warm(SecularSolve<R>& s, R lam) {
 
 // Interval of root i, origin pole and bracket from the warm start lam (as secular_root).
 template <typename R>
-__device__ __forceinline__ void secular_begin(const R* __restrict__ eps, int M, int i, R Lbound, R lam,
+NQCD_SECULAR_HD void secular_begin(const R* __restrict__ eps, int M, int i, R Lbound, R lam,
                                               SecularSolve<R>& s) {
     const bool first = i == 0, last = i == M;
     s.i = i;
@@ -218,7 +233,7 @@ __device__ __forceinline__ void secular_begin(const R* __restrict__ eps, int M, 
 // One evaluation of f: the midpoint test that picks the origin pole, or one Newton step (as
 // secular_root).  Returns true when the root is done; then l = s.o + s.d, z0^2 = 1 / s.fp.
 template <typename R>
-__device__ __forceinline__ bool secular_eval(const R* __restrict__ eps, const R* __restrict__ V2, int M, R h, R lam,
+NQCD_SECULAR_HD bool secular_eval(const R* __restrict__ eps, const R* __restrict__ V2, int M, R h, R lam,
                                              SecularSolve<R>& s, unsigned long long* nonconv) {
     if (s.need_mid) {
         R sm = R(0);
