@@ -175,6 +175,9 @@ NQCD_SECULAR_HD void secular_root(const R* __restrict__ eps, const R* __restrict
 // The same solve as resumable state, one evaluation of f at a time, so that a lane can start its
 // next root while the other lanes of its warp still iterate theirs (MDEF: seven roots per lane).
 // need_mid: the origin pole is still to be chosen by the sign of f at the interval's midpoint.
+// secular_begin repeats secular_root's choice of interval, origin and bracket (secular_root keeps
+// its own scalar form: the kernels that call it are at their register limit), and
+// tests/test_secular_host.py checks that both forms give the same roots bit for bit.
 template <typename R>
 struct SecularSolve {
     R a, b, o, d, dlo, dhi, other, fp, mid;
