@@ -1530,7 +1530,12 @@ int nqcd_run_host(nqcd_handle* h, int64_t ntraj, const double* r0, const double*
     int64_t h2d = 0;
     const int rc = set_initial_common(h, ntraj, nullptr, nullptr, nullptr, &h2d);
     if (rc) return rc;
-    return run_impl(h, t0, t1, dt, seed, out, stats, r0, v0);
+    const int rr = run_impl(h, t0, t1, dt, seed, out, stats, r0, v0);
+    // a run that failed on the device may not have copied the initial conditions: a later
+    // nqcd_run must not start from the previous ones (a non-finite final state, NQCD_ERR_NAN,
+    // leaves them in place)
+    if (rr == NQCD_ERR_CUDA || rr == NQCD_ERR_OOM || rr == NQCD_ERR_TIMEOUT) h->initial_set = false;
+    return rr;
 }
 
 int nqcd_get_final(nqcd_handle* h, double* r, double* v, double* sig_re, double* sig_im, int32_t* state,
