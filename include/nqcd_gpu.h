@@ -255,7 +255,9 @@ int nqcd_run(nqcd_handle* h, double t0, double t1, double dt, uint64_t seed, nqc
  * host-to-device transfer overlaps the dynamics (pinned host buffers make the
  * copies asynchronous; see nqcd_pin_host); every other configuration runs the
  * two calls in turn.  r0 and v0 may be reused when the call returns; a later
- * nqcd_run repeats the run from the same initial conditions. */
+ * nqcd_run repeats the run from the same initial conditions, except after a
+ * device error (NQCD_ERR_CUDA, NQCD_ERR_OOM, NQCD_ERR_TIMEOUT), which leaves
+ * the handle needing nqcd_set_initial (NQCD_ERR_STATE from nqcd_run). */
 int nqcd_run_host(nqcd_handle* h, int64_t ntraj, const double* r0, const double* v0, double t0, double t1, double dt,
                   uint64_t seed, nqcd_outputs* out, nqcd_stats* stats);
 
